@@ -1,0 +1,394 @@
+"""Frame-rate benchmark of the GB300 renderer (shadow pass + camera pass + shading).
+
+Workload (default): the scene-scale configuration — 64 meshes totalling 262,144
+triangles, 32 materials with 1024^2 albedo/normal/metal-roughness textures and
+full mips, a 4096^2 D32 shadow map with 3x3 PCF, 1920x1080 output, 8 camera
+frames along a seeded Catmull-Rom spline (seed 0). Synthetic, seeded inputs.
+
+A step is one frame (camera i mod 8). `value` is frames/s over the device time
+of the frames (CUDA events on the renderer's stream; the scene constants are
+uploaded inside the frame, everything else is resident); L2 is flushed by a
+256 MiB write between frames, outside the timed events. `e2e` is frames/s
+through the C ABI with host buffers: per frame, the scene constants and all
+object transforms go host->device from pinned memory and the RGBA8 frame comes
+back device->host into pinned memory, wall-clock timed.
+
+--impl reference times the CPU restatement of the reference's path (the oracle,
+oracle/rz_oracle.cpp; Rosy itself needs Vulkan on Windows and cannot run here)
+on all host threads, on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1080p frames/s/GPU (plain path)"
+UNIT = "frames/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_scene(name: str):
+    from rosy_gb300 import scene as sc
+
+    if name == "scene_scale":
+        return sc.scene_scale(seed=0)
+    if name == "random_triangles":
+        s = sc.random_triangles(seed=0)
+        return s
+    raise SystemExit(f"unknown config {name}")
+
+
+def workload_config(name: str, s) -> dict:
+    return {
+        "workload": name, "triangles": s.triangle_count, "meshes": len(s.meshes),
+        "materials": len(s.materials), "textures": len(s.textures),
+        "texture_size": s.textures[0].width if s.textures else 0,
+        "width": s.width, "height": s.height, "shadow_map": s.shadow_size,
+        "pcf": "3x3" if int(s.draw_config["pcf_mode"][0]) == 1 else "5-tap",
+        "frames_on_spline": len(s.cameras), "seed": 0, "samples_per_pixel": 1,
+        "l2": "flushed between frames (256 MiB write)",
+    }
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        import tempfile
+
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(int(os.environ.get("LOCAL_RANK", "0")))],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for i, n in enumerate(names):
+                if r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("RZ_BENCH_BACKEND") != "gloo" else "gloo")
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(s, seconds: float) -> tuple[dict, dict]:
+    """Times the CPU restatement on a bounded sample: whole frames of the same
+    workload, as many as fit in `seconds` (at least one)."""
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    oracle.build()
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        oracle.render(s.with_camera(n), threads=threads)
+        n += 1
+        if time.perf_counter() - t0 >= seconds or n >= 8:
+            break
+    dt = time.perf_counter() - t0
+    extra = {}
+    r = oracle.render(s.with_camera(0), threads=threads, texel_bytes=True)
+    extra["texel_bytes"] = r["texel_bytes"]
+    extra["oracle_ids"] = r["ids"]
+    return ({"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+             "sample": f"{n} full frame(s) of the same workload (cameras 0..{n - 1}), {dt:.1f} s"}, extra)
+
+
+def shade_bytes(s, ids: np.ndarray, texel_bytes: int | None) -> int | None:
+    """Algorithmic bytes of the shading kernel: visibility read, RGBA8 + D32 out,
+    the vertices of the visible triangles, materials, and the compulsory texels."""
+    if texel_bytes is None:
+        return None
+    W, H = s.width, s.height
+    vis = ids[ids > 0].astype(np.int64) - 1
+    # opaque list == all surfaces here; map triangle ids to vertex indices
+    surf = s.surfaces
+    counts = (surf["index_count"] // 3).astype(np.int64)
+    base = np.concatenate([[0], np.cumsum(counts)])
+    tri = np.unique(vis)
+    d = np.searchsorted(base, tri, side="right") - 1
+    mesh = surf["mesh_index"][d]
+    mt = np.asarray(s.meshes, np.int64)
+    first = mt[mesh, 2] + surf["start_index"][d].astype(np.int64) + 3 * (tri - base[d])
+    verts = np.unique(np.concatenate([s.indices[first + k].astype(np.int64) + mt[mesh, 0] for k in range(3)]))
+    return 8 * W * H + 4 * W * H + 4 * W * H + 64 * len(verts) + 64 * len(s.materials) + int(texel_bytes)
+
+
+def raster_bytes(s, pass_name: str) -> int:
+    """Algorithmic bytes of a raster pass: vertex pull once, indices, objects, target write."""
+    V = len(s.vertices)
+    T = s.triangle_count
+    D = len(s.surfaces)
+    if pass_name == "shadow":
+        return 64 * V + 12 * T + 164 * D + 4 * s.shadow_size ** 2
+    return 64 * V + 12 * T + 164 * D + 8 * s.width * s.height
+
+
+def run_rz(args):
+    import torch
+
+    rank, ws = dist_init()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from rosy_gb300 import build as rzbuild
+
+    rzbuild.build()
+    from rosy_gb300.graphics import Graphics
+
+    s = make_scene(args.config)
+    g = Graphics()
+    g.init(s.width, s.height, s.shadow_size, device=torch.cuda.current_device())
+    g.set_asset(s)
+    g.set_graphic_objects(s.objects, s.surfaces)
+    g.set_draw_config(s.draw_config)
+    stream = torch.cuda.ExternalStream(g.stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    cams = [np.ascontiguousarray(c) for c in s.cameras]
+
+    for i in range(args.warmup):
+        g.update(cams[i % len(cams)])
+        g.render()
+    g.sync()
+
+    # --- timed region: device time of each frame ---
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = Clocks()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+            g.update(cams[i % len(cams)])
+            g.render()
+            ends[i].record(stream)
+    g.sync()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ck = clocks.stop()
+    frame_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = max_over_ranks(sum(frame_ms), ws)
+    value = ws * args.steps / (total_ms / 1e3)
+
+    # --- per-stage times (same frames, stage events on) ---
+    g.set_stage_timing(True)
+    stage_acc = {}
+    n_stage = min(args.steps, 200)
+    for i in range(n_stage):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        g.update(cams[i % len(cams)])
+        g.render()
+        g.sync()
+        for k, v in g.stage_times().items():
+            stage_acc[k] = stage_acc.get(k, 0.0) + v
+    stage_ms = {k: v / n_stage for k, v in stage_acc.items()}
+    g.set_stage_timing(False)
+    stats = g.stats()
+
+    # --- e2e through the C ABI with host buffers ---
+    color_host = torch.empty((s.height, s.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    objects_host = torch.empty(s.objects.shape, dtype=torch.float32, pin_memory=True).numpy()
+    objects_host[:] = s.objects
+    scene_host = [torch.empty(408, dtype=torch.uint8, pin_memory=True).numpy() for _ in cams]
+    for k, c in enumerate(cams):
+        scene_host[k][:] = np.frombuffer(c.tobytes(), np.uint8)
+    n_e2e = min(args.steps, 200)
+    g.sync()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for i in range(n_e2e):
+        g.update(scene_host[i % len(cams)].view(cams[0].dtype))
+        g.update_objects(0, objects_host)
+        g.render()
+        g.read_frame(color_host)
+        g.sync()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    e2e_value = ws * n_e2e / e2e_s
+
+    # --- roofline of the dominant kernel ---
+    hbm, peak_kind = peaks()
+    dominant = max(stage_ms, key=stage_ms.get)
+    cpu = None
+    extra = {}
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, extra = cpu_baseline(s, args.cpu_seconds)
+    out0 = g.download() if rank == 0 else None
+    algo = {
+        "shadow_raster": raster_bytes(s, "shadow"),
+        "camera_raster": raster_bytes(s, "camera"),
+        "shade": shade_bytes(s, out0["ids"], extra.get("texel_bytes")) if out0 is not None else None,
+        "shadow_clear": 4 * s.shadow_size ** 2,
+        "camera_clear": 8 * s.width * s.height,
+    }
+    roof = None
+    if rank == 0:
+        stage = dominant
+        b = algo.get(stage)
+        if b is None:  # no algorithmic byte count for this stage: report the shading kernel
+            stage = "shade"
+            b = algo["shade"]
+        if b is not None:
+            ach = b / (stage_ms[stage] / 1e3) / 1e9
+            roof = {"kernel": stage, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(ach / hbm, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                    if peak_kind == "measured" else "fallback 6.8 TB/s",
+                    "algorithmic_bytes_per_launch": int(b), "ms_per_launch": round(stage_ms[stage], 5),
+                    "traffic": None}
+    parity = None
+    if rank == 0 and extra.get("oracle_ids") is not None:
+        parity = bool(np.array_equal(out0["ids"], extra["oracle_ids"]))
+    g.deinit()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": workload_config(args.config, s),
+            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": 408 + int(s.objects.nbytes),
+                    "d2h_bytes_per_step": int(s.width * s.height * 4), "steps": n_e2e},
+            "gpu_launches": int(stats.kernel_launches) * args.steps,
+            "roofline": roof,
+            "stage_ms": {k: round(v, 5) for k, v in stage_ms.items()},
+            "mtriangles_per_s": round(value * s.triangle_count / 1e6, 1),
+            "cpu_baseline": cpu,
+            "clocks": ck,
+            "visibility_matches_oracle_frame0": parity,
+            "algorithmic_bytes": {k: (int(v) if v is not None else None) for k, v in algo.items()},
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    s = make_scene(args.config)
+    from oracle import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    for i in range(min(args.warmup, 1)):
+        oracle.render(s.with_camera(i), threads=threads)
+    t0 = time.perf_counter()
+    n = 0
+    while n < args.steps:
+        oracle.render(s.with_camera(n), threads=threads)
+        n += 1
+        if time.perf_counter() - t0 >= args.cpu_seconds:
+            break
+    dt = time.perf_counter() - t0
+    v = n / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": 1, "steps": n,
+        "warmup": min(args.warmup, 1), "ms_per_step": round(1e3 * dt / n, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": workload_config(args.config, s),
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} full frame(s), capped at {args.cpu_seconds:.0f} s"},
+        "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (Vulkan, Windows-only) cannot run here; its path is timed as the scalar CPU "
+                "restatement in oracle/rz_oracle.cpp on all host threads",
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="rz", choices=["rz", "reference"])
+    ap.add_argument("--config", default="scene_scale", choices=["scene_scale", "random_triangles"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "rz":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_rz(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,337 @@
+/*
+ * rosy_gb300 — C ABI of the GB300 (sm_103a) frame renderer that replaces Rosy's
+ * shadow depth pass + mesh forward pass.
+ *
+ * The reference interface is `rosy::graphics` (src/Engine/Graphics.h:11-21) and
+ * the inner seams of its Vulkan backend `graphics_device`:
+ *   set_asset           src/Engine/Graphics.cpp:3525   -> rz_set_asset
+ *   set_graphic_objects src/Engine/Graphics.cpp:4691   -> rz_set_objects
+ *   (go_update upload)  src/Engine/Graphics.cpp:5120-5138 -> rz_update_objects
+ *   update              src/Engine/Graphics.cpp:6016   -> rz_update
+ *   render              src/Engine/Graphics.cpp:4934   -> rz_render
+ *   init / deinit       src/Engine/Graphics.cpp:6119-6170, 6217-6228 -> rz_create / rz_destroy
+ *   resize              src/Engine/Graphics.cpp:6200   -> rz_resize
+ *
+ * Windowing, swapchain, imgui and debug lines are not part of this path: the
+ * frame is rendered into headless device buffers (RGBA8 sRGB colour, D32 depth,
+ * a 64-bit visibility buffer and the D32 shadow map) that the caller reads with
+ * rz_get_frame (device pointers) or rz_read_frame (copy to host memory).
+ *
+ * Every entry point returns an rz_result (the numeric values 0..15 are those of
+ * rosy::result, src/Engine/Types.h:13-31). No entry point throws. One context
+ * is used by one host thread at a time; there is no global mutable state except
+ * the CUDA runtime's own.
+ */
+#ifndef ROSY_GB300_H
+#define ROSY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RZ_ABI_VERSION 1u
+
+/* Opaque renderer context (one per host thread). */
+struct rz_ctx;
+typedef struct rz_ctx rz_ctx;
+#define RZ_INVALID_INDEX 0xFFFFFFFFu /* UINT32_MAX == absent, src/shaders/data.slang:135-137 */
+
+typedef enum rz_result {
+    RZ_OK = 0,
+    RZ_STATE_CHANGED = 1,
+    RZ_ERROR = 2,
+    RZ_INVALID_ARGUMENT = 3,
+    RZ_ALLOCATION_FAILURE = 4,
+    RZ_GRAPHICS_INIT_FAILURE = 5,
+    RZ_GRAPHICS_FRAME_FAILURE = 6,
+    RZ_GRAPHICS_SWAPCHAIN_FAILURE = 7,
+    RZ_OPEN_FAILED = 8,
+    RZ_WRITE_FAILED = 9,
+    RZ_COPY_FAILED = 10,
+    RZ_READ_FAILED = 11,
+    RZ_CREATE_FAILED = 12,
+    RZ_UPDATE_FAILED = 13,
+    RZ_OVERFLOW = 14,
+    RZ_INVALID_STATE = 15,
+    /* Added by this library: rz_sync gave up waiting (the reference waits on a
+     * fence with a timeout at src/Engine/Graphics.cpp:4940). */
+    RZ_TIMEOUT = 16
+} rz_result;
+
+/* One vertex: rosy_asset::position (src/Asset/Asset.h:92-99), read by the shaders
+ * as BasicInputVertex (src/shaders/data.slang:24-30). 64 bytes, tightly packed. */
+typedef struct rz_vertex {
+    float position[3];
+    float normal[3];
+    float tangent[4];
+    float color[4];
+    float uv[2];
+} rz_vertex;
+
+/* A mesh: its vertices and mesh-local u32 indices (rosy_asset::mesh,
+ * src/Asset/Asset.h:101-106). The renderer concatenates all meshes the way
+ * set_asset does (src/Engine/Graphics.cpp:4310-4334); indices stay mesh-local. */
+typedef struct rz_mesh {
+    const rz_vertex* positions;
+    uint32_t position_count;
+    uint32_t index_count;
+    const uint32_t* indices;
+} rz_mesh;
+
+/* Asset material (rosy_asset::material, src/Asset/Asset.h:27-46). rz_set_asset
+ * packs it into the 64-byte gpu_material (src/Engine/Graphics.cpp:345-360) with
+ * the index mapping of src/Engine/Graphics.cpp:4071-4150: an image index that
+ * is out of range becomes "absent"; a sampler index that is out of range (or
+ * given for an absent image) selects the default sampler. */
+typedef struct rz_material {
+    float base_color_factor[4];
+    float metallic_factor;
+    float roughness_factor;
+    float alpha_cutoff;
+    uint32_t alpha_mode;     /* 0 opaque, 1 mask, 2 blend (any non-zero => blended list) */
+    uint32_t double_sided;   /* carried, unused by the path (as in the reference) */
+    uint32_t color_image_index;
+    uint32_t color_sampler_index;
+    uint32_t normal_image_index;
+    uint32_t normal_sampler_index;
+    uint32_t metallic_image_index;
+    uint32_t metallic_sampler_index;
+    uint32_t mixmap_image_index;
+    uint32_t mixmap_sampler_index;
+} rz_material;
+
+/* Asset sampler (rosy_asset::sampler, src/Asset/Asset.h:48-54). Filter codes
+ * 0..2 => nearest, anything else => linear (src/Engine/Graphics.cpp:250-262);
+ * wrap codes 0 clamp-to-edge, 1 mirrored repeat, else repeat (264-278). The
+ * mip mode of asset samplers is linear (src/Engine/Graphics.cpp:3996-4014). */
+typedef struct rz_sampler {
+    uint16_t min_filter;
+    uint16_t mag_filter;
+    uint16_t wrap_s;
+    uint16_t wrap_t;
+} rz_sampler;
+
+/* Image types (src/Asset/Asset.h:108-112). Colour, metallic-roughness and mixmap
+ * images are sampled as sRGB, normal maps as UNORM (Graphics.cpp:3632-3647). */
+#define RZ_IMAGE_COLOR 0u
+#define RZ_IMAGE_NORMAL_MAP 1u
+#define RZ_IMAGE_METALLIC_ROUGHNESS 2u
+#define RZ_IMAGE_MIXMAP 3u
+
+/* A texture: RGBA8 texels of `levels` mip levels, concatenated level 0 first;
+ * level l is max(1, width>>l) x max(1, height>>l), rows top to bottom.
+ * (The reference loads BC7 .dds mips; decoded RGBA8 stands in for them.) */
+typedef struct rz_texture {
+    uint32_t width;
+    uint32_t height;
+    uint32_t levels;
+    uint32_t image_type;
+    const void* texels;
+} rz_texture;
+
+/* Per-object transforms: graphic_object_data (src/Engine/Graphics.cpp:422-427),
+ * BasicGraphicsData in the shaders (src/shaders/data.slang:32-36). Column-major
+ * (glm) matrices, 164 bytes. */
+typedef struct rz_object {
+    float transform[16];
+    float to_object_space_transform[16];
+    float normal_transform[9];
+} rz_object;
+
+/* One draw: rosy::surface_graphics_data (src/Engine/Types.h:39-48), with u32 in
+ * place of size_t. Surfaces are given in scene order; the shadow list is all of
+ * them, the opaque list those with blended == 0, the blended list the others
+ * (src/Engine/Graphics.cpp:4715-4735). */
+typedef struct rz_surface {
+    uint32_t mesh_index;
+    uint32_t graphic_objects_offset;
+    uint32_t graphics_object_index;
+    uint32_t material_index; /* RZ_INVALID_INDEX => no material */
+    uint32_t index_count;
+    uint32_t start_index;
+    uint32_t blended;
+} rz_surface;
+
+/* Scene constants: byte-identical to gpu_scene_data (src/Engine/Graphics.cpp:
+ * 281-306) / SceneData (src/shaders/data.slang:45-70), 408 bytes. */
+typedef struct rz_scene_data {
+    float view[16];
+    float proj[16];
+    float view_projection[16];
+    float shadow_projection_near[16];
+    float sun_position[4];
+    float camera_position[4];
+    float ambient_color[4];
+    float sunlight_color[4];
+    uint32_t flip_lights[4];
+    uint32_t flip_tangents[4];
+    float draw_extent[2];
+    float light_intensity;
+    uint32_t csm_index_sampler; /* ignored: the shadow map is the one this frame rendered */
+    uint32_t csm_index_near;    /* ignored */
+    uint32_t fragment_output;
+    uint32_t light_enabled;
+    uint32_t tangent_space_enabled;
+    uint32_t shadows_enabled;
+    uint32_t normal_maps_enabled;
+    uint32_t inverse_bnt;
+    uint32_t ignore_asset_tangent_sign;
+    uint32_t ensure_orthogonal_bitangent;
+    uint32_t brdf_lighting_enabled;
+} rz_scene_data;
+
+/* PCF kernels for the shadow lookup. */
+#define RZ_PCF_5TAP 0u /* the reference's pattern, src/shaders/pcf.slang:1-11 */
+#define RZ_PCF_3X3 1u  /* 3x3 grid, one texel apart (option) */
+
+/* Fixed-function state that the reference takes from read_level_state rather
+ * than from gpu_scene_data: draw_config (src/Engine/Graphics.cpp:5010-5015) and
+ * the light's depth bias (5222-5231). Defaults: src/Engine/Level.cpp:1246-1255. */
+typedef struct rz_draw_config {
+    uint32_t cull_enabled;                  /* 1 => cull FRONT faces */
+    uint32_t reverse_winding_order_enabled; /* 1 => front face is counter-clockwise */
+    uint32_t depth_bias_enabled;            /* shadow pass only */
+    float depth_bias_constant;
+    float depth_bias_clamp;
+    float depth_bias_slope_factor;
+    uint32_t pcf_mode;                      /* RZ_PCF_* */
+    uint32_t reserved;
+} rz_draw_config;
+
+/* Context creation: the headless analogue of graphics::init's config
+ * (src/Engine/Types.h:33-37). */
+typedef struct rz_config {
+    uint32_t width;            /* colour/depth extent */
+    uint32_t height;
+    uint32_t shadow_map_size;  /* square D32 shadow map (the reference uses 4096, Graphics.cpp:2524) */
+    uint32_t samples;          /* rasterisation samples per pixel: 1 */
+    int32_t device;            /* CUDA device ordinal */
+    uint32_t reserved[3];
+} rz_config;
+
+/* Device pointers of the last rendered frame. colour: RGBA8, sRGB-encoded RGB
+ * (the B8G8R8A8_SRGB swapchain blit of src/Engine/Graphics.cpp:5845-5879, with
+ * R in byte 0); depth: f32 reverse-Z (cleared to 0); visibility: per pixel
+ * (depth_bits << 32) | (triangle_id + 1), 0 = background; shadow map: f32. */
+typedef struct rz_frame_out {
+    void* color_rgba8;
+    void* depth_f32;
+    void* visibility_u64;
+    void* shadow_map_f32;
+    uint32_t width;
+    uint32_t height;
+    uint32_t shadow_map_size;
+    uint32_t reserved;
+} rz_frame_out;
+
+/* Counters of the last frame (graphics_stats, src/Engine/DebugUI.h:7-13). */
+typedef struct rz_stats {
+    uint32_t draw_call_count;
+    uint32_t triangle_count;
+    uint32_t shadow_setup_records;  /* raster setup records written, shadow pass */
+    uint32_t camera_setup_records;  /* raster setup records written, camera pass */
+    uint64_t shadow_stamps;         /* 8x4-pixel stamps rasterised, shadow pass */
+    uint64_t camera_stamps;         /* 8x4-pixel stamps rasterised, camera pass */
+    uint32_t error_flags;           /* device-side error bits of the last frame */
+    uint32_t kernel_launches;       /* kernels enqueued by the last rz_render */
+} rz_stats;
+
+/* graphics::init (src/Engine/Graphics.h:17): creates the CUDA stream and the
+ * frame buffers on cfg->device. */
+int rz_create(struct rz_ctx** out_ctx, const rz_config* cfg);
+
+/* graphics::deinit (src/Engine/Graphics.h:21). Accepts NULL. */
+void rz_destroy(struct rz_ctx* ctx);
+
+/* graphics::resize (src/Engine/Graphics.h:20): new colour/depth extent. */
+int rz_resize(struct rz_ctx* ctx, uint32_t width, uint32_t height);
+
+/* graphics_device::set_asset (src/Engine/Graphics.cpp:3525): copies meshes,
+ * materials, textures and samplers into device memory. Blocks until the copy is
+ * done (the reference waits on an immediate-submit fence). */
+int rz_set_asset(struct rz_ctx* ctx,
+                 const rz_mesh* meshes, uint32_t mesh_count,
+                 const rz_material* materials, uint32_t material_count,
+                 const rz_texture* textures, uint32_t texture_count,
+                 const rz_sampler* samplers, uint32_t sampler_count);
+
+/* graphics_device::set_graphic_objects (src/Engine/Graphics.cpp:4691): the
+ * object transforms and the surface list in scene order. Rejects an empty
+ * scene (RZ_INVALID_ARGUMENT, as 4693-4697), out-of-range mesh/object/material
+ * indices or index ranges, and non-blended surfaces whose material has a
+ * non-zero alpha_mode (the opaque list never holds those in the engine,
+ * src/Engine/Level.cpp:1056-1061, and this renderer's visibility pass relies on it). */
+int rz_set_objects(struct rz_ctx* ctx,
+                   const rz_object* objects, uint32_t object_count,
+                   const rz_surface* surfaces, uint32_t surface_count);
+
+/* Mob transform update (src/Engine/Graphics.cpp:5120-5138): overwrite
+ * objects [offset, offset+count) before the next frame; enqueued on the stream. */
+int rz_update_objects(struct rz_ctx* ctx, uint32_t offset, const rz_object* objects, uint32_t count);
+
+/* Fixed-function state of the next frames (see rz_draw_config). */
+int rz_set_draw_config(struct rz_ctx* ctx, const rz_draw_config* cfg);
+
+/* graphics_device::update (src/Engine/Graphics.cpp:6016): the scene constants
+ * of the next frame. The 408 bytes are staged in pinned memory and copied on
+ * the stream, so a frame always uses its own constants (the reference writes
+ * the next frame's buffer, 5064-5065; that one-frame lag is not reproduced). */
+int rz_update(struct rz_ctx* ctx, const rz_scene_data* scene);
+
+/* graphics_device::render (src/Engine/Graphics.cpp:4934): enqueues the shadow
+ * pass, the camera pass and the shading pass on the context's stream and
+ * returns without waiting. Errors found on the device (an overflowing
+ * raster work queue, for instance) are reported by the next rz_sync. */
+int rz_render(struct rz_ctx* ctx);
+
+/* Waits for the stream, at most timeout_ms milliseconds (0 = no limit).
+ * Returns RZ_TIMEOUT if the frame is still running, RZ_OVERFLOW or
+ * RZ_GRAPHICS_FRAME_FAILURE if the device flagged an error in a frame. */
+int rz_sync(struct rz_ctx* ctx, uint32_t timeout_ms);
+
+/* Device pointers of the frame buffers (valid until the next rz_resize/rz_destroy). */
+int rz_get_frame(struct rz_ctx* ctx, rz_frame_out* out);
+
+/* Enqueues device-to-host copies of the colour (width*height*4 bytes) and/or
+ * depth (width*height*4 bytes) images; NULL skips one. Complete after rz_sync. */
+int rz_read_frame(struct rz_ctx* ctx, void* color_host, size_t color_bytes,
+                  void* depth_host, size_t depth_bytes);
+
+/* Counters of the last completed frame (call after rz_sync). */
+int rz_get_stats(struct rz_ctx* ctx, rz_stats* out);
+
+/* Frame stages timed by rz_get_stage_times (CUDA events on the context's stream). */
+#define RZ_STAGE_SHADOW_CLEAR 0u  /* shadow-map clear */
+#define RZ_STAGE_SHADOW_SETUP 1u  /* shadow draw matrices + triangle setup */
+#define RZ_STAGE_SHADOW_RASTER 2u /* shadow raster */
+#define RZ_STAGE_CAMERA_CLEAR 3u  /* visibility clear + camera draw constants */
+#define RZ_STAGE_CAMERA_SETUP 4u  /* camera triangle setup */
+#define RZ_STAGE_CAMERA_RASTER 5u /* camera raster (visibility buffer) */
+#define RZ_STAGE_SHADE 6u         /* deferred shading + sRGB encode */
+#define RZ_STAGE_COUNT 7u
+
+/* Enables (1) or disables (0) per-stage event timing of the following frames.
+ * This is a diagnostic switch: it adds event records between the stages. */
+int rz_set_stage_timing(struct rz_ctx* ctx, uint32_t enable);
+
+/* Milliseconds spent in each stage of the last completed frame (call after
+ * rz_sync). Writes min(capacity, RZ_STAGE_COUNT) values and the count. */
+int rz_get_stage_times(struct rz_ctx* ctx, float* ms, uint32_t capacity, uint32_t* count);
+
+/* The context's cudaStream_t, for callers that time or chain work on it. */
+void* rz_get_stream(struct rz_ctx* ctx);
+
+/* Human-readable message of the last failing call on this context. */
+const char* rz_last_error(struct rz_ctx* ctx);
+
+/* RZ_ABI_VERSION of the loaded library. */
+uint32_t rz_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ROSY_GB300_H */

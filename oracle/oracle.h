@@ -1,0 +1,66 @@
+/*
+ * ORACLE — test infrastructure only. A scalar CPU restatement of Rosy's shadow
+ * depth pass and mesh forward pass, used by the tests, by the smoke check and
+ * as the timed CPU baseline of bench.py. The renderer library never calls it.
+ *
+ * Parity status: unpinned by the reference. Rosy has no tests, golden images or
+ * known-answer vectors, and it cannot be built or run here (Windows/VS2022,
+ * Vulkan SDK, empty submodules, no graphics stack on either machine), so this
+ * restatement is pinned by hand-derived known-answer tests instead.
+ */
+#ifndef RZ_ORACLE_H
+#define RZ_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/rosy_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_scene {
+    const rz_vertex* vertices;      /* all meshes concatenated */
+    uint32_t vertex_count;
+    uint32_t index_count;
+    const uint32_t* indices;        /* mesh-local, all meshes concatenated */
+    const uint32_t* meshes;         /* 4 per mesh: vertex_offset, vertex_count, index_offset, index_count */
+    uint32_t mesh_count;
+    uint32_t object_count;
+    const rz_object* objects;
+    const rz_surface* surfaces;
+    uint32_t surface_count;
+    uint32_t material_count;
+    const rz_material* materials;
+    const rz_texture* textures;
+    uint32_t texture_count;
+    uint32_t sampler_count;
+    const rz_sampler* samplers;
+    const rz_scene_data* scene;
+    const rz_draw_config* draw_config;
+    uint32_t width;
+    uint32_t height;
+    uint32_t shadow_size;
+    uint32_t reserved;
+} oracle_scene;
+
+typedef struct oracle_out {
+    uint8_t* color;      /* width*height*4, RGBA8 sRGB (may be NULL) */
+    float* depth;        /* width*height (may be NULL) */
+    uint32_t* ids;       /* width*height, triangle id + 1, 0 = background (may be NULL) */
+    float* shadow;       /* shadow_size^2 (may be NULL) */
+    double* color_f64;   /* width*height*4, FP64 shading, sRGB-encoded in [0,1] before 8-bit rounding (may be NULL) */
+    uint64_t* texel_bytes; /* if non-NULL: compulsory texture + shadow-map bytes the shading touched */
+} oracle_out;
+
+/* Renders one frame. threads <= 0 uses all hardware threads. Returns 0 on success. */
+int oracle_render(const oracle_scene* scene, oracle_out* out, int threads);
+
+/* Only the raster passes: the shadow map and the camera pass's depth/ids. */
+int oracle_raster(const oracle_scene* scene, oracle_out* out, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

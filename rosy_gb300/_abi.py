@@ -1,0 +1,85 @@
+"""ctypes mirror of include/rosy_gb300.h and marshalling of a Scene into it."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import scene as sc
+
+
+class RzVertex(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("normal", C.c_float * 3), ("tangent", C.c_float * 4),
+                ("color", C.c_float * 4), ("uv", C.c_float * 2)]
+
+
+class RzMesh(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("position_count", C.c_uint32),
+                ("index_count", C.c_uint32), ("indices", C.c_void_p)]
+
+
+class RzTexture(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32),
+                ("image_type", C.c_uint32), ("texels", C.c_void_p)]
+
+
+class RzConfig(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("shadow_map_size", C.c_uint32),
+                ("samples", C.c_uint32), ("device", C.c_int32), ("reserved", C.c_uint32 * 3)]
+
+
+class RzFrameOut(C.Structure):
+    _fields_ = [("color_rgba8", C.c_void_p), ("depth_f32", C.c_void_p), ("visibility_u64", C.c_void_p),
+                ("shadow_map_f32", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("shadow_map_size", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class RzStats(C.Structure):
+    _fields_ = [("draw_call_count", C.c_uint32), ("triangle_count", C.c_uint32),
+                ("shadow_setup_records", C.c_uint32), ("camera_setup_records", C.c_uint32),
+                ("shadow_stamps", C.c_uint64), ("camera_stamps", C.c_uint64),
+                ("error_flags", C.c_uint32), ("kernel_launches", C.c_uint32)]
+
+
+assert C.sizeof(RzVertex) == 64
+assert C.sizeof(RzMesh) == 24
+assert C.sizeof(RzTexture) == 24
+
+
+def ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+class Marshalled:
+    """Keeps the numpy/ctypes buffers of one scene alive while C code uses them."""
+
+    def __init__(self, s: "sc.Scene"):
+        self.scene = s
+        self.vertices = np.ascontiguousarray(s.vertices, np.float32)
+        self.indices = np.ascontiguousarray(s.indices, np.uint32)
+        self.mesh_table = np.ascontiguousarray(np.asarray(s.meshes, np.uint32).reshape(-1, 4))
+        self.meshes = (RzMesh * len(s.meshes))()
+        for i, (vo, vc, io, ic) in enumerate(s.meshes):
+            self.meshes[i].positions = ptr(self.vertices) + int(vo) * 64
+            self.meshes[i].position_count = int(vc)
+            self.meshes[i].index_count = int(ic)
+            self.meshes[i].indices = ptr(self.indices) + int(io) * 4
+        self.objects = np.ascontiguousarray(s.objects, np.float32)
+        self.surfaces = np.ascontiguousarray(s.surfaces)
+        self.materials = np.ascontiguousarray(s.materials)
+        self.samplers = np.ascontiguousarray(s.samplers)
+        self.tex_data = [np.ascontiguousarray(t.texels, np.uint8) for t in s.textures]
+        self.textures = (RzTexture * max(1, len(s.textures)))()
+        for i, t in enumerate(s.textures):
+            self.textures[i].width = t.width
+            self.textures[i].height = t.height
+            self.textures[i].levels = t.levels
+            self.textures[i].image_type = t.image_type
+            self.textures[i].texels = ptr(self.tex_data[i])
+        self.scene_rec = np.ascontiguousarray(s.scene)
+        self.draw_config = np.ascontiguousarray(s.draw_config)
+
+    @property
+    def n_textures(self) -> int:
+        return len(self.scene.textures)

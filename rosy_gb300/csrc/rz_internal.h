@@ -1,0 +1,148 @@
+// Internal device-side layouts of the renderer (host + device). Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rosy_gb300.h"
+
+namespace rz {
+
+// One draw of a pass: surface_graphics_data resolved against the mesh table
+// (src/Engine/Graphics.cpp:5268-5288 shadow loop, 5631-5653 opaque loop).
+struct DrawRec {
+    uint32_t vertex_base;  // first vertex of the mesh in the concatenated vertex buffer
+    uint32_t first_index;  // mesh.index_offset + start_index
+    uint32_t tri_count;    // index_count / 3
+    uint32_t object;       // graphic_objects_offset + graphics_object_index
+    int32_t material;      // -1 = none
+    uint32_t tri_base;     // first triangle id of this draw within the pass
+    uint32_t pad[2];
+};
+static_assert(sizeof(DrawRec) == 32, "DrawRec layout");
+
+// gpu_material, src/Engine/Graphics.cpp:345-360, packed as in 4071-4150.
+struct GpuMaterial {
+    float color[4];
+    float metallic_factor, roughness_factor, alpha_cutoff;
+    uint32_t alpha_mode;
+    uint32_t tex[4];      // color, normal, metallic, mixmap image index; UINT32_MAX = absent
+    uint32_t sampler[4];  // sampler index; == sampler_count selects the default sampler
+};
+static_assert(sizeof(GpuMaterial) == 64, "gpu_material is 64 bytes");
+
+// Bindless texture table entry. Texels are RGBA8 in one pool, level-major,
+// each level row-major (the caller's layout).
+struct TexDesc {
+    uint32_t width, height, levels, srgb;
+    uint64_t base;             // first texel (u32 units) of level 0 in the pool
+    uint32_t level_off[16];    // texel offset of each level from base
+};
+
+// Per-draw constants of the camera pass computed on the device each frame:
+// MVP = viewproj * W, CSM = (ndc_to_tc * shadowProjNear) * W, and the camera and
+// sun positions in object space (src/shaders/basic.slang:76-77, 114, 116).
+struct DrawConsts {
+    float mvp[16];
+    float csm[16];
+    float cam_obj[4];
+    float sun_obj[4];
+};
+
+// Sampler state: bit 0 min linear, bit 1 mag linear, bit 2 mip linear,
+// bits 4-5 wrap u, bits 6-7 wrap v (0 clamp, 1 mirrored repeat, 2 repeat).
+typedef uint32_t SamplerBits;
+
+// Raster setup record, one per (sub-)triangle with S > 0 ordering; 64 bytes.
+struct TriRecord {
+    int32_t X0, Y0, X1, Y1, X2, Y2;  // 8-bit sub-pixel fixed point
+    float z0, dzdx, dzdy, bias;      // depth plane (per sub-pixel) and constant depth bias
+    uint32_t p0;                     // px0 | py0 << 16 (bounding box, pixels)
+    uint32_t p1;                     // px1 | py1 << 16 (inclusive)
+    uint32_t id;                     // camera pass: triangle id + 1
+    uint32_t stamps;                 // number of 8x4 stamps of the bounding box
+    uint64_t stamp_offset;           // exclusive prefix of stamps over all records
+};
+static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
+
+constexpr int kStampW = 8;
+constexpr int kStampH = 4;
+constexpr int kChunkStamps = 16;      // stamps per raster work chunk
+constexpr int kSetupThreads = 256;    // triangles per setup CTA
+constexpr float kGuardBand = 64.0f;
+
+// Device error bits (rz_stats.error_flags).
+constexpr uint32_t kErrRecordOverflow = 1u << 0;
+constexpr uint32_t kErrStampOverflow = 1u << 1;
+constexpr uint32_t kErrLookbackTimeout = 1u << 2;
+constexpr uint32_t kErrBadIndex = 1u << 3;
+
+// Per-pass scratch header, cleared before each pass.
+struct PassHeader {
+    uint32_t ticket;          // CTA tile ticket of the setup kernel
+    uint32_t records;         // records written
+    uint64_t stamps;          // total stamps
+    uint32_t chunks;          // ceil(stamps / kChunkStamps)
+    uint32_t pad[3];
+};
+
+// Pass description handed to the setup/raster launchers.
+struct PassParams {
+    const DrawRec* draws;
+    uint32_t draw_count;
+    uint32_t tri_total;
+    const float* mvp;         // MVP of draw d at mvp + mvp_stride * d
+    uint32_t mvp_stride;
+    const float4* pos;        // positions (x, y, z, pad)
+    const uint32_t* indices;
+    uint32_t vertex_count;
+    int width, height;        // viewport
+    int cull_front, ccw_front;
+    int bias_enabled;
+    float bias_constant, bias_clamp, bias_slope;
+    int write_id;             // 1: camera pass (64-bit depth|id keys); 0: shadow (depth only)
+    TriRecord* records;
+    uint32_t record_capacity;
+    uint64_t* tile_status;    // one word per setup CTA
+    uint32_t* chunk_map;
+    uint32_t chunk_capacity;
+    PassHeader* header;
+    uint32_t* error_flags;
+    void* target;             // uint64_t* visibility or uint32_t* shadow depth bits
+};
+
+struct ShadeParams {
+    const uint64_t* vis;
+    const float* shadow;
+    int shadow_size;
+    uint32_t* color;          // RGBA8 out
+    float* depth;             // D32 out
+    int width, height;
+    const DrawRec* draws;     // opaque list
+    uint32_t draw_count;
+    const DrawConsts* consts; // per opaque draw
+    const rz_vertex* vertices;
+    const uint32_t* indices;
+    const rz_object* objects;
+    const GpuMaterial* materials;
+    const TexDesc* textures;
+    uint32_t texture_count;
+    const SamplerBits* samplers;  // sampler_count + 1 entries (last = default)
+    uint32_t sampler_count;
+    const uint32_t* texels;
+    const rz_scene_data* scene;
+    uint32_t pcf_mode;
+    const float* srgb_table;      // 256 entries
+};
+
+// Launchers (rz_raster.cu / rz_shade.cu). All enqueue on `stream`.
+void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const float* proj16,
+                 float* out_mvp, cudaStream_t stream);
+void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const rz_scene_data* scene,
+                        DrawConsts* out, cudaStream_t stream);
+void launch_setup(const PassParams& p, cudaStream_t stream);
+void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream);
+void launch_shade(const ShadeParams& p, cudaStream_t stream);
+int setup_ctas(uint32_t tri_total);
+
+}  // namespace rz

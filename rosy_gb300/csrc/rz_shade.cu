@@ -1,0 +1,604 @@
+// Deferred-style shading of the camera pass.
+//
+// Reference path: vertexMain (src/shaders/basic.slang:16-119) and fragmentMain
+// (137-344) with pcf (src/shaders/pcf.slang:1-11) and the BRDF helpers
+// (src/shaders/lighting.slang:5-43), evaluated once per pixel for the triangle
+// that won the depth test, then the RGBA16F draw image (Graphics.cpp:1905-1908)
+// and the blit to the sRGB swapchain (5845-5879).
+//
+// Instead of interpolating rasterised varyings, each pixel re-fetches the three
+// vertices of its triangle (64-byte records, vertex pulling as the reference
+// does through buffer device addresses), runs the vertex-stage math on them,
+// and interpolates with perspective-correct barycentrics computed from the
+// clip positions in 2D homogeneous form. Texture level selection uses the
+// derivative of the interpolated uv across the pixel's 2x2 quad (the value at
+// the quad's top-left, right and lower neighbours, which is what a helper
+// invocation would compute).
+//
+// The operation order matches the oracle's fp32 path, and the file is built
+// with -fmad=false, so everything except powf/log2f is bit-identical to it.
+#include <cuda_fp16.h>
+
+#include "rz_device.cuh"
+
+namespace rz {
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V3 mul3(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ V3 normalize(V3 a) {
+    const float l = sqrtf(dot(a, a));
+    return {a.x / l, a.y / l, a.z / l};
+}
+__device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+__device__ __forceinline__ V3 mulm3v(const float* N, V3 v) {
+    return {N[0] * v.x + N[3] * v.y + N[6] * v.z, N[1] * v.x + N[4] * v.y + N[7] * v.z, N[2] * v.x + N[5] * v.y + N[8] * v.z};
+}
+
+// ---------------------------------------------------------------------------
+// per-draw constants
+// ---------------------------------------------------------------------------
+
+__global__ void k_prep_camera(const DrawRec* __restrict__ draws, uint32_t n, const rz_object* __restrict__ objects,
+                              const rz_scene_data* __restrict__ sd, DrawConsts* __restrict__ out) {
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    const rz_object& gd = objects[draws[d].object];
+    float W[16], VP[16], C[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        W[i] = gd.transform[i];
+        VP[i] = sd->view_projection[i];
+    }
+    mat4_mul(VP, W, C);
+    DrawConsts& o = out[d];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) o.mvp[i] = C[i];
+    // (ndc_to_tc * shadowProjNear) * W, ndc_to_tc rows (0.5,0,0,0.5) (0,0.5,0,0.5) (0,0,1,0) (0,0,0,1)
+    float A[16];
+    const float* P = sd->shadow_projection_near;
+#pragma unroll
+    for (int col = 0; col < 4; ++col) {
+        const float x = P[col * 4 + 0], y = P[col * 4 + 1], z = P[col * 4 + 2], w = P[col * 4 + 3];
+        A[col * 4 + 0] = 0.5f * x + 0.5f * w;
+        A[col * 4 + 1] = 0.5f * y + 0.5f * w;
+        A[col * 4 + 2] = z;
+        A[col * 4 + 3] = w;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            o.csm[c * 4 + r] = A[0 * 4 + r] * W[c * 4 + 0] + A[1 * 4 + r] * W[c * 4 + 1] + A[2 * 4 + r] * W[c * 4 + 2] +
+                               A[3 * 4 + r] * W[c * 4 + 3];
+    const float* T = gd.to_object_space_transform;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        o.cam_obj[r] = T[0 * 4 + r] * sd->camera_position[0] + T[1 * 4 + r] * sd->camera_position[1] +
+                       T[2 * 4 + r] * sd->camera_position[2] + T[3 * 4 + r] * sd->camera_position[3];
+        o.sun_obj[r] = T[0 * 4 + r] * sd->sun_position[0] + T[1 * 4 + r] * sd->sun_position[1] +
+                       T[2 * 4 + r] * sd->sun_position[2] + T[3 * 4 + r] * sd->sun_position[3];
+    }
+}
+
+void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const rz_scene_data* scene,
+                        DrawConsts* out, cudaStream_t stream) {
+    if (n == 0) return;
+    k_prep_camera<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, scene, out);
+}
+
+// ---------------------------------------------------------------------------
+// vertex stage
+// ---------------------------------------------------------------------------
+
+struct VsOut {
+    V3 normal, worldNormal, viewDir, lightDir, tangent, bitangent;
+    float color[4];
+    float uv[2];
+    float sigma;
+    float csm[4];
+};
+
+// vertexMain, src/shaders/basic.slang:16-119 (outputs used by fragmentMain).
+__device__ __forceinline__ void vertex_main(const rz_scene_data& sd, const rz_object& gd, const DrawConsts& dc,
+                                            bool has_material, bool material_has_normal_map, const rz_vertex& v, VsOut& o) {
+    float nt[4] = {v.tangent[0], v.tangent[1], v.tangent[2], v.tangent[3]};
+    if (sd.ignore_asset_tangent_sign == 1) nt[3] = 1.0f;
+    if (sd.flip_tangents[0] == 1) nt[0] = nt[0] * -1.0f;
+    if (sd.flip_tangents[1] == 1) nt[1] = nt[1] * -1.0f;
+    if (sd.flip_tangents[2] == 1) nt[2] = nt[2] * -1.0f;
+    if (sd.flip_tangents[3] == 1) nt[3] = nt[3] * -1.0f;
+    bool tse = sd.tangent_space_enabled == 1;
+    if (has_material && !material_has_normal_map) tse = false;
+    const V3 vpos{v.position[0], v.position[1], v.position[2]};
+    V3 normal{v.normal[0], v.normal[1], v.normal[2]};
+    V3 tangent{nt[0], nt[1], nt[2]};
+    V3 bitangent = cross(normal, tangent) * nt[3];
+    if (sd.ensure_orthogonal_bitangent == 1) {
+        const V3 normal_projection = bitangent * dot(normal, bitangent);
+        const V3 ortho_n = normalize(normal - normal_projection);
+        const V3 tangent_projection = normal_projection - bitangent * dot(tangent, bitangent);
+        const V3 ortho_t = normalize(tangent - tangent_projection);
+        bitangent = cross(ortho_n, ortho_t) * nt[3];
+    }
+    V3 viewDir, lightDir;
+    if (tse) {
+        viewDir = V3{dc.cam_obj[0], dc.cam_obj[1], dc.cam_obj[2]} - vpos;
+        lightDir = V3{dc.sun_obj[0], dc.sun_obj[1], dc.sun_obj[2]} - vpos;
+    } else {
+        const float* M = gd.transform;
+        float wp[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) wp[r] = M[0 * 4 + r] * vpos.x + M[1 * 4 + r] * vpos.y + M[2 * 4 + r] * vpos.z + M[3 * 4 + r] * 1.0f;
+        viewDir = V3{sd.camera_position[0] - wp[0], sd.camera_position[1] - wp[1], sd.camera_position[2] - wp[2]};
+        lightDir = V3{sd.sun_position[0] - wp[0], sd.sun_position[1] - wp[1], sd.sun_position[2] - wp[2]};
+        normal = normalize(mulm3v(gd.normal_transform, V3{v.normal[0], v.normal[1], v.normal[2]}));
+        tangent = normalize(mulm3v(gd.normal_transform, V3{nt[0], nt[1], nt[2]}));
+        tangent = normalize(tangent - normal * dot(normal, tangent));
+    }
+    if (sd.flip_lights[0] == 1) lightDir.x = lightDir.x * -1.0f;
+    if (sd.flip_lights[1] == 1) lightDir.y = lightDir.y * -1.0f;
+    if (sd.flip_lights[2] == 1) lightDir.z = lightDir.z * -1.0f;
+    o.normal = normal;
+    o.worldNormal = mulm3v(gd.normal_transform, V3{v.normal[0], v.normal[1], v.normal[2]});
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o.color[k] = v.color[k];
+    o.tangent = V3{nt[0], nt[1], nt[2]};
+    o.bitangent = bitangent;
+    o.viewDir = viewDir;
+    o.lightDir = lightDir;
+    o.sigma = nt[3];
+    o.uv[0] = v.uv[0];
+    o.uv[1] = v.uv[1];
+    const float* B = dc.csm;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        o.csm[r] = B[0 * 4 + r] * vpos.x + B[1 * 4 + r] * vpos.y + B[2 * 4 + r] * vpos.z + B[3 * 4 + r];
+}
+
+// Perspective-correct barycentrics at pixel centre (px, py), 2D homogeneous form.
+__device__ __forceinline__ void barycentrics(const float4& c0, const float4& c1, const float4& c2, int px, int py, int W,
+                                             int H, float b[3]) {
+    const float xn = (float)(2 * px + 1 - W) / (float)W;
+    const float yn = (float)(2 * py + 1 - H) / (float)H;
+    const V3 v0{c0.x, c0.y, c0.w}, v1{c1.x, c1.y, c1.w}, v2{c2.x, c2.y, c2.w};
+    const V3 p{xn, yn, 1.0f};
+    const float b0 = dot(cross(v1, v2), p), b1 = dot(cross(v2, v0), p), b2 = dot(cross(v0, v1), p);
+    const float s = b0 + b1 + b2;
+    b[0] = b0 / s;
+    b[1] = b1 / s;
+    b[2] = b2 / s;
+}
+
+struct Frag {
+    V3 normal, worldNormal, viewDir, lightDir, tangent, bitangent;
+    float color[4];
+    float uv[2];
+    float sigma;
+    float csm[4];
+    float duvdx[2], duvdy[2];
+};
+
+// ---------------------------------------------------------------------------
+// textures
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int wrap_coord(int i, int size, int mode) {
+    if (mode == 0) return min(max(i, 0), size - 1);
+    if (mode == 2) {
+        int m = i % size;
+        return m < 0 ? m + size : m;
+    }
+    int t = i % (2 * size);
+    if (t < 0) t += 2 * size;
+    int a = t - size;
+    a = a >= 0 ? a : -(1 + a);
+    return size - 1 - a;
+}
+
+struct Sampler {
+    const ShadeParams* P;
+    const float* srgb;  // shared-memory table
+
+    __device__ __forceinline__ void texel(const TexDesc& t, uint32_t off, int w, int i, int j, float out[4]) const {
+        const uint32_t v = __ldg(&P->texels[t.base + off + (uint32_t)j * (uint32_t)w + (uint32_t)i]);
+        const uint32_t r = v & 0xffu, g = (v >> 8) & 0xffu, b = (v >> 16) & 0xffu, a = v >> 24;
+        if (t.srgb) {
+            out[0] = srgb[r];
+            out[1] = srgb[g];
+            out[2] = srgb[b];
+        } else {
+            out[0] = (float)r / 255.0f;
+            out[1] = (float)g / 255.0f;
+            out[2] = (float)b / 255.0f;
+        }
+        out[3] = (float)a / 255.0f;
+    }
+
+    __device__ void sample_level(const TexDesc& t, int level, bool linear, SamplerBits st, float u, float v, float out[4]) const {
+        const int w = max(1, (int)(t.width >> level)), h = max(1, (int)(t.height >> level));
+        const uint32_t off = t.level_off[level];
+        const int wu = (st >> 4) & 3, wv = (st >> 6) & 3;
+        if (!linear) {
+            const int i = (int)floorf(u * (float)w), j = (int)floorf(v * (float)h);
+            texel(t, off, w, wrap_coord(i, w, wu), wrap_coord(j, h, wv), out);
+            return;
+        }
+        const float uu = u * (float)w - 0.5f, vv = v * (float)h - 0.5f;
+        const float fi = floorf(uu), fj = floorf(vv);
+        const float a = uu - fi, b = vv - fj;
+        const int i0 = (int)fi, j0 = (int)fj;
+        const int x0 = wrap_coord(i0, w, wu), x1 = wrap_coord(i0 + 1, w, wu);
+        const int y0 = wrap_coord(j0, h, wv), y1 = wrap_coord(j0 + 1, h, wv);
+        float t00[4], t10[4], t01[4], t11[4];
+        texel(t, off, w, x0, y0, t00);
+        texel(t, off, w, x1, y0, t10);
+        texel(t, off, w, x0, y1, t01);
+        texel(t, off, w, x1, y1, t11);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float top = t00[k] + a * (t10[k] - t00[k]);
+            const float bot = t01[k] + a * (t11[k] - t01[k]);
+            out[k] = top + b * (bot - top);
+        }
+    }
+
+    __device__ void sample(uint32_t tex_index, uint32_t sampler_index, const Frag& f, float out[4]) const {
+        if (tex_index >= P->texture_count) {
+            out[0] = out[1] = out[2] = out[3] = 0.0f;
+            return;
+        }
+        const TexDesc& t = P->textures[tex_index];
+        const SamplerBits st = P->samplers[min(sampler_index, P->sampler_count)];
+        const float w0 = (float)t.width, h0 = (float)t.height;
+        const float ax = f.duvdx[0] * w0, ay = f.duvdx[1] * h0, bx = f.duvdy[0] * w0, by = f.duvdy[1] * h0;
+        const float rx2 = ax * ax + ay * ay, ry2 = bx * bx + by * by;
+        const float rho2 = fmaxf(rx2, ry2);
+        const int q = (int)t.levels - 1;
+        if (!(rho2 > 1.0f)) {
+            sample_level(t, 0, (st & 2u) != 0, st, f.uv[0], f.uv[1], out);
+            return;
+        }
+        const bool min_linear = (st & 1u) != 0;
+        if (!(st & 4u)) {
+            int d = 0;
+            float thr = 2.0f;
+            while (d < q && rho2 > thr) {
+                ++d;
+                thr = thr * 4.0f;
+            }
+            sample_level(t, d, min_linear, st, f.uv[0], f.uv[1], out);
+            return;
+        }
+        const float lambda = 0.5f * log2f(rho2);
+        const float dp = fminf(lambda, (float)q);
+        const int dlo = (int)floorf(dp);
+        const int dhi = min(dlo + 1, q);
+        const float delta = dp - (float)dlo;
+        float a[4];
+        sample_level(t, dlo, min_linear, st, f.uv[0], f.uv[1], a);
+        if (delta > 0.0f && dhi != dlo) {
+            float b[4];
+            sample_level(t, dhi, min_linear, st, f.uv[0], f.uv[1], b);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) out[k] = a[k] + delta * (b[k] - a[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) out[k] = a[k];
+        }
+    }
+};
+
+// SampleCmpLevelZero, linear, clamp-to-edge, GREATER_OR_EQUAL (Graphics.cpp:2697-2725).
+__device__ __forceinline__ float sample_cmp(const float* __restrict__ shadow, int S, float u, float v, float dref) {
+    const float uu = u * (float)S - 0.5f, vv = v * (float)S - 0.5f;
+    const float fi = floorf(uu), fj = floorf(vv);
+    const float a = uu - fi, b = vv - fj;
+    const int i0 = (int)fmaxf(fminf(fi, (float)(S + 1)), -2.0f), j0 = (int)fmaxf(fminf(fj, (float)(S + 1)), -2.0f);
+    const int x0 = min(max(i0, 0), S - 1), x1 = min(max(i0 + 1, 0), S - 1);
+    const int y0 = min(max(j0, 0), S - 1), y1 = min(max(j0 + 1, 0), S - 1);
+    const float c00 = dref >= __ldg(&shadow[(size_t)y0 * S + x0]) ? 1.0f : 0.0f;
+    const float c10 = dref >= __ldg(&shadow[(size_t)y0 * S + x1]) ? 1.0f : 0.0f;
+    const float c01 = dref >= __ldg(&shadow[(size_t)y1 * S + x0]) ? 1.0f : 0.0f;
+    const float c11 = dref >= __ldg(&shadow[(size_t)y1 * S + x1]) ? 1.0f : 0.0f;
+    const float top = c00 + a * (c10 - c00);
+    const float bot = c01 + a * (c11 - c01);
+    return top + b * (bot - top);
+}
+
+// pcf.slang:1-11 (5 taps) and the 3x3 option.
+__device__ float pcf(const float* __restrict__ shadow, int S, const float csm[4], uint32_t mode) {
+    float result = 0.0f;
+    if (mode == RZ_PCF_3X3) {
+        const float o = 1.0f / (float)S;
+        for (int j = -1; j <= 1; ++j)
+            for (int i = -1; i <= 1; ++i)
+                result += sample_cmp(shadow, S, csm[0] + (float)i * o, csm[1] + (float)j * o, csm[2]);
+        return result * (1.0f / 9.0f);
+    }
+    const float o = 0.00025f;
+    result += sample_cmp(shadow, S, csm[0] - o, csm[1] - o, csm[2]);
+    result += sample_cmp(shadow, S, csm[0] + o * 2.0f, csm[1], csm[2]);
+    result += sample_cmp(shadow, S, csm[0], csm[1] + o * 2.0f, csm[2]);
+    result += sample_cmp(shadow, S, csm[0] + o * 2.0f, csm[1] + o * 2.0f, csm[2]);
+    result += sample_cmp(shadow, S, csm[0] - o * 2.0f, csm[1] - o * 2.0f, csm[2]);
+    return result * (1.0f / 5.0f);
+}
+
+// lighting.slang:5-43
+__device__ __forceinline__ V3 schlick_fresnel(float vDotH, V3 f0) {
+    const float p = powf(clamp01(1.0f - vDotH), 5.0f);
+    return {f0.x + (1.0f - f0.x) * p, f0.y + (1.0f - f0.y) * p, f0.z + (1.0f - f0.z) * p};
+}
+__device__ __forceinline__ float distribution_ggx(V3 N, V3 H, float roughness) {
+    const float PI = 3.14159265359f;
+    const float a = roughness * roughness;
+    const float a2 = a * a;
+    const float NdotH = fmaxf(dot(N, H), 0.0f);
+    const float NdotH2 = NdotH * NdotH;
+    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+    denom = PI * denom * denom;
+    return a2 / denom;
+}
+__device__ __forceinline__ float geometry_schlick_ggx(float NdotV, float roughness) {
+    const float r = roughness + 1.0f;
+    const float k = (r * r) / 8.0f;
+    return NdotV / (NdotV * (1.0f - k) + k);
+}
+__device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughness) {
+    const float NdotV = fmaxf(dot(N, V), 0.0f);
+    const float NdotL = fmaxf(dot(N, L), 0.0f);
+    return geometry_schlick_ggx(NdotL, roughness) * geometry_schlick_ggx(NdotV, roughness);
+}
+
+// fragmentMain, src/shaders/basic.slang:137-344. Returns false on discard.
+__device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, const GpuMaterial* md, const Frag& bv,
+                              const Sampler& smp, float out[4]) {
+    const V3 ambientLight{sd.ambient_color[0], sd.ambient_color[1], sd.ambient_color[2]};
+    float outFragColor[4] = {bv.color[0], bv.color[1], bv.color[2], bv.color[3]};
+    float imageTextureColor[4] = {outFragColor[0], outFragColor[1], outFragColor[2], outFragColor[3]};
+    float alpha = bv.color[3];
+    float sampledRoughness = 0.0f, sampledMetallic = 0.0f;
+    V3 lightNormal = normalize(bv.normal);
+    const V3 lightDir = normalize(bv.lightDir);
+    const V3 bitangent = bv.bitangent;
+    if (md) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) outFragColor[k] = md->color[k];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) imageTextureColor[k] = outFragColor[k];
+        alpha = fminf(md->color[3], alpha);
+        if (sd.normal_maps_enabled == 1 && md->tex[1] != RZ_INVALID_INDEX) {
+            float s[4];
+            smp.sample(md->tex[1], md->sampler[1], bv, s);
+            const V3 m{s[0] * 2.0f - 1.0f, s[1] * 2.0f - 1.0f, s[2] * 2.0f - 1.0f};
+            const V3 n = normalize(bv.normal);
+            const V3 t = normalize(bv.tangent - n * dot(bv.tangent, n));
+            const V3 b = normalize(cross(bv.normal, bv.tangent) * bv.sigma);
+            lightNormal = normalize(t * m.x + b * m.y + n * m.z);
+        }
+        if (md->tex[0] != RZ_INVALID_INDEX) {
+            smp.sample(md->tex[0], md->sampler[0], bv, imageTextureColor);
+            alpha = fminf(imageTextureColor[3], alpha);
+        }
+        float s[4];
+        if (md->tex[3] != RZ_INVALID_INDEX) smp.sample(md->tex[3], md->sampler[3], bv, s);
+        else smp.sample(md->tex[2], md->sampler[2], bv, s);
+        sampledRoughness = s[1];
+        sampledMetallic = s[2];
+    }
+    const V3 V = normalize(bv.viewDir);
+    const V3 L = lightDir;
+    const V3 N = lightNormal;
+    const V3 H = normalize(L + V);
+    const float cosTheta = clamp01(dot(L, N));
+    const float cosPhi = clamp01(dot(H, N));
+    const float lDotN = cosTheta;
+    const float lDotH = clamp01(dot(L, H));
+    const float nDotV = clamp01(dot(N, V));
+    V3 c3;
+    bool set = true;
+    switch (sd.fragment_output) {
+        case 0: c3 = V3{imageTextureColor[0], imageTextureColor[1], imageTextureColor[2]}; break;
+        case 1: c3 = normalize(bv.worldNormal) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 2: c3 = normalize(bv.tangent) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 3: c3 = normalize(bv.lightDir) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 4: c3 = normalize(bv.viewDir) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 5: c3 = V3{bv.color[0], bv.color[1], bv.color[2]}; break;
+        case 6: c3 = lightNormal * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 7: c3 = bitangent * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 8: c3 = V3{cosTheta, cosTheta, cosTheta} * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 9: c3 = V3{cosPhi, cosPhi, cosPhi} * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 10: c3 = V3{lDotH, lDotH, lDotH} * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 11: c3 = V3{nDotV, nDotV, nDotV} * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 12: c3 = V3{bv.uv[0], bv.uv[1], 0.0f}; break;
+        case 13: c3 = V3{sampledRoughness, 0.05f, 0.05f}; break;
+        case 14: c3 = V3{sampledMetallic, 0.05f, 0.05f}; break;
+        case 15: c3 = V3{1.0f - alpha, 0.05f, 0.05f}; break;
+        default: set = false; break;
+    }
+    if (set) {
+        outFragColor[0] = c3.x;
+        outFragColor[1] = c3.y;
+        outFragColor[2] = c3.z;
+        outFragColor[3] = alpha;
+    }
+    if (sd.light_enabled > 0) {
+        float shadowFactor = 1.0f;
+        if (sd.shadows_enabled == 1) shadowFactor = pcf(P.shadow, P.shadow_size, bv.csm, P.pcf_mode);
+        if (sd.brdf_lighting_enabled == 0) {
+            const float ml = fmaxf(cosTheta, 0.0f);
+            const V3 sunLight{sd.sunlight_color[0] * ml, sd.sunlight_color[1] * ml, sd.sunlight_color[2] * ml};
+            outFragColor[0] = outFragColor[0] * fmaxf(ambientLight.x, sunLight.x * shadowFactor);
+            outFragColor[1] = outFragColor[1] * fmaxf(ambientLight.y, sunLight.y * shadowFactor);
+            outFragColor[2] = outFragColor[2] * fmaxf(ambientLight.z, sunLight.z * shadowFactor);
+            outFragColor[3] = outFragColor[3] * alpha;
+        } else {
+            const float roughness = sampledRoughness;
+            const float metallic = sampledMetallic;
+            const float f04 = 0.04f;
+            const V3 f0{f04 * (1.0f - metallic) + outFragColor[0] * metallic, f04 * (1.0f - metallic) + outFragColor[1] * metallic,
+                        f04 * (1.0f - metallic) + outFragColor[2] * metallic};
+            const float ndf = distribution_ggx(N, H, roughness);
+            const float g = geometry_smith(N, V, L, roughness);
+            const V3 f = schlick_fresnel(fmaxf(dot(H, V), 0.0f), f0);
+            V3 kD{1.0f - f.x, 1.0f - f.y, 1.0f - f.z};
+            kD = kD * (1.0f - metallic);
+            const V3 numerator = f * (ndf * g);
+            const float denominator = 4.0f * nDotV * lDotN + 0.0001f;
+            const V3 specular{numerator.x / denominator, numerator.y / denominator, numerator.z / denominator};
+            const float pi = 3.14159265f;
+            const V3 diffuse{outFragColor[0] / pi, outFragColor[1] / pi, outFragColor[2] / pi};
+            const float li = sd.light_intensity;
+            const V3 sunLight{sd.sunlight_color[0] * li, sd.sunlight_color[1] * li, sd.sunlight_color[2] * li};
+            V3 brdf = mul3(mul3(kD, diffuse) + specular, sunLight) * lDotN;
+            brdf = V3{fmaxf(ambientLight.x * diffuse.x, brdf.x * shadowFactor), fmaxf(ambientLight.y * diffuse.y, brdf.y * shadowFactor),
+                      fmaxf(ambientLight.z * diffuse.z, brdf.z * shadowFactor)};
+            outFragColor[0] = brdf.x;
+            outFragColor[1] = brdf.y;
+            outFragColor[2] = brdf.z;
+            outFragColor[3] = alpha;
+        }
+    }
+    if (md) {
+        if (md->alpha_mode == 1 && alpha < md->alpha_cutoff) return false;
+        outFragColor[3] = alpha;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = outFragColor[k];
+    return true;
+}
+
+__device__ __forceinline__ uint32_t encode_srgb8(float c) {
+    if (!(c > 0.0f)) c = 0.0f;
+    if (c > 1.0f) c = 1.0f;
+    const float s = c <= 0.0031308f ? c * 12.92f : 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+    return (uint32_t)floorf(s * 255.0f + 0.5f);
+}
+__device__ __forceinline__ uint32_t encode_unorm8(float c) {
+    if (!(c > 0.0f)) c = 0.0f;
+    if (c > 1.0f) c = 1.0f;
+    return (uint32_t)floorf(c * 255.0f + 0.5f);
+}
+__device__ __forceinline__ float half_round(float x) { return __half2float(__float2half_rn(x)); }
+
+// Shade triangle `tri` (pass-global id) at pixel (px, py).
+__device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const Sampler& smp, uint32_t tri, int px, int py,
+                            float out[4]) {
+    const uint32_t d = find_draw(P.draws, P.draw_count, tri);
+    const DrawRec dr = P.draws[d];
+    const DrawConsts& dc = P.consts[d];
+    const rz_object& gd = P.objects[dr.object];
+    const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
+    const bool has_nm = md ? (md->tex[1] != RZ_INVALID_INDEX) : false;
+    const uint32_t t = tri - dr.tri_base;
+    uint32_t vi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) vi[k] = __ldg(&P.indices[dr.first_index + 3u * t + k]) + dr.vertex_base;
+    float4 clip[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const rz_vertex& v = P.vertices[vi[k]];
+        clip[k] = transform_point(dc.mvp, v.position[0], v.position[1], v.position[2]);
+    }
+    float b[3], bq0[3], bqx[3], bqy[3];
+    barycentrics(clip[0], clip[1], clip[2], px, py, P.width, P.height, b);
+    const int qx = px & ~1, qy = py & ~1;
+    barycentrics(clip[0], clip[1], clip[2], qx, qy, P.width, P.height, bq0);
+    barycentrics(clip[0], clip[1], clip[2], qx + 1, qy, P.width, P.height, bqx);
+    barycentrics(clip[0], clip[1], clip[2], qx, qy + 1, P.width, P.height, bqy);
+    Frag f;
+    float u0[2], ux[2], uy[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        VsOut o;
+        vertex_main(sd, gd, dc, md != nullptr, has_nm, P.vertices[vi[k]], o);
+        const float w = b[k];
+        if (k == 0) {
+            f.normal = o.normal * w;
+            f.worldNormal = o.worldNormal * w;
+            f.viewDir = o.viewDir * w;
+            f.lightDir = o.lightDir * w;
+            f.tangent = o.tangent * w;
+            f.bitangent = o.bitangent * w;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) f.color[i] = o.color[i] * w;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                f.uv[i] = o.uv[i] * w;
+                u0[i] = o.uv[i] * bq0[0];
+                ux[i] = o.uv[i] * bqx[0];
+                uy[i] = o.uv[i] * bqy[0];
+            }
+            f.sigma = o.sigma * w;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) f.csm[i] = o.csm[i] * w;
+        } else {
+            f.normal = f.normal + o.normal * w;
+            f.worldNormal = f.worldNormal + o.worldNormal * w;
+            f.viewDir = f.viewDir + o.viewDir * w;
+            f.lightDir = f.lightDir + o.lightDir * w;
+            f.tangent = f.tangent + o.tangent * w;
+            f.bitangent = f.bitangent + o.bitangent * w;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) f.color[i] = f.color[i] + o.color[i] * w;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                f.uv[i] = f.uv[i] + o.uv[i] * w;
+                u0[i] = u0[i] + o.uv[i] * bq0[k];
+                ux[i] = ux[i] + o.uv[i] * bqx[k];
+                uy[i] = uy[i] + o.uv[i] * bqy[k];
+            }
+            f.sigma = f.sigma + o.sigma * w;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) f.csm[i] = f.csm[i] + o.csm[i] * w;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        f.duvdx[i] = ux[i] - u0[i];
+        f.duvdy[i] = uy[i] - u0[i];
+    }
+    return fragment_main(P, sd, md, f, smp, out);
+}
+
+__global__ void __launch_bounds__(256) k_shade(ShadeParams P) {
+    __shared__ float s_srgb[256];
+    s_srgb[threadIdx.y * blockDim.x + threadIdx.x] = P.srgb_table[threadIdx.y * blockDim.x + threadIdx.x];
+    __syncthreads();
+    const int px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= P.width || py >= P.height) return;
+    const size_t p = (size_t)py * P.width + px;
+    const unsigned long long key = P.vis[p];
+    const uint32_t id = (uint32_t)key;
+    float col[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // clear colour, src/Engine/Graphics.cpp:5416-5419
+    if (id != 0) {
+        const Sampler smp{&P, s_srgb};
+        float o[4];
+        if (shade_pixel(P, *P.scene, smp, id - 1u, px, py, o)) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) col[k] = o[k];
+        }
+    }
+    const uint32_t r = encode_srgb8(half_round(col[0]));
+    const uint32_t g = encode_srgb8(half_round(col[1]));
+    const uint32_t b = encode_srgb8(half_round(col[2]));
+    const uint32_t a = encode_unorm8(half_round(col[3]));
+    P.color[p] = r | (g << 8) | (b << 16) | (a << 24);
+    P.depth[p] = __uint_as_float((uint32_t)(key >> 32));
+}
+
+void launch_shade(const ShadeParams& p, cudaStream_t stream) {
+    const dim3 block(16, 16);
+    const dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
+    k_shade<<<grid, block, 0, stream>>>(p);
+}
+
+}  // namespace rz

@@ -1,0 +1,181 @@
+"""Python host mirror of Rosy's renderer interface over the C ABI.
+
+``Graphics`` follows ``rosy::graphics`` (src/Engine/Graphics.h:11-21):
+init / update / render / resize / deinit, every call returning or raising on a
+``rosy::result`` code, plus the inner seams the engine drives through
+``graphics::update`` (set_asset, set_graphic_objects, the mob transform update;
+src/Engine/Graphics.cpp:6172-6197). Rendering is headless: the frame stays in
+device memory, readable as device pointers or copied to host arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi, _lib
+from .scene import Scene
+
+
+class Graphics:
+    def __init__(self):
+        self._ctx = C.c_void_p()
+        self._lib = None
+        self._marshalled = None
+        self.viewport_width = 0
+        self.viewport_height = 0
+        self.shadow_size = 0
+
+    # -- rosy::graphics -----------------------------------------------------------
+    def init(self, width: int, height: int, shadow_size: int = 4096, device: int = 0) -> None:
+        """graphics::init: creates the context (stream + frame buffers) on `device`."""
+        self._lib = _lib.load()
+        cfg = _abi.RzConfig(width=width, height=height, shadow_map_size=shadow_size, samples=1, device=device)
+        rc = self._lib.rz_create(C.byref(self._ctx), C.byref(cfg))
+        if rc != 0:
+            raise _lib.RzError(rc, "rz_create")
+        self.viewport_width, self.viewport_height, self.shadow_size = width, height, shadow_size
+
+    def _check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            raise _lib.RzError(rc, what, self._lib.rz_last_error(self._ctx).decode(errors="replace"))
+
+    def set_asset(self, scene: Scene) -> None:
+        """graphics_device::set_asset: meshes, materials, textures, samplers."""
+        m = _abi.Marshalled(scene)
+        self._marshalled = m
+        self._check(self._lib.rz_set_asset(
+            self._ctx, C.cast(m.meshes, C.c_void_p), len(scene.meshes),
+            _abi.ptr(m.materials), len(m.materials),
+            C.cast(m.textures, C.c_void_p), m.n_textures,
+            _abi.ptr(m.samplers), len(m.samplers)), "rz_set_asset")
+
+    def set_graphic_objects(self, objects: np.ndarray, surfaces: np.ndarray) -> None:
+        """graphics_device::set_graphic_objects: transforms + surface list in scene order."""
+        objects = np.ascontiguousarray(objects, np.float32)
+        surfaces = np.ascontiguousarray(surfaces)
+        self._check(self._lib.rz_set_objects(self._ctx, _abi.ptr(objects), len(objects),
+                                             _abi.ptr(surfaces), len(surfaces)), "rz_set_objects")
+
+    def update_objects(self, offset: int, objects: np.ndarray) -> None:
+        """The go_update upload (mob transforms) of src/Engine/Graphics.cpp:5120-5138."""
+        objects = np.ascontiguousarray(objects, np.float32)
+        self._check(self._lib.rz_update_objects(self._ctx, offset, _abi.ptr(objects), len(objects)),
+                    "rz_update_objects")
+
+    def set_draw_config(self, draw_config: np.ndarray) -> None:
+        dc = np.ascontiguousarray(draw_config)
+        self._check(self._lib.rz_set_draw_config(self._ctx, _abi.ptr(dc)), "rz_set_draw_config")
+
+    def update(self, scene_data: np.ndarray) -> None:
+        """graphics::update: the scene constants (gpu_scene_data) of the next frame."""
+        sd = np.ascontiguousarray(scene_data)
+        assert sd.nbytes == 408
+        self._check(self._lib.rz_update(self._ctx, _abi.ptr(sd)), "rz_update")
+
+    def render(self) -> None:
+        """graphics::render: enqueue the frame on the context's stream."""
+        self._check(self._lib.rz_render(self._ctx), "rz_render")
+
+    def resize(self, width: int, height: int) -> None:
+        self._check(self._lib.rz_resize(self._ctx, width, height), "rz_resize")
+        self.viewport_width, self.viewport_height = width, height
+
+    def deinit(self) -> None:
+        if self._lib is not None and self._ctx:
+            self._lib.rz_destroy(self._ctx)
+        self._ctx = C.c_void_p()
+
+    # -- headless outputs -------------------------------------------------------------
+    def sync(self, timeout_ms: int = 0) -> None:
+        self._check(self._lib.rz_sync(self._ctx, timeout_ms), "rz_sync")
+
+    def sync_code(self, timeout_ms: int = 0) -> int:
+        return int(self._lib.rz_sync(self._ctx, timeout_ms))
+
+    def frame(self) -> _abi.RzFrameOut:
+        out = _abi.RzFrameOut()
+        self._check(self._lib.rz_get_frame(self._ctx, C.byref(out)), "rz_get_frame")
+        return out
+
+    def read_frame(self, color: np.ndarray | None = None, depth: np.ndarray | None = None) -> None:
+        """Enqueues device-to-host copies into caller arrays (complete after sync())."""
+        cp = _abi.ptr(color) if color is not None else None
+        dp = _abi.ptr(depth) if depth is not None else None
+        self._check(self._lib.rz_read_frame(self._ctx, cp, color.nbytes if color is not None else 0,
+                                            dp, depth.nbytes if depth is not None else 0), "rz_read_frame")
+
+    def stats(self) -> _abi.RzStats:
+        s = _abi.RzStats()
+        self._check(self._lib.rz_get_stats(self._ctx, C.byref(s)), "rz_get_stats")
+        return s
+
+    STAGES = ("shadow_clear", "shadow_setup", "shadow_raster", "camera_clear", "camera_setup",
+              "camera_raster", "shade")
+
+    def set_stage_timing(self, enable: bool) -> None:
+        self._check(self._lib.rz_set_stage_timing(self._ctx, 1 if enable else 0), "rz_set_stage_timing")
+
+    def stage_times(self) -> dict:
+        """Milliseconds per stage of the last completed frame (stage timing must be on)."""
+        buf = (C.c_float * 16)()
+        n = C.c_uint32()
+        self._check(self._lib.rz_get_stage_times(self._ctx, buf, 16, C.byref(n)), "rz_get_stage_times")
+        return {self.STAGES[i]: float(buf[i]) for i in range(n.value)}
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.rz_get_stream(self._ctx) or 0)
+
+    def download(self) -> dict:
+        """Colour (H,W,4) u8, depth (H,W) f32, ids (H,W) u32 and shadow (S,S) f32 of the last frame."""
+        f = self.frame()
+        W, H, S = self.viewport_width, self.viewport_height, self.shadow_size
+        self.sync()
+        out = {
+            "vis": device_array(f.visibility_u64, (H, W), np.uint64),
+            "shadow": device_array(f.shadow_map_f32, (S, S), np.float32),
+        }
+        color = np.empty((H, W, 4), np.uint8)
+        depth = np.empty((H, W), np.float32)
+        self.read_frame(color, depth)
+        self.sync()
+        out["color"] = color
+        out["depth"] = depth
+        out["ids"] = (out["vis"] & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        out["vis_depth"] = (out["vis"] >> np.uint64(32)).astype(np.uint32).view(np.float32)
+        return out
+
+
+class _DeviceView:
+    def __init__(self, ptr: int, shape, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def device_array(ptr: int, shape, dtype) -> np.ndarray:
+    """Copies a device buffer of the renderer to a host numpy array (torch as plumbing)."""
+    import torch
+
+    dt = np.dtype(dtype)
+    if dt == np.uint64:  # torch has no uint64 copy path on every version: move raw int64
+        view = torch.as_tensor(_DeviceView(ptr, shape, "<i8"), device="cuda")
+        return view.cpu().numpy().view(np.uint64)
+    view = torch.as_tensor(_DeviceView(ptr, shape, dt.str), device="cuda")
+    return view.cpu().numpy()
+
+
+def render_scene(scene: Scene, device: int = 0) -> dict:
+    """Convenience: one frame of `scene` through the C ABI, downloaded to host arrays."""
+    g = Graphics()
+    g.init(scene.width, scene.height, scene.shadow_size, device)
+    try:
+        g.set_asset(scene)
+        g.set_graphic_objects(scene.objects, scene.surfaces)
+        g.set_draw_config(scene.draw_config)
+        g.update(scene.scene)
+        g.render()
+        g.sync()
+        return g.download()
+    finally:
+        g.deinit()

@@ -1,0 +1,73 @@
+"""CPU checks of the C ABI: the library builds, loads, and exports every symbol
+include/rosy_gb300.h declares; the ctypes mirror has the header's layouts."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from rosy_gb300 import _abi, _lib
+from rosy_gb300 import scene as sc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "rosy_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rz_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_the_bound_symbols():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(renderer_lib):
+    for name in declared_functions():
+        assert hasattr(renderer_lib, name), name
+    assert renderer_lib.rz_abi_version() == 1
+
+
+def test_record_layouts():
+    assert C.sizeof(_abi.RzVertex) == 64
+    assert sc.OBJECT_FLOATS * 4 == 164
+    assert sc.SCENE_DTYPE.itemsize == 408
+    assert sc.SURFACE_DTYPE.itemsize == 28
+    assert sc.SAMPLER_DTYPE.itemsize == 8
+    assert sc.DRAW_CONFIG_DTYPE.itemsize == 32
+    assert C.sizeof(_abi.RzConfig) == 32
+    assert C.sizeof(_abi.RzFrameOut) == 48
+    assert C.sizeof(_abi.RzStats) == 40
+
+
+def test_header_compiles_as_c_and_matches_sizes(tmp_path):
+    src = tmp_path / "sizes.c"
+    src.write_text(
+        '#include "rosy_gb300.h"\n#include <stdio.h>\n'
+        'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(rz_vertex), sizeof(rz_object),'
+        ' sizeof(rz_scene_data), sizeof(rz_surface), sizeof(rz_material), sizeof(rz_sampler),'
+        ' sizeof(rz_draw_config), sizeof(rz_texture), sizeof(rz_mesh)); return 0;}\n')
+    exe = tmp_path / "sizes"
+    import subprocess
+
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert [int(x) for x in got] == [64, 164, 408, 28, sc.MATERIAL_DTYPE.itemsize, 8, 32, 24, 24]
+
+
+def test_calls_without_a_context_are_rejected(renderer_lib):
+    P = C.c_void_p
+    assert renderer_lib.rz_render(None) == 3
+    assert renderer_lib.rz_sync(None, 0) == 3
+    out = C.c_void_p()
+    assert renderer_lib.rz_create(C.byref(out), None) == 3
+    renderer_lib.rz_destroy(None)
+
+
+def test_create_rejects_bad_config_without_touching_the_gpu(renderer_lib):
+    out = C.c_void_p()
+    cfg = _abi.RzConfig(width=0, height=10, shadow_map_size=16, samples=1, device=0)
+    assert renderer_lib.rz_create(C.byref(out), C.byref(cfg)) == 3
+    cfg = _abi.RzConfig(width=10, height=10, shadow_map_size=16, samples=3, device=0)
+    assert renderer_lib.rz_create(C.byref(out), C.byref(cfg)) == 3

@@ -1,0 +1,148 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bar: visibility (triangle id per pixel), depth and the shadow map are
+bit-exact; the RGBA8 sRGB colour is within 1/255 per channel.
+"""
+import numpy as np
+import pytest
+
+from kat_scenes import flat_scene, one_surface_per_triangle
+from rosy_gb300 import scene as sc
+from rosy_gb300.graphics import render_scene
+
+COLOR_TOL = 1  # 1/255 per channel
+
+
+def check_parity(s, ref, out, color_tol=COLOR_TOL):
+    assert np.array_equal(out["ids"], ref["ids"]), f"ids differ at {np.count_nonzero(out['ids'] != ref['ids'])} pixels"
+    assert np.array_equal(out["depth"].view(np.uint32), ref["depth"].view(np.uint32)), "depth differs"
+    assert np.array_equal(out["shadow"].view(np.uint32), ref["shadow"].view(np.uint32)), \
+        f"shadow map differs at {np.count_nonzero(out['shadow'] != ref['shadow'])} texels"
+    d = np.abs(out["color"].astype(np.int32) - ref["color"].astype(np.int32))
+    assert d.max() <= color_tol, f"colour differs by {d.max()} at {np.count_nonzero(d > color_tol)} channels"
+
+
+def run(s, oracle):
+    ref = oracle.render(s)
+    out = render_scene(s)
+    return ref, out
+
+
+def variants():
+    v = {}
+    v["tiny_s0"] = lambda: sc.tiny(0)
+    v["tiny_s1"] = lambda: sc.tiny(1)
+    v["random_triangles_640x360"] = lambda: sc.random_triangles()
+    v["random_triangles_s7_odd_size"] = lambda: sc.random_triangles(seed=7, triangles=1000, width=333, height=217,
+                                                                    shadow_size=300, texture_size=128)
+
+    def inside():  # camera inside the cube: near-plane and guard-band clipping
+        s = sc.random_triangles(seed=3, triangles=2000, width=320, height=200, shadow_size=256, texture_size=64)
+        view = sc.camera_look_at_origin((0.2, 0.1, 0.3))
+        proj = sc.projection(320 / 200, np.radians(90.0))
+        s.scene = sc.scene_record(view, proj, s.scene["sun_position"][0], np.eye(4), (0.2, 0.1, 0.3), 320, 200)
+        s.scene["shadow_projection_near"] = s.cameras[0]["shadow_projection_near"]
+        return s
+    v["camera_inside_clipping"] = inside
+
+    def nocull():
+        s = sc.random_triangles(seed=4, triangles=800, width=256, height=256, shadow_size=256, texture_size=64)
+        s.draw_config["cull_enabled"] = 0
+        return s
+    v["cull_disabled"] = nocull
+
+    def reverse():
+        s = sc.random_triangles(seed=5, triangles=800, width=256, height=144, shadow_size=256, texture_size=64)
+        s.draw_config["reverse_winding_order_enabled"] = 1
+        return s
+    v["reverse_winding"] = reverse
+
+    def pcf3():
+        s = sc.random_triangles(seed=6, triangles=800, width=256, height=144, shadow_size=512, texture_size=64,
+                                pcf_mode=sc.PCF_3X3)
+        return s
+    v["pcf_3x3"] = pcf3
+
+    def nobias():
+        s = sc.random_triangles(seed=8, triangles=800, width=256, height=144, shadow_size=512, texture_size=64)
+        s.draw_config["depth_bias_enabled"] = 0
+        return s
+    v["bias_disabled"] = nobias
+
+    def lambert():
+        s = sc.random_triangles(seed=9, triangles=800, width=256, height=144, shadow_size=512, texture_size=64)
+        s.scene["brdf_lighting_enabled"] = 0
+        return s
+    v["lambert"] = lambert
+
+    def small_scene():
+        return sc.scene_scale(seed=1, meshes=8, triangles_per_mesh=512, materials=4, texture_size=64, width=320,
+                              height=180, shadow_size=512, frames=2)
+    v["scene_scale_small"] = small_scene
+
+    def world_space():
+        s = sc.scene_scale(seed=2, meshes=6, triangles_per_mesh=512, materials=3, texture_size=64, width=320,
+                           height=180, shadow_size=512, frames=2)
+        s.scene["tangent_space_enabled"] = 0
+        s.scene["ensure_orthogonal_bitangent"] = 1
+        s.scene["flip_tangents"] = (1, 0, 1, 0)
+        s.scene["flip_lights"] = (0, 1, 0, 1)
+        return s
+    v["world_space_flips"] = world_space
+    return v
+
+
+VARIANTS = variants()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(VARIANTS))
+def test_parity(gpu, oracle, name):
+    s = VARIANTS[name]()
+    ref, out = run(s, oracle)
+    assert (ref["ids"] > 0).any()
+    check_parity(s, ref, out)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", list(range(16)))
+def test_fragment_output_modes(gpu, oracle, mode):
+    s = sc.scene_scale(seed=3, meshes=4, triangles_per_mesh=512, materials=2, texture_size=32, width=160,
+                       height=96, shadow_size=256, frames=1)
+    s.scene["fragment_output"] = mode
+    ref, out = run(s, oracle)
+    check_parity(s, ref, out)
+
+
+@pytest.mark.gpu
+def test_kat_scenes_on_gpu(gpu, oracle):
+    a, b, c, d = (1.5, 1.5, 0.5), (5.5, 1.5, 0.5), (5.5, 5.5, 0.5), (1.5, 5.5, 0.5)
+    t = ((0.0, 0.0, 0.4), (8.0, 0.0, 0.4), (0.0, 8.0, 0.4))
+    for s in (flat_scene([(a, b, c), (a, c, d)]), one_surface_per_triangle(flat_scene([t, t, t])),
+              flat_scene([((0.0, 0.0, 1.5), (8.0, 0.0, 0.5), (0.0, 8.0, 0.5))])):
+        ref, out = run(s, oracle)
+        check_parity(s, ref, out)
+
+
+@pytest.mark.gpu
+def test_frames_along_spline_reuse_context(gpu, oracle):
+    """One context, several frames with new scene constants (graph replay)."""
+    from rosy_gb300.graphics import Graphics
+
+    s = sc.scene_scale(seed=4, meshes=8, triangles_per_mesh=512, materials=4, texture_size=64, width=320,
+                       height=180, shadow_size=512, frames=4)
+    g = Graphics()
+    g.init(s.width, s.height, s.shadow_size)
+    try:
+        g.set_asset(s)
+        g.set_graphic_objects(s.objects, s.surfaces)
+        g.set_draw_config(s.draw_config)
+        for i in range(4):
+            si = s.with_camera(i)
+            g.update(si.scene)
+            g.render()
+            g.sync()
+            out = g.download()
+            check_parity(si, oracle.render(si), out)
+    finally:
+        g.deinit()
