@@ -260,6 +260,8 @@ def run_rz(args):
             stage_acc[k] = stage_acc.get(k, 0.0) + v
     stage_ms = {k: v / n_stage for k, v in stage_acc.items()}
     g.set_stage_timing(False)
+    g.render()  # back to the graph path
+    g.sync()
     stats = g.stats()
 
     # --- e2e through the C ABI with host buffers ---

@@ -209,7 +209,11 @@ typedef struct rz_config {
     uint32_t shadow_map_size;  /* square D32 shadow map (the reference uses 4096, Graphics.cpp:2524) */
     uint32_t samples;          /* rasterisation samples per pixel: 1 */
     int32_t device;            /* CUDA device ordinal */
-    uint32_t reserved[3];
+    uint32_t queue_chunks;     /* raster work-queue depth per pass, in chunks of 16
+                                  8x4-pixel stamps; 0 = sized from the scene. A frame
+                                  that needs more reports RZ_OVERFLOW and the queue
+                                  grows for the next frame. */
+    uint32_t reserved[2];
 } rz_config;
 
 /* Device pointers of the last rendered frame. colour: RGBA8, sRGB-encoded RGB

@@ -25,7 +25,8 @@ class RzTexture(C.Structure):
 
 class RzConfig(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("shadow_map_size", C.c_uint32),
-                ("samples", C.c_uint32), ("device", C.c_int32), ("reserved", C.c_uint32 * 3)]
+                ("samples", C.c_uint32), ("device", C.c_int32), ("queue_chunks", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class RzFrameOut(C.Structure):

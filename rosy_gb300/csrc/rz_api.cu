@@ -54,6 +54,7 @@ struct rz_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     uint32_t width = 0, height = 0, shadow_size = 0;
+    uint32_t queue_chunks = 0;  // fixed work-queue depth (0 = sized from the scene)
     std::string last_error;
 
     // frame buffers
@@ -169,6 +170,7 @@ int size_pass(rz_ctx* c, PassBuffers& p, uint32_t tris, uint64_t stamps_hint) {
     const uint32_t rec_cap = tris + tris / 4 + 4096;
     const uint32_t tiles = (uint32_t)setup_ctas(tris) + 1;
     uint64_t chunks = (stamps_hint + kChunkStamps - 1) / kChunkStamps + 1024;
+    if (c->queue_chunks) chunks = c->queue_chunks;
     if (chunks > 0xFFFFFFFFull) chunks = 0xFFFFFFFFull;
     if (rec_cap > p.record_capacity) {
         dfree(p.records);
@@ -188,10 +190,15 @@ int size_pass(rz_ctx* c, PassBuffers& p, uint32_t tris, uint64_t stamps_hint) {
     return RZ_OK;
 }
 
+// Stamps a pass may need: never more than every triangle covering the whole
+// target; otherwise room for 256 full-screen layers of overdraw plus 16 stamps
+// per triangle. A frame that needs more reports RZ_OVERFLOW and the capacity
+// grows for the next frame.
 uint64_t default_stamp_hint(uint32_t tris, uint32_t w, uint32_t h) {
     const uint64_t screen = ((uint64_t)w / kStampW + 1) * ((uint64_t)h / kStampH + 1);
-    uint64_t hint = (uint64_t)tris * 4 + screen * 8;
-    return hint;
+    const uint64_t bound = (uint64_t)tris * screen;
+    const uint64_t hint = screen * 256 + (uint64_t)tris * 16;
+    return bound < hint ? bound : hint;
 }
 
 SamplerBits sampler_bits(const rz_sampler& s) {
@@ -360,6 +367,7 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
     c->width = cfg->width;
     c->height = cfg->height;
     c->shadow_size = cfg->shadow_map_size;
+    c->queue_chunks = cfg->queue_chunks;
     auto bail = [&](int code) {
         rz_destroy(c);
         return code;
@@ -707,7 +715,8 @@ int rz_render(rz_ctx* c) {
         drop_graph(c);
         auto grow = [&](PassBuffers& p, uint32_t tris) -> int {
             if (c->grow_chunks) {
-                const uint64_t want = (uint64_t)p.chunk_capacity * 4;
+                c->queue_chunks = 0;
+                const uint64_t want = (uint64_t)p.chunk_capacity * 4 + 1024;
                 dfree(p.chunk_map);
                 p.chunk_capacity = 0;
                 RZ_CUDA(c, dalloc(&p.chunk_map, (size_t)want), "chunk map");
@@ -727,7 +736,8 @@ int rz_render(rz_ctx* c) {
         c->grow_records = c->grow_chunks = false;
         if (rc != RZ_OK) return rc;
     }
-    if (c->use_graph) {
+    // Stage timing records events between the stages and enqueues directly.
+    if (c->use_graph && !c->timing) {
         if (c->graph_dirty || !c->graph) {
             cudaGraph_t g = nullptr;
             RZ_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");

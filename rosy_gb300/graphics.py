@@ -27,10 +27,11 @@ class Graphics:
         self.shadow_size = 0
 
     # -- rosy::graphics -----------------------------------------------------------
-    def init(self, width: int, height: int, shadow_size: int = 4096, device: int = 0) -> None:
+    def init(self, width: int, height: int, shadow_size: int = 4096, device: int = 0, queue_chunks: int = 0) -> None:
         """graphics::init: creates the context (stream + frame buffers) on `device`."""
         self._lib = _lib.load()
-        cfg = _abi.RzConfig(width=width, height=height, shadow_map_size=shadow_size, samples=1, device=device)
+        cfg = _abi.RzConfig(width=width, height=height, shadow_map_size=shadow_size, samples=1, device=device,
+                            queue_chunks=queue_chunks)
         rc = self._lib.rz_create(C.byref(self._ctx), C.byref(cfg))
         if rc != 0:
             raise _lib.RzError(rc, "rz_create")
@@ -175,6 +176,8 @@ def render_scene(scene: Scene, device: int = 0) -> dict:
         g.set_draw_config(scene.draw_config)
         g.update(scene.scene)
         g.render()
+        if g.sync_code() == 14:  # RZ_OVERFLOW: the work queue grew; render the frame again
+            g.render()
         g.sync()
         return g.download()
     finally:

@@ -146,3 +146,16 @@ def test_frames_along_spline_reuse_context(gpu, oracle):
             check_parity(si, oracle.render(si), out)
     finally:
         g.deinit()
+
+
+@pytest.mark.gpu
+def test_parity_scene_scale_full_size(gpu, oracle):
+    """The bench workload itself (262,144 triangles, 1920x1080, 4096^2 shadow map,
+    32 materials x 3 textures of 1024^2): bit-exact visibility/depth/shadow, colour
+    within 1/255, on the first and a later spline frame."""
+    s = sc.scene_scale(seed=0)
+    for cam in (0, 5):
+        si = s.with_camera(cam)
+        ref, out = run(si, oracle)
+        assert (ref["ids"] > 0).mean() > 0.05
+        check_parity(si, ref, out)
