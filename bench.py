@@ -245,6 +245,11 @@ def run_rz(args):
     frame_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = max_over_ranks(sum(frame_ms), ws)
     value = ws * args.steps / (total_ms / 1e3)
+    if args.profile:  # short run for ncu: the timed frames only
+        g.deinit()
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "frames_per_s": round(value, 2)}))
+        return
 
     # --- per-stage times (same frames, stage events on) ---
     g.set_stage_timing(True)
@@ -291,6 +296,9 @@ def run_rz(args):
     extra = {}
     if rank == 0 and not args.no_cpu_baseline:
         cpu, extra = cpu_baseline(s, args.cpu_seconds)
+    g.update(cams[0])
+    g.render()
+    g.sync()
     out0 = g.download() if rank == 0 else None
     algo = {
         "shadow_raster": raster_bytes(s, "shadow"),
@@ -326,6 +334,8 @@ def run_rz(args):
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": 408 + int(s.objects.nbytes),
                     "d2h_bytes_per_step": int(s.width * s.height * 4), "steps": n_e2e},
             "gpu_launches": int(stats.kernel_launches) * args.steps,
+            "raster_work": {"shadow_records": int(stats.shadow_setup_records), "shadow_stamps": int(stats.shadow_stamps),
+                            "camera_records": int(stats.camera_setup_records), "camera_stamps": int(stats.camera_stamps)},
             "roofline": roof,
             "stage_ms": {k: round(v, 5) for k, v in stage_ms.items()},
             "mtriangles_per_s": round(value * s.triangle_count / 1e6, 1),
@@ -383,6 +393,7 @@ def main():
     ap.add_argument("--config", default="scene_scale", choices=["scene_scale", "random_triangles"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="timed frames only (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "rz":
         args.warmup = 3

@@ -99,6 +99,8 @@ struct rz_ctx {
     uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0;
     float* d_shadow_mvp = nullptr;
     DrawConsts* d_camera_consts = nullptr;
+    float4* d_varyings = nullptr;
+    uint32_t varying_count = 0;
     bool have_objects = false;
 
     // raster scratch
@@ -314,6 +316,8 @@ int enqueue_frame(rz_ctx* c) {
     sh.draws = c->d_opaque_draws;
     sh.draw_count = c->opaque_draw_count;
     sh.consts = c->d_camera_consts;
+    sh.varyings = c->d_varyings;
+    sh.varying_count = c->varying_count;
     sh.vertices = c->d_vertices;
     sh.indices = c->d_indices;
     sh.objects = c->d_objects;
@@ -326,6 +330,7 @@ int enqueue_frame(rz_ctx* c) {
     sh.scene = c->d_scene;
     sh.pcf_mode = c->draw_config.pcf_mode;
     sh.srgb_table = c->d_srgb;
+    launch_vertex(sh, s);
     launch_shade(sh, s);
     stamp(c, 7);
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
@@ -434,6 +439,7 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_opaque_draws);
     dfree(c->d_shadow_mvp);
     dfree(c->d_camera_consts);
+    dfree(c->d_varyings);
     if (c->h_scene) cudaFreeHost(c->h_scene);
     if (c->h_report) cudaFreeHost(c->h_report);
     if (c->h_objects) cudaFreeHost(c->h_objects);
@@ -603,7 +609,7 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     if (object_count == 0 || !objects || surface_count == 0 || !surfaces)
         return fail(c, RZ_INVALID_ARGUMENT, "empty scene");
     std::vector<DrawRec> shadow, opaque;
-    uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0, blended_draws = 0;
+    uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0, blended_draws = 0, varyings = 0;
     const uint32_t mesh_count = (uint32_t)(c->mesh_table.size() / 4);
     for (uint32_t i = 0; i < surface_count; ++i) {
         const rz_surface& s = surfaces[i];
@@ -631,6 +637,10 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
             ++blended_draws;
         } else {
             d.tri_base = opaque_tris;
+            d.varying_base = varyings;
+            d.vertex_count = mt[1];
+            if ((uint64_t)varyings + mt[1] >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many vertices");
+            varyings += mt[1];
             opaque.push_back(d);
             opaque_tris += d.tri_count;
         }
@@ -644,6 +654,7 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     dfree(c->d_opaque_draws);
     dfree(c->d_shadow_mvp);
     dfree(c->d_camera_consts);
+    dfree(c->d_varyings);
     if (c->h_objects) cudaFreeHost(c->h_objects);
     c->h_objects = nullptr;
     RZ_CUDA(c, dalloc(&c->d_objects, object_count), "object buffer");
@@ -652,6 +663,7 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     RZ_CUDA(c, dalloc(&c->d_opaque_draws, std::max<size_t>(opaque.size(), 1)), "opaque draw list");
     RZ_CUDA(c, dalloc(&c->d_shadow_mvp, std::max<size_t>(shadow.size(), 1) * 16), "shadow matrices");
     RZ_CUDA(c, dalloc(&c->d_camera_consts, std::max<size_t>(opaque.size(), 1)), "camera constants");
+    RZ_CUDA(c, dalloc(&c->d_varyings, std::max<size_t>(varyings, 1) * 8), "varying records");
     RZ_CUDA(c, cudaMemcpy(c->d_objects, objects, (size_t)object_count * sizeof(rz_object), cudaMemcpyHostToDevice), "upload objects");
     if (!shadow.empty())
         RZ_CUDA(c, cudaMemcpy(c->d_shadow_draws, shadow.data(), shadow.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
@@ -664,6 +676,7 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     c->shadow_tris = shadow_tris;
     c->opaque_tris = opaque_tris;
     c->blended_tris = blended_tris;
+    c->varying_count = varyings;
     int rc = size_pass(c, c->shadow_pass, shadow_tris, default_stamp_hint(shadow_tris, c->shadow_size, c->shadow_size));
     if (rc != RZ_OK) return rc;
     rc = size_pass(c, c->camera_pass, opaque_tris, default_stamp_hint(opaque_tris, c->width, c->height));
@@ -711,28 +724,32 @@ int rz_render(rz_ctx* c) {
     if (ready != RZ_OK) return ready;
     cudaSetDevice(c->device);
     if (c->grow_records || c->grow_chunks) {
+        // Size the queues from what the overflowing frame needed (exact counts
+        // from the device), with 25% headroom.
         cudaStreamSynchronize(c->stream);
         drop_graph(c);
-        auto grow = [&](PassBuffers& p, uint32_t tris) -> int {
-            if (c->grow_chunks) {
-                c->queue_chunks = 0;
-                const uint64_t want = (uint64_t)p.chunk_capacity * 4 + 1024;
+        c->queue_chunks = 0;
+        auto grow = [&](PassBuffers& p, const PassHeader& h) -> int {
+            const uint64_t want_chunks = (h.stamps + kChunkStamps - 1) / kChunkStamps;
+            const uint64_t want_recs = h.records_needed;
+            if (want_chunks > p.chunk_capacity) {
+                const uint64_t n = std::min<uint64_t>(want_chunks + want_chunks / 4 + 1024, 0xFFFFFFFFull);
                 dfree(p.chunk_map);
                 p.chunk_capacity = 0;
-                RZ_CUDA(c, dalloc(&p.chunk_map, (size_t)want), "chunk map");
-                p.chunk_capacity = (uint32_t)std::min<uint64_t>(want, 0xFFFFFFFFull);
+                RZ_CUDA(c, dalloc(&p.chunk_map, (size_t)n), "chunk map");
+                p.chunk_capacity = (uint32_t)n;
             }
-            if (c->grow_records) {
-                const uint64_t want = (uint64_t)p.record_capacity * 2 + tris;
+            if (want_recs > p.record_capacity) {
+                const uint64_t n = std::min<uint64_t>(want_recs + want_recs / 4 + 1024, 0xFFFFFFull);
                 dfree(p.records);
                 p.record_capacity = 0;
-                RZ_CUDA(c, dalloc(&p.records, (size_t)want), "raster records");
-                p.record_capacity = (uint32_t)std::min<uint64_t>(want, 0xFFFFFFull);
+                RZ_CUDA(c, dalloc(&p.records, (size_t)n), "raster records");
+                p.record_capacity = (uint32_t)n;
             }
             return RZ_OK;
         };
-        int rc = grow(c->shadow_pass, c->shadow_tris);
-        if (rc == RZ_OK) rc = grow(c->camera_pass, c->opaque_tris);
+        int rc = grow(c->shadow_pass, c->h_report->shadow);
+        if (rc == RZ_OK) rc = grow(c->camera_pass, c->h_report->camera);
         c->grow_records = c->grow_chunks = false;
         if (rc != RZ_OK) return rc;
     }
@@ -836,7 +853,7 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->shadow_stamps = c->h_report->shadow.stamps;
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->error_flags;
-    out->kernel_launches = (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u;
+    out->kernel_launches = (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u + (c->varying_count ? 1u : 0u);
     return RZ_OK;
 }
 

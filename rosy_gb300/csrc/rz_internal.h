@@ -17,7 +17,8 @@ struct DrawRec {
     uint32_t object;       // graphic_objects_offset + graphics_object_index
     int32_t material;      // -1 = none
     uint32_t tri_base;     // first triangle id of this draw within the pass
-    uint32_t pad[2];
+    uint32_t varying_base; // camera pass: first varying record of this draw (one per mesh vertex)
+    uint32_t vertex_count; // vertices of the draw's mesh
 };
 static_assert(sizeof(DrawRec) == 32, "DrawRec layout");
 
@@ -82,8 +83,9 @@ struct PassHeader {
     uint32_t ticket;          // CTA tile ticket of the setup kernel
     uint32_t records;         // records written
     uint64_t stamps;          // total stamps
-    uint32_t chunks;          // ceil(stamps / kChunkStamps)
-    uint32_t pad[3];
+    uint32_t chunks;          // ceil(stamps / kChunkStamps), clamped to the capacity
+    uint32_t records_needed;  // records the frame produced (may exceed the capacity)
+    uint32_t pad[2];
 };
 
 // Pass description handed to the setup/raster launchers.
@@ -121,6 +123,8 @@ struct ShadeParams {
     const DrawRec* draws;     // opaque list
     uint32_t draw_count;
     const DrawConsts* consts; // per opaque draw
+    float4* varyings;         // 8 float4 per (draw, mesh vertex), written by k_vertex
+    uint32_t varying_count;
     const rz_vertex* vertices;
     const uint32_t* indices;
     const rz_object* objects;
@@ -142,6 +146,7 @@ void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objec
                         DrawConsts* out, cudaStream_t stream);
 void launch_setup(const PassParams& p, cudaStream_t stream);
 void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream);
+void launch_vertex(const ShadeParams& p, cudaStream_t stream);
 void launch_shade(const ShadeParams& p, cudaStream_t stream);
 int setup_ctas(uint32_t tri_total);
 

@@ -198,28 +198,20 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
     float Mr[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) Mr[i] = __ldg(&M[i]);
-    CV poly[9];
+    CV v[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float4 p = __ldg(&P.pos[vi[k]]);
         const float4 c = transform_point(Mr, p.x, p.y, p.z);
-        poly[k] = CV{c.x, c.y, c.z, c.w};
+        v[k] = CV{c.x, c.y, c.z, c.w};
     }
-    const unsigned o0 = outcode(poly[0]), o1 = outcode(poly[1]), o2 = outcode(poly[2]);
+    const unsigned o0 = outcode(v[0]), o1 = outcode(v[1]), o2 = outcode(v[2]);
     if (o0 & o1 & o2) return;
-    int n = 3;
-    if (o0 | o1 | o2) {
-        n = clip_polygon(poly, o0 | o1 | o2);
-        if (n < 3) return;
-        for (int i = 0; i < n; ++i)
-            if (!(poly[i].w > 0.0f)) return;
-    } else {
-        if (!(poly[0].w > 0.0f) || !(poly[1].w > 0.0f) || !(poly[2].w > 0.0f)) return;
-    }
     const float hw = (float)P.width * 0.5f, hh = (float)P.height * 0.5f;
     const uint32_t id = P.write_id ? (tri + 1u) : 0u;
-    if (n == 3) {
-        const SV a = to_screen(poly[0], hw, hh), b = to_screen(poly[1], hw, hh), c = to_screen(poly[2], hw, hh);
+    if (!(o0 | o1 | o2)) {
+        if (!(v[0].w > 0.0f) || !(v[1].w > 0.0f) || !(v[2].w > 0.0f)) return;
+        const SV a = to_screen(v[0], hw, hh), b = to_screen(v[1], hw, hh), c = to_screen(v[2], hw, hh);
         const int64_t S = area2(a, b, c);
         if (S == 0) return;
         const bool front = P.ccw_front ? (S < 0) : (S > 0);
@@ -232,6 +224,15 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         }
         return;
     }
+    // rare path: clip against the planes the vertices violate, fan-triangulate
+    CV poly[9];
+    poly[0] = v[0];
+    poly[1] = v[1];
+    poly[2] = v[2];
+    const int n = clip_polygon(poly, o0 | o1 | o2);
+    if (n < 3) return;
+    for (int i = 0; i < n; ++i)
+        if (!(poly[i].w > 0.0f)) return;
     SV sv[9];
     for (int i = 0; i < n; ++i) sv[i] = to_screen(poly[i], hw, hh);
     int64_t S = 0;
@@ -240,13 +241,13 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
     const bool front = P.ccw_front ? (S < 0) : (S > 0);
     if (P.cull_front && front) return;
     for (int i = 1; i + 1 < n; ++i) {
-        const int64_t s = area2(sv[0], sv[i], sv[i + 1]);
-        if (s == 0 || ((s > 0) != (S > 0))) continue;
+        const int64_t si = area2(sv[0], sv[i], sv[i + 1]);
+        if (si == 0 || ((si > 0) != (S > 0))) continue;
         TriRecord r;
-        if (s > 0) {
-            if (make_record(sv[0], sv[i], sv[i + 1], s, P, id, r)) emit(r);
+        if (si > 0) {
+            if (make_record(sv[0], sv[i], sv[i + 1], si, P, id, r)) emit(r);
         } else {
-            if (make_record(sv[0], sv[i + 1], sv[i], -s, P, id, r)) emit(r);
+            if (make_record(sv[0], sv[i + 1], sv[i], -si, P, id, r)) emit(r);
         }
     }
 }
@@ -254,7 +255,9 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
 struct CountEmit {
     uint32_t recs = 0;
     uint64_t stamps = 0;
+    TriRecord first;  // kept for the common case of a single record
     __device__ void operator()(const TriRecord& r) {
+        if (recs == 0) first = r;
         ++recs;
         stamps += r.stamps;
     }
@@ -335,53 +338,74 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     }
     const uint64_t excl = warp_prefix + incl - mine;
 
-    // Decoupled look-back: publish this tile's aggregate, accumulate predecessors.
-    if (threadIdx.x == 0) {
+    // Decoupled look-back (warp 0): publish this tile's aggregate, then sum the
+    // predecessors' values 32 at a time until an inclusive prefix is found.
+    if (warp == 0) {
         const uint64_t agg_recs = total >> kStampBits, agg_stamps = total & kStampMask;
         volatile unsigned long long* status = reinterpret_cast<volatile unsigned long long*>(P.tile_status);
         uint64_t pre_recs = 0, pre_stamps = 0;
         if (tile == 0) {
-            status[0] = kFlagIncl | to_status(agg_recs, agg_stamps);
+            if (lane == 0) status[0] = kFlagIncl | to_status(agg_recs, agg_stamps);
         } else {
-            status[tile] = kFlagAgg | to_status(agg_recs, agg_stamps);
-            int64_t p = (int64_t)tile - 1;
+            if (lane == 0) status[tile] = kFlagAgg | to_status(agg_recs, agg_stamps);
+            int64_t base = (int64_t)tile - 1;
             uint32_t spins = 0;
-            while (p >= 0) {
-                const uint64_t s = status[p];
-                const uint64_t flag = s & (3ull << 62);
-                if (flag == 0) {
+            for (;;) {
+                const int64_t p = base - lane;
+                const uint64_t sv = p >= 0 ? (uint64_t)status[p] : kFlagIncl;
+                const uint64_t flag = sv & (3ull << 62);
+                const unsigned incl = __ballot_sync(0xffffffffu, flag == kFlagIncl);
+                const unsigned zero = __ballot_sync(0xffffffffu, flag == 0);
+                const unsigned last = incl ? (unsigned)(__ffs(incl) - 1) : 31u;
+                const unsigned need = last == 31u ? 0xffffffffu : ((2u << last) - 1u);
+                if (zero & need) {
                     if (++spins > (1u << 22)) {
-                        atomicOr(P.error_flags, kErrLookbackTimeout);
+                        if (lane == 0) atomicOr(P.error_flags, kErrLookbackTimeout);
                         break;
                     }
                     __nanosleep(32);
                     continue;
                 }
-                pre_recs += (s >> kStatusStampBits) & kStatusRecMask;
-                pre_stamps += s & kStatusStampMask;
-                if (flag == kFlagIncl) break;
-                --p;
+                uint64_t rr = (unsigned)lane <= last ? (sv >> kStatusStampBits) & kStatusRecMask : 0;
+                uint64_t ss = (unsigned)lane <= last ? sv & kStatusStampMask : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    rr += __shfl_xor_sync(0xffffffffu, rr, o);
+                    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                }
+                pre_recs += rr;
+                pre_stamps += ss;
+                if (incl) break;
+                base -= 32;
             }
-            __threadfence();
-            status[tile] = kFlagIncl | to_status(pre_recs + agg_recs, pre_stamps + agg_stamps);
+            if (lane == 0) {
+                __threadfence();
+                status[tile] = kFlagIncl | to_status(pre_recs + agg_recs, pre_stamps + agg_stamps);
+            }
         }
-        if (pre_recs + agg_recs > kStatusRecMask || pre_stamps + agg_stamps > kStatusStampMask)
-            atomicOr(P.error_flags, kErrStampOverflow);
-        s_base_recs = pre_recs;
-        s_base_stamps = pre_stamps;
-        if (tile == gridDim.x - 1) {
-            const uint64_t st = pre_stamps + agg_stamps;
-            uint64_t chunks = (st + kChunkStamps - 1) / kChunkStamps;
-            if (chunks > P.chunk_capacity) chunks = P.chunk_capacity;
-            P.header->records = (uint32_t)((pre_recs + agg_recs) < (uint64_t)P.record_capacity ? (pre_recs + agg_recs) : (uint64_t)P.record_capacity);
-            P.header->stamps = st;
-            P.header->chunks = (uint32_t)chunks;
+        if (lane == 0) {
+            if (pre_recs + agg_recs > kStatusRecMask || pre_stamps + agg_stamps > kStatusStampMask)
+                atomicOr(P.error_flags, kErrStampOverflow);
+            s_base_recs = pre_recs;
+            s_base_stamps = pre_stamps;
+            if (tile == gridDim.x - 1) {
+                const uint64_t st = pre_stamps + agg_stamps;
+                uint64_t chunks = (st + kChunkStamps - 1) / kChunkStamps;
+                if (chunks > P.chunk_capacity) chunks = P.chunk_capacity;
+                P.header->records = (uint32_t)((pre_recs + agg_recs) < (uint64_t)P.record_capacity
+                                                   ? (pre_recs + agg_recs) : (uint64_t)P.record_capacity);
+                P.header->stamps = st;
+                P.header->chunks = (uint32_t)chunks;
+                const uint64_t need = pre_recs + agg_recs;
+                P.header->records_needed = need > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)need;
+            }
         }
     }
     __syncthreads();
     if (cnt.recs == 0) return;
     WriteEmit w{&P, (uint32_t)(s_base_recs + (excl >> kStampBits)), s_base_stamps + (excl & kStampMask)};
-    setup_triangle(P, tri, w);
+    if (cnt.recs == 1) w(cnt.first);
+    else setup_triangle(P, tri, w);
 }
 
 int setup_ctas(uint32_t tri_total) { return (int)((tri_total + kSetupThreads - 1) / kSetupThreads); }
@@ -396,8 +420,22 @@ void launch_setup(const PassParams& p, cudaStream_t stream) {
 // raster
 // ---------------------------------------------------------------------------
 
+// Edge e (from vertex a to vertex b of the S>0-ordered triangle) at sample P:
+//   E = dx*(PY - ay) - dy*(PX - ax),   dx = bx - ax, dy = by - ay,
+// covered iff E > 0, or E == 0 on a top-left edge (dy < 0, or dy == 0 and dx > 0).
+// With the top-left decision folded into the constant (E' = E - 1 on the other
+// edges) the test is E' >= 0 for all three edges. Per record each lane keeps its
+// constant offset from the stamp origin; per stamp the origin value is two wide
+// multiply-adds, and a stamp whose best corner fails an edge is skipped whole.
+struct EdgeSetup {
+    int64_t c;        // E' at the sample (0, 0) minus nothing: E'(P) = c + dx*PY - dy*PX
+    int32_t dx, dy;
+    int64_t lane_off; // dx*(ly*256) - dy*(lx*256) for this lane's pixel in the stamp
+    int64_t max_off;  // largest lane_off over the stamp (trivial reject)
+};
+
 template <bool kWriteId>
-__global__ void __launch_bounds__(256) k_raster(PassParams P) {
+__global__ void __launch_bounds__(256, 4) k_raster(PassParams P) {
     const uint32_t chunks = P.header->chunks;
     const uint64_t total = P.header->stamps;
     const int lane = threadIdx.x & 31;
@@ -407,10 +445,8 @@ __global__ void __launch_bounds__(256) k_raster(PassParams P) {
         uint64_t s = (uint64_t)k * kChunkStamps;
         const uint64_t s_end = (s + kChunkStamps < total) ? (s + kChunkStamps) : total;
         uint32_t r = P.chunk_map[k];
-        // per-record state (warp-uniform)
-        uint64_t r_begin = 0, r_end = 0;
-        int32_t ex[3], ey[3], edx[3], edy[3];
-        bool tl[3];
+        uint64_t r_end = 0;
+        EdgeSetup e[3];
         int32_t X0 = 0, Y0 = 0;
         float z0 = 0.f, dzdx = 0.f, dzdy = 0.f, bias = 0.f;
         int px0 = 0, py0 = 0, px1 = 0, py1 = 0;
@@ -421,7 +457,7 @@ __global__ void __launch_bounds__(256) k_raster(PassParams P) {
                 if (loaded) ++r;
                 if (r >= P.record_capacity) break;
                 const int4* src = reinterpret_cast<const int4*>(P.records + r);
-                const int4 q0 = src[0], q1 = src[1], q2 = src[2], q3 = src[3];
+                const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
                 const int32_t X[3] = {q0.x, q0.z, q1.x}, Y[3] = {q0.y, q0.w, q1.y};
                 X0 = q0.x;
                 Y0 = q0.y;
@@ -435,17 +471,20 @@ __global__ void __launch_bounds__(256) k_raster(PassParams P) {
                 py1 = (uint32_t)q2.w >> 16;
                 id = (uint32_t)q3.x;
                 const uint32_t stamps = (uint32_t)q3.y;
-                r_begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
+                const uint64_t r_begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
                 r_end = r_begin + stamps;
                 nsx = (uint32_t)((px1 - px0) / kStampW + 1);
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
                     const int a = (i + 1) % 3, b = (i + 2) % 3;
-                    ex[i] = X[a];
-                    ey[i] = Y[a];
-                    edx[i] = X[b] - X[a];
-                    edy[i] = Y[b] - Y[a];
-                    tl[i] = edy[i] < 0 || (edy[i] == 0 && edx[i] > 0);
+                    const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+                    const bool tl = dy < 0 || (dy == 0 && dx > 0);
+                    e[i].dx = dx;
+                    e[i].dy = dy;
+                    e[i].c = (int64_t)dy * X[a] - (int64_t)dx * Y[a] - (tl ? 0 : 1);
+                    e[i].lane_off = (int64_t)dx * (ly * 256) - (int64_t)dy * (lx * 256);
+                    e[i].max_off = (dx > 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) +
+                                   (dy < 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
                 }
                 loaded = true;
                 if (s < r_begin) {  // cannot happen with a consistent chunk map
@@ -456,17 +495,21 @@ __global__ void __launch_bounds__(256) k_raster(PassParams P) {
                 sy = i / nsx;
                 sx = i - sy * nsx;
             }
-            const int px = px0 + (int)sx * kStampW + lx;
-            const int py = py0 + (int)sy * kStampH + ly;
-            if (px <= px1 && py <= py1) {
-                const int32_t PX = px * 256 + 128, PY = py * 256 + 128;
-                bool in = true;
+            const int sx0 = px0 + (int)sx * kStampW, sy0 = py0 + (int)sy * kStampH;
+            const int32_t PXo = sx0 * 256 + 128, PYo = sy0 * 256 + 128;
+            int64_t eo[3];
+            bool any_out = false;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const int64_t E = (int64_t)edx[i] * (int64_t)(PY - ey[i]) - (int64_t)edy[i] * (int64_t)(PX - ex[i]);
-                    in = in && (E > 0 || (E == 0 && tl[i]));
-                }
-                if (in) {
+            for (int i = 0; i < 3; ++i) {
+                eo[i] = e[i].c + (int64_t)e[i].dx * PYo - (int64_t)e[i].dy * PXo;
+                any_out |= (eo[i] + e[i].max_off) < 0;
+            }
+            if (!any_out) {
+                const int px = sx0 + lx, py = sy0 + ly;
+                const int64_t E0 = eo[0] + e[0].lane_off, E1 = eo[1] + e[1].lane_off, E2 = eo[2] + e[2].lane_off;
+                const bool in = ((int32_t)(E0 >> 32) | (int32_t)(E1 >> 32) | (int32_t)(E2 >> 32)) >= 0;
+                if (in && px <= px1 && py <= py1) {
+                    const int32_t PX = px * 256 + 128, PY = py * 256 + 128;
                     float z = fmaf(dzdx, (float)(PX - X0), fmaf(dzdy, (float)(PY - Y0), z0));
                     if (!kWriteId) z = z + bias;
                     if (!(z > 0.0f)) z = 0.0f;

@@ -6,10 +6,11 @@
 // that won the depth test, then the RGBA16F draw image (Graphics.cpp:1905-1908)
 // and the blit to the sRGB swapchain (5845-5879).
 //
-// Instead of interpolating rasterised varyings, each pixel re-fetches the three
-// vertices of its triangle (64-byte records, vertex pulling as the reference
-// does through buffer device addresses), runs the vertex-stage math on them,
-// and interpolates with perspective-correct barycentrics computed from the
+// The vertex stage runs once per (draw, mesh vertex) in k_vertex, pulling the
+// 64-byte vertex records as the reference does through buffer device addresses,
+// and writes a 128-byte varying record. k_shade then shades each pixel once for
+// the triangle that won its depth test: it gathers the three varying records
+// and interpolates them with perspective-correct barycentrics computed from the
 // clip positions in 2D homogeneous form. Texture level selection uses the
 // derivative of the interpolated uv across the pixel's 2x2 quad (the value at
 // the quad's top-left, right and lower neighbours, which is what a helper
@@ -191,6 +192,7 @@ struct Frag {
 
 __device__ __forceinline__ int wrap_coord(int i, int size, int mode) {
     if (mode == 0) return min(max(i, 0), size - 1);
+    if (mode == 2 && (size & (size - 1)) == 0) return i & (size - 1);  // == i mod size for powers of two
     if (mode == 2) {
         int m = i % size;
         return m < 0 ? m + size : m;
@@ -204,7 +206,8 @@ __device__ __forceinline__ int wrap_coord(int i, int size, int mode) {
 
 struct Sampler {
     const ShadeParams* P;
-    const float* srgb;  // shared-memory table
+    const float* srgb;   // shared-memory table: sRGB byte -> linear
+    const float* unorm;  // shared-memory table: byte -> byte / 255
 
     __device__ __forceinline__ void texel(const TexDesc& t, uint32_t off, int w, int i, int j, float out[4]) const {
         const uint32_t v = __ldg(&P->texels[t.base + off + (uint32_t)j * (uint32_t)w + (uint32_t)i]);
@@ -214,11 +217,11 @@ struct Sampler {
             out[1] = srgb[g];
             out[2] = srgb[b];
         } else {
-            out[0] = (float)r / 255.0f;
-            out[1] = (float)g / 255.0f;
-            out[2] = (float)b / 255.0f;
+            out[0] = unorm[r];
+            out[1] = unorm[g];
+            out[2] = unorm[b];
         }
-        out[3] = (float)a / 255.0f;
+        out[3] = unorm[a];
     }
 
     __device__ void sample_level(const TexDesc& t, int level, bool linear, SamplerBits st, float u, float v, float out[4]) const {
@@ -488,24 +491,69 @@ __device__ __forceinline__ uint32_t encode_unorm8(float c) {
 }
 __device__ __forceinline__ float half_round(float x) { return __half2float(__float2half_rn(x)); }
 
-// Shade triangle `tri` (pass-global id) at pixel (px, py).
-__device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const Sampler& smp, uint32_t tri, int px, int py,
-                            float out[4]) {
-    const uint32_t d = find_draw(P.draws, P.draw_count, tri);
+// Varying record of one (draw, vertex): the vertex-stage outputs the fragment
+// stage reads plus the clip position, 32 floats:
+//   0-2 normal, 3-5 viewDir, 6-8 lightDir, 9-11 tangent, 12 sigma, 13-16 color,
+//   17-18 uv, 19-22 csm.near, 23-25 worldNormal, 26-28 bitangent, 29-31 clip x, y, w.
+constexpr int kVaryingF4 = 8;
+
+__device__ __forceinline__ uint32_t find_draw_by_varying(const DrawRec* __restrict__ draws, uint32_t n, uint32_t i) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&draws[mid].varying_base) <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The vertex stage, once per (draw, mesh vertex).
+__global__ void __launch_bounds__(256) k_vertex(ShadeParams P) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.varying_count) return;
+    const uint32_t d = find_draw_by_varying(P.draws, P.draw_count, i);
     const DrawRec dr = P.draws[d];
     const DrawConsts& dc = P.consts[d];
     const rz_object& gd = P.objects[dr.object];
     const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
     const bool has_nm = md ? (md->tex[1] != RZ_INVALID_INDEX) : false;
+    const rz_vertex& v = P.vertices[dr.vertex_base + (i - dr.varying_base)];
+    VsOut o;
+    vertex_main(*P.scene, gd, dc, md != nullptr, has_nm, v, o);
+    const float4 clip = transform_point(dc.mvp, v.position[0], v.position[1], v.position[2]);
+    float4* dst = P.varyings + (size_t)i * kVaryingF4;
+    dst[0] = make_float4(o.normal.x, o.normal.y, o.normal.z, o.viewDir.x);
+    dst[1] = make_float4(o.viewDir.y, o.viewDir.z, o.lightDir.x, o.lightDir.y);
+    dst[2] = make_float4(o.lightDir.z, o.tangent.x, o.tangent.y, o.tangent.z);
+    dst[3] = make_float4(o.sigma, o.color[0], o.color[1], o.color[2]);
+    dst[4] = make_float4(o.color[3], o.uv[0], o.uv[1], o.csm[0]);
+    dst[5] = make_float4(o.csm[1], o.csm[2], o.csm[3], o.worldNormal.x);
+    dst[6] = make_float4(o.worldNormal.y, o.worldNormal.z, o.bitangent.x, o.bitangent.y);
+    dst[7] = make_float4(o.bitangent.z, clip.x, clip.y, clip.w);
+}
+
+void launch_vertex(const ShadeParams& p, cudaStream_t stream) {
+    if (p.varying_count == 0) return;
+    k_vertex<<<(p.varying_count + 255) / 256, 256, 0, stream>>>(p);
+}
+
+// Shade triangle `tri` (pass-global id) at pixel (px, py) from the varying
+// records of its three vertices.
+__device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const Sampler& smp, uint32_t tri, int px, int py,
+                            float out[4]) {
+    const uint32_t d = find_draw(P.draws, P.draw_count, tri);
+    const DrawRec dr = P.draws[d];
+    const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
     const uint32_t t = tri - dr.tri_base;
-    uint32_t vi[3];
+    const float4* rec[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) vi[k] = __ldg(&P.indices[dr.first_index + 3u * t + k]) + dr.vertex_base;
+    for (int k = 0; k < 3; ++k)
+        rec[k] = P.varyings + (size_t)(__ldg(&P.indices[dr.first_index + 3u * t + k]) + dr.varying_base) * kVaryingF4;
     float4 clip[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const rz_vertex& v = P.vertices[vi[k]];
-        clip[k] = transform_point(dc.mvp, v.position[0], v.position[1], v.position[2]);
+        const float4 q = __ldg(rec[k] + 7);
+        clip[k] = make_float4(q.y, q.z, 0.0f, q.w);
     }
     float b[3], bq0[3], bqx[3], bqy[3];
     barycentrics(clip[0], clip[1], clip[2], px, py, P.width, P.height, b);
@@ -513,51 +561,63 @@ __device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const
     barycentrics(clip[0], clip[1], clip[2], qx, qy, P.width, P.height, bq0);
     barycentrics(clip[0], clip[1], clip[2], qx + 1, qy, P.width, P.height, bqx);
     barycentrics(clip[0], clip[1], clip[2], qx, qy + 1, P.width, P.height, bqy);
+    const bool debug_extra = sd.fragment_output == 1 || sd.fragment_output == 7;
     Frag f;
     float u0[2], ux[2], uy[2];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        VsOut o;
-        vertex_main(sd, gd, dc, md != nullptr, has_nm, P.vertices[vi[k]], o);
+        const float4 a0 = __ldg(rec[k] + 0), a1 = __ldg(rec[k] + 1), a2 = __ldg(rec[k] + 2);
+        const float4 a3 = __ldg(rec[k] + 3), a4 = __ldg(rec[k] + 4), a5 = __ldg(rec[k] + 5);
+        float4 a6 = make_float4(0.f, 0.f, 0.f, 0.f), a7 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (debug_extra) {
+            a6 = __ldg(rec[k] + 6);
+            a7 = __ldg(rec[k] + 7);
+        }
+        const V3 normal{a0.x, a0.y, a0.z}, viewDir{a0.w, a1.x, a1.y}, lightDir{a1.z, a1.w, a2.x};
+        const V3 tangent{a2.y, a2.z, a2.w}, worldNormal{a5.w, a6.x, a6.y}, bitangent{a6.z, a6.w, a7.x};
+        const float sigma = a3.x;
+        const float color[4] = {a3.y, a3.z, a3.w, a4.x};
+        const float uv[2] = {a4.y, a4.z};
+        const float csm[4] = {a4.w, a5.x, a5.y, a5.z};
         const float w = b[k];
         if (k == 0) {
-            f.normal = o.normal * w;
-            f.worldNormal = o.worldNormal * w;
-            f.viewDir = o.viewDir * w;
-            f.lightDir = o.lightDir * w;
-            f.tangent = o.tangent * w;
-            f.bitangent = o.bitangent * w;
+            f.normal = normal * w;
+            f.worldNormal = worldNormal * w;
+            f.viewDir = viewDir * w;
+            f.lightDir = lightDir * w;
+            f.tangent = tangent * w;
+            f.bitangent = bitangent * w;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) f.color[i] = o.color[i] * w;
+            for (int i = 0; i < 4; ++i) f.color[i] = color[i] * w;
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                f.uv[i] = o.uv[i] * w;
-                u0[i] = o.uv[i] * bq0[0];
-                ux[i] = o.uv[i] * bqx[0];
-                uy[i] = o.uv[i] * bqy[0];
+                f.uv[i] = uv[i] * w;
+                u0[i] = uv[i] * bq0[0];
+                ux[i] = uv[i] * bqx[0];
+                uy[i] = uv[i] * bqy[0];
             }
-            f.sigma = o.sigma * w;
+            f.sigma = sigma * w;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) f.csm[i] = o.csm[i] * w;
+            for (int i = 0; i < 4; ++i) f.csm[i] = csm[i] * w;
         } else {
-            f.normal = f.normal + o.normal * w;
-            f.worldNormal = f.worldNormal + o.worldNormal * w;
-            f.viewDir = f.viewDir + o.viewDir * w;
-            f.lightDir = f.lightDir + o.lightDir * w;
-            f.tangent = f.tangent + o.tangent * w;
-            f.bitangent = f.bitangent + o.bitangent * w;
+            f.normal = f.normal + normal * w;
+            f.worldNormal = f.worldNormal + worldNormal * w;
+            f.viewDir = f.viewDir + viewDir * w;
+            f.lightDir = f.lightDir + lightDir * w;
+            f.tangent = f.tangent + tangent * w;
+            f.bitangent = f.bitangent + bitangent * w;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) f.color[i] = f.color[i] + o.color[i] * w;
+            for (int i = 0; i < 4; ++i) f.color[i] = f.color[i] + color[i] * w;
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                f.uv[i] = f.uv[i] + o.uv[i] * w;
-                u0[i] = u0[i] + o.uv[i] * bq0[k];
-                ux[i] = ux[i] + o.uv[i] * bqx[k];
-                uy[i] = uy[i] + o.uv[i] * bqy[k];
+                f.uv[i] = f.uv[i] + uv[i] * w;
+                u0[i] = u0[i] + uv[i] * bq0[k];
+                ux[i] = ux[i] + uv[i] * bqx[k];
+                uy[i] = uy[i] + uv[i] * bqy[k];
             }
-            f.sigma = f.sigma + o.sigma * w;
+            f.sigma = f.sigma + sigma * w;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) f.csm[i] = f.csm[i] + o.csm[i] * w;
+            for (int i = 0; i < 4; ++i) f.csm[i] = f.csm[i] + csm[i] * w;
         }
     }
 #pragma unroll
@@ -569,8 +629,12 @@ __device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const
 }
 
 __global__ void __launch_bounds__(256) k_shade(ShadeParams P) {
-    __shared__ float s_srgb[256];
-    s_srgb[threadIdx.y * blockDim.x + threadIdx.x] = P.srgb_table[threadIdx.y * blockDim.x + threadIdx.x];
+    __shared__ float s_srgb[256], s_unorm[256];
+    {
+        const int t = threadIdx.y * blockDim.x + threadIdx.x;
+        s_srgb[t] = P.srgb_table[t];
+        s_unorm[t] = (float)t / 255.0f;
+    }
     __syncthreads();
     const int px = blockIdx.x * blockDim.x + threadIdx.x;
     const int py = blockIdx.y * blockDim.y + threadIdx.y;
@@ -580,7 +644,7 @@ __global__ void __launch_bounds__(256) k_shade(ShadeParams P) {
     const uint32_t id = (uint32_t)key;
     float col[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // clear colour, src/Engine/Graphics.cpp:5416-5419
     if (id != 0) {
-        const Sampler smp{&P, s_srgb};
+        const Sampler smp{&P, s_srgb, s_unorm};
         float o[4];
         if (shade_pixel(P, *P.scene, smp, id - 1u, px, py, o)) {
 #pragma unroll
