@@ -325,6 +325,30 @@ int rz_set_stage_timing(struct rz_ctx* ctx, uint32_t enable);
  * rz_sync). Writes min(capacity, RZ_STAGE_COUNT) values and the count. */
 int rz_get_stage_times(struct rz_ctx* ctx, float* ms, uint32_t capacity, uint32_t* count);
 
+/* Shadow depth pass for callers that cannot allocate device memory while they
+ * run (engines that own every device allocation through their own allocator or
+ * a fixed budget, frame loops that must not call cudaMalloc/cudaFree). This entry
+ * point has no counterpart in the reference. It rasterises one draw into a D32
+ * depth target exactly as rz_render's shadow pass does (clear to 0, MVP =
+ * projection * world, clipping, culling, depth bias, GREATER_OR_EQUAL), using
+ * only a fixed scratch array compiled into the library (about 1.6 MiB per
+ * device, held until the process exits); it allocates nothing.
+ *   positions: device array of vertex_count float4 (x, y, z, unused)
+ *   indices:   device array of index_count u32 (a multiple of 3, at most
+ *              3 * 16384: larger draws return RZ_INVALID_ARGUMENT)
+ *   projection, world: host column-major 4x4 matrices
+ *   depth_out: device array of width * height floats, overwritten
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it.
+ * Returns RZ_OVERFLOW if the coverage needs more than the fixed work queue
+ * (65,536 chunks of 16 8x4-pixel stamps). Calls share the scratch array: calls
+ * that overlap on the GPU race and must be serialised by the caller. The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture starts on that device. */
+int rz_shadow_depth_static(const void* positions, uint32_t vertex_count, const uint32_t* indices,
+                           uint32_t index_count, const float projection[16], const float world[16],
+                           const rz_draw_config* cfg, uint32_t width, uint32_t height, float* depth_out,
+                           void* stream);
+
 /* The context's cudaStream_t, for callers that time or chain work on it. */
 void* rz_get_stream(struct rz_ctx* ctx);
 

@@ -25,7 +25,7 @@ EXPORTS = [
     "rz_create", "rz_destroy", "rz_resize", "rz_set_asset", "rz_set_objects", "rz_update_objects",
     "rz_set_draw_config", "rz_update", "rz_render", "rz_sync", "rz_get_frame", "rz_read_frame",
     "rz_get_stats", "rz_get_stream", "rz_last_error", "rz_abi_version", "rz_set_stage_timing",
-    "rz_get_stage_times",
+    "rz_get_stage_times", "rz_shadow_depth_static",
 ]
 
 _lib = None
@@ -71,6 +71,9 @@ def load(build_if_missing: bool = False):
     lib.rz_last_error.restype = C.c_char_p
     lib.rz_set_stage_timing.argtypes = [P, u32]
     lib.rz_get_stage_times.argtypes = [P, C.POINTER(C.c_float), u32, C.POINTER(u32)]
+    lib.rz_shadow_depth_static.argtypes = [P, u32, P, u32, C.POINTER(C.c_float), C.POINTER(C.c_float), P, u32, u32,
+                                           P, P]
+    lib.rz_shadow_depth_static.restype = C.c_int
     lib.rz_abi_version.argtypes = []
     lib.rz_abi_version.restype = u32
     for name in ("rz_create", "rz_resize", "rz_set_asset", "rz_set_objects", "rz_update_objects",
