@@ -331,7 +331,7 @@ int rz_get_stage_times(struct rz_ctx* ctx, float* ms, uint32_t capacity, uint32_
  * point has no counterpart in the reference. It rasterises one draw into a D32
  * depth target exactly as rz_render's shadow pass does (clear to 0, MVP =
  * projection * world, clipping, culling, depth bias, GREATER_OR_EQUAL), using
- * only a fixed scratch array compiled into the library (about 1.6 MiB per
+ * only a fixed scratch array compiled into the library (about 2.9 MiB per
  * device, held until the process exits); it allocates nothing.
  *   positions: device array of vertex_count float4 (x, y, z, unused)
  *   indices:   device array of index_count u32 (a multiple of 3, at most

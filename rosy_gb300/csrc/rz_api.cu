@@ -20,6 +20,8 @@ namespace {
 struct PassBuffers {
     TriRecord* records = nullptr;
     uint32_t record_capacity = 0;
+    TriRecord* small_records = nullptr;
+    uint32_t small_capacity = 0;
     uint64_t* tile_status = nullptr;
     uint32_t tile_capacity = 0;
     uint32_t* chunk_map = nullptr;
@@ -161,6 +163,8 @@ int alloc_frame_buffers(rz_ctx* c) {
 
 void free_pass(PassBuffers& p) {
     dfree(p.records);
+    dfree(p.small_records);
+    p.small_capacity = 0;
     dfree(p.tile_status);
     dfree(p.chunk_map);
     p.record_capacity = p.tile_capacity = p.chunk_capacity = 0;
@@ -178,6 +182,11 @@ int size_pass(rz_ctx* c, PassBuffers& p, uint32_t tris, uint64_t stamps_hint) {
         dfree(p.records);
         RZ_CUDA(c, dalloc(&p.records, rec_cap), "raster records");
         p.record_capacity = rec_cap;
+    }
+    if (rec_cap > p.small_capacity) {
+        dfree(p.small_records);
+        RZ_CUDA(c, dalloc(&p.small_records, rec_cap), "small raster records");
+        p.small_capacity = rec_cap;
     }
     if (tiles > p.tile_capacity) {
         dfree(p.tile_status);
@@ -234,6 +243,8 @@ PassParams pass_params(rz_ctx* c, bool camera) {
         p.write_id = 1;
         p.records = c->camera_pass.records;
         p.record_capacity = c->camera_pass.record_capacity;
+        p.small_records = c->camera_pass.small_records;
+        p.small_capacity = c->camera_pass.small_capacity;
         p.tile_status = c->camera_pass.tile_status;
         p.chunk_map = c->camera_pass.chunk_map;
         p.chunk_capacity = c->camera_pass.chunk_capacity;
@@ -254,6 +265,8 @@ PassParams pass_params(rz_ctx* c, bool camera) {
         p.write_id = 0;
         p.records = c->shadow_pass.records;
         p.record_capacity = c->shadow_pass.record_capacity;
+        p.small_records = c->shadow_pass.small_records;
+        p.small_capacity = c->shadow_pass.small_capacity;
         p.tile_status = c->shadow_pass.tile_status;
         p.chunk_map = c->shadow_pass.chunk_map;
         p.chunk_capacity = c->shadow_pass.chunk_capacity;
@@ -746,6 +759,13 @@ int rz_render(rz_ctx* c) {
                 RZ_CUDA(c, dalloc(&p.records, (size_t)n), "raster records");
                 p.record_capacity = (uint32_t)n;
             }
+            if (h.small_records > p.small_capacity) {
+                const uint64_t n = std::min<uint64_t>((uint64_t)h.small_records + h.small_records / 4 + 1024, 0xFFFFFFFFull);
+                dfree(p.small_records);
+                p.small_capacity = 0;
+                RZ_CUDA(c, dalloc(&p.small_records, (size_t)n), "small raster records");
+                p.small_capacity = (uint32_t)n;
+            }
             return RZ_OK;
         };
         int rc = grow(c->shadow_pass, c->h_report->shadow);
@@ -848,8 +868,8 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     std::memset(out, 0, sizeof(*out));
     out->draw_call_count = c->shadow_draw_count + c->opaque_draw_count + c->blended_draw_count;
     out->triangle_count = c->shadow_tris + c->opaque_tris + c->blended_tris;
-    out->shadow_setup_records = c->h_report->shadow.records;
-    out->camera_setup_records = c->h_report->camera.records;
+    out->shadow_setup_records = c->h_report->shadow.records + c->h_report->shadow.small_records;
+    out->camera_setup_records = c->h_report->camera.records + c->h_report->camera.small_records;
     out->shadow_stamps = c->h_report->shadow.stamps;
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->error_flags;

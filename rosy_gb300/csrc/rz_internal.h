@@ -81,12 +81,20 @@ constexpr uint32_t kErrBadIndex = 1u << 3;
 // Per-pass scratch header, cleared before each pass.
 struct PassHeader {
     uint32_t ticket;          // CTA tile ticket of the setup kernel
-    uint32_t records;         // records written
-    uint64_t stamps;          // total stamps
+    uint32_t records;         // large records written
+    uint64_t stamps;          // total stamps of the large records
     uint32_t chunks;          // ceil(stamps / kChunkStamps), clamped to the capacity
-    uint32_t records_needed;  // records the frame produced (may exceed the capacity)
-    uint32_t pad[2];
+    uint32_t records_needed;  // large records the frame produced (may exceed the capacity)
+    uint32_t small_records;   // small records appended (may exceed the capacity)
+    uint32_t small_cursor;    // raster: next small record to take
+    uint32_t chunk_cursor;    // raster: next chunk to take
+    uint32_t pad[3];
 };
+static_assert(sizeof(PassHeader) == 48, "PassHeader layout");
+
+// A record is "small" when the triangle's own extent (not its clamped bounding
+// box) is at most kSmallExtent pixels in x and y: one lane rasterises it.
+constexpr int kSmallExtent = 8;
 
 // Pass description handed to the setup/raster launchers.
 struct PassParams {
@@ -103,8 +111,10 @@ struct PassParams {
     int bias_enabled;
     float bias_constant, bias_clamp, bias_slope;
     int write_id;             // 1: camera pass (64-bit depth|id keys); 0: shadow (depth only)
-    TriRecord* records;
+    TriRecord* records;       // large records (stamp-balanced raster)
     uint32_t record_capacity;
+    TriRecord* small_records; // small records (one lane each)
+    uint32_t small_capacity;
     uint64_t* tile_status;    // one word per setup CTA
     uint32_t* chunk_map;
     uint32_t chunk_capacity;

@@ -133,15 +133,16 @@ __device__ __forceinline__ int64_t area2(const SV& a, const SV& b, const SV& c) 
     return (int64_t)(b.X - a.X) * (int64_t)(c.Y - a.Y) - (int64_t)(c.X - a.X) * (int64_t)(b.Y - a.Y);
 }
 
-// Builds the record of a triangle ordered with S > 0. Returns false if its
-// pixel bounding box is empty.
-__device__ __forceinline__ bool make_record(const SV& v0, const SV& v1, const SV& v2, int64_t S, const PassParams& P,
-                                            uint32_t id, TriRecord& r) {
+// Builds the record of a triangle ordered with S > 0. Returns 0 if its pixel
+// bounding box is empty, 2 for a small triangle (extent at most kSmallExtent
+// pixels each way, rasterised by one lane), 1 otherwise.
+__device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV& v2, int64_t S, const PassParams& P,
+                                           uint32_t id, TriRecord& r) {
     const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
     const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
     const int px0 = max((minX + 127) >> 8, 0), px1 = min((maxX - 128) >> 8, P.width - 1);
     const int py0 = max((minY + 127) >> 8, 0), py1 = min((maxY - 128) >> 8, P.height - 1);
-    if (px0 > px1 || py0 > py1) return false;
+    if (px0 > px1 || py0 > py1) return 0;
     const float fX1 = (float)(v1.X - v0.X), fY1 = (float)(v1.Y - v0.Y);
     const float fX2 = (float)(v2.X - v0.X), fY2 = (float)(v2.Y - v0.Y);
     const float fS = (float)S;
@@ -177,7 +178,8 @@ __device__ __forceinline__ bool make_record(const SV& v0, const SV& v1, const SV
     const uint32_t nsy = (uint32_t)((py1 - py0) / kStampH + 1);
     r.stamps = nsx * nsy;
     r.stamp_offset = 0;
-    return true;
+    const bool small = (maxX - minX) <= kSmallExtent * 256 && (maxY - minY) <= kSmallExtent * 256;
+    return small ? 2 : 1;
 }
 
 // Runs the fixed-function front end for one triangle and hands each record to `emit`.
@@ -217,11 +219,8 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         const bool front = P.ccw_front ? (S < 0) : (S > 0);
         if (P.cull_front && front) return;
         TriRecord r;
-        if (S > 0) {
-            if (make_record(a, b, c, S, P, id, r)) emit(r);
-        } else {
-            if (make_record(a, c, b, -S, P, id, r)) emit(r);
-        }
+        const int kind = S > 0 ? make_record(a, b, c, S, P, id, r) : make_record(a, c, b, -S, P, id, r);
+        if (kind) emit(r, kind == 2);
         return;
     }
     // rare path: clip against the planes the vertices violate, fan-triangulate
@@ -244,40 +243,61 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         const int64_t si = area2(sv[0], sv[i], sv[i + 1]);
         if (si == 0 || ((si > 0) != (S > 0))) continue;
         TriRecord r;
-        if (si > 0) {
-            if (make_record(sv[0], sv[i], sv[i + 1], si, P, id, r)) emit(r);
-        } else {
-            if (make_record(sv[0], sv[i + 1], sv[i], -si, P, id, r)) emit(r);
-        }
+        const int kind = si > 0 ? make_record(sv[0], sv[i], sv[i + 1], si, P, id, r)
+                                : make_record(sv[0], sv[i + 1], sv[i], -si, P, id, r);
+        if (kind) emit(r, kind == 2);
     }
 }
 
+__device__ __forceinline__ void store_record(TriRecord* dst, const TriRecord& r) {
+    const int4* s4 = reinterpret_cast<const int4*>(&r);
+    int4* d4 = reinterpret_cast<int4*>(dst);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d4[i] = s4[i];
+}
+
+// Phase A: count the records (small and large) a triangle produces.
 struct CountEmit {
-    uint32_t recs = 0;
-    uint64_t stamps = 0;
-    TriRecord first;  // kept for the common case of a single record
-    __device__ void operator()(const TriRecord& r) {
-        if (recs == 0) first = r;
+    uint32_t recs = 0;     // large
+    uint64_t stamps = 0;   // of the large ones
+    uint32_t small = 0;
+    TriRecord first;       // the first record, kept for the common case of exactly one
+    bool first_small = false;
+    __device__ void operator()(const TriRecord& r, bool is_small) {
+        if (recs + small == 0) {
+            first = r;
+            first_small = is_small;
+        }
+        if (is_small) {
+            ++small;
+            return;
+        }
         ++recs;
         stamps += r.stamps;
     }
 };
 
+// Phase B: large records at their compacted index with their stamp offsets,
+// small records at their slot in the small list (whose order does not matter:
+// the depth test is an atomic max).
 struct WriteEmit {
     const PassParams* P;
     uint32_t rec;
     uint64_t stamp;
-    __device__ void operator()(TriRecord& r) {
+    uint32_t small;
+    __device__ void operator()(TriRecord& r, bool is_small) {
+        if (is_small) {
+            if (small < P->small_capacity) store_record(P->small_records + small, r);
+            else atomicOr(P->error_flags, kErrRecordOverflow);
+            ++small;
+            return;
+        }
         if (rec >= P->record_capacity) {
             atomicOr(P->error_flags, kErrRecordOverflow);
             return;
         }
         r.stamp_offset = stamp;
-        TriRecord* dst = P->records + rec;
-        const int4* s4 = reinterpret_cast<const int4*>(&r);
-        int4* d4 = reinterpret_cast<int4*>(dst);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) d4[i] = s4[i];
+        store_record(P->records + rec, r);
         // chunks whose first stamp lies inside this record start here
         uint64_t k = (stamp + kChunkStamps - 1) / kChunkStamps;
         const uint64_t end = stamp + r.stamps;
@@ -311,6 +331,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     __shared__ uint32_t s_tile;
     __shared__ uint64_t s_warp[kSetupThreads / 32];
     __shared__ uint64_t s_base_recs, s_base_stamps;
+    __shared__ uint32_t s_small_warp[kSetupThreads / 32];
+    __shared__ uint32_t s_small_base;
     if (threadIdx.x == 0) s_tile = atomicAdd(&P.header->ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -328,7 +350,16 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
         const uint64_t v = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += v;
     }
-    if (lane == 31) s_warp[warp] = incl;
+    uint32_t small_incl = cnt.small;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, small_incl, o);
+        if (lane >= o) small_incl += v;
+    }
+    if (lane == 31) {
+        s_warp[warp] = incl;
+        s_small_warp[warp] = small_incl;
+    }
     __syncthreads();
     uint64_t warp_prefix = 0, total = 0;
 #pragma unroll
@@ -337,6 +368,14 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
         total += s_warp[w];
     }
     const uint64_t excl = warp_prefix + incl - mine;
+    uint32_t small_prefix = 0, small_total = 0;
+#pragma unroll
+    for (int w = 0; w < kSetupThreads / 32; ++w) {
+        if (w < warp) small_prefix += s_small_warp[w];
+        small_total += s_small_warp[w];
+    }
+    const uint32_t small_excl = small_prefix + small_incl - cnt.small;
+    if (threadIdx.x == 32) s_small_base = small_total ? atomicAdd(&P.header->small_records, small_total) : 0u;
 
     // Decoupled look-back (warp 0): publish this tile's aggregate, then sum the
     // predecessors' values 32 at a time until an inclusive prefix is found.
@@ -402,9 +441,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
         }
     }
     __syncthreads();
-    if (cnt.recs == 0) return;
-    WriteEmit w{&P, (uint32_t)(s_base_recs + (excl >> kStampBits)), s_base_stamps + (excl & kStampMask)};
-    if (cnt.recs == 1) w(cnt.first);
+    if (cnt.recs + cnt.small == 0) return;
+    WriteEmit w{&P, (uint32_t)(s_base_recs + (excl >> kStampBits)), s_base_stamps + (excl & kStampMask),
+                s_small_base + small_excl};
+    if (cnt.recs + cnt.small == 1) w(cnt.first, cnt.first_small);
     else setup_triangle(P, tri, w);
 }
 
@@ -424,116 +464,299 @@ void launch_setup(const PassParams& p, cudaStream_t stream) {
 //   E = dx*(PY - ay) - dy*(PX - ax),   dx = bx - ax, dy = by - ay,
 // covered iff E > 0, or E == 0 on a top-left edge (dy < 0, or dy == 0 and dx > 0).
 // With the top-left decision folded into the constant (E' = E - 1 on the other
-// edges) the test is E' >= 0 for all three edges. Per record each lane keeps its
-// constant offset from the stamp origin; per stamp the origin value is two wide
-// multiply-adds, and a stamp whose best corner fails an edge is skipped whole.
-struct EdgeSetup {
-    int64_t c;        // E' at the sample (0, 0) minus nothing: E'(P) = c + dx*PY - dy*PX
-    int32_t dx, dy;
-    int64_t lane_off; // dx*(ly*256) - dy*(lx*256) for this lane's pixel in the stamp
-    int64_t max_off;  // largest lane_off over the stamp (trivial reject)
-};
+// edges) the test is E' >= 0 on all three edges.
 
 template <bool kWriteId>
-__global__ void __launch_bounds__(256, 4) k_raster(PassParams P) {
-    const uint32_t chunks = P.header->chunks;
-    const uint64_t total = P.header->stamps;
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const int lx = lane & (kStampW - 1), ly = lane >> 3;
-    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < chunks; k += warps) {
-        uint64_t s = (uint64_t)k * kChunkStamps;
-        const uint64_t s_end = (s + kChunkStamps < total) ? (s + kChunkStamps) : total;
-        uint32_t r = P.chunk_map[k];
-        uint64_t r_end = 0;
-        EdgeSetup e[3];
-        int32_t X0 = 0, Y0 = 0;
-        float z0 = 0.f, dzdx = 0.f, dzdy = 0.f, bias = 0.f;
-        int px0 = 0, py0 = 0, px1 = 0, py1 = 0;
-        uint32_t nsx = 1, sx = 0, sy = 0, id = 0;
-        bool loaded = false;
-        while (s < s_end) {
-            if (!loaded || s >= r_end) {
-                if (loaded) ++r;
-                if (r >= P.record_capacity) break;
-                const int4* src = reinterpret_cast<const int4*>(P.records + r);
-                const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
-                const int32_t X[3] = {q0.x, q0.z, q1.x}, Y[3] = {q0.y, q0.w, q1.y};
-                X0 = q0.x;
-                Y0 = q0.y;
-                z0 = __int_as_float(q1.z);
-                dzdx = __int_as_float(q1.w);
-                dzdy = __int_as_float(q2.x);
-                bias = __int_as_float(q2.y);
-                px0 = q2.z & 0xffff;
-                py0 = (uint32_t)q2.z >> 16;
-                px1 = q2.w & 0xffff;
-                py1 = (uint32_t)q2.w >> 16;
-                id = (uint32_t)q3.x;
-                const uint32_t stamps = (uint32_t)q3.y;
-                const uint64_t r_begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
-                r_end = r_begin + stamps;
-                nsx = (uint32_t)((px1 - px0) / kStampW + 1);
+__device__ __forceinline__ void write_fragment(const PassParams& P, int px, int py, float z, uint32_t id) {
+    if (!(z > 0.0f)) z = 0.0f;
+    if (z > 1.0f) z = 1.0f;
+    const size_t p = (size_t)py * (size_t)P.width + (size_t)px;
+    if (kWriteId) {
+        const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
+        atomicMax(reinterpret_cast<unsigned long long*>(P.target) + p, key);
+    } else {
+        atomicMax(reinterpret_cast<unsigned int*>(P.target) + p, __float_as_uint(z));
+    }
+}
+
+// One lane rasterises one small triangle: its extent is at most kSmallExtent
+// pixels each way (2048 sub-pixels), so every edge value and product fits in 32 bits.
+template <bool kWriteId>
+__device__ __forceinline__ void raster_small(const PassParams& P, const TriRecord* rec) {
+    const int4* src = reinterpret_cast<const int4*>(rec);
+    const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
+    const int32_t X[3] = {q0.x, q0.z, q1.x}, Y[3] = {q0.y, q0.w, q1.y};
+    const float z0 = __int_as_float(q1.z), dzdx = __int_as_float(q1.w), dzdy = __int_as_float(q2.x);
+    const float bias = __int_as_float(q2.y);
+    const int px0 = q2.z & 0xffff, py0 = (uint32_t)q2.z >> 16, px1 = q2.w & 0xffff, py1 = (uint32_t)q2.w >> 16;
+    const uint32_t id = (uint32_t)q3.x;
+    // edge constants relative to vertex 0 (all values < 2^12 sub-pixels, products < 2^24)
+    int32_t dx[3], dy[3], c[3];
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const int a = (i + 1) % 3, b = (i + 2) % 3;
-                    const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
-                    const bool tl = dy < 0 || (dy == 0 && dx > 0);
-                    e[i].dx = dx;
-                    e[i].dy = dy;
-                    e[i].c = (int64_t)dy * X[a] - (int64_t)dx * Y[a] - (tl ? 0 : 1);
-                    e[i].lane_off = (int64_t)dx * (ly * 256) - (int64_t)dy * (lx * 256);
-                    e[i].max_off = (dx > 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) +
-                                   (dy < 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
-                }
-                loaded = true;
-                if (s < r_begin) {  // cannot happen with a consistent chunk map
-                    atomicOr(P.error_flags, kErrStampOverflow);
-                    break;
-                }
-                const uint32_t i = (uint32_t)(s - r_begin);
-                sy = i / nsx;
-                sx = i - sy * nsx;
-            }
-            const int sx0 = px0 + (int)sx * kStampW, sy0 = py0 + (int)sy * kStampH;
-            const int32_t PXo = sx0 * 256 + 128, PYo = sy0 * 256 + 128;
-            int64_t eo[3];
-            bool any_out = false;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                eo[i] = e[i].c + (int64_t)e[i].dx * PYo - (int64_t)e[i].dy * PXo;
-                any_out |= (eo[i] + e[i].max_off) < 0;
-            }
-            if (!any_out) {
-                const int px = sx0 + lx, py = sy0 + ly;
-                const int64_t E0 = eo[0] + e[0].lane_off, E1 = eo[1] + e[1].lane_off, E2 = eo[2] + e[2].lane_off;
-                const bool in = ((int32_t)(E0 >> 32) | (int32_t)(E1 >> 32) | (int32_t)(E2 >> 32)) >= 0;
-                if (in && px <= px1 && py <= py1) {
-                    const int32_t PX = px * 256 + 128, PY = py * 256 + 128;
-                    float z = fmaf(dzdx, (float)(PX - X0), fmaf(dzdy, (float)(PY - Y0), z0));
-                    if (!kWriteId) z = z + bias;
-                    if (!(z > 0.0f)) z = 0.0f;
-                    if (z > 1.0f) z = 1.0f;
-                    const size_t p = (size_t)py * (size_t)P.width + (size_t)px;
-                    if (kWriteId) {
-                        const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
-                        atomicMax(reinterpret_cast<unsigned long long*>(P.target) + p, key);
-                    } else {
-                        atomicMax(reinterpret_cast<unsigned int*>(P.target) + p, __float_as_uint(z));
-                    }
-                }
-            }
-            ++s;
-            if (++sx == nsx) {
-                sx = 0;
-                ++sy;
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, b = (i + 2) % 3;
+        dx[i] = X[b] - X[a];
+        dy[i] = Y[b] - Y[a];
+        const bool tl = dy[i] < 0 || (dy[i] == 0 && dx[i] > 0);
+        // E' at (PX, PY) = c + dx*(PY - Y0) - dy*(PX - X0)
+        c[i] = dy[i] * (X[a] - X[0]) - dx[i] * (Y[a] - Y[0]) - (tl ? 0 : 1);
+    }
+    for (int py = py0; py <= py1; ++py) {
+        const int32_t ry = py * 256 + 128 - Y[0];
+        for (int px = px0; px <= px1; ++px) {
+            const int32_t rx = px * 256 + 128 - X[0];
+            const int32_t e0 = c[0] + dx[0] * ry - dy[0] * rx;
+            const int32_t e1 = c[1] + dx[1] * ry - dy[1] * rx;
+            const int32_t e2 = c[2] + dx[2] * ry - dy[2] * rx;
+            if ((e0 | e1 | e2) >= 0) {
+                float z = fmaf(dzdx, (float)rx, fmaf(dzdy, (float)ry, z0));
+                if (!kWriteId) z = z + bias;
+                write_fragment<kWriteId>(P, px, py, z, id);
             }
         }
     }
 }
 
+// Triangles up to this extent (pixels, each way) take the incremental 32-bit
+// path: every edge value over the bounding box plus a stamp of overhang is
+// below 2 * ((90 + 8) * 256)^2 < 2^31.
+constexpr int kMediumExtent = 90;
+
+struct LargeRecord {
+    int64_t c[3];      // E' at sub-pixel (0, 0): E'(P) = c + dx*PY - dy*PX
+    int32_t dx[3], dy[3];
+    int64_t max_off[3], min_off[3];  // range of the lane offsets over the stamp
+    int32_t X0, Y0;
+    float z0, dzdx, dzdy, bias;
+    int px0, py0, px1, py1;
+    uint32_t id, nsx;
+    uint64_t begin, end;
+    bool short_edges;  // all |dx|, |dy| < 2^18: partial-edge values and lane offsets fit in 32 bits
+    bool medium;       // extent <= kMediumExtent px and near_origin: incremental 32-bit walk
+    bool near_origin;  // |PX - X0|, |PY - Y0| < 2^23 over the box: float offsets exact
+};
+
+__device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L) {
+    const int4* src = reinterpret_cast<const int4*>(rec);
+    const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
+    const int32_t X[3] = {q0.x, q0.z, q1.x}, Y[3] = {q0.y, q0.w, q1.y};
+    L.X0 = q0.x;
+    L.Y0 = q0.y;
+    L.z0 = __int_as_float(q1.z);
+    L.dzdx = __int_as_float(q1.w);
+    L.dzdy = __int_as_float(q2.x);
+    L.bias = __int_as_float(q2.y);
+    L.px0 = q2.z & 0xffff;
+    L.py0 = (uint32_t)q2.z >> 16;
+    L.px1 = q2.w & 0xffff;
+    L.py1 = (uint32_t)q2.w >> 16;
+    L.id = (uint32_t)q3.x;
+    L.begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
+    L.end = L.begin + (uint32_t)q3.y;
+    L.nsx = (uint32_t)((L.px1 - L.px0) / kStampW + 1);
+    bool short_edges = true;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, b = (i + 2) % 3;
+        const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+        const bool tl = dy < 0 || (dy == 0 && dx > 0);
+        L.dx[i] = dx;
+        L.dy[i] = dy;
+        L.c[i] = (int64_t)dy * X[a] - (int64_t)dx * Y[a] - (tl ? 0 : 1);
+        L.max_off[i] = (dx > 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy < 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
+        L.min_off[i] = (dx < 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy > 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
+        short_edges = short_edges && abs(dx) < (1 << 18) && abs(dy) < (1 << 18);
+    }
+    L.short_edges = short_edges;
+    const int64_t lo_x = (int64_t)L.px0 * 256 + 128 - L.X0, hi_x = (int64_t)L.px1 * 256 + 128 - L.X0 + kStampW * 256;
+    const int64_t lo_y = (int64_t)L.py0 * 256 + 128 - L.Y0, hi_y = (int64_t)L.py1 * 256 + 128 - L.Y0 + kStampH * 256;
+    const int64_t lim = 1ll << 23;
+    L.near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
+    const int32_t ex = max(X[0], max(X[1], X[2])) - min(X[0], min(X[1], X[2]));
+    const int32_t ey = max(Y[0], max(Y[1], Y[2])) - min(Y[0], min(Y[1], Y[2]));
+    L.medium = L.near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
+}
+
+// Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
+template <bool kWriteId>
+__device__ __forceinline__ void raster_stamp(const PassParams& P, const LargeRecord& L, uint32_t sx, uint32_t sy, int lx,
+                                             int ly) {
+    const int sx0 = L.px0 + (int)sx * kStampW, sy0 = L.py0 + (int)sy * kStampH;
+    const int32_t PXo = sx0 * 256 + 128, PYo = sy0 * 256 + 128;
+    int64_t eo[3];
+    bool reject = false, accept = true;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        eo[i] = L.c[i] + (int64_t)L.dx[i] * PYo - (int64_t)L.dy[i] * PXo;
+        reject |= eo[i] + L.max_off[i] < 0;
+        accept &= eo[i] + L.min_off[i] >= 0;
+    }
+    if (reject) return;
+    const int px = sx0 + lx, py = sy0 + ly;
+    bool in = px <= L.px1 && py <= L.py1;
+    if (!accept) {
+        if (L.short_edges) {
+            // partial edges: |eo| < 2^30 and the lane offset < 2^30, so 32 bits suffice
+            int32_t hi = 0;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const bool edge_accept = eo[i] + L.min_off[i] >= 0;
+                const int32_t e = (int32_t)eo[i] + L.dx[i] * (ly * 256) - L.dy[i] * (lx * 256);
+                hi |= edge_accept ? 0 : e;
+            }
+            in = in && hi >= 0;
+        } else {
+            int32_t hi = 0;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const int64_t e = eo[i] + (int64_t)L.dx[i] * (ly * 256) - (int64_t)L.dy[i] * (lx * 256);
+                hi |= (int32_t)(e >> 32);
+            }
+            in = in && hi >= 0;
+        }
+    }
+    if (!in) return;
+    float fx, fy;
+    if (L.near_origin) {
+        // exact: both terms are integers below 2^24
+        fx = (float)(PXo - L.X0) + (float)(lx * 256);
+        fy = (float)(PYo - L.Y0) + (float)(ly * 256);
+    } else {
+        fx = (float)(px * 256 + 128 - L.X0);
+        fy = (float)(py * 256 + 128 - L.Y0);
+    }
+    float z = fmaf(L.dzdx, fx, fmaf(L.dzdy, fy, L.z0));
+    if (!kWriteId) z = z + L.bias;
+    write_fragment<kWriteId>(P, px, py, z, L.id);
+}
+
+// Incremental walk over the stamps of a medium record in raster order. Each
+// lane holds its edge values and its float offsets from vertex 0; moving one
+// stamp right adds a constant, moving to the next stamp row restarts from the
+// row's first stamp. The float offsets stay exact integers below 2^24, so the
+// depth is bit-identical to fma(dzdx, (float)(PX-X0), fma(dzdy, (float)(PY-Y0), z0)).
+struct MediumWalk {
+    int32_t e[3], er[3], stepx[3], stepy[3];
+    float fx, fxr, fy, zrow;
+    int px, pxr, py;
+    uint32_t sx, sy;
+};
+
+__device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, uint32_t sy, int lx, int ly, MediumWalk& w) {
+    w.sx = sx;
+    w.sy = sy;
+    w.pxr = L.px0 + lx;
+    w.px = w.pxr + (int)sx * kStampW;
+    w.py = L.py0 + (int)sy * kStampH + ly;
+    const int32_t PX = w.px * 256 + 128, PY = w.py * 256 + 128, PXr = w.pxr * 256 + 128;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        w.e[i] = (int32_t)(L.c[i] + (int64_t)L.dx[i] * PY - (int64_t)L.dy[i] * PX);
+        w.er[i] = (int32_t)(L.c[i] + (int64_t)L.dx[i] * PY - (int64_t)L.dy[i] * PXr);
+        w.stepx[i] = -L.dy[i] * (kStampW * 256);
+        w.stepy[i] = L.dx[i] * (kStampH * 256);
+    }
+    w.fx = (float)(PX - L.X0);
+    w.fxr = (float)(PXr - L.X0);
+    w.fy = (float)(PY - L.Y0);
+    w.zrow = fmaf(L.dzdy, w.fy, L.z0);
+}
+
+template <bool kWriteId>
+__device__ __forceinline__ void medium_step(const PassParams& P, const LargeRecord& L, MediumWalk& w) {
+    if (((w.e[0] | w.e[1] | w.e[2]) >= 0) && w.px <= L.px1 && w.py <= L.py1) {
+        float z = fmaf(L.dzdx, w.fx, w.zrow);
+        if (!kWriteId) z = z + L.bias;
+        write_fragment<kWriteId>(P, w.px, w.py, z, L.id);
+    }
+    if (++w.sx == L.nsx) {
+        w.sx = 0;
+        ++w.sy;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            w.er[i] += w.stepy[i];
+            w.e[i] = w.er[i];
+        }
+        w.px = w.pxr;
+        w.py += kStampH;
+        w.fx = w.fxr;
+        w.fy += (float)(kStampH * 256);
+        w.zrow = fmaf(L.dzdy, w.fy, L.z0);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) w.e[i] += w.stepx[i];
+        w.px += kStampW;
+        w.fx += (float)(kStampW * 256);
+    }
+}
+
+// Persistent raster: warps first take batches of 32 small records (one per
+// lane) from a shared cursor, then the chunks of kChunkStamps stamps of the
+// large records in a fixed grid-stride order (a shared cursor per chunk would
+// serialise on one L2 line).
+template <bool kWriteId>
+__global__ void __launch_bounds__(256) k_raster(PassParams P) {
+    const int lane = threadIdx.x & 31;
+    const int lx = lane & (kStampW - 1), ly = lane >> 3;
+    const uint32_t n_small = min(P.header->small_records, P.small_capacity);
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&P.header->small_cursor, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_small) break;
+        if (base + lane < n_small) raster_small<kWriteId>(P, P.small_records + base + lane);
+    }
+    const uint32_t chunks = P.header->chunks;
+    const uint64_t total = P.header->stamps;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < chunks; k += warps) {
+        uint64_t s = (uint64_t)k * kChunkStamps;
+        const uint64_t s_end = (s + kChunkStamps < total) ? (s + kChunkStamps) : total;
+        uint32_t r = P.chunk_map[k];
+        if (r >= P.record_capacity) continue;
+        LargeRecord L;
+        load_large(P.records + r, L);
+        if (s < L.begin) {  // cannot happen with a consistent chunk map
+            atomicOr(P.error_flags, kErrStampOverflow);
+            continue;
+        }
+        uint32_t i = (uint32_t)(s - L.begin);
+        uint32_t sy = i / L.nsx, sx = i - sy * L.nsx;
+        MediumWalk w;
+        if (L.medium) medium_start(L, sx, sy, lx, ly, w);
+        while (s < s_end) {
+            if (s >= L.end) {
+                if (++r >= P.record_capacity) break;
+                load_large(P.records + r, L);
+                sx = 0;
+                sy = 0;
+                if (L.medium) medium_start(L, 0, 0, lx, ly, w);
+            }
+            if (L.medium) {
+                medium_step<kWriteId>(P, L, w);
+            } else {
+                raster_stamp<kWriteId>(P, L, sx, sy, lx, ly);
+                if (++sx == L.nsx) {
+                    sx = 0;
+                    ++sy;
+                }
+            }
+            ++s;
+        }
+    }
+}
+
 void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream) {
-    const int blocks = sm_count * 8;
+    // persistent grid: as many CTAs as can be resident at once
+    static int occ[2] = {0, 0};
+    const int t = p.write_id ? 1 : 0;
+    if (!occ[t]) {
+        int n = 0;
+        if (p.write_id) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<true>, 256, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<false>, 256, 0);
+        occ[t] = n > 0 ? n : 1;
+    }
+    const int blocks = sm_count * occ[t];
     if (p.write_id) k_raster<true><<<blocks, 256, 0, stream>>>(p);
     else k_raster<false><<<blocks, 256, 0, stream>>>(p);
 }

@@ -12,7 +12,7 @@
 // Limits: at most kStaticMaxTriangles triangles per call and kStaticChunks work
 // chunks (kStaticChunks * 16 stamps of 8x4 pixels). Larger inputs are rejected
 // with RZ_INVALID_ARGUMENT; a call whose coverage needs more chunks returns
-// RZ_OVERFLOW. The array (about 1.6 MiB) stays resident on every device that
+// RZ_OVERFLOW. The array (about 2.9 MiB) stays resident on every device that
 // loads the library until the process exits. All calls share it: calls that
 // overlap on the GPU (on different streams, or from different host threads)
 // race on it and must be serialised by the caller.
@@ -33,14 +33,15 @@ constexpr uint32_t kStaticChunks = 65536;
 
 // Byte layout of the scratch array (every part 256-byte aligned).
 constexpr size_t kOffRecords = 0;
-constexpr size_t kOffChunks = kOffRecords + (size_t)kStaticRecords * sizeof(TriRecord);
+constexpr size_t kOffSmall = kOffRecords + (size_t)kStaticRecords * sizeof(TriRecord);
+constexpr size_t kOffChunks = kOffSmall + (size_t)kStaticRecords * sizeof(TriRecord);
 constexpr size_t kOffTiles = kOffChunks + (size_t)kStaticChunks * sizeof(uint32_t);
 constexpr size_t kOffHeader = kOffTiles + ((kStaticTiles * sizeof(uint64_t) + 255) / 256) * 256;
 constexpr size_t kOffDraw = kOffHeader + 256;
 constexpr size_t kOffMvp = kOffDraw + 256;
 constexpr size_t kOffFlags = kOffMvp + 256;
 constexpr size_t kStaticBytes = kOffFlags + 256;
-static_assert(kOffChunks % 256 == 0 && kOffTiles % 256 == 0, "scratch parts are 256-byte aligned");
+static_assert(kOffSmall % 256 == 0 && kOffChunks % 256 == 0 && kOffTiles % 256 == 0, "scratch parts are 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
@@ -144,6 +145,8 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.write_id = 0;
         p.records = reinterpret_cast<TriRecord*>(scratch + kOffRecords);
         p.record_capacity = kStaticRecords;
+        p.small_records = reinterpret_cast<TriRecord*>(scratch + kOffSmall);
+        p.small_capacity = kStaticRecords;
         p.tile_status = reinterpret_cast<uint64_t*>(scratch + kOffTiles);
         p.chunk_map = reinterpret_cast<uint32_t*>(scratch + kOffChunks);
         p.chunk_capacity = kStaticChunks;
