@@ -209,7 +209,7 @@ typedef struct rz_config {
     uint32_t shadow_map_size;  /* square D32 shadow map (the reference uses 4096, Graphics.cpp:2524) */
     uint32_t samples;          /* rasterisation samples per pixel: 1 */
     int32_t device;            /* CUDA device ordinal */
-    uint32_t queue_chunks;     /* raster work-queue depth per pass, in chunks of 16
+    uint32_t queue_chunks;     /* raster work-queue depth per pass, in chunks of 32
                                   8x4-pixel stamps; 0 = sized from the scene. A frame
                                   that needs more reports RZ_OVERFLOW and the queue
                                   grows for the next frame. */
@@ -340,7 +340,7 @@ int rz_get_stage_times(struct rz_ctx* ctx, float* ms, uint32_t capacity, uint32_
  *   depth_out: device array of width * height floats, overwritten
  * Runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it.
  * Returns RZ_OVERFLOW if the coverage needs more than the fixed work queue
- * (65,536 chunks of 16 8x4-pixel stamps). Calls share the scratch array: calls
+ * (65,536 chunks of 32 8x4-pixel stamps). Calls share the scratch array: calls
  * that overlap on the GPU race and must be serialised by the caller. The first
  * call on a device looks up the array's device address; make it before any
  * stream capture starts on that device. */

@@ -68,7 +68,7 @@ static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
 
 constexpr int kStampW = 8;
 constexpr int kStampH = 4;
-constexpr int kChunkStamps = 16;      // stamps per raster work chunk
+constexpr int kChunkStamps = 32;      // stamps per raster work chunk
 constexpr int kSetupThreads = 256;    // triangles per setup CTA
 constexpr float kGuardBand = 64.0f;
 

@@ -523,23 +523,31 @@ __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecor
 constexpr int kMediumExtent = 90;
 
 struct LargeRecord {
-    int64_t c[3];      // E' at sub-pixel (0, 0): E'(P) = c + dx*PY - dy*PX
+    int32_t X[3], Y[3];
     int32_t dx[3], dy[3];
+    uint32_t tl_bias[3];  // 0 on top-left edges, 1 otherwise
+    // generic path only (not medium):
+    int64_t c[3];         // E' at sub-pixel (0, 0): E'(P) = c + dx*PY - dy*PX
     int64_t max_off[3], min_off[3];  // range of the lane offsets over the stamp
+    bool short_edges;     // all |dx|, |dy| < 2^18: partial-edge values and lane offsets fit in 32 bits
+    bool medium;          // extent <= kMediumExtent px and near_origin: incremental 32-bit walk
+    bool near_origin;     // |PX - X0|, |PY - Y0| < 2^23 over the box: float offsets exact
     int32_t X0, Y0;
     float z0, dzdx, dzdy, bias;
     int px0, py0, px1, py1;
     uint32_t id, nsx;
     uint64_t begin, end;
-    bool short_edges;  // all |dx|, |dy| < 2^18: partial-edge values and lane offsets fit in 32 bits
-    bool medium;       // extent <= kMediumExtent px and near_origin: incremental 32-bit walk
-    bool near_origin;  // |PX - X0|, |PY - Y0| < 2^23 over the box: float offsets exact
 };
 
 __device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L) {
     const int4* src = reinterpret_cast<const int4*>(rec);
     const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
-    const int32_t X[3] = {q0.x, q0.z, q1.x}, Y[3] = {q0.y, q0.w, q1.y};
+    L.X[0] = q0.x;
+    L.Y[0] = q0.y;
+    L.X[1] = q0.z;
+    L.Y[1] = q0.w;
+    L.X[2] = q1.x;
+    L.Y[2] = q1.y;
     L.X0 = q0.x;
     L.Y0 = q0.y;
     L.z0 = __int_as_float(q1.z);
@@ -554,27 +562,32 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L)
     L.begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
     L.end = L.begin + (uint32_t)q3.y;
     L.nsx = (uint32_t)((L.px1 - L.px0) / kStampW + 1);
-    bool short_edges = true;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const int a = (i + 1) % 3, b = (i + 2) % 3;
-        const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
-        const bool tl = dy < 0 || (dy == 0 && dx > 0);
-        L.dx[i] = dx;
-        L.dy[i] = dy;
-        L.c[i] = (int64_t)dy * X[a] - (int64_t)dx * Y[a] - (tl ? 0 : 1);
+        L.dx[i] = L.X[b] - L.X[a];
+        L.dy[i] = L.Y[b] - L.Y[a];
+        L.tl_bias[i] = (L.dy[i] < 0 || (L.dy[i] == 0 && L.dx[i] > 0)) ? 0u : 1u;
+    }
+    const int32_t lo_x = L.px0 * 256 + 128 - L.X0, hi_x = L.px1 * 256 + 128 - L.X0 + kStampW * 256;
+    const int32_t lo_y = L.py0 * 256 + 128 - L.Y0, hi_y = L.py1 * 256 + 128 - L.Y0 + kStampH * 256;
+    const int32_t lim = 1 << 23;
+    L.near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
+    const int32_t ex = max(L.X[0], max(L.X[1], L.X[2])) - min(L.X[0], min(L.X[1], L.X[2]));
+    const int32_t ey = max(L.Y[0], max(L.Y[1], L.Y[2])) - min(L.Y[0], min(L.Y[1], L.Y[2]));
+    L.medium = L.near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
+    if (L.medium) return;
+    bool short_edges = true;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3;
+        const int32_t dx = L.dx[i], dy = L.dy[i];
+        L.c[i] = (int64_t)dy * L.X[a] - (int64_t)dx * L.Y[a] - L.tl_bias[i];
         L.max_off[i] = (dx > 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy < 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
         L.min_off[i] = (dx < 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy > 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
         short_edges = short_edges && abs(dx) < (1 << 18) && abs(dy) < (1 << 18);
     }
     L.short_edges = short_edges;
-    const int64_t lo_x = (int64_t)L.px0 * 256 + 128 - L.X0, hi_x = (int64_t)L.px1 * 256 + 128 - L.X0 + kStampW * 256;
-    const int64_t lo_y = (int64_t)L.py0 * 256 + 128 - L.Y0, hi_y = (int64_t)L.py1 * 256 + 128 - L.Y0 + kStampH * 256;
-    const int64_t lim = 1ll << 23;
-    L.near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
-    const int32_t ex = max(X[0], max(X[1], X[2])) - min(X[0], min(X[1], X[2]));
-    const int32_t ey = max(Y[0], max(Y[1], Y[2])) - min(Y[0], min(Y[1], Y[2]));
-    L.medium = L.near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
 }
 
 // Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
@@ -642,23 +655,29 @@ struct MediumWalk {
     uint32_t sx, sy;
 };
 
+// Edge values relative to vertex 0 in wrapping 32-bit arithmetic: for a medium
+// triangle the true value at every pixel of the walk fits in int32, so the
+// wrapped result equals it.
 __device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, uint32_t sy, int lx, int ly, MediumWalk& w) {
     w.sx = sx;
     w.sy = sy;
     w.pxr = L.px0 + lx;
     w.px = w.pxr + (int)sx * kStampW;
     w.py = L.py0 + (int)sy * kStampH + ly;
-    const int32_t PX = w.px * 256 + 128, PY = w.py * 256 + 128, PXr = w.pxr * 256 + 128;
+    const int32_t rx = w.px * 256 + 128 - L.X0, ry = w.py * 256 + 128 - L.Y0, rxr = w.pxr * 256 + 128 - L.X0;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        w.e[i] = (int32_t)(L.c[i] + (int64_t)L.dx[i] * PY - (int64_t)L.dy[i] * PX);
-        w.er[i] = (int32_t)(L.c[i] + (int64_t)L.dx[i] * PY - (int64_t)L.dy[i] * PXr);
-        w.stepx[i] = -L.dy[i] * (kStampW * 256);
-        w.stepy[i] = L.dx[i] * (kStampH * 256);
+        const int a = (i + 1) % 3;
+        const uint32_t dx = (uint32_t)L.dx[i], dy = (uint32_t)L.dy[i];
+        const uint32_t c = dy * (uint32_t)(L.X[a] - L.X0) - dx * (uint32_t)(L.Y[a] - L.Y0) - L.tl_bias[i];
+        w.e[i] = (int32_t)(c + dx * (uint32_t)ry - dy * (uint32_t)rx);
+        w.er[i] = (int32_t)(c + dx * (uint32_t)ry - dy * (uint32_t)rxr);
+        w.stepx[i] = (int32_t)(0u - dy * (uint32_t)(kStampW * 256));
+        w.stepy[i] = (int32_t)(dx * (uint32_t)(kStampH * 256));
     }
-    w.fx = (float)(PX - L.X0);
-    w.fxr = (float)(PXr - L.X0);
-    w.fy = (float)(PY - L.Y0);
+    w.fx = (float)rx;
+    w.fxr = (float)rxr;
+    w.fy = (float)ry;
     w.zrow = fmaf(L.dzdy, w.fy, L.z0);
 }
 
@@ -674,7 +693,7 @@ __device__ __forceinline__ void medium_step(const PassParams& P, const LargeReco
         ++w.sy;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            w.er[i] += w.stepy[i];
+            w.er[i] = (int32_t)((uint32_t)w.er[i] + (uint32_t)w.stepy[i]);
             w.e[i] = w.er[i];
         }
         w.px = w.pxr;
@@ -684,7 +703,7 @@ __device__ __forceinline__ void medium_step(const PassParams& P, const LargeReco
         w.zrow = fmaf(L.dzdy, w.fy, L.z0);
     } else {
 #pragma unroll
-        for (int i = 0; i < 3; ++i) w.e[i] += w.stepx[i];
+        for (int i = 0; i < 3; ++i) w.e[i] = (int32_t)((uint32_t)w.e[i] + (uint32_t)w.stepx[i]);
         w.px += kStampW;
         w.fx += (float)(kStampW * 256);
     }
@@ -695,7 +714,7 @@ __device__ __forceinline__ void medium_step(const PassParams& P, const LargeReco
 // large records in a fixed grid-stride order (a shared cursor per chunk would
 // serialise on one L2 line).
 template <bool kWriteId>
-__global__ void __launch_bounds__(256) k_raster(PassParams P) {
+__global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
     const int lane = threadIdx.x & 31;
     const int lx = lane & (kStampW - 1), ly = lane >> 3;
     const uint32_t n_small = min(P.header->small_records, P.small_capacity);

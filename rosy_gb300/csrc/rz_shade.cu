@@ -204,6 +204,97 @@ __device__ __forceinline__ int wrap_coord(int i, int size, int mode) {
     return size - 1 - a;
 }
 
+// Where a texture.Sample call reads: the level(s), the wrapped texel columns
+// and rows and the filter weights. It depends only on the texture's size and
+// level count, the sampler and the uv/derivatives, so textures that share those
+// share one SampleCoords (the three material textures usually do).
+struct LevelCoords {
+    uint32_t off;   // texel offset of the level
+    int w;          // level width (row pitch)
+    int x0, x1, y0, y1;
+    float a, b;     // bilinear weights (unused for nearest)
+};
+
+struct SampleCoords {
+    uint32_t width, height, levels;
+    SamplerBits st;
+    bool valid;
+    bool linear;    // filter within the level(s)
+    bool two;       // blend two levels
+    float delta;
+    LevelCoords l0, l1;
+};
+
+__device__ __forceinline__ void level_coords(const TexDesc& t, int level, bool linear, SamplerBits st, float u, float v,
+                                             LevelCoords& c) {
+    const int w = max(1, (int)(t.width >> level)), h = max(1, (int)(t.height >> level));
+    c.off = t.level_off[level];
+    c.w = w;
+    const int wu = (st >> 4) & 3, wv = (st >> 6) & 3;
+    if (!linear) {
+        const int i = (int)floorf(u * (float)w), j = (int)floorf(v * (float)h);
+        c.x0 = wrap_coord(i, w, wu);
+        c.y0 = wrap_coord(j, h, wv);
+        c.x1 = c.x0;
+        c.y1 = c.y0;
+        c.a = c.b = 0.0f;
+        return;
+    }
+    const float uu = u * (float)w - 0.5f, vv = v * (float)h - 0.5f;
+    const float fi = floorf(uu), fj = floorf(vv);
+    c.a = uu - fi;
+    c.b = vv - fj;
+    const int i0 = (int)fi, j0 = (int)fj;
+    c.x0 = wrap_coord(i0, w, wu);
+    c.x1 = wrap_coord(i0 + 1, w, wu);
+    c.y0 = wrap_coord(j0, h, wv);
+    c.y1 = wrap_coord(j0 + 1, h, wv);
+}
+
+// Level selection of texture.Sample with implicit derivatives (Vulkan LOD rules).
+__device__ __forceinline__ void sample_coords(const TexDesc& t, SamplerBits st, const float uv[2], const float duvdx[2],
+                                              const float duvdy[2], SampleCoords& c) {
+    c.width = t.width;
+    c.height = t.height;
+    c.levels = t.levels;
+    c.st = st;
+    c.valid = true;
+    const float w0 = (float)t.width, h0 = (float)t.height;
+    const float ax = duvdx[0] * w0, ay = duvdx[1] * h0, bx = duvdy[0] * w0, by = duvdy[1] * h0;
+    const float rx2 = ax * ax + ay * ay, ry2 = bx * bx + by * by;
+    const float rho2 = fmaxf(rx2, ry2);
+    const int q = (int)t.levels - 1;
+    c.two = false;
+    c.delta = 0.0f;
+    if (!(rho2 > 1.0f)) {  // magnification: level 0
+        c.linear = (st & 2u) != 0;
+        level_coords(t, 0, c.linear, st, uv[0], uv[1], c.l0);
+        return;
+    }
+    c.linear = (st & 1u) != 0;
+    if (!(st & 4u)) {  // nearest mip: d = ceil(lambda + 0.5) - 1
+        int d = 0;
+        float thr = 2.0f;
+        while (d < q && rho2 > thr) {
+            ++d;
+            thr = thr * 4.0f;
+        }
+        level_coords(t, d, c.linear, st, uv[0], uv[1], c.l0);
+        return;
+    }
+    const float lambda = 0.5f * log2f(rho2);
+    const float dp = fminf(lambda, (float)q);
+    const int dlo = (int)floorf(dp);
+    const int dhi = min(dlo + 1, q);
+    const float delta = dp - (float)dlo;
+    level_coords(t, dlo, c.linear, st, uv[0], uv[1], c.l0);
+    if (delta > 0.0f && dhi != dlo) {
+        c.two = true;
+        c.delta = delta;
+        level_coords(t, dhi, c.linear, st, uv[0], uv[1], c.l1);
+    }
+}
+
 struct Sampler {
     const ShadeParams* P;
     const float* srgb;   // shared-memory table: sRGB byte -> linear
@@ -224,76 +315,43 @@ struct Sampler {
         out[3] = unorm[a];
     }
 
-    __device__ void sample_level(const TexDesc& t, int level, bool linear, SamplerBits st, float u, float v, float out[4]) const {
-        const int w = max(1, (int)(t.width >> level)), h = max(1, (int)(t.height >> level));
-        const uint32_t off = t.level_off[level];
-        const int wu = (st >> 4) & 3, wv = (st >> 6) & 3;
+    __device__ __forceinline__ void fetch_level(const TexDesc& t, const LevelCoords& c, bool linear, float out[4]) const {
         if (!linear) {
-            const int i = (int)floorf(u * (float)w), j = (int)floorf(v * (float)h);
-            texel(t, off, w, wrap_coord(i, w, wu), wrap_coord(j, h, wv), out);
+            texel(t, c.off, c.w, c.x0, c.y0, out);
             return;
         }
-        const float uu = u * (float)w - 0.5f, vv = v * (float)h - 0.5f;
-        const float fi = floorf(uu), fj = floorf(vv);
-        const float a = uu - fi, b = vv - fj;
-        const int i0 = (int)fi, j0 = (int)fj;
-        const int x0 = wrap_coord(i0, w, wu), x1 = wrap_coord(i0 + 1, w, wu);
-        const int y0 = wrap_coord(j0, h, wv), y1 = wrap_coord(j0 + 1, h, wv);
         float t00[4], t10[4], t01[4], t11[4];
-        texel(t, off, w, x0, y0, t00);
-        texel(t, off, w, x1, y0, t10);
-        texel(t, off, w, x0, y1, t01);
-        texel(t, off, w, x1, y1, t11);
+        texel(t, c.off, c.w, c.x0, c.y0, t00);
+        texel(t, c.off, c.w, c.x1, c.y0, t10);
+        texel(t, c.off, c.w, c.x0, c.y1, t01);
+        texel(t, c.off, c.w, c.x1, c.y1, t11);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float top = t00[k] + a * (t10[k] - t00[k]);
-            const float bot = t01[k] + a * (t11[k] - t01[k]);
-            out[k] = top + b * (bot - top);
+            const float top = t00[k] + c.a * (t10[k] - t00[k]);
+            const float bot = t01[k] + c.a * (t11[k] - t01[k]);
+            out[k] = top + c.b * (bot - top);
         }
     }
 
-    __device__ void sample(uint32_t tex_index, uint32_t sampler_index, const Frag& f, float out[4]) const {
-        if (tex_index >= P->texture_count) {
+    // texture.Sample(sampler, uv) with implicit derivatives. `cache` holds the
+    // coordinates of the previous call and is reused when the texture's size,
+    // levels and sampler match.
+    __device__ void sample(uint32_t tex_index, uint32_t sampler_index, const Frag& f, SampleCoords& cache, float out[4]) const {
+        if (tex_index >= P->texture_count) {  // absent image: robust null descriptor reads 0
             out[0] = out[1] = out[2] = out[3] = 0.0f;
             return;
         }
         const TexDesc& t = P->textures[tex_index];
         const SamplerBits st = P->samplers[min(sampler_index, P->sampler_count)];
-        const float w0 = (float)t.width, h0 = (float)t.height;
-        const float ax = f.duvdx[0] * w0, ay = f.duvdx[1] * h0, bx = f.duvdy[0] * w0, by = f.duvdy[1] * h0;
-        const float rx2 = ax * ax + ay * ay, ry2 = bx * bx + by * by;
-        const float rho2 = fmaxf(rx2, ry2);
-        const int q = (int)t.levels - 1;
-        if (!(rho2 > 1.0f)) {
-            sample_level(t, 0, (st & 2u) != 0, st, f.uv[0], f.uv[1], out);
-            return;
-        }
-        const bool min_linear = (st & 1u) != 0;
-        if (!(st & 4u)) {
-            int d = 0;
-            float thr = 2.0f;
-            while (d < q && rho2 > thr) {
-                ++d;
-                thr = thr * 4.0f;
-            }
-            sample_level(t, d, min_linear, st, f.uv[0], f.uv[1], out);
-            return;
-        }
-        const float lambda = 0.5f * log2f(rho2);
-        const float dp = fminf(lambda, (float)q);
-        const int dlo = (int)floorf(dp);
-        const int dhi = min(dlo + 1, q);
-        const float delta = dp - (float)dlo;
-        float a[4];
-        sample_level(t, dlo, min_linear, st, f.uv[0], f.uv[1], a);
-        if (delta > 0.0f && dhi != dlo) {
+        if (!(cache.valid && cache.width == t.width && cache.height == t.height && cache.levels == t.levels &&
+              cache.st == st))
+            sample_coords(t, st, f.uv, f.duvdx, f.duvdy, cache);
+        fetch_level(t, cache.l0, cache.linear, out);
+        if (cache.two) {
             float b[4];
-            sample_level(t, dhi, min_linear, st, f.uv[0], f.uv[1], b);
+            fetch_level(t, cache.l1, cache.linear, b);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) out[k] = a[k] + delta * (b[k] - a[k]);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) out[k] = a[k];
+            for (int k = 0; k < 4; ++k) out[k] = out[k] + cache.delta * (b[k] - out[k]);
         }
     }
 };
@@ -315,16 +373,56 @@ __device__ __forceinline__ float sample_cmp(const float* __restrict__ shadow, in
     return top + b * (bot - top);
 }
 
+// 3x3 PCF: nine bilinear compare taps one texel apart. The taps' texel
+// positions are computed one by one (as the single-tap path would), and when
+// they fall on consecutive columns/rows - the usual case - the 16 compares of
+// the shared 4x4 block are done once; otherwise each tap reads its own texels.
+__device__ float pcf3x3(const float* __restrict__ shadow, int S, const float csm[4]) {
+    const float o = 1.0f / (float)S;
+    int xi[3], yj[3];
+    float a[3], b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float uu = (csm[0] + (float)(k - 1) * o) * (float)S - 0.5f;
+        const float vv = (csm[1] + (float)(k - 1) * o) * (float)S - 0.5f;
+        const float fi = floorf(uu), fj = floorf(vv);
+        a[k] = uu - fi;
+        b[k] = vv - fj;
+        xi[k] = (int)fmaxf(fminf(fi, (float)(S + 1)), -2.0f);
+        yj[k] = (int)fmaxf(fminf(fj, (float)(S + 1)), -2.0f);
+    }
+    const float dref = csm[2];
+    float result = 0.0f;
+    if (xi[1] == xi[0] + 1 && xi[2] == xi[0] + 2 && yj[1] == yj[0] + 1 && yj[2] == yj[0] + 2) {
+        float c[4][4];
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+            const size_t row = (size_t)min(max(yj[0] + y, 0), S - 1) * S;
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+                c[y][x] = dref >= __ldg(&shadow[row + min(max(xi[0] + x, 0), S - 1)]) ? 1.0f : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float top = c[j][i] + a[i] * (c[j][i + 1] - c[j][i]);
+                const float bot = c[j + 1][i] + a[i] * (c[j + 1][i + 1] - c[j + 1][i]);
+                result += top + b[j] * (bot - top);
+            }
+        }
+        return result * (1.0f / 9.0f);
+    }
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i)
+            result += sample_cmp(shadow, S, csm[0] + (float)i * o, csm[1] + (float)j * o, csm[2]);
+    return result * (1.0f / 9.0f);
+}
+
 // pcf.slang:1-11 (5 taps) and the 3x3 option.
 __device__ float pcf(const float* __restrict__ shadow, int S, const float csm[4], uint32_t mode) {
     float result = 0.0f;
-    if (mode == RZ_PCF_3X3) {
-        const float o = 1.0f / (float)S;
-        for (int j = -1; j <= 1; ++j)
-            for (int i = -1; i <= 1; ++i)
-                result += sample_cmp(shadow, S, csm[0] + (float)i * o, csm[1] + (float)j * o, csm[2]);
-        return result * (1.0f / 9.0f);
-    }
+    if (mode == RZ_PCF_3X3) return pcf3x3(shadow, S, csm);
     const float o = 0.00025f;
     result += sample_cmp(shadow, S, csm[0] - o, csm[1] - o, csm[2]);
     result += sample_cmp(shadow, S, csm[0] + o * 2.0f, csm[1], csm[2]);
@@ -371,6 +469,8 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
     V3 lightNormal = normalize(bv.normal);
     const V3 lightDir = normalize(bv.lightDir);
     const V3 bitangent = bv.bitangent;
+    SampleCoords cache;
+    cache.valid = false;
     if (md) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) outFragColor[k] = md->color[k];
@@ -379,7 +479,7 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
         alpha = fminf(md->color[3], alpha);
         if (sd.normal_maps_enabled == 1 && md->tex[1] != RZ_INVALID_INDEX) {
             float s[4];
-            smp.sample(md->tex[1], md->sampler[1], bv, s);
+            smp.sample(md->tex[1], md->sampler[1], bv, cache, s);
             const V3 m{s[0] * 2.0f - 1.0f, s[1] * 2.0f - 1.0f, s[2] * 2.0f - 1.0f};
             const V3 n = normalize(bv.normal);
             const V3 t = normalize(bv.tangent - n * dot(bv.tangent, n));
@@ -387,12 +487,12 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
             lightNormal = normalize(t * m.x + b * m.y + n * m.z);
         }
         if (md->tex[0] != RZ_INVALID_INDEX) {
-            smp.sample(md->tex[0], md->sampler[0], bv, imageTextureColor);
+            smp.sample(md->tex[0], md->sampler[0], bv, cache, imageTextureColor);
             alpha = fminf(imageTextureColor[3], alpha);
         }
         float s[4];
-        if (md->tex[3] != RZ_INVALID_INDEX) smp.sample(md->tex[3], md->sampler[3], bv, s);
-        else smp.sample(md->tex[2], md->sampler[2], bv, s);
+        if (md->tex[3] != RZ_INVALID_INDEX) smp.sample(md->tex[3], md->sampler[3], bv, cache, s);
+        else smp.sample(md->tex[2], md->sampler[2], bv, cache, s);
         sampledRoughness = s[1];
         sampledMetallic = s[2];
     }

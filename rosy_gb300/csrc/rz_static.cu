@@ -10,7 +10,7 @@
 // inputs and the output; nothing is allocated here.
 //
 // Limits: at most kStaticMaxTriangles triangles per call and kStaticChunks work
-// chunks (kStaticChunks * 16 stamps of 8x4 pixels). Larger inputs are rejected
+// chunks (kStaticChunks * 32 stamps of 8x4 pixels). Larger inputs are rejected
 // with RZ_INVALID_ARGUMENT; a call whose coverage needs more chunks returns
 // RZ_OVERFLOW. The array (about 2.9 MiB) stays resident on every device that
 // loads the library until the process exits. All calls share it: calls that
