@@ -587,10 +587,10 @@ void barycentrics(const T c0[4], const T c1[4], const T c2[4], int px, int py, i
     const V3<T> v0{c0[0], c0[1], c0[3]}, v1{c1[0], c1[1], c1[3]}, v2{c2[0], c2[1], c2[3]};
     const V3<T> p{xn, yn, T(1)};
     const T b0 = dot(cross(v1, v2), p), b1 = dot(cross(v2, v0), p), b2 = dot(cross(v0, v1), p);
-    const T s = b0 + b1 + b2;
-    b[0] = b0 / s;
-    b[1] = b1 / s;
-    b[2] = b2 / s;
+    const T inv = T(1) / (b0 + b1 + b2);
+    b[0] = b0 * inv;
+    b[1] = b1 * inv;
+    b[2] = b2 * inv;
 }
 
 template <class T>

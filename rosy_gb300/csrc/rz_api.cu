@@ -55,6 +55,8 @@ struct rz_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;          // shadow pass branch of the frame graph
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint32_t width = 0, height = 0, shadow_size = 0;
     uint32_t queue_chunks = 0;  // fixed work-queue depth (0 = sized from the scene)
     std::string last_error;
@@ -281,43 +283,7 @@ void stamp(rz_ctx* c, int i) {
 }
 
 // Enqueues one frame (everything after the scene/object uploads).
-int enqueue_frame(rz_ctx* c) {
-    cudaStream_t s = c->stream;
-    stamp(c, 0);
-    RZ_CUDA(c, cudaMemsetAsync(c->d_error, 0, sizeof(uint32_t), s), "clear error flags");
-    RZ_CUDA(c, cudaMemsetAsync(c->d_headers, 0, 2 * sizeof(PassHeader), s), "clear pass headers");
-    // shadow pass: clear to 0 (src/Engine/Graphics.cpp:5208-5213)
-    RZ_CUDA(c, cudaMemsetAsync(c->d_shadow, 0, (size_t)c->shadow_size * c->shadow_size * 4, s), "clear shadow map");
-    if (c->shadow_tris)
-        RZ_CUDA(c, cudaMemsetAsync(c->shadow_pass.tile_status, 0, (size_t)setup_ctas(c->shadow_tris) * 8, s), "clear tiles");
-    stamp(c, 1);
-    if (c->shadow_tris) {
-        launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_scene->shadow_projection_near,
-                    c->d_shadow_mvp, s);
-        const PassParams sp = pass_params(c, false);
-        launch_setup(sp, s);
-        stamp(c, 2);
-        launch_raster(sp, c->sm_count, s);
-    } else {
-        stamp(c, 2);
-    }
-    stamp(c, 3);
-    // camera pass: depth cleared to 0 (5585), opaque list
-    RZ_CUDA(c, cudaMemsetAsync(c->d_vis, 0, (size_t)c->width * c->height * 8, s), "clear visibility");
-    if (c->opaque_tris) {
-        RZ_CUDA(c, cudaMemsetAsync(c->camera_pass.tile_status, 0, (size_t)setup_ctas(c->opaque_tris) * 8, s), "clear tiles");
-    }
-    launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_scene, c->d_camera_consts, s);
-    stamp(c, 4);
-    if (c->opaque_tris) {
-        const PassParams cp = pass_params(c, true);
-        launch_setup(cp, s);
-        stamp(c, 5);
-        launch_raster(cp, c->sm_count, s);
-    } else {
-        stamp(c, 5);
-    }
-    stamp(c, 6);
+ShadeParams shade_params(rz_ctx* c) {
     ShadeParams sh{};
     sh.vis = c->d_vis;
     sh.shadow = reinterpret_cast<const float*>(c->d_shadow);
@@ -343,9 +309,89 @@ int enqueue_frame(rz_ctx* c) {
     sh.scene = c->d_scene;
     sh.pcf_mode = c->draw_config.pcf_mode;
     sh.srgb_table = c->d_srgb;
+    return sh;
+}
+
+// Shadow pass (src/Engine/Graphics.cpp:5195-5292): clear to 0, per-draw
+// matrices, setup, raster.
+void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
+    ClearList cl{};
+    cl.ptr[0] = c->d_shadow;
+    cl.bytes[0] = (size_t)c->shadow_size * c->shadow_size * 4;
+    cl.ptr[1] = c->d_headers + 0;
+    cl.bytes[1] = sizeof(PassHeader);
+    cl.count = 2;
+    if (c->shadow_tris) {
+        cl.ptr[2] = c->shadow_pass.tile_status;
+        cl.bytes[2] = (size_t)setup_ctas(c->shadow_tris) * 8;
+        cl.count = 3;
+    }
+    launch_clear(cl, c->sm_count, s);
+    if (stamps) stamp(c, 1);
+    if (c->shadow_tris) {
+        launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_scene->shadow_projection_near,
+                    c->d_shadow_mvp, s);
+        const PassParams sp = pass_params(c, false);
+        launch_setup(sp, s);
+        if (stamps) stamp(c, 2);
+        launch_raster(sp, c->sm_count, s);
+    } else if (stamps) {
+        stamp(c, 2);
+    }
+}
+
+// Camera pass (5566-5653): visibility cleared to 0, opaque list, then the
+// vertex stage of the shading.
+void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& sh) {
+    ClearList cl{};
+    cl.ptr[0] = c->d_vis;
+    cl.bytes[0] = (size_t)c->width * c->height * 8;
+    cl.ptr[1] = c->d_headers + 1;
+    cl.bytes[1] = sizeof(PassHeader);
+    cl.count = 2;
+    if (c->opaque_tris) {
+        cl.ptr[2] = c->camera_pass.tile_status;
+        cl.bytes[2] = (size_t)setup_ctas(c->opaque_tris) * 8;
+        cl.count = 3;
+    }
+    launch_clear(cl, c->sm_count, s);
+    launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_scene, c->d_camera_consts, s);
+    if (stamps) stamp(c, 4);
+    if (c->opaque_tris) {
+        const PassParams cp = pass_params(c, true);
+        launch_setup(cp, s);
+        if (stamps) stamp(c, 5);
+        launch_raster(cp, c->sm_count, s);
+    } else if (stamps) {
+        stamp(c, 5);
+    }
     launch_vertex(sh, s);
+}
+
+// Enqueues one frame (everything after the scene/object uploads). With stage
+// timing the stages run one after the other on the main stream between
+// events; otherwise the shadow pass runs on a side stream concurrently with the
+// camera pass, joining before the shading (which reads the shadow map).
+int enqueue_frame(rz_ctx* c) {
+    cudaStream_t s = c->stream;
+    const ShadeParams sh = shade_params(c);
+    RZ_CUDA(c, cudaMemsetAsync(c->d_error, 0, sizeof(uint32_t), s), "clear error flags");
+    if (c->timing) {
+        stamp(c, 0);
+        enqueue_shadow(c, s, true);
+        stamp(c, 3);
+        enqueue_camera(c, s, true, sh);
+        stamp(c, 6);
+    } else {
+        RZ_CUDA(c, cudaEventRecord(c->fork, s), "fork");
+        RZ_CUDA(c, cudaStreamWaitEvent(c->side, c->fork, 0), "fork");
+        enqueue_shadow(c, c->side, false);
+        enqueue_camera(c, s, false, sh);
+        RZ_CUDA(c, cudaEventRecord(c->join, c->side), "join");
+        RZ_CUDA(c, cudaStreamWaitEvent(s, c->join, 0), "join");
+    }
     launch_shade(sh, s);
-    stamp(c, 7);
+    if (c->timing) stamp(c, 7);
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
     RZ_CUDA(c, cudaMemcpyAsync(&c->h_report->error_flags, c->d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
             "read error flags");
@@ -393,7 +439,11 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
     if (cudaSetDevice(c->device) != cudaSuccess) return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RZ_GRAPHICS_INIT_FAILURE);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess)
+        return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->objects_copied, cudaEventDisableTiming) != cudaSuccess)
@@ -461,6 +511,10 @@ void rz_destroy(rz_ctx* c) {
         if (e) cudaEventDestroy(e);
     if (c->scene_copied) cudaEventDestroy(c->scene_copied);
     if (c->objects_copied) cudaEventDestroy(c->objects_copied);
+    if (c->side) cudaStreamSynchronize(c->side);
+    if (c->fork) cudaEventDestroy(c->fork);
+    if (c->join) cudaEventDestroy(c->join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -873,7 +927,8 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->shadow_stamps = c->h_report->shadow.stamps;
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->error_flags;
-    out->kernel_launches = (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u + (c->varying_count ? 1u : 0u);
+    // clears (2) + prep (1) + prep_camera (1) + setup/raster per pass with triangles + vertex + shade
+    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u + (c->varying_count ? 1u : 0u);
     return RZ_OK;
 }
 

@@ -149,7 +149,15 @@ struct ShadeParams {
     const float* srgb_table;      // 256 entries
 };
 
+// Up to four buffers to zero in one launch (16-byte stores, byte tail).
+struct ClearList {
+    void* ptr[4];
+    size_t bytes[4];
+    int count;
+};
+
 // Launchers (rz_raster.cu / rz_shade.cu). All enqueue on `stream`.
+void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream);
 void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const float* proj16,
                  float* out_mvp, cudaStream_t stream);
 void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const rz_scene_data* scene,

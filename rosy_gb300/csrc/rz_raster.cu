@@ -55,6 +55,33 @@ void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, con
 }
 
 // ---------------------------------------------------------------------------
+// clears (the load-op CLEAR of the depth attachments, scratch headers)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_clear(ClearList L) {
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (int b = 0; b < L.count; ++b) {
+        uint4* p = static_cast<uint4*>(L.ptr[b]);
+        const size_t n16 = L.bytes[b] / 16;
+        for (size_t i = tid; i < n16; i += stride) p[i] = make_uint4(0u, 0u, 0u, 0u);
+        const size_t tail = L.bytes[b] - n16 * 16;
+        if (tid < tail) reinterpret_cast<unsigned char*>(L.ptr[b])[n16 * 16 + tid] = 0;
+    }
+}
+
+void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream) {
+    size_t most = 0;
+    for (int b = 0; b < list.count; ++b) most = list.bytes[b] > most ? list.bytes[b] : most;
+    if (most == 0) return;
+    size_t blocks = (most / 16 + 255) / 256;
+    const size_t cap = (size_t)sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    k_clear<<<(unsigned)blocks, 256, 0, stream>>>(list);
+}
+
+// ---------------------------------------------------------------------------
 // triangle setup
 // ---------------------------------------------------------------------------
 

