@@ -47,6 +47,7 @@ struct FrameReport {
     uint32_t pad;
     PassHeader shadow;
     PassHeader camera;
+    PassHeader blended;
 };
 
 }  // namespace
@@ -99,6 +100,10 @@ struct rz_ctx {
     cudaEvent_t objects_copied = nullptr;
     DrawRec* d_shadow_draws = nullptr;
     DrawRec* d_opaque_draws = nullptr;
+    DrawRec* d_blended_draws = nullptr;
+    DrawConsts* d_blended_consts = nullptr;
+    uint32_t blended_varying_base = 0;  // first varying record of the blended draws
+    uint2* d_color16 = nullptr;         // RGBA16F draw image (only with blended surfaces)
     uint32_t shadow_draw_count = 0, opaque_draw_count = 0, blended_draw_count = 0;
     uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0;
     float* d_shadow_mvp = nullptr;
@@ -108,8 +113,8 @@ struct rz_ctx {
     bool have_objects = false;
 
     // raster scratch
-    PassBuffers shadow_pass, camera_pass;
-    PassHeader* d_headers = nullptr;  // [0] shadow, [1] camera
+    PassBuffers shadow_pass, camera_pass, blended_pass;
+    PassHeader* d_headers = nullptr;  // [0] shadow, [1] camera, [2] blended
     uint32_t* d_error = nullptr;
     FrameReport* h_report = nullptr;  // pinned
     bool grow_records = false, grow_chunks = false;
@@ -225,7 +230,7 @@ SamplerBits sampler_bits(const rz_sampler& s) {
     return b | (wu << 4) | (wv << 6);
 }
 
-PassParams pass_params(rz_ctx* c, bool camera) {
+PassParams pass_params(rz_ctx* c, bool camera, bool blended = false) {
     PassParams p{};
     p.pos = c->d_pos;
     p.indices = c->d_indices;
@@ -233,7 +238,28 @@ PassParams pass_params(rz_ctx* c, bool camera) {
     p.cull_front = c->draw_config.cull_enabled ? 1 : 0;
     p.ccw_front = c->draw_config.reverse_winding_order_enabled ? 1 : 0;
     p.error_flags = c->d_error;
-    if (camera) {
+    if (blended) {
+        // blended list: cull none, no depth write, records kept in submission order
+        p.draws = c->d_blended_draws;
+        p.draw_count = c->blended_draw_count;
+        p.tri_total = c->blended_tris;
+        p.mvp = reinterpret_cast<const float*>(c->d_blended_consts);
+        p.mvp_stride = sizeof(DrawConsts) / sizeof(float);
+        p.width = (int)c->width;
+        p.height = (int)c->height;
+        p.cull_front = 0;
+        p.write_id = 1;
+        p.ordered = 1;
+        p.records = c->blended_pass.records;
+        p.record_capacity = c->blended_pass.record_capacity;
+        p.small_records = c->blended_pass.small_records;
+        p.small_capacity = c->blended_pass.small_capacity;
+        p.tile_status = c->blended_pass.tile_status;
+        p.chunk_map = c->blended_pass.chunk_map;
+        p.chunk_capacity = c->blended_pass.chunk_capacity;
+        p.header = c->d_headers + 2;
+        p.target = nullptr;
+    } else if (camera) {
         p.draws = c->d_opaque_draws;
         p.draw_count = c->opaque_draw_count;
         p.tri_total = c->opaque_tris;
@@ -296,7 +322,7 @@ ShadeParams shade_params(rz_ctx* c) {
     sh.draw_count = c->opaque_draw_count;
     sh.consts = c->d_camera_consts;
     sh.varyings = c->d_varyings;
-    sh.varying_count = c->varying_count;
+    sh.varying_count = c->blended_varying_base;  // the opaque draws' records
     sh.vertices = c->d_vertices;
     sh.indices = c->d_indices;
     sh.objects = c->d_objects;
@@ -309,6 +335,7 @@ ShadeParams shade_params(rz_ctx* c) {
     sh.scene = c->d_scene;
     sh.pcf_mode = c->draw_config.pcf_mode;
     sh.srgb_table = c->d_srgb;
+    sh.color16 = c->blended_tris ? c->d_color16 : nullptr;
     return sh;
 }
 
@@ -366,6 +393,23 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
         stamp(c, 5);
     }
     launch_vertex(sh, s);
+    if (c->blended_tris) {
+        ClearList bl{};
+        bl.ptr[0] = c->d_headers + 2;
+        bl.bytes[0] = sizeof(PassHeader);
+        bl.ptr[1] = c->blended_pass.tile_status;
+        bl.bytes[1] = (size_t)setup_ctas(c->blended_tris) * 8;
+        bl.count = 2;
+        launch_clear(bl, c->sm_count, s);
+        launch_prep_camera(c->d_blended_draws, c->blended_draw_count, c->d_objects, c->d_scene, c->d_blended_consts, s);
+        launch_setup(pass_params(c, true, true), s);
+        ShadeParams bs = sh;
+        bs.draws = c->d_blended_draws;
+        bs.draw_count = c->blended_draw_count;
+        bs.consts = c->d_blended_consts;
+        bs.varying_count = c->varying_count;
+        launch_vertex_range(bs, c->blended_varying_base, s);
+    }
 }
 
 // Enqueues one frame (everything after the scene/object uploads). With stage
@@ -391,11 +435,23 @@ int enqueue_frame(rz_ctx* c) {
         RZ_CUDA(c, cudaStreamWaitEvent(s, c->join, 0), "join");
     }
     launch_shade(sh, s);
+    if (c->blended_tris) {
+        BlendParams bp{};
+        bp.sh = sh;
+        bp.sh.draws = c->d_blended_draws;
+        bp.sh.draw_count = c->blended_draw_count;
+        bp.sh.consts = c->d_blended_consts;
+        bp.records = c->blended_pass.records;
+        bp.header = c->d_headers + 2;
+        bp.record_capacity = c->blended_pass.record_capacity;
+        bp.depth = c->d_depth;
+        launch_blend(bp, s);
+    }
     if (c->timing) stamp(c, 7);
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
     RZ_CUDA(c, cudaMemcpyAsync(&c->h_report->error_flags, c->d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
             "read error flags");
-    RZ_CUDA(c, cudaMemcpyAsync(&c->h_report->shadow, c->d_headers, 2 * sizeof(PassHeader), cudaMemcpyDeviceToHost, s),
+    RZ_CUDA(c, cudaMemcpyAsync(&c->h_report->shadow, c->d_headers, 3 * sizeof(PassHeader), cudaMemcpyDeviceToHost, s),
             "read pass headers");
     return RZ_OK;
 }
@@ -449,7 +505,7 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         cudaEventCreateWithFlags(&c->objects_copied, cudaEventDisableTiming) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (alloc_frame_buffers(c) != RZ_OK) return bail(RZ_ALLOCATION_FAILURE);
-    if (dalloc(&c->d_scene, 1) != cudaSuccess || dalloc(&c->d_headers, 2) != cudaSuccess ||
+    if (dalloc(&c->d_scene, 1) != cudaSuccess || dalloc(&c->d_headers, 3) != cudaSuccess ||
         dalloc(&c->d_error, 1) != cudaSuccess || dalloc(&c->d_srgb, 256) != cudaSuccess)
         return bail(RZ_ALLOCATION_FAILURE);
     if (cudaMallocHost(&c->h_scene, sizeof(rz_scene_data)) != cudaSuccess ||
@@ -503,6 +559,10 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_shadow_mvp);
     dfree(c->d_camera_consts);
     dfree(c->d_varyings);
+    dfree(c->d_blended_draws);
+    dfree(c->d_blended_consts);
+    dfree(c->d_color16);
+    free_pass(c->blended_pass);
     if (c->h_scene) cudaFreeHost(c->h_scene);
     if (c->h_report) cudaFreeHost(c->h_report);
     if (c->h_objects) cudaFreeHost(c->h_objects);
@@ -530,6 +590,10 @@ int rz_resize(rz_ctx* c, uint32_t width, uint32_t height) {
     c->height = height;
     const int rc = alloc_frame_buffers(c);
     if (rc != RZ_OK) return rc;
+    if (c->d_color16) {
+        dfree(c->d_color16);
+        RZ_CUDA(c, dalloc(&c->d_color16, (size_t)width * height), "RGBA16F draw image");
+    }
     if (c->have_objects) {
         const int r2 = size_pass(c, c->camera_pass, c->opaque_tris, default_stamp_hint(c->opaque_tris, width, height));
         if (r2 != RZ_OK) return r2;
@@ -675,7 +739,7 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     // src/Engine/Graphics.cpp:4693-4697: an empty scene is an invalid argument
     if (object_count == 0 || !objects || surface_count == 0 || !surfaces)
         return fail(c, RZ_INVALID_ARGUMENT, "empty scene");
-    std::vector<DrawRec> shadow, opaque;
+    std::vector<DrawRec> shadow, opaque, blended;
     uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0, blended_draws = 0, varyings = 0;
     const uint32_t mesh_count = (uint32_t)(c->mesh_table.size() / 4);
     for (uint32_t i = 0; i < surface_count; ++i) {
@@ -700,8 +764,11 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
         if ((uint64_t)shadow_tris + d.tri_count >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many triangles");
         shadow_tris += d.tri_count;
         if (s.blended) {
+            d.tri_base = blended_tris;
+            d.vertex_count = mt[1];
             blended_tris += d.tri_count;
             ++blended_draws;
+            blended.push_back(d);
         } else {
             d.tri_base = opaque_tris;
             d.varying_base = varyings;
@@ -712,7 +779,13 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
             opaque_tris += d.tri_count;
         }
     }
-    if (blended_draws) return fail(c, RZ_INVALID_ARGUMENT, "blended surfaces are not supported by this build");
+    // varying records of the blended draws follow the opaque ones
+    const uint32_t blended_varying_base = varyings;
+    for (DrawRec& d : blended) {
+        if ((uint64_t)varyings + d.vertex_count >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many vertices");
+        d.varying_base = varyings;
+        varyings += d.vertex_count;
+    }
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graph(c);
@@ -722,6 +795,9 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     dfree(c->d_shadow_mvp);
     dfree(c->d_camera_consts);
     dfree(c->d_varyings);
+    dfree(c->d_blended_draws);
+    dfree(c->d_blended_consts);
+    dfree(c->d_color16);
     if (c->h_objects) cudaFreeHost(c->h_objects);
     c->h_objects = nullptr;
     RZ_CUDA(c, dalloc(&c->d_objects, object_count), "object buffer");
@@ -730,12 +806,18 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     RZ_CUDA(c, dalloc(&c->d_opaque_draws, std::max<size_t>(opaque.size(), 1)), "opaque draw list");
     RZ_CUDA(c, dalloc(&c->d_shadow_mvp, std::max<size_t>(shadow.size(), 1) * 16), "shadow matrices");
     RZ_CUDA(c, dalloc(&c->d_camera_consts, std::max<size_t>(opaque.size(), 1)), "camera constants");
+    RZ_CUDA(c, dalloc(&c->d_blended_draws, std::max<size_t>(blended.size(), 1)), "blended draw list");
+    RZ_CUDA(c, dalloc(&c->d_blended_consts, std::max<size_t>(blended.size(), 1)), "blended constants");
+    if (!blended.empty())
+        RZ_CUDA(c, dalloc(&c->d_color16, (size_t)c->width * c->height), "RGBA16F draw image");
     RZ_CUDA(c, dalloc(&c->d_varyings, std::max<size_t>(varyings, 1) * 8), "varying records");
     RZ_CUDA(c, cudaMemcpy(c->d_objects, objects, (size_t)object_count * sizeof(rz_object), cudaMemcpyHostToDevice), "upload objects");
     if (!shadow.empty())
         RZ_CUDA(c, cudaMemcpy(c->d_shadow_draws, shadow.data(), shadow.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
     if (!opaque.empty())
         RZ_CUDA(c, cudaMemcpy(c->d_opaque_draws, opaque.data(), opaque.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
+    if (!blended.empty())
+        RZ_CUDA(c, cudaMemcpy(c->d_blended_draws, blended.data(), blended.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
     c->object_count = object_count;
     c->shadow_draw_count = (uint32_t)shadow.size();
     c->opaque_draw_count = (uint32_t)opaque.size();
@@ -744,6 +826,11 @@ int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, c
     c->opaque_tris = opaque_tris;
     c->blended_tris = blended_tris;
     c->varying_count = varyings;
+    c->blended_varying_base = blended_varying_base;
+    if (blended_tris) {
+        const int rb = size_pass(c, c->blended_pass, blended_tris, default_stamp_hint(blended_tris, c->width, c->height));
+        if (rb != RZ_OK) return rb;
+    }
     int rc = size_pass(c, c->shadow_pass, shadow_tris, default_stamp_hint(shadow_tris, c->shadow_size, c->shadow_size));
     if (rc != RZ_OK) return rc;
     rc = size_pass(c, c->camera_pass, opaque_tris, default_stamp_hint(opaque_tris, c->width, c->height));
@@ -824,6 +911,7 @@ int rz_render(rz_ctx* c) {
         };
         int rc = grow(c->shadow_pass, c->h_report->shadow);
         if (rc == RZ_OK) rc = grow(c->camera_pass, c->h_report->camera);
+        if (rc == RZ_OK && c->blended_tris) rc = grow(c->blended_pass, c->h_report->blended);
         c->grow_records = c->grow_chunks = false;
         if (rc != RZ_OK) return rc;
     }
@@ -928,7 +1016,8 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->error_flags;
     // clears (2) + prep (1) + prep_camera (1) + setup/raster per pass with triangles + vertex + shade
-    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u + (c->varying_count ? 1u : 0u);
+    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u + (c->varying_count ? 1u : 0u) +
+                           (c->blended_tris ? 5u : 0u);
     return RZ_OK;
 }
 

@@ -111,6 +111,7 @@ struct PassParams {
     int bias_enabled;
     float bias_constant, bias_clamp, bias_slope;
     int write_id;             // 1: camera pass (64-bit depth|id keys); 0: shadow (depth only)
+    int ordered;              // 1: keep every record in submission order (blended list)
     TriRecord* records;       // large records (stamp-balanced raster)
     uint32_t record_capacity;
     TriRecord* small_records; // small records (one lane each)
@@ -147,6 +148,16 @@ struct ShadeParams {
     const rz_scene_data* scene;
     uint32_t pcf_mode;
     const float* srgb_table;      // 256 entries
+    uint2* color16;               // if set: k_shade stores the RGBA16F draw image here instead of RGBA8
+};
+
+// The blended list (src/Engine/Graphics.cpp:5654-5691) over the opaque result.
+struct BlendParams {
+    ShadeParams sh;               // blended draws, their constants and varyings
+    const TriRecord* records;     // setup records of the blended triangles, in submission order
+    const PassHeader* header;
+    uint32_t record_capacity;
+    const float* depth;           // opaque depth
 };
 
 // Up to four buffers to zero in one launch (16-byte stores, byte tail).
@@ -165,6 +176,10 @@ void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objec
 void launch_setup(const PassParams& p, cudaStream_t stream);
 void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream);
 void launch_vertex(const ShadeParams& p, cudaStream_t stream);
+// k_vertex over the varying records [first, varying_count) of the draws in p
+// (whose varying_base values start at `first`).
+void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stream);
+void launch_blend(const BlendParams& p, cudaStream_t stream);
 void launch_shade(const ShadeParams& p, cudaStream_t stream);
 int setup_ctas(uint32_t tri_total);
 

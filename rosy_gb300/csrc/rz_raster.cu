@@ -205,7 +205,7 @@ __device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV&
     const uint32_t nsy = (uint32_t)((py1 - py0) / kStampH + 1);
     r.stamps = nsx * nsy;
     r.stamp_offset = 0;
-    const bool small = (maxX - minX) <= kSmallExtent * 256 && (maxY - minY) <= kSmallExtent * 256;
+    const bool small = !P.ordered && (maxX - minX) <= kSmallExtent * 256 && (maxY - minY) <= kSmallExtent * 256;
     return small ? 2 : 1;
 }
 

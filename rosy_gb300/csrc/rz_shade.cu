@@ -622,9 +622,9 @@ __device__ __forceinline__ uint32_t find_draw_by_varying(const DrawRec* __restri
     return lo;
 }
 
-// The vertex stage, once per (draw, mesh vertex).
-__global__ void __launch_bounds__(256) k_vertex(ShadeParams P) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// The vertex stage, once per (draw, mesh vertex): records [first, varying_count).
+__global__ void __launch_bounds__(256) k_vertex(ShadeParams P, uint32_t first) {
+    const uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.varying_count) return;
     const uint32_t d = find_draw_by_varying(P.draws, P.draw_count, i);
     const DrawRec dr = P.draws[d];
@@ -648,8 +648,13 @@ __global__ void __launch_bounds__(256) k_vertex(ShadeParams P) {
 }
 
 void launch_vertex(const ShadeParams& p, cudaStream_t stream) {
-    if (p.varying_count == 0) return;
-    k_vertex<<<(p.varying_count + 255) / 256, 256, 0, stream>>>(p);
+    if (p.varying_count == 0 || p.draw_count == 0) return;
+    k_vertex<<<(p.varying_count + 255) / 256, 256, 0, stream>>>(p, 0u);
+}
+
+void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stream) {
+    if (p.varying_count <= first || p.draw_count == 0) return;
+    k_vertex<<<(p.varying_count - first + 255) / 256, 256, 0, stream>>>(p, first);
 }
 
 // Shade triangle `tri` (pass-global id) at pixel (px, py) from the varying
@@ -766,18 +771,139 @@ __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
             for (int k = 0; k < 4; ++k) col[k] = o[k];
         }
     }
+    P.depth[p] = __uint_as_float((uint32_t)(key >> 32));
+    if (P.color16) {  // blended surfaces follow: keep the RGBA16F draw image
+        const __half2 rg = __floats2half2_rn(col[0], col[1]), ba = __floats2half2_rn(col[2], col[3]);
+        P.color16[p] = make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&ba));
+        return;
+    }
     const uint32_t r = encode_srgb8(half_round(col[0]));
     const uint32_t g = encode_srgb8(half_round(col[1]));
     const uint32_t b = encode_srgb8(half_round(col[2]));
     const uint32_t a = encode_unorm8(half_round(col[3]));
     P.color[p] = r | (g << 8) | (b << 16) | (a << 24);
-    P.depth[p] = __uint_as_float((uint32_t)(key >> 32));
 }
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
     const dim3 block(16, 16);
     const dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
     k_shade<<<grid, block, 0, stream>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// blended list
+// ---------------------------------------------------------------------------
+
+// One CTA per 16x16 tile. The blended records overlapping the tile are
+// compacted into shared memory in submission order, then every pixel walks
+// them in that order: coverage with the raster's integer edge test, the
+// GREATER_OR_EQUAL test against the opaque depth (no write), fragmentMain
+// (discard honoured), and SRC_ALPHA / ONE_MINUS_SRC_ALPHA on colour, ONE / ZERO
+// on alpha, rounded to the RGBA16F draw image after each blend
+// (src/Engine/Graphics.cpp:5654-5691). Then the sRGB blit.
+constexpr int kBlendBatch = 1024;
+
+__global__ void __launch_bounds__(256) k_blend(BlendParams B) {
+    __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ uint32_t s_list[kBlendBatch];
+    __shared__ uint32_t s_count[256 / 32 + 1];
+    const ShadeParams& P = B.sh;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    s_srgb[tid] = P.srgb_table[tid];
+    s_unorm[tid] = (float)tid / 255.0f;
+    const int tx0 = blockIdx.x * 16, ty0 = blockIdx.y * 16;
+    const int px = tx0 + threadIdx.x, py = ty0 + threadIdx.y;
+    const bool inside = px < P.width && py < P.height;
+    const size_t p = inside ? (size_t)py * P.width + px : 0;
+    float col[4] = {0.f, 0.f, 0.f, 0.f};
+    float dst_depth = 0.f;
+    if (inside) {
+        const uint2 c = P.color16[p];
+        const __half2 rg = *reinterpret_cast<const __half2*>(&c.x), ba = *reinterpret_cast<const __half2*>(&c.y);
+        col[0] = __low2float(rg);
+        col[1] = __high2float(rg);
+        col[2] = __low2float(ba);
+        col[3] = __high2float(ba);
+        dst_depth = B.depth[p];
+    }
+    const Sampler smp{&P, s_srgb, s_unorm};
+    const uint32_t n = min(B.header->records, B.record_capacity);
+    const int lane = tid & 31, warp = tid >> 5;
+    for (uint32_t start = 0; start < n; start += kBlendBatch) {
+        // ordered compaction of the records whose box meets this tile (4 per thread)
+        uint32_t mask = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t r = start + 4 * tid + k;
+            if (r < n) {
+                const TriRecord& rec = B.records[r];
+                const int bx0 = rec.p0 & 0xffff, by0 = rec.p0 >> 16, bx1 = rec.p1 & 0xffff, by1 = rec.p1 >> 16;
+                if (bx1 >= tx0 && bx0 <= tx0 + 15 && by1 >= ty0 && by0 <= ty0 + 15) mask |= 1u << k;
+            }
+        }
+        const uint32_t cnt = __popc(mask);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        __syncthreads();
+        if (lane == 31) s_count[warp] = incl;
+        __syncthreads();
+        uint32_t base = 0, total = 0;
+        for (int w = 0; w < 8; ++w) {
+            if (w < warp) base += s_count[w];
+            total += s_count[w];
+        }
+        uint32_t pos = base + incl - cnt;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (mask & (1u << k)) s_list[pos++] = start + 4 * tid + k;
+        __syncthreads();
+        if (inside) {
+            const int32_t PX = px * 256 + 128, PY = py * 256 + 128;
+            for (uint32_t j = 0; j < total; ++j) {
+                const TriRecord& rec = B.records[s_list[j]];
+                const int bx0 = rec.p0 & 0xffff, by0 = rec.p0 >> 16, bx1 = rec.p1 & 0xffff, by1 = rec.p1 >> 16;
+                if (px < bx0 || px > bx1 || py < by0 || py > by1) continue;
+                const int32_t X[3] = {rec.X0, rec.X1, rec.X2}, Y[3] = {rec.Y0, rec.Y1, rec.Y2};
+                bool in = true;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int a = (i + 1) % 3, b = (i + 2) % 3;
+                    const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+                    const bool tl = dy < 0 || (dy == 0 && dx > 0);
+                    const int64_t E = (int64_t)dx * (int64_t)(PY - Y[a]) - (int64_t)dy * (int64_t)(PX - X[a]);
+                    in = in && (E > 0 || (E == 0 && tl));
+                }
+                if (!in) continue;
+                float z = fmaf(rec.dzdx, (float)(PX - rec.X0), fmaf(rec.dzdy, (float)(PY - rec.Y0), rec.z0));
+                if (!(z > 0.0f)) z = 0.0f;
+                if (z > 1.0f) z = 1.0f;
+                if (!(z >= dst_depth)) continue;
+                float s4[4];
+                if (!shade_pixel(P, *P.scene, smp, rec.id - 1u, px, py, s4)) continue;
+                const float a = s4[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) col[k] = half_round(s4[k] * a + col[k] * (1.0f - a));
+                col[3] = half_round(a);
+            }
+        }
+        __syncthreads();
+    }
+    if (!inside) return;
+    const uint32_t r = encode_srgb8(col[0]);
+    const uint32_t g = encode_srgb8(col[1]);
+    const uint32_t b = encode_srgb8(col[2]);
+    const uint32_t a = encode_unorm8(col[3]);
+    P.color[p] = r | (g << 8) | (b << 16) | (a << 24);
+}
+
+void launch_blend(const BlendParams& p, cudaStream_t stream) {
+    const dim3 block(16, 16);
+    const dim3 grid((p.sh.width + 15) / 16, (p.sh.height + 15) / 16);
+    k_blend<<<grid, block, 0, stream>>>(p);
 }
 
 }  // namespace rz

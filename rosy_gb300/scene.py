@@ -535,3 +535,50 @@ def tiny(seed: int = 0) -> Scene:
     """A few hundred triangles at 96x64 for fast tests."""
     return random_triangles(seed=seed, triangles=256, width=96, height=64, shadow_size=128,
                             texture_size=64)
+
+
+def with_blended(s: Scene, fraction: float = 0.5, alpha: float = 0.6, mask_cutoff: float | None = None,
+                 seed: int = 0) -> Scene:
+    """The same scene with the trailing `fraction` of every surface's triangles
+    split off into a blended surface (alpha_mode 2, base colour alpha `alpha`),
+    or, with `mask_cutoff`, an alpha-mask surface (alpha_mode 1) whose colour
+    texture alpha varies so that some fragments are discarded."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mats = [m for m in s.materials]
+    textures = list(s.textures)
+    new_mats = []
+    for m in s.materials:
+        b = m.copy()
+        b["alpha_mode"] = 1 if mask_cutoff is not None else 2
+        b["alpha_cutoff"] = mask_cutoff if mask_cutoff is not None else 0.0
+        b["base_color_factor"][3] = alpha
+        if mask_cutoff is not None and b["color_image_index"] != U32_MAX:
+            t = textures[int(b["color_image_index"])]
+            tex = t.texels.copy().reshape(-1, 4)
+            tex[:, 3] = rng.integers(0, 256, len(tex))
+            textures.append(Texture(t.width, t.height, t.levels, t.image_type, tex.reshape(-1)))
+            b["color_image_index"] = len(textures) - 1
+        new_mats.append(b)
+    materials = np.concatenate([np.asarray(mats, MATERIAL_DTYPE).reshape(-1), np.asarray(new_mats, MATERIAL_DTYPE).reshape(-1)])
+    nm = len(s.materials)
+    surfs = []
+    for sf in s.surfaces:
+        tris = int(sf["index_count"]) // 3
+        keep = tris - int(tris * fraction)
+        a = sf.copy()
+        a["index_count"] = keep * 3
+        surfs.append(a)
+        if keep < tris:
+            b = sf.copy()
+            b["start_index"] = sf["start_index"] + keep * 3
+            b["index_count"] = (tris - keep) * 3
+            b["blended"] = 1
+            if sf["material_index"] != U32_MAX:
+                b["material_index"] = sf["material_index"] + nm
+            surfs.append(b)
+    out = Scene(**{k: getattr(s, k) for k in s.__dataclass_fields__})
+    out.surfaces = np.asarray(surfs, SURFACE_DTYPE).reshape(-1)
+    out.materials = materials
+    out.textures = textures
+    out.name = s.name + ("_mask" if mask_cutoff is not None else "_blended")
+    return out

@@ -89,6 +89,15 @@ def variants():
         s.scene["flip_lights"] = (0, 1, 0, 1)
         return s
     v["world_space_flips"] = world_space
+
+    v["blended_random_triangles"] = lambda: sc.with_blended(
+        sc.random_triangles(seed=12, triangles=600, width=256, height=160, shadow_size=256, texture_size=64), 0.5)
+    v["blended_scene_scale"] = lambda: sc.with_blended(
+        sc.scene_scale(seed=5, meshes=6, triangles_per_mesh=512, materials=3, texture_size=64, width=320, height=180,
+                       shadow_size=512, frames=1), 0.3, alpha=0.45)
+    v["alpha_mask"] = lambda: sc.with_blended(
+        sc.random_triangles(seed=13, triangles=400, width=200, height=120, shadow_size=256, texture_size=32), 0.5,
+        alpha=1.0, mask_cutoff=0.5)
     return v
 
 

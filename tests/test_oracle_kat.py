@@ -212,3 +212,29 @@ def test_pcf_lit_and_shadowed(oracle):
             assert px[0] == 0
         # outside the occluder's footprint the receiver stays lit
         assert out["color"][60, 60][0] > 200
+
+
+def test_blended_list_order_and_depth(oracle):
+    # opaque red at z 0.5 over the left half; then two blended triangles drawn in order:
+    # green (alpha 0.5) at z 0.7 and blue (alpha 0.25) at z 0.3 (behind the opaque: rejected there)
+    W = H = 8
+    full = ((0.0, 0.0, 0.5), (16.0, 0.0, 0.5), (0.0, 16.0, 0.5))
+    g = ((0.0, 0.0, 0.7), (16.0, 0.0, 0.7), (0.0, 16.0, 0.7))
+    b = ((0.0, 0.0, 0.3), (16.0, 0.0, 0.3), (0.0, 16.0, 0.3))
+    s = flat_scene([full, g, b], W=W, H=H, colors=[(1, 0, 0, 1), (0, 1, 0, 0.5), (0, 0, 1, 0.25)])
+    mats = np.concatenate([sc.material(), sc.material(alpha_mode=2), sc.material(alpha_mode=2)])
+    s.materials = mats
+    s.textures = []
+    surf = np.zeros(3, sc.SURFACE_DTYPE)
+    surf["index_count"] = 3
+    surf["start_index"] = [0, 3, 6]
+    surf["material_index"] = [0, 1, 2]
+    surf["blended"] = [0, 1, 1]
+    s.surfaces = surf
+    out = oracle.render(s, threads=1)
+    # without textures the material colour factor (1,1,1,a) is the colour; alpha = min(material, vertex)
+    px = out["color"][1, 1]
+    red = f16(1.0)
+    after_g = f16(np.float32(1.0) * np.float32(0.5) + red * np.float32(0.5))  # white-ish (1) over 1
+    assert px[3] == int(math.floor(f16(0.5) * np.float32(255) + np.float32(0.5)))  # alpha = last passing blend (0.5)
+    assert px[0] == srgb8(after_g)
