@@ -87,8 +87,9 @@ struct PassHeader {
     uint32_t records_needed;  // large records the frame produced (may exceed the capacity)
     uint32_t small_records;   // small records appended (may exceed the capacity)
     uint32_t small_cursor;    // raster: next small record to take
-    uint32_t chunk_cursor;    // raster: next chunk to take
-    uint32_t pad[3];
+    uint32_t done;            // setup CTAs finished (unordered passes)
+    uint32_t pad;
+    uint64_t alloc;           // unordered passes: (records << 40) | stamps allocated so far
 };
 static_assert(sizeof(PassHeader) == 48, "PassHeader layout");
 

@@ -404,9 +404,35 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     const uint32_t small_excl = small_prefix + small_incl - cnt.small;
     if (threadIdx.x == 32) s_small_base = small_total ? atomicAdd(&P.header->small_records, small_total) : 0u;
 
+    // Unordered passes (shadow, opaque camera pass): the depth test is an atomic
+    // max, so records may land in any order; one 64-bit atomicAdd per CTA
+    // allocates its record slots and its stamp range. The ordered blended list
+    // keeps submission order with a decoupled look-back instead.
+    if (!P.ordered) {
+        if (threadIdx.x == 0) {
+            const uint64_t old = atomicAdd(reinterpret_cast<unsigned long long*>(&P.header->alloc), (unsigned long long)total);
+            s_base_recs = old >> kStampBits;
+            s_base_stamps = old & kStampMask;
+            __threadfence();
+            if (atomicAdd(&P.header->done, 1u) == gridDim.x - 1) {
+                // last CTA: publish the totals for the raster and the host
+                const uint64_t fin = atomicAdd(reinterpret_cast<unsigned long long*>(&P.header->alloc), 0ull);
+                const uint64_t recs = fin >> kStampBits, st = fin & kStampMask;
+                uint64_t chunks = (st + kChunkStamps - 1) / kChunkStamps;
+                if (chunks > P.chunk_capacity) {
+                    chunks = P.chunk_capacity;
+                    atomicOr(P.error_flags, kErrStampOverflow);
+                }
+                P.header->records = (uint32_t)(recs < (uint64_t)P.record_capacity ? recs : (uint64_t)P.record_capacity);
+                P.header->stamps = st;
+                P.header->chunks = (uint32_t)chunks;
+                P.header->records_needed = recs > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)recs;
+            }
+        }
+    }
     // Decoupled look-back (warp 0): publish this tile's aggregate, then sum the
     // predecessors' values 32 at a time until an inclusive prefix is found.
-    if (warp == 0) {
+    if (P.ordered && warp == 0) {
         const uint64_t agg_recs = total >> kStampBits, agg_stamps = total & kStampMask;
         volatile unsigned long long* status = reinterpret_cast<volatile unsigned long long*>(P.tile_status);
         uint64_t pre_recs = 0, pre_stamps = 0;
@@ -553,10 +579,6 @@ struct LargeRecord {
     int32_t X[3], Y[3];
     int32_t dx[3], dy[3];
     uint32_t tl_bias[3];  // 0 on top-left edges, 1 otherwise
-    // generic path only (not medium):
-    int64_t c[3];         // E' at sub-pixel (0, 0): E'(P) = c + dx*PY - dy*PX
-    int64_t max_off[3], min_off[3];  // range of the lane offsets over the stamp
-    bool short_edges;     // all |dx|, |dy| < 2^18: partial-edge values and lane offsets fit in 32 bits
     bool medium;          // extent <= kMediumExtent px and near_origin: incremental 32-bit walk
     bool near_origin;     // |PX - X0|, |PY - Y0| < 2^23 over the box: float offsets exact
     int32_t X0, Y0;
@@ -603,44 +625,53 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L)
     const int32_t ex = max(L.X[0], max(L.X[1], L.X[2])) - min(L.X[0], min(L.X[1], L.X[2]));
     const int32_t ey = max(L.Y[0], max(L.Y[1], L.Y[2])) - min(L.Y[0], min(L.Y[1], L.Y[2]));
     L.medium = L.near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
-    if (L.medium) return;
+}
+
+// Edge constants of the generic (64-bit) path.
+struct GenericEdges {
+    int64_t c[3];                    // E' at sub-pixel (0, 0): E'(P) = c + dx*PY - dy*PX
+    int64_t max_off[3], min_off[3];  // range of the lane offsets over the stamp
+    bool short_edges;                // all |dx|, |dy| < 2^18: partial-edge values and lane offsets fit in 32 bits
+};
+
+__device__ __forceinline__ void generic_edges(const LargeRecord& L, GenericEdges& G) {
     bool short_edges = true;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const int a = (i + 1) % 3;
         const int32_t dx = L.dx[i], dy = L.dy[i];
-        L.c[i] = (int64_t)dy * L.X[a] - (int64_t)dx * L.Y[a] - L.tl_bias[i];
-        L.max_off[i] = (dx > 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy < 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
-        L.min_off[i] = (dx < 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy > 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
+        G.c[i] = (int64_t)dy * L.X[a] - (int64_t)dx * L.Y[a] - L.tl_bias[i];
+        G.max_off[i] = (dx > 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy < 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
+        G.min_off[i] = (dx < 0 ? (int64_t)dx * ((kStampH - 1) * 256) : 0) + (dy > 0 ? -(int64_t)dy * ((kStampW - 1) * 256) : 0);
         short_edges = short_edges && abs(dx) < (1 << 18) && abs(dy) < (1 << 18);
     }
-    L.short_edges = short_edges;
+    G.short_edges = short_edges;
 }
 
 // Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
 template <bool kWriteId>
-__device__ __forceinline__ void raster_stamp(const PassParams& P, const LargeRecord& L, uint32_t sx, uint32_t sy, int lx,
-                                             int ly) {
+__device__ __forceinline__ void raster_stamp(const PassParams& P, const LargeRecord& L, const GenericEdges& G, uint32_t sx,
+                                             uint32_t sy, int lx, int ly) {
     const int sx0 = L.px0 + (int)sx * kStampW, sy0 = L.py0 + (int)sy * kStampH;
     const int32_t PXo = sx0 * 256 + 128, PYo = sy0 * 256 + 128;
     int64_t eo[3];
     bool reject = false, accept = true;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        eo[i] = L.c[i] + (int64_t)L.dx[i] * PYo - (int64_t)L.dy[i] * PXo;
-        reject |= eo[i] + L.max_off[i] < 0;
-        accept &= eo[i] + L.min_off[i] >= 0;
+        eo[i] = G.c[i] + (int64_t)L.dx[i] * PYo - (int64_t)L.dy[i] * PXo;
+        reject |= eo[i] + G.max_off[i] < 0;
+        accept &= eo[i] + G.min_off[i] >= 0;
     }
     if (reject) return;
     const int px = sx0 + lx, py = sy0 + ly;
     bool in = px <= L.px1 && py <= L.py1;
     if (!accept) {
-        if (L.short_edges) {
+        if (G.short_edges) {
             // partial edges: |eo| < 2^30 and the lane offset < 2^30, so 32 bits suffice
             int32_t hi = 0;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                const bool edge_accept = eo[i] + L.min_off[i] >= 0;
+                const bool edge_accept = eo[i] + G.min_off[i] >= 0;
                 const int32_t e = (int32_t)eo[i] + L.dx[i] * (ly * 256) - L.dy[i] * (lx * 256);
                 hi |= edge_accept ? 0 : e;
             }
@@ -759,35 +790,36 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
         uint64_t s = (uint64_t)k * kChunkStamps;
         const uint64_t s_end = (s + kChunkStamps < total) ? (s + kChunkStamps) : total;
         uint32_t r = P.chunk_map[k];
-        if (r >= P.record_capacity) continue;
-        LargeRecord L;
-        load_large(P.records + r, L);
-        if (s < L.begin) {  // cannot happen with a consistent chunk map
-            atomicOr(P.error_flags, kErrStampOverflow);
-            continue;
-        }
-        uint32_t i = (uint32_t)(s - L.begin);
-        uint32_t sy = i / L.nsx, sx = i - sy * L.nsx;
-        MediumWalk w;
-        if (L.medium) medium_start(L, sx, sy, lx, ly, w);
         while (s < s_end) {
-            if (s >= L.end) {
-                if (++r >= P.record_capacity) break;
-                load_large(P.records + r, L);
-                sx = 0;
-                sy = 0;
-                if (L.medium) medium_start(L, 0, 0, lx, ly, w);
+            if (r >= P.record_capacity) break;
+            LargeRecord L;
+            load_large(P.records + r, L);
+            if (s < L.begin || s >= L.end) {  // cannot happen with a consistent chunk map
+                atomicOr(P.error_flags, kErrStampOverflow);
+                break;
             }
+            const uint64_t seg_end = s_end < L.end ? s_end : L.end;
+            const uint32_t n = (uint32_t)(seg_end - s);
+            const uint32_t i = (uint32_t)(s - L.begin);
+            const uint32_t sy = i / L.nsx, sx = i - sy * L.nsx;
             if (L.medium) {
-                medium_step<kWriteId>(P, L, w);
+                MediumWalk w;
+                medium_start(L, sx, sy, lx, ly, w);
+                for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId>(P, L, w);
             } else {
-                raster_stamp<kWriteId>(P, L, sx, sy, lx, ly);
-                if (++sx == L.nsx) {
-                    sx = 0;
-                    ++sy;
+                GenericEdges G;
+                generic_edges(L, G);
+                uint32_t x = sx, y = sy;
+                for (uint32_t j = 0; j < n; ++j) {
+                    raster_stamp<kWriteId>(P, L, G, x, y, lx, ly);
+                    if (++x == L.nsx) {
+                        x = 0;
+                        ++y;
+                    }
                 }
             }
-            ++s;
+            s = seg_end;
+            ++r;
         }
     }
 }

@@ -632,7 +632,15 @@ __global__ void __launch_bounds__(256) k_vertex(ShadeParams P, uint32_t first) {
     const rz_object& gd = P.objects[dr.object];
     const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
     const bool has_nm = md ? (md->tex[1] != RZ_INVALID_INDEX) : false;
-    const rz_vertex& v = P.vertices[dr.vertex_base + (i - dr.varying_base)];
+    // the 64-byte vertex record as four 16-byte loads
+    const float4* vp = reinterpret_cast<const float4*>(P.vertices + dr.vertex_base + (i - dr.varying_base));
+    const float4 q0 = __ldg(vp), q1 = __ldg(vp + 1), q2 = __ldg(vp + 2), q3 = __ldg(vp + 3);
+    rz_vertex v;
+    v.position[0] = q0.x; v.position[1] = q0.y; v.position[2] = q0.z;
+    v.normal[0] = q0.w; v.normal[1] = q1.x; v.normal[2] = q1.y;
+    v.tangent[0] = q1.z; v.tangent[1] = q1.w; v.tangent[2] = q2.x; v.tangent[3] = q2.y;
+    v.color[0] = q2.z; v.color[1] = q2.w; v.color[2] = q3.x; v.color[3] = q3.y;
+    v.uv[0] = q3.z; v.uv[1] = q3.w;
     VsOut o;
     vertex_main(*P.scene, gd, dc, md != nullptr, has_nm, v, o);
     const float4 clip = transform_point(dc.mvp, v.position[0], v.position[1], v.position[2]);
