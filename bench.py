@@ -45,6 +45,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def measured_traffic(stage: str):
+    """DRAM bytes per launch of a kernel from the committed ncu summary of this
+    workload (profiles/dram_traffic_scene_scale_1080p.json), or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_scene_scale_1080p.json")
+    try:
+        return json.load(open(p))["dram_bytes_per_launch"].get(stage)
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def make_scene(name: str):
     from rosy_gb300 import scene as sc
 
@@ -320,7 +330,9 @@ def run_rz(args):
                     "frac": round(ach / hbm, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                     if peak_kind == "measured" else "fallback 6.8 TB/s",
                     "algorithmic_bytes_per_launch": int(b), "ms_per_launch": round(stage_ms[stage], 5),
-                    "traffic": None}
+                    "traffic": measured_traffic(stage) if args.config == "scene_scale" else None,
+                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                      "profiles/dram_traffic_scene_scale_1080p.json"}
     parity = None
     if rank == 0 and extra.get("oracle_ids") is not None:
         parity = bool(np.array_equal(out0["ids"], extra["oracle_ids"]))
