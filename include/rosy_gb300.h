@@ -228,7 +228,8 @@ typedef struct rz_frame_out {
     uint32_t width;
     uint32_t height;
     uint32_t shadow_map_size;
-    uint32_t reserved;
+    uint32_t triangle_id_base; /* ids in the visibility buffer are triangle_id_base + (index of the
+                                  triangle in the view's opaque list) + 1; 0 for view 0 */
 } rz_frame_out;
 
 /* Counters of the last frame (graphics_stats, src/Engine/DebugUI.h:7-13). */
@@ -306,6 +307,42 @@ int rz_read_frame(struct rz_ctx* ctx, void* color_host, size_t color_bytes,
 
 /* Counters of the last completed frame (call after rz_sync). */
 int rz_get_stats(struct rz_ctx* ctx, rz_stats* out);
+
+/* Batched views. A context holds scenes and views: scene 0 is the one
+ * rz_set_asset / rz_set_objects define, rz_add_scene appends more (each with its
+ * own asset, objects and surfaces), and rz_set_views replaces the view list
+ * (initially one view of scene 0 with rz_config's extent). rz_render renders
+ * every view: each stage of the frame is one launch over all views, captured in
+ * one CUDA graph. This has no counterpart in the reference, which renders one
+ * camera per frame; it is the batching of many views of uneven size. */
+typedef struct rz_view {
+    uint32_t scene;            /* scene index */
+    uint32_t width;            /* colour/depth extent */
+    uint32_t height;
+    uint32_t shadow_map_size;  /* the view's own square shadow map */
+    rz_draw_config draw_config;
+} rz_view;
+
+/* Appends a scene (asset + objects + surfaces, as rz_set_asset + rz_set_objects
+ * take them) and returns its index in *scene_index. */
+int rz_add_scene(struct rz_ctx* ctx,
+                 const rz_mesh* meshes, uint32_t mesh_count,
+                 const rz_material* materials, uint32_t material_count,
+                 const rz_texture* textures, uint32_t texture_count,
+                 const rz_sampler* samplers, uint32_t sampler_count,
+                 const rz_object* objects, uint32_t object_count,
+                 const rz_surface* surfaces, uint32_t surface_count,
+                 uint32_t* scene_index);
+
+/* Replaces the list of views rendered by rz_render. Views keep the scene
+ * constants already given to the same index. */
+int rz_set_views(struct rz_ctx* ctx, const rz_view* views, uint32_t count);
+
+/* Scene constants (gpu_scene_data) of one view for the next frame; rz_update is view 0. */
+int rz_update_view(struct rz_ctx* ctx, uint32_t view, const rz_scene_data* scene);
+
+/* Device pointers of one view's frame buffers (rz_get_frame is view 0). */
+int rz_get_view_frame(struct rz_ctx* ctx, uint32_t view, rz_frame_out* out);
 
 /* Frame stages timed by rz_get_stage_times (CUDA events on the context's stream). */
 #define RZ_STAGE_SHADOW_CLEAR 0u  /* shadow-map clear */

@@ -29,10 +29,22 @@ class RzConfig(C.Structure):
                 ("reserved", C.c_uint32 * 2)]
 
 
+class RzDrawConfig(C.Structure):
+    _fields_ = [("cull_enabled", C.c_uint32), ("reverse_winding_order_enabled", C.c_uint32),
+                ("depth_bias_enabled", C.c_uint32), ("depth_bias_constant", C.c_float),
+                ("depth_bias_clamp", C.c_float), ("depth_bias_slope_factor", C.c_float),
+                ("pcf_mode", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class RzView(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("shadow_map_size", C.c_uint32), ("draw_config", RzDrawConfig)]
+
+
 class RzFrameOut(C.Structure):
     _fields_ = [("color_rgba8", C.c_void_p), ("depth_f32", C.c_void_p), ("visibility_u64", C.c_void_p),
                 ("shadow_map_f32", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
-                ("shadow_map_size", C.c_uint32), ("reserved", C.c_uint32)]
+                ("shadow_map_size", C.c_uint32), ("triangle_id_base", C.c_uint32)]
 
 
 class RzStats(C.Structure):
@@ -43,6 +55,7 @@ class RzStats(C.Structure):
 
 
 assert C.sizeof(RzVertex) == 64
+assert C.sizeof(RzView) == 48
 assert C.sizeof(RzMesh) == 24
 assert C.sizeof(RzTexture) == 24
 

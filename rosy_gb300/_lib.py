@@ -25,7 +25,8 @@ EXPORTS = [
     "rz_create", "rz_destroy", "rz_resize", "rz_set_asset", "rz_set_objects", "rz_update_objects",
     "rz_set_draw_config", "rz_update", "rz_render", "rz_sync", "rz_get_frame", "rz_read_frame",
     "rz_get_stats", "rz_get_stream", "rz_last_error", "rz_abi_version", "rz_set_stage_timing",
-    "rz_get_stage_times", "rz_shadow_depth_static",
+    "rz_get_stage_times", "rz_shadow_depth_static", "rz_add_scene", "rz_set_views", "rz_update_view",
+    "rz_get_view_frame",
 ]
 
 _lib = None
@@ -74,6 +75,12 @@ def load(build_if_missing: bool = False):
     lib.rz_shadow_depth_static.argtypes = [P, u32, P, u32, C.POINTER(C.c_float), C.POINTER(C.c_float), P, u32, u32,
                                            P, P]
     lib.rz_shadow_depth_static.restype = C.c_int
+    lib.rz_add_scene.argtypes = [P, P, u32, P, u32, P, u32, P, u32, P, u32, P, u32, C.POINTER(u32)]
+    lib.rz_set_views.argtypes = [P, P, u32]
+    lib.rz_update_view.argtypes = [P, u32, P]
+    lib.rz_get_view_frame.argtypes = [P, u32, C.POINTER(_abi.RzFrameOut)]
+    for name in ("rz_add_scene", "rz_set_views", "rz_update_view", "rz_get_view_frame"):
+        getattr(lib, name).restype = C.c_int
     lib.rz_abi_version.argtypes = []
     lib.rz_abi_version.restype = u32
     for name in ("rz_create", "rz_resize", "rz_set_asset", "rz_set_objects", "rz_update_objects",

@@ -2,10 +2,19 @@
 // Rosy's graphics_device for the shadow pass + scene pass. One CUDA stream per
 // context stands in for the Vulkan queue and its command buffer; a frame is a
 // fixed sequence of clears and kernels that is captured once into a CUDA graph
-// and replayed until the scene layout changes.
+// and replayed until the layout changes.
+//
+// A context holds scenes (an asset plus its objects and surfaces; scene 0 is the
+// one rz_set_asset / rz_set_objects define) and views (a camera with its own
+// extent, shadow map, draw state and scene constants onto one scene). Every
+// kernel of a frame runs once over all views: draws carry their view, and each
+// view's targets are ranges of shared pools. The single-view API is a batch of
+// one view.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -50,67 +59,91 @@ struct FrameReport {
     PassHeader blended;
 };
 
+// A scene: its slice of the concatenated asset and object arrays, and its surfaces.
+struct SceneHost {
+    uint32_t mesh_base = 0, mesh_count = 0;
+    uint32_t material_base = 0, material_count = 0;
+    uint32_t texture_base = 0, texture_count = 0;
+    uint32_t sampler_base = 0, sampler_count = 0;
+    uint32_t object_base = 0, object_count = 0;
+    std::vector<rz_surface> surfaces;
+    bool has_objects = false;
+};
+
+struct ViewHost {
+    uint32_t scene = 0;
+    uint32_t width = 0, height = 0, shadow = 0;
+    rz_draw_config dc{};
+    bool has_scene_data = false;
+};
+
+constexpr uint32_t kDefaultSampler = 0xFFFFFFFFu;  // any index >= the sampler count selects the default
+
 }  // namespace
 
 struct rz_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;          // shadow pass branch of the frame graph
+    cudaStream_t side = nullptr;  // shadow pass branch of the frame graph
     cudaEvent_t fork = nullptr, join = nullptr;
-    uint32_t width = 0, height = 0, shadow_size = 0;
-    uint32_t queue_chunks = 0;  // fixed work-queue depth (0 = sized from the scene)
+    uint32_t queue_chunks = 0;    // fixed work-queue depth (0 = sized from the scene)
     std::string last_error;
 
-    // frame buffers
+    // asset of all scenes, concatenated (host copies of the small arrays, device arrays)
+    std::vector<rz_vertex> verts;
+    std::vector<float4> pos;
+    std::vector<uint32_t> idx;
+    std::vector<uint32_t> mesh_table;  // 4 per mesh: vertex_offset, vertex_count, index_offset, index_count
+    std::vector<GpuMaterial> materials;
+    std::vector<TexDesc> tex_descs;
+    std::vector<uint32_t*> tex_allocs;  // one device allocation per texture
+    std::vector<SamplerBits> samplers;  // without the default sampler
+    std::vector<rz_object> objects;
+    std::vector<SceneHost> scenes;
+    rz_vertex* d_vertices = nullptr;
+    float4* d_pos = nullptr;
+    uint32_t* d_indices = nullptr;
+    GpuMaterial* d_materials = nullptr;
+    TexDesc* d_textures = nullptr;
+    SamplerBits* d_samplers = nullptr;
+    rz_object* d_objects = nullptr;
+    rz_object* h_objects = nullptr;  // pinned staging for rz_update_objects
+    size_t h_objects_capacity = 0;
+    cudaEvent_t objects_copied = nullptr;
+    float* d_srgb = nullptr;
+    bool asset_dirty = true;         // device asset arrays need an upload
+
+    // views
+    std::vector<ViewHost> views;
+    rz_scene_data* d_scene_data = nullptr;  // one per view
+    rz_scene_data* h_scene_data = nullptr;  // pinned staging, one per view
+    uint32_t scene_data_capacity = 0;
+    cudaEvent_t scene_copied = nullptr;
+    ViewRec* d_views = nullptr;
+    std::vector<ViewRec> view_recs;
+    std::vector<uint32_t> view_id_base;  // first opaque triangle id of each view
     uint64_t* d_vis = nullptr;
     uint32_t* d_color = nullptr;
     float* d_depth = nullptr;
     uint32_t* d_shadow = nullptr;
+    uint2* d_color16 = nullptr;
+    size_t pix_capacity = 0, shadow_capacity = 0, color16_capacity = 0;
+    size_t pix_total = 0, shadow_total = 0;
+    uint32_t shade_blocks = 0;
 
-    // scene constants
-    rz_scene_data* d_scene = nullptr;
-    rz_scene_data* h_scene = nullptr;  // pinned staging
-    cudaEvent_t scene_copied = nullptr;
-    bool have_scene = false;
-    rz_draw_config draw_config{};
-
-    // asset
-    rz_vertex* d_vertices = nullptr;
-    float4* d_pos = nullptr;
-    uint32_t vertex_count = 0;
-    uint32_t* d_indices = nullptr;
-    uint32_t index_count = 0;
-    std::vector<uint32_t> mesh_table;  // 4 per mesh
-    std::vector<uint32_t> mesh_vertex_max;  // largest index used by each mesh's index buffer
-    GpuMaterial* d_materials = nullptr;
-    std::vector<GpuMaterial> materials;
-    TexDesc* d_textures = nullptr;
-    uint32_t texture_count = 0;
-    uint32_t* d_texels = nullptr;
-    SamplerBits* d_samplers = nullptr;
-    uint32_t sampler_count = 0;
-    float* d_srgb = nullptr;
-    bool have_asset = false;
-
-    // objects and draw lists
-    rz_object* d_objects = nullptr;
-    rz_object* h_objects = nullptr;  // pinned staging for rz_update_objects
-    uint32_t object_count = 0;
-    cudaEvent_t objects_copied = nullptr;
+    // draw lists over all views
     DrawRec* d_shadow_draws = nullptr;
     DrawRec* d_opaque_draws = nullptr;
     DrawRec* d_blended_draws = nullptr;
-    DrawConsts* d_blended_consts = nullptr;
-    uint32_t blended_varying_base = 0;  // first varying record of the blended draws
-    uint2* d_color16 = nullptr;         // RGBA16F draw image (only with blended surfaces)
     uint32_t shadow_draw_count = 0, opaque_draw_count = 0, blended_draw_count = 0;
     uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0;
     float* d_shadow_mvp = nullptr;
     DrawConsts* d_camera_consts = nullptr;
+    DrawConsts* d_blended_consts = nullptr;
     float4* d_varyings = nullptr;
-    uint32_t varying_count = 0;
-    bool have_objects = false;
+    uint32_t varying_count = 0, blended_varying_base = 0;
+    bool layout_dirty = true;        // draw lists, pools and view table need a rebuild
 
     // raster scratch
     PassBuffers shadow_pass, camera_pass, blended_pass;
@@ -142,39 +175,24 @@ int cuda_fail(rz_ctx* ctx, cudaError_t e, const char* what) {
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define RZ_CUDA(ctx, expr, what)                         \
-    do {                                                 \
-        cudaError_t _e = (expr);                         \
+#define RZ_CUDA(ctx, expr, what)                                \
+    do {                                                        \
+        cudaError_t _e = (expr);                                \
         if (_e != cudaSuccess) return cuda_fail(ctx, _e, what); \
     } while (0)
 
-void free_frame_buffers(rz_ctx* c) {
-    dfree(c->d_vis);
-    dfree(c->d_color);
-    dfree(c->d_depth);
-    dfree(c->d_shadow);
-}
-
-int alloc_frame_buffers(rz_ctx* c) {
-    const size_t np = (size_t)c->width * c->height;
-    RZ_CUDA(c, dalloc(&c->d_vis, np), "visibility buffer");
-    RZ_CUDA(c, dalloc(&c->d_color, np), "colour buffer");
-    RZ_CUDA(c, dalloc(&c->d_depth, np), "depth buffer");
-    RZ_CUDA(c, dalloc(&c->d_shadow, (size_t)c->shadow_size * c->shadow_size), "shadow map");
-    RZ_CUDA(c, cudaMemset(c->d_vis, 0, np * 8), "clear visibility");
-    RZ_CUDA(c, cudaMemset(c->d_color, 0, np * 4), "clear colour");
-    RZ_CUDA(c, cudaMemset(c->d_depth, 0, np * 4), "clear depth");
-    RZ_CUDA(c, cudaMemset(c->d_shadow, 0, (size_t)c->shadow_size * c->shadow_size * 4), "clear shadow");
-    return RZ_OK;
+void drop_graph(rz_ctx* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_dirty = true;
 }
 
 void free_pass(PassBuffers& p) {
     dfree(p.records);
     dfree(p.small_records);
-    p.small_capacity = 0;
     dfree(p.tile_status);
     dfree(p.chunk_map);
-    p.record_capacity = p.tile_capacity = p.chunk_capacity = 0;
+    p.record_capacity = p.small_capacity = p.tile_capacity = p.chunk_capacity = 0;
 }
 
 // Sizes the raster scratch of a pass: one record per triangle plus room for
@@ -200,7 +218,7 @@ int size_pass(rz_ctx* c, PassBuffers& p, uint32_t tris, uint64_t stamps_hint) {
         RZ_CUDA(c, dalloc(&p.tile_status, tiles), "tile status");
         p.tile_capacity = tiles;
     }
-    if (chunks > p.chunk_capacity) {
+    if (chunks > p.chunk_capacity || c->queue_chunks) {
         dfree(p.chunk_map);
         RZ_CUDA(c, dalloc(&p.chunk_map, (size_t)chunks), "chunk map");
         p.chunk_capacity = (uint32_t)chunks;
@@ -208,12 +226,12 @@ int size_pass(rz_ctx* c, PassBuffers& p, uint32_t tris, uint64_t stamps_hint) {
     return RZ_OK;
 }
 
-// Stamps a pass may need: never more than every triangle covering the whole
+// Stamps a pass may need: never more than every triangle covering its whole
 // target; otherwise room for 256 full-screen layers of overdraw plus 16 stamps
 // per triangle. A frame that needs more reports RZ_OVERFLOW and the capacity
 // grows for the next frame.
-uint64_t default_stamp_hint(uint32_t tris, uint32_t w, uint32_t h) {
-    const uint64_t screen = ((uint64_t)w / kStampW + 1) * ((uint64_t)h / kStampH + 1);
+uint64_t stamp_hint(uint32_t tris, uint64_t target_pixels) {
+    const uint64_t screen = target_pixels / (kStampW * kStampH) + 1;
     const uint64_t bound = (uint64_t)tris * screen;
     const uint64_t hint = screen * 256 + (uint64_t)tris * 16;
     return bound < hint ? bound : hint;
@@ -230,94 +248,415 @@ SamplerBits sampler_bits(const rz_sampler& s) {
     return b | (wu << 4) | (wv << 6);
 }
 
-PassParams pass_params(rz_ctx* c, bool camera, bool blended = false) {
+void free_asset(rz_ctx* c) {
+    for (uint32_t* p : c->tex_allocs) cudaFree(p);
+    c->tex_allocs.clear();
+    c->verts.clear();
+    c->pos.clear();
+    c->idx.clear();
+    c->mesh_table.clear();
+    c->materials.clear();
+    c->tex_descs.clear();
+    c->samplers.clear();
+    c->objects.clear();
+    c->scenes.clear();
+    c->asset_dirty = true;
+    c->layout_dirty = true;
+}
+
+// Appends an asset to the concatenated arrays as a new scene (no objects yet).
+// Meshes are concatenated as set_asset does (src/Engine/Graphics.cpp:4310-4334)
+// and materials packed with its index mapping (4071-4150).
+int append_asset(rz_ctx* c, const rz_mesh* meshes, uint32_t mesh_count, const rz_material* mats, uint32_t mat_count,
+                 const rz_texture* textures, uint32_t tex_count, const rz_sampler* samplers, uint32_t sampler_count,
+                 SceneHost& out) {
+    if (mesh_count == 0 || !meshes) return fail(c, RZ_INVALID_ARGUMENT, "asset has no meshes");
+    if ((mat_count && !mats) || (tex_count && !textures) || (sampler_count && !samplers))
+        return fail(c, RZ_INVALID_ARGUMENT, "null array with non-zero count");
+    uint64_t nv = c->verts.size(), ni = c->idx.size();
+    for (uint32_t m = 0; m < mesh_count; ++m) {
+        if ((meshes[m].position_count && !meshes[m].positions) || (meshes[m].index_count && !meshes[m].indices))
+            return fail(c, RZ_INVALID_ARGUMENT, "mesh with null data");
+        for (uint32_t i = 0; i < meshes[m].index_count; ++i)
+            if (meshes[m].indices[i] >= meshes[m].position_count)
+                return fail(c, RZ_INVALID_ARGUMENT, "mesh " + std::to_string(m) + " index out of range");
+        nv += meshes[m].position_count;
+        ni += meshes[m].index_count;
+    }
+    if (nv >= 0xFFFFFFFFull || ni >= 0xFFFFFFFFull) return fail(c, RZ_OVERFLOW, "asset too large");
+    for (uint32_t i = 0; i < tex_count; ++i) {
+        const rz_texture& t = textures[i];
+        if (t.width == 0 || t.height == 0 || t.levels == 0 || t.levels > 16 || !t.texels)
+            return fail(c, RZ_INVALID_ARGUMENT, "texture " + std::to_string(i) + " is malformed");
+        uint32_t max_levels = 1;
+        while ((t.width >> max_levels) || (t.height >> max_levels)) ++max_levels;
+        if (t.levels > max_levels) return fail(c, RZ_INVALID_ARGUMENT, "texture has too many levels");
+    }
+    SceneHost sh;
+    sh.mesh_base = (uint32_t)(c->mesh_table.size() / 4);
+    sh.mesh_count = mesh_count;
+    sh.material_base = (uint32_t)c->materials.size();
+    sh.material_count = mat_count;
+    sh.texture_base = (uint32_t)c->tex_descs.size();
+    sh.texture_count = tex_count;
+    sh.sampler_base = (uint32_t)c->samplers.size();
+    sh.sampler_count = sampler_count;
+    sh.object_base = (uint32_t)c->objects.size();
+    for (uint32_t m = 0; m < mesh_count; ++m) {
+        const rz_mesh& mesh = meshes[m];
+        c->mesh_table.push_back((uint32_t)c->verts.size());
+        c->mesh_table.push_back(mesh.position_count);
+        c->mesh_table.push_back((uint32_t)c->idx.size());
+        c->mesh_table.push_back(mesh.index_count);
+        for (uint32_t i = 0; i < mesh.position_count; ++i) {
+            c->verts.push_back(mesh.positions[i]);
+            c->pos.push_back(make_float4(mesh.positions[i].position[0], mesh.positions[i].position[1],
+                                         mesh.positions[i].position[2], 1.0f));
+        }
+        c->idx.insert(c->idx.end(), mesh.indices, mesh.indices + mesh.index_count);
+    }
+    for (uint32_t i = 0; i < mat_count; ++i) {
+        const rz_material& m = mats[i];
+        GpuMaterial g{};
+        for (int k = 0; k < 4; ++k) g.color[k] = m.base_color_factor[k];
+        g.metallic_factor = m.metallic_factor;
+        g.roughness_factor = m.roughness_factor;
+        g.alpha_cutoff = m.alpha_cutoff;
+        g.alpha_mode = m.alpha_mode;
+        const uint32_t img[4] = {m.color_image_index, m.normal_image_index, m.metallic_image_index, m.mixmap_image_index};
+        const uint32_t smp[4] = {m.color_sampler_index, m.normal_sampler_index, m.metallic_sampler_index, m.mixmap_sampler_index};
+        for (int k = 0; k < 4; ++k) {
+            g.tex[k] = RZ_INVALID_INDEX;
+            g.sampler[k] = kDefaultSampler;
+            if (img[k] < tex_count) {
+                g.tex[k] = sh.texture_base + img[k];
+                if (smp[k] < sampler_count) g.sampler[k] = sh.sampler_base + smp[k];
+            }
+        }
+        c->materials.push_back(g);
+    }
+    for (uint32_t i = 0; i < tex_count; ++i) {
+        const rz_texture& t = textures[i];
+        TexDesc d{};
+        d.width = t.width;
+        d.height = t.height;
+        d.levels = t.levels;
+        d.srgb = t.image_type == RZ_IMAGE_NORMAL_MAP ? 0u : 1u;
+        uint64_t off = 0;
+        for (uint32_t l = 0; l < t.levels; ++l) {
+            d.level_off[l] = (uint32_t)off;
+            off += (uint64_t)std::max(1u, t.width >> l) * std::max(1u, t.height >> l);
+        }
+        if (off >= 0xFFFFFFFFull) return fail(c, RZ_OVERFLOW, "texture too large");
+        uint32_t* dp = nullptr;
+        RZ_CUDA(c, dalloc(&dp, (size_t)off), "texture");
+        c->tex_allocs.push_back(dp);
+        RZ_CUDA(c, cudaMemcpy(dp, t.texels, (size_t)off * 4, cudaMemcpyHostToDevice), "upload texels");
+        d.base = reinterpret_cast<uint64_t>(dp);
+        c->tex_descs.push_back(d);
+    }
+    for (uint32_t i = 0; i < sampler_count; ++i) c->samplers.push_back(sampler_bits(samplers[i]));
+    out = sh;
+    c->asset_dirty = true;
+    c->layout_dirty = true;
+    return RZ_OK;
+}
+
+// Validates a scene's surfaces against its asset and objects.
+int check_surfaces(rz_ctx* c, const SceneHost& sh, uint32_t object_count, const rz_surface* surfaces, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const rz_surface& s = surfaces[i];
+        if (s.mesh_index >= sh.mesh_count) return fail(c, RZ_INVALID_ARGUMENT, "surface mesh index out of range");
+        const uint64_t obj = (uint64_t)s.graphic_objects_offset + s.graphics_object_index;
+        if (obj >= object_count) return fail(c, RZ_INVALID_ARGUMENT, "surface object index out of range");
+        const uint32_t* mt = &c->mesh_table[4 * (sh.mesh_base + s.mesh_index)];
+        if ((uint64_t)s.start_index + s.index_count > mt[3])
+            return fail(c, RZ_INVALID_ARGUMENT, "surface index range outside its mesh");
+        const bool has_mat = s.material_index < sh.material_count;
+        if (!s.blended && has_mat && c->materials[sh.material_base + s.material_index].alpha_mode != 0)
+            return fail(c, RZ_INVALID_ARGUMENT, "opaque surface with a non-opaque material");
+    }
+    return RZ_OK;
+}
+
+int upload_asset(rz_ctx* c) {
+    cudaStreamSynchronize(c->stream);
+    dfree(c->d_vertices);
+    dfree(c->d_pos);
+    dfree(c->d_indices);
+    dfree(c->d_materials);
+    dfree(c->d_textures);
+    dfree(c->d_samplers);
+    const size_t nv = c->verts.size(), ni = c->idx.size();
+    RZ_CUDA(c, dalloc(&c->d_vertices, std::max<size_t>(nv, 1)), "vertex buffer");
+    RZ_CUDA(c, dalloc(&c->d_pos, std::max<size_t>(nv, 1)), "position stream");
+    RZ_CUDA(c, dalloc(&c->d_indices, std::max<size_t>(ni, 1)), "index buffer");
+    RZ_CUDA(c, dalloc(&c->d_materials, std::max<size_t>(c->materials.size(), 1)), "material buffer");
+    RZ_CUDA(c, dalloc(&c->d_textures, std::max<size_t>(c->tex_descs.size(), 1)), "texture table");
+    RZ_CUDA(c, dalloc(&c->d_samplers, c->samplers.size() + 1), "sampler table");
+    if (nv) {
+        RZ_CUDA(c, cudaMemcpy(c->d_vertices, c->verts.data(), nv * sizeof(rz_vertex), cudaMemcpyHostToDevice), "upload vertices");
+        RZ_CUDA(c, cudaMemcpy(c->d_pos, c->pos.data(), nv * sizeof(float4), cudaMemcpyHostToDevice), "upload positions");
+    }
+    if (ni) RZ_CUDA(c, cudaMemcpy(c->d_indices, c->idx.data(), ni * 4, cudaMemcpyHostToDevice), "upload indices");
+    if (!c->materials.empty())
+        RZ_CUDA(c, cudaMemcpy(c->d_materials, c->materials.data(), c->materials.size() * sizeof(GpuMaterial),
+                              cudaMemcpyHostToDevice), "upload materials");
+    if (!c->tex_descs.empty())
+        RZ_CUDA(c, cudaMemcpy(c->d_textures, c->tex_descs.data(), c->tex_descs.size() * sizeof(TexDesc),
+                              cudaMemcpyHostToDevice), "upload texture table");
+    std::vector<SamplerBits> sb = c->samplers;
+    // default sampler: linear/linear, nearest mip, repeat (src/Engine/Graphics.cpp:3421-3438)
+    sb.push_back(1u | 2u | (2u << 4) | (2u << 6));
+    RZ_CUDA(c, cudaMemcpy(c->d_samplers, sb.data(), sb.size() * sizeof(SamplerBits), cudaMemcpyHostToDevice), "upload samplers");
+    c->asset_dirty = false;
+    c->layout_dirty = true;
+    return RZ_OK;
+}
+
+int upload_objects(rz_ctx* c) {
+    cudaStreamSynchronize(c->stream);
+    dfree(c->d_objects);
+    const size_t n = c->objects.size();
+    RZ_CUDA(c, dalloc(&c->d_objects, std::max<size_t>(n, 1)), "object buffer");
+    if (n) RZ_CUDA(c, cudaMemcpy(c->d_objects, c->objects.data(), n * sizeof(rz_object), cudaMemcpyHostToDevice), "upload objects");
+    if (n > c->h_objects_capacity) {
+        if (c->h_objects) cudaFreeHost(c->h_objects);
+        c->h_objects = nullptr;
+        c->h_objects_capacity = 0;
+        RZ_CUDA(c, cudaMallocHost(&c->h_objects, n * sizeof(rz_object)), "object staging");
+        c->h_objects_capacity = n;
+    }
+    c->layout_dirty = true;  // the graph holds the object buffer's address
+    return RZ_OK;
+}
+
+int ensure_scene_data(rz_ctx* c, uint32_t n) {
+    if (n <= c->scene_data_capacity) return RZ_OK;
+    cudaStreamSynchronize(c->stream);
+    rz_scene_data* d = nullptr;
+    rz_scene_data* h = nullptr;
+    RZ_CUDA(c, dalloc(&d, n), "scene constants");
+    RZ_CUDA(c, cudaMallocHost(&h, n * sizeof(rz_scene_data)), "scene staging");
+    std::memset(h, 0, n * sizeof(rz_scene_data));
+    if (c->scene_data_capacity) {
+        RZ_CUDA(c, cudaMemcpy(d, c->d_scene_data, c->scene_data_capacity * sizeof(rz_scene_data), cudaMemcpyDeviceToDevice),
+                "copy scene constants");
+        std::memcpy(h, c->h_scene_data, c->scene_data_capacity * sizeof(rz_scene_data));
+    }
+    dfree(c->d_scene_data);
+    if (c->h_scene_data) cudaFreeHost(c->h_scene_data);
+    c->d_scene_data = d;
+    c->h_scene_data = h;
+    c->scene_data_capacity = n;
+    c->layout_dirty = true;
+    return RZ_OK;
+}
+
+// Rebuilds the draw lists over all views, the target pools and the view table.
+int build_layout(rz_ctx* c) {
+    if (c->views.empty()) return fail(c, RZ_INVALID_STATE, "no views");
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    // pools
+    size_t pix = 0, shadow = 0;
+    uint32_t blocks = 0;
+    std::vector<size_t> pix_off, shadow_off;
+    std::vector<uint32_t> block_base;
+    for (const ViewHost& v : c->views) {
+        pix_off.push_back(pix);
+        shadow_off.push_back(shadow);
+        block_base.push_back(blocks);
+        pix += (size_t)v.width * v.height;
+        shadow += (size_t)v.shadow * v.shadow;
+        blocks += ((v.width + 15) / 16) * ((v.height + 15) / 16);
+    }
+    // draw lists, view-major, each view's surfaces in scene order (src/Engine/Graphics.cpp:4715-4735)
+    std::vector<DrawRec> shadow_list, opaque, blended;
+    uint64_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0, varyings = 0;
+    c->view_id_base.assign(c->views.size(), 0);
+    for (uint32_t vi = 0; vi < c->views.size(); ++vi) {
+        const ViewHost& v = c->views[vi];
+        c->view_id_base[vi] = (uint32_t)opaque_tris;
+        if (v.scene >= c->scenes.size()) return fail(c, RZ_INVALID_STATE, "view refers to a missing scene");
+        const SceneHost& sh = c->scenes[v.scene];
+        if (!sh.has_objects) return fail(c, RZ_INVALID_STATE, "scene has no objects (rz_set_objects)");
+        if (!v.has_scene_data) return fail(c, RZ_INVALID_STATE, "view has no scene constants (rz_update)");
+        for (const rz_surface& s : sh.surfaces) {
+            const uint32_t* mt = &c->mesh_table[4 * (sh.mesh_base + s.mesh_index)];
+            DrawRec d{};
+            d.vertex_base = mt[0];
+            d.first_index = mt[2] + s.start_index;
+            d.tri_count = s.index_count / 3;
+            d.object = sh.object_base + s.graphic_objects_offset + s.graphics_object_index;
+            d.material = s.material_index < sh.material_count ? (int32_t)(sh.material_base + s.material_index) : -1;
+            d.vertex_count = mt[1];
+            d.view = vi;
+            d.tri_base = (uint32_t)shadow_tris;
+            shadow_list.push_back(d);
+            shadow_tris += d.tri_count;
+            if (s.blended) {
+                d.tri_base = (uint32_t)blended_tris;
+                blended.push_back(d);
+                blended_tris += d.tri_count;
+            } else {
+                d.tri_base = (uint32_t)opaque_tris;
+                d.varying_base = (uint32_t)varyings;
+                varyings += d.vertex_count;
+                opaque.push_back(d);
+                opaque_tris += d.tri_count;
+            }
+        }
+    }
+    const uint64_t blended_varying_base = varyings;
+    for (DrawRec& d : blended) {
+        d.varying_base = (uint32_t)varyings;
+        varyings += d.vertex_count;
+    }
+    if (shadow_tris >= 0xFFFFFFF0ull || varyings >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many triangles");
+    // buffers
+    if (pix > c->pix_capacity) {
+        dfree(c->d_vis);
+        dfree(c->d_color);
+        dfree(c->d_depth);
+        c->pix_capacity = 0;
+        RZ_CUDA(c, dalloc(&c->d_vis, pix), "visibility buffers");
+        RZ_CUDA(c, dalloc(&c->d_color, pix), "colour buffers");
+        RZ_CUDA(c, dalloc(&c->d_depth, pix), "depth buffers");
+        RZ_CUDA(c, cudaMemset(c->d_color, 0, pix * 4), "clear colour");
+        RZ_CUDA(c, cudaMemset(c->d_depth, 0, pix * 4), "clear depth");
+        c->pix_capacity = pix;
+    }
+    if (shadow > c->shadow_capacity) {
+        dfree(c->d_shadow);
+        c->shadow_capacity = 0;
+        RZ_CUDA(c, dalloc(&c->d_shadow, shadow), "shadow maps");
+        c->shadow_capacity = shadow;
+    }
+    if (!blended.empty() && pix > c->color16_capacity) {
+        dfree(c->d_color16);
+        c->color16_capacity = 0;
+        RZ_CUDA(c, dalloc(&c->d_color16, pix), "RGBA16F draw images");
+        c->color16_capacity = pix;
+    }
+    c->view_recs.resize(c->views.size());
+    for (uint32_t vi = 0; vi < c->views.size(); ++vi) {
+        const ViewHost& v = c->views[vi];
+        ViewRec r{};
+        r.width = (int)v.width;
+        r.height = (int)v.height;
+        r.shadow_w = r.shadow_h = (int)v.shadow;
+        r.cull_front = v.dc.cull_enabled ? 1 : 0;
+        r.ccw_front = v.dc.reverse_winding_order_enabled ? 1 : 0;
+        r.bias_enabled = v.dc.depth_bias_enabled ? 1 : 0;
+        r.bias_constant = v.dc.depth_bias_constant;
+        r.bias_clamp = v.dc.depth_bias_clamp;
+        r.bias_slope = v.dc.depth_bias_slope_factor;
+        r.pcf_mode = v.dc.pcf_mode;
+        r.shade_block_base = block_base[vi];
+        r.vis = c->d_vis + pix_off[vi];
+        r.color = c->d_color + pix_off[vi];
+        r.depth = c->d_depth + pix_off[vi];
+        r.shadow = c->d_shadow + shadow_off[vi];
+        r.color16 = c->d_color16 ? c->d_color16 + pix_off[vi] : nullptr;
+        r.scene = c->d_scene_data + vi;
+        c->view_recs[vi] = r;
+    }
+    dfree(c->d_views);
+    dfree(c->d_shadow_draws);
+    dfree(c->d_opaque_draws);
+    dfree(c->d_blended_draws);
+    dfree(c->d_shadow_mvp);
+    dfree(c->d_camera_consts);
+    dfree(c->d_blended_consts);
+    dfree(c->d_varyings);
+    RZ_CUDA(c, dalloc(&c->d_views, c->view_recs.size()), "view table");
+    RZ_CUDA(c, dalloc(&c->d_shadow_draws, std::max<size_t>(shadow_list.size(), 1)), "shadow draw list");
+    RZ_CUDA(c, dalloc(&c->d_opaque_draws, std::max<size_t>(opaque.size(), 1)), "opaque draw list");
+    RZ_CUDA(c, dalloc(&c->d_blended_draws, std::max<size_t>(blended.size(), 1)), "blended draw list");
+    RZ_CUDA(c, dalloc(&c->d_shadow_mvp, std::max<size_t>(shadow_list.size(), 1) * 16), "shadow matrices");
+    RZ_CUDA(c, dalloc(&c->d_camera_consts, std::max<size_t>(opaque.size(), 1)), "camera constants");
+    RZ_CUDA(c, dalloc(&c->d_blended_consts, std::max<size_t>(blended.size(), 1)), "blended constants");
+    RZ_CUDA(c, dalloc(&c->d_varyings, std::max<size_t>((size_t)varyings, 1) * 8), "varying records");
+    RZ_CUDA(c, cudaMemcpy(c->d_views, c->view_recs.data(), c->view_recs.size() * sizeof(ViewRec), cudaMemcpyHostToDevice),
+            "upload views");
+    if (!shadow_list.empty())
+        RZ_CUDA(c, cudaMemcpy(c->d_shadow_draws, shadow_list.data(), shadow_list.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
+    if (!opaque.empty())
+        RZ_CUDA(c, cudaMemcpy(c->d_opaque_draws, opaque.data(), opaque.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
+    if (!blended.empty())
+        RZ_CUDA(c, cudaMemcpy(c->d_blended_draws, blended.data(), blended.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
+    c->shadow_draw_count = (uint32_t)shadow_list.size();
+    c->opaque_draw_count = (uint32_t)opaque.size();
+    c->blended_draw_count = (uint32_t)blended.size();
+    c->shadow_tris = (uint32_t)shadow_tris;
+    c->opaque_tris = (uint32_t)opaque_tris;
+    c->blended_tris = (uint32_t)blended_tris;
+    c->varying_count = (uint32_t)varyings;
+    c->blended_varying_base = (uint32_t)blended_varying_base;
+    c->pix_total = pix;
+    c->shadow_total = shadow;
+    c->shade_blocks = blocks;
+    int rc = size_pass(c, c->shadow_pass, c->shadow_tris, stamp_hint(c->shadow_tris, shadow));
+    if (rc == RZ_OK) rc = size_pass(c, c->camera_pass, c->opaque_tris, stamp_hint(c->opaque_tris, pix));
+    if (rc == RZ_OK && c->blended_tris) rc = size_pass(c, c->blended_pass, c->blended_tris, stamp_hint(c->blended_tris, pix));
+    if (rc != RZ_OK) return rc;
+    c->layout_dirty = false;
+    return RZ_OK;
+}
+
+PassParams pass_params(rz_ctx* c, int kind) {
     PassParams p{};
     p.pos = c->d_pos;
     p.indices = c->d_indices;
-    p.vertex_count = c->vertex_count;
-    p.cull_front = c->draw_config.cull_enabled ? 1 : 0;
-    p.ccw_front = c->draw_config.reverse_winding_order_enabled ? 1 : 0;
+    p.vertex_count = (uint32_t)c->verts.size();
+    p.views = c->d_views;
     p.error_flags = c->d_error;
-    if (blended) {
-        // blended list: cull none, no depth write, records kept in submission order
+    PassBuffers* pb;
+    if (kind == 2) {  // blended list: cull none, records kept in submission order
         p.draws = c->d_blended_draws;
         p.draw_count = c->blended_draw_count;
         p.tri_total = c->blended_tris;
         p.mvp = reinterpret_cast<const float*>(c->d_blended_consts);
         p.mvp_stride = sizeof(DrawConsts) / sizeof(float);
-        p.width = (int)c->width;
-        p.height = (int)c->height;
-        p.cull_front = 0;
         p.write_id = 1;
         p.ordered = 1;
-        p.records = c->blended_pass.records;
-        p.record_capacity = c->blended_pass.record_capacity;
-        p.small_records = c->blended_pass.small_records;
-        p.small_capacity = c->blended_pass.small_capacity;
-        p.tile_status = c->blended_pass.tile_status;
-        p.chunk_map = c->blended_pass.chunk_map;
-        p.chunk_capacity = c->blended_pass.chunk_capacity;
         p.header = c->d_headers + 2;
-        p.target = nullptr;
-    } else if (camera) {
+        pb = &c->blended_pass;
+    } else if (kind == 1) {
         p.draws = c->d_opaque_draws;
         p.draw_count = c->opaque_draw_count;
         p.tri_total = c->opaque_tris;
         p.mvp = reinterpret_cast<const float*>(c->d_camera_consts);
         p.mvp_stride = sizeof(DrawConsts) / sizeof(float);
-        p.width = (int)c->width;
-        p.height = (int)c->height;
-        p.bias_enabled = 0;
         p.write_id = 1;
-        p.records = c->camera_pass.records;
-        p.record_capacity = c->camera_pass.record_capacity;
-        p.small_records = c->camera_pass.small_records;
-        p.small_capacity = c->camera_pass.small_capacity;
-        p.tile_status = c->camera_pass.tile_status;
-        p.chunk_map = c->camera_pass.chunk_map;
-        p.chunk_capacity = c->camera_pass.chunk_capacity;
         p.header = c->d_headers + 1;
-        p.target = c->d_vis;
+        pb = &c->camera_pass;
     } else {
         p.draws = c->d_shadow_draws;
         p.draw_count = c->shadow_draw_count;
         p.tri_total = c->shadow_tris;
         p.mvp = c->d_shadow_mvp;
         p.mvp_stride = 16;
-        p.width = (int)c->shadow_size;
-        p.height = (int)c->shadow_size;
-        p.bias_enabled = c->draw_config.depth_bias_enabled ? 1 : 0;
-        p.bias_constant = c->draw_config.depth_bias_constant;
-        p.bias_clamp = c->draw_config.depth_bias_clamp;
-        p.bias_slope = c->draw_config.depth_bias_slope_factor;
         p.write_id = 0;
-        p.records = c->shadow_pass.records;
-        p.record_capacity = c->shadow_pass.record_capacity;
-        p.small_records = c->shadow_pass.small_records;
-        p.small_capacity = c->shadow_pass.small_capacity;
-        p.tile_status = c->shadow_pass.tile_status;
-        p.chunk_map = c->shadow_pass.chunk_map;
-        p.chunk_capacity = c->shadow_pass.chunk_capacity;
         p.header = c->d_headers + 0;
-        p.target = c->d_shadow;
+        pb = &c->shadow_pass;
     }
+    p.records = pb->records;
+    p.record_capacity = pb->record_capacity;
+    p.small_records = pb->small_records;
+    p.small_capacity = pb->small_capacity;
+    p.tile_status = pb->tile_status;
+    p.chunk_map = pb->chunk_map;
+    p.chunk_capacity = pb->chunk_capacity;
     return p;
 }
 
-void stamp(rz_ctx* c, int i) {
-    if (c->timing) cudaEventRecord(c->stage_ev[i], c->stream);
-}
-
-// Enqueues one frame (everything after the scene/object uploads).
 ShadeParams shade_params(rz_ctx* c) {
     ShadeParams sh{};
-    sh.vis = c->d_vis;
-    sh.shadow = reinterpret_cast<const float*>(c->d_shadow);
-    sh.shadow_size = (int)c->shadow_size;
-    sh.color = c->d_color;
-    sh.depth = c->d_depth;
-    sh.width = (int)c->width;
-    sh.height = (int)c->height;
+    sh.views = c->d_views;
+    sh.view_count = (uint32_t)c->views.size();
+    sh.shade_blocks = c->shade_blocks;
     sh.draws = c->d_opaque_draws;
     sh.draw_count = c->opaque_draw_count;
     sh.consts = c->d_camera_consts;
@@ -328,23 +667,24 @@ ShadeParams shade_params(rz_ctx* c) {
     sh.objects = c->d_objects;
     sh.materials = c->d_materials;
     sh.textures = c->d_textures;
-    sh.texture_count = c->texture_count;
+    sh.texture_count = (uint32_t)c->tex_descs.size();
     sh.samplers = c->d_samplers;
-    sh.sampler_count = c->sampler_count;
-    sh.texels = c->d_texels;
-    sh.scene = c->d_scene;
-    sh.pcf_mode = c->draw_config.pcf_mode;
+    sh.sampler_count = (uint32_t)c->samplers.size();
     sh.srgb_table = c->d_srgb;
-    sh.color16 = c->blended_tris ? c->d_color16 : nullptr;
+    sh.blended = c->blended_tris ? 1 : 0;
     return sh;
 }
 
-// Shadow pass (src/Engine/Graphics.cpp:5195-5292): clear to 0, per-draw
-// matrices, setup, raster.
+void stamp(rz_ctx* c, int i) {
+    if (c->timing) cudaEventRecord(c->stage_ev[i], c->stream);
+}
+
+// Shadow passes of all views (src/Engine/Graphics.cpp:5195-5292): clear to 0,
+// per-draw matrices, setup, raster.
 void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
     ClearList cl{};
     cl.ptr[0] = c->d_shadow;
-    cl.bytes[0] = (size_t)c->shadow_size * c->shadow_size * 4;
+    cl.bytes[0] = c->shadow_total * 4;
     cl.ptr[1] = c->d_headers + 0;
     cl.bytes[1] = sizeof(PassHeader);
     cl.count = 2;
@@ -356,9 +696,8 @@ void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
     launch_clear(cl, c->sm_count, s);
     if (stamps) stamp(c, 1);
     if (c->shadow_tris) {
-        launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_scene->shadow_projection_near,
-                    c->d_shadow_mvp, s);
-        const PassParams sp = pass_params(c, false);
+        launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s);
+        const PassParams sp = pass_params(c, 0);
         launch_setup(sp, s);
         if (stamps) stamp(c, 2);
         launch_raster(sp, c->sm_count, s);
@@ -367,25 +706,30 @@ void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
     }
 }
 
-// Camera pass (5566-5653): visibility cleared to 0, opaque list, then the
-// vertex stage of the shading.
+// Camera passes of all views (5566-5653): visibility cleared to 0, opaque list,
+// then the vertex stage of the shading; the blended list's setup.
 void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& sh) {
     ClearList cl{};
     cl.ptr[0] = c->d_vis;
-    cl.bytes[0] = (size_t)c->width * c->height * 8;
+    cl.bytes[0] = c->pix_total * 8;
     cl.ptr[1] = c->d_headers + 1;
-    cl.bytes[1] = sizeof(PassHeader);
+    cl.bytes[1] = 2 * sizeof(PassHeader);  // camera and blended headers
     cl.count = 2;
     if (c->opaque_tris) {
-        cl.ptr[2] = c->camera_pass.tile_status;
-        cl.bytes[2] = (size_t)setup_ctas(c->opaque_tris) * 8;
-        cl.count = 3;
+        cl.ptr[cl.count] = c->camera_pass.tile_status;
+        cl.bytes[cl.count] = (size_t)setup_ctas(c->opaque_tris) * 8;
+        ++cl.count;
+    }
+    if (c->blended_tris) {
+        cl.ptr[cl.count] = c->blended_pass.tile_status;
+        cl.bytes[cl.count] = (size_t)setup_ctas(c->blended_tris) * 8;
+        ++cl.count;
     }
     launch_clear(cl, c->sm_count, s);
-    launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_scene, c->d_camera_consts, s);
+    launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s);
     if (stamps) stamp(c, 4);
     if (c->opaque_tris) {
-        const PassParams cp = pass_params(c, true);
+        const PassParams cp = pass_params(c, 1);
         launch_setup(cp, s);
         if (stamps) stamp(c, 5);
         launch_raster(cp, c->sm_count, s);
@@ -394,15 +738,8 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
     }
     launch_vertex(sh, s);
     if (c->blended_tris) {
-        ClearList bl{};
-        bl.ptr[0] = c->d_headers + 2;
-        bl.bytes[0] = sizeof(PassHeader);
-        bl.ptr[1] = c->blended_pass.tile_status;
-        bl.bytes[1] = (size_t)setup_ctas(c->blended_tris) * 8;
-        bl.count = 2;
-        launch_clear(bl, c->sm_count, s);
-        launch_prep_camera(c->d_blended_draws, c->blended_draw_count, c->d_objects, c->d_scene, c->d_blended_consts, s);
-        launch_setup(pass_params(c, true, true), s);
+        launch_prep_camera(c->d_blended_draws, c->blended_draw_count, c->d_objects, c->d_views, c->d_blended_consts, s);
+        launch_setup(pass_params(c, 2), s);
         ShadeParams bs = sh;
         bs.draws = c->d_blended_draws;
         bs.draw_count = c->blended_draw_count;
@@ -414,8 +751,8 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
 
 // Enqueues one frame (everything after the scene/object uploads). With stage
 // timing the stages run one after the other on the main stream between
-// events; otherwise the shadow pass runs on a side stream concurrently with the
-// camera pass, joining before the shading (which reads the shadow map).
+// events; otherwise the shadow passes run on a side stream concurrently with
+// the camera passes, joining before the shading (which reads the shadow maps).
 int enqueue_frame(rz_ctx* c) {
     cudaStream_t s = c->stream;
     const ShadeParams sh = shade_params(c);
@@ -444,7 +781,6 @@ int enqueue_frame(rz_ctx* c) {
         bp.records = c->blended_pass.records;
         bp.header = c->d_headers + 2;
         bp.record_capacity = c->blended_pass.record_capacity;
-        bp.depth = c->d_depth;
         launch_blend(bp, s);
     }
     if (c->timing) stamp(c, 7);
@@ -458,16 +794,66 @@ int enqueue_frame(rz_ctx* c) {
 
 int check_ready(rz_ctx* c) {
     if (!c) return RZ_INVALID_ARGUMENT;
-    if (!c->have_asset) return fail(c, RZ_INVALID_STATE, "rz_set_asset has not been called");
-    if (!c->have_objects) return fail(c, RZ_INVALID_STATE, "rz_set_objects has not been called");
-    if (!c->have_scene) return fail(c, RZ_INVALID_STATE, "rz_update has not been called");
+    if (c->scenes.empty()) return fail(c, RZ_INVALID_STATE, "rz_set_asset has not been called");
+    for (const ViewHost& v : c->views) {
+        if (v.scene >= c->scenes.size()) return fail(c, RZ_INVALID_STATE, "view refers to a missing scene");
+        if (!c->scenes[v.scene].has_objects) return fail(c, RZ_INVALID_STATE, "rz_set_objects has not been called");
+        if (!v.has_scene_data) return fail(c, RZ_INVALID_STATE, "rz_update has not been called");
+    }
     return RZ_OK;
 }
 
-void drop_graph(rz_ctx* c) {
-    if (c->graph) cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
-    c->graph_dirty = true;
+// Resizes the raster queues from what an overflowing frame needed (exact counts
+// reported by the device), with 25% headroom.
+int grow_queues(rz_ctx* c) {
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    c->queue_chunks = 0;
+    auto grow = [&](PassBuffers& p, const PassHeader& h) -> int {
+        const uint64_t want_chunks = (h.stamps + kChunkStamps - 1) / kChunkStamps;
+        const uint64_t want_recs = h.records_needed;
+        if (want_chunks > p.chunk_capacity) {
+            const uint64_t n = std::min<uint64_t>(want_chunks + want_chunks / 4 + 1024, 0xFFFFFFFFull);
+            dfree(p.chunk_map);
+            p.chunk_capacity = 0;
+            RZ_CUDA(c, dalloc(&p.chunk_map, (size_t)n), "chunk map");
+            p.chunk_capacity = (uint32_t)n;
+        }
+        if (want_recs > p.record_capacity) {
+            const uint64_t n = std::min<uint64_t>(want_recs + want_recs / 4 + 1024, 0xFFFFFFull);
+            dfree(p.records);
+            p.record_capacity = 0;
+            RZ_CUDA(c, dalloc(&p.records, (size_t)n), "raster records");
+            p.record_capacity = (uint32_t)n;
+        }
+        if (h.small_records > p.small_capacity) {
+            const uint64_t n = std::min<uint64_t>((uint64_t)h.small_records + h.small_records / 4 + 1024, 0xFFFFFFFFull);
+            dfree(p.small_records);
+            p.small_capacity = 0;
+            RZ_CUDA(c, dalloc(&p.small_records, (size_t)n), "small raster records");
+            p.small_capacity = (uint32_t)n;
+        }
+        return RZ_OK;
+    };
+    int rc = grow(c->shadow_pass, c->h_report->shadow);
+    if (rc == RZ_OK) rc = grow(c->camera_pass, c->h_report->camera);
+    if (rc == RZ_OK && c->blended_tris) rc = grow(c->blended_pass, c->h_report->blended);
+    c->grow_records = c->grow_chunks = false;
+    return rc;
+}
+
+rz_frame_out frame_of(rz_ctx* c, uint32_t v) {
+    rz_frame_out o{};
+    const ViewRec& r = c->view_recs[v];
+    o.color_rgba8 = r.color;
+    o.depth_f32 = r.depth;
+    o.visibility_u64 = r.vis;
+    o.shadow_map_f32 = r.shadow;
+    o.width = (uint32_t)r.width;
+    o.height = (uint32_t)r.height;
+    o.shadow_map_size = (uint32_t)r.shadow_w;
+    o.triangle_id_base = c->view_id_base[v];
+    return o;
 }
 
 }  // namespace
@@ -484,9 +870,6 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
     if (cfg->samples != 1) return RZ_INVALID_ARGUMENT;
     rz_ctx* c = new rz_ctx();
     c->device = cfg->device;
-    c->width = cfg->width;
-    c->height = cfg->height;
-    c->shadow_size = cfg->shadow_map_size;
     c->queue_chunks = cfg->queue_chunks;
     auto bail = [&](int code) {
         rz_destroy(c);
@@ -504,13 +887,10 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->objects_copied, cudaEventDisableTiming) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
-    if (alloc_frame_buffers(c) != RZ_OK) return bail(RZ_ALLOCATION_FAILURE);
-    if (dalloc(&c->d_scene, 1) != cudaSuccess || dalloc(&c->d_headers, 3) != cudaSuccess ||
-        dalloc(&c->d_error, 1) != cudaSuccess || dalloc(&c->d_srgb, 256) != cudaSuccess)
+    if (dalloc(&c->d_headers, 3) != cudaSuccess || dalloc(&c->d_error, 1) != cudaSuccess ||
+        dalloc(&c->d_srgb, 256) != cudaSuccess)
         return bail(RZ_ALLOCATION_FAILURE);
-    if (cudaMallocHost(&c->h_scene, sizeof(rz_scene_data)) != cudaSuccess ||
-        cudaMallocHost(&c->h_report, sizeof(FrameReport)) != cudaSuccess)
-        return bail(RZ_ALLOCATION_FAILURE);
+    if (cudaMallocHost(&c->h_report, sizeof(FrameReport)) != cudaSuccess) return bail(RZ_ALLOCATION_FAILURE);
     std::memset(c->h_report, 0, sizeof(FrameReport));
     // sRGB decode table (colour, metallic-roughness and mixmap images are sRGB
     // formats, src/Engine/Graphics.cpp:3632-3647): IEC 61966-2-1 in double, rounded to float.
@@ -520,14 +900,21 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         table[i] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
     }
     if (cudaMemcpy(c->d_srgb, table, sizeof(table), cudaMemcpyHostToDevice) != cudaSuccess) return bail(RZ_ERROR);
-    // reference defaults, src/Engine/Level.cpp:1246-1255
-    c->draw_config.cull_enabled = 1;
-    c->draw_config.reverse_winding_order_enabled = 0;
-    c->draw_config.depth_bias_enabled = 1;
-    c->draw_config.depth_bias_constant = -21.882f;
-    c->draw_config.depth_bias_clamp = -20.937f;
-    c->draw_config.depth_bias_slope_factor = -3.0f;
-    c->draw_config.pcf_mode = RZ_PCF_5TAP;
+    // view 0 with the reference defaults (src/Engine/Level.cpp:1246-1255)
+    ViewHost v;
+    v.scene = 0;
+    v.width = cfg->width;
+    v.height = cfg->height;
+    v.shadow = cfg->shadow_map_size;
+    v.dc.cull_enabled = 1;
+    v.dc.reverse_winding_order_enabled = 0;
+    v.dc.depth_bias_enabled = 1;
+    v.dc.depth_bias_constant = -21.882f;
+    v.dc.depth_bias_clamp = -20.937f;
+    v.dc.depth_bias_slope_factor = -3.0f;
+    v.dc.pcf_mode = RZ_PCF_5TAP;
+    c->views.push_back(v);
+    if (ensure_scene_data(c, 1) != RZ_OK) return bail(RZ_ALLOCATION_FAILURE);
     const char* g = std::getenv("RZ_NO_GRAPH");
     c->use_graph = !(g && g[0] == '1');
     *out = c;
@@ -538,32 +925,37 @@ void rz_destroy(rz_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     drop_graph(c);
-    free_frame_buffers(c);
+    free_asset(c);
     free_pass(c->shadow_pass);
     free_pass(c->camera_pass);
-    dfree(c->d_scene);
-    dfree(c->d_headers);
-    dfree(c->d_error);
-    dfree(c->d_srgb);
+    free_pass(c->blended_pass);
     dfree(c->d_vertices);
     dfree(c->d_pos);
     dfree(c->d_indices);
     dfree(c->d_materials);
     dfree(c->d_textures);
-    dfree(c->d_texels);
     dfree(c->d_samplers);
     dfree(c->d_objects);
+    dfree(c->d_srgb);
+    dfree(c->d_scene_data);
+    dfree(c->d_views);
+    dfree(c->d_vis);
+    dfree(c->d_color);
+    dfree(c->d_depth);
+    dfree(c->d_shadow);
+    dfree(c->d_color16);
     dfree(c->d_shadow_draws);
     dfree(c->d_opaque_draws);
+    dfree(c->d_blended_draws);
     dfree(c->d_shadow_mvp);
     dfree(c->d_camera_consts);
-    dfree(c->d_varyings);
-    dfree(c->d_blended_draws);
     dfree(c->d_blended_consts);
-    dfree(c->d_color16);
-    free_pass(c->blended_pass);
-    if (c->h_scene) cudaFreeHost(c->h_scene);
+    dfree(c->d_varyings);
+    dfree(c->d_headers);
+    dfree(c->d_error);
+    if (c->h_scene_data) cudaFreeHost(c->h_scene_data);
     if (c->h_report) cudaFreeHost(c->h_report);
     if (c->h_objects) cudaFreeHost(c->h_objects);
     if (c->frame_done) cudaEventDestroy(c->frame_done);
@@ -571,7 +963,6 @@ void rz_destroy(rz_ctx* c) {
         if (e) cudaEventDestroy(e);
     if (c->scene_copied) cudaEventDestroy(c->scene_copied);
     if (c->objects_copied) cudaEventDestroy(c->objects_copied);
-    if (c->side) cudaStreamSynchronize(c->side);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
     if (c->side) cudaStreamDestroy(c->side);
@@ -582,22 +973,9 @@ void rz_destroy(rz_ctx* c) {
 int rz_resize(rz_ctx* c, uint32_t width, uint32_t height) {
     if (!c) return RZ_INVALID_ARGUMENT;
     if (width == 0 || height == 0 || width > 16384 || height > 16384) return fail(c, RZ_INVALID_ARGUMENT, "bad extent");
-    cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    drop_graph(c);
-    free_frame_buffers(c);
-    c->width = width;
-    c->height = height;
-    const int rc = alloc_frame_buffers(c);
-    if (rc != RZ_OK) return rc;
-    if (c->d_color16) {
-        dfree(c->d_color16);
-        RZ_CUDA(c, dalloc(&c->d_color16, (size_t)width * height), "RGBA16F draw image");
-    }
-    if (c->have_objects) {
-        const int r2 = size_pass(c, c->camera_pass, c->opaque_tris, default_stamp_hint(c->opaque_tris, width, height));
-        if (r2 != RZ_OK) return r2;
-    }
+    c->views[0].width = width;
+    c->views[0].height = height;
+    c->layout_dirty = true;
     return RZ_OK;
 }
 
@@ -605,249 +983,120 @@ int rz_set_asset(rz_ctx* c, const rz_mesh* meshes, uint32_t mesh_count, const rz
                  const rz_texture* textures, uint32_t tex_count, const rz_sampler* samplers, uint32_t sampler_count) {
     if (!c) return RZ_INVALID_ARGUMENT;
     if (mesh_count == 0 || !meshes) return fail(c, RZ_INVALID_ARGUMENT, "asset has no meshes");
-    if ((mat_count && !mats) || (tex_count && !textures) || (sampler_count && !samplers))
-        return fail(c, RZ_INVALID_ARGUMENT, "null array with non-zero count");
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graph(c);
-    // meshes: concatenated vertex and index buffers (src/Engine/Graphics.cpp:4310-4334)
-    uint64_t nv = 0, ni = 0;
-    for (uint32_t m = 0; m < mesh_count; ++m) {
-        if ((meshes[m].position_count && !meshes[m].positions) || (meshes[m].index_count && !meshes[m].indices))
-            return fail(c, RZ_INVALID_ARGUMENT, "mesh with null data");
-        nv += meshes[m].position_count;
-        ni += meshes[m].index_count;
+    free_asset(c);
+    SceneHost sh;
+    const int rc = append_asset(c, meshes, mesh_count, mats, mat_count, textures, tex_count, samplers, sampler_count, sh);
+    if (rc != RZ_OK) {
+        free_asset(c);
+        return rc;
     }
-    if (nv >= 0xFFFFFFFFull || ni >= 0xFFFFFFFFull) return fail(c, RZ_OVERFLOW, "asset too large");
-    std::vector<rz_vertex> verts;
-    std::vector<float4> pos;
-    std::vector<uint32_t> idx;
-    verts.reserve(nv);
-    pos.reserve(nv);
-    idx.reserve(ni);
-    c->mesh_table.assign(4 * mesh_count, 0);
-    c->mesh_vertex_max.assign(mesh_count, 0);
-    for (uint32_t m = 0; m < mesh_count; ++m) {
-        const rz_mesh& mesh = meshes[m];
-        c->mesh_table[4 * m + 0] = (uint32_t)verts.size();
-        c->mesh_table[4 * m + 1] = mesh.position_count;
-        c->mesh_table[4 * m + 2] = (uint32_t)idx.size();
-        c->mesh_table[4 * m + 3] = mesh.index_count;
-        for (uint32_t i = 0; i < mesh.position_count; ++i) {
-            verts.push_back(mesh.positions[i]);
-            pos.push_back(make_float4(mesh.positions[i].position[0], mesh.positions[i].position[1],
-                                      mesh.positions[i].position[2], 1.0f));
-        }
-        for (uint32_t i = 0; i < mesh.index_count; ++i) {
-            if (mesh.indices[i] >= mesh.position_count)
-                return fail(c, RZ_INVALID_ARGUMENT, "mesh " + std::to_string(m) + " index out of range");
-            idx.push_back(mesh.indices[i]);
-        }
-    }
-    // materials (src/Engine/Graphics.cpp:4071-4150)
-    std::vector<GpuMaterial> gm(mat_count);
-    for (uint32_t i = 0; i < mat_count; ++i) {
-        const rz_material& m = mats[i];
-        GpuMaterial g{};
-        for (int k = 0; k < 4; ++k) g.color[k] = m.base_color_factor[k];
-        g.metallic_factor = m.metallic_factor;
-        g.roughness_factor = m.roughness_factor;
-        g.alpha_cutoff = m.alpha_cutoff;
-        g.alpha_mode = m.alpha_mode;
-        const uint32_t img[4] = {m.color_image_index, m.normal_image_index, m.metallic_image_index, m.mixmap_image_index};
-        const uint32_t smp[4] = {m.color_sampler_index, m.normal_sampler_index, m.metallic_sampler_index, m.mixmap_sampler_index};
-        for (int k = 0; k < 4; ++k) {
-            g.tex[k] = RZ_INVALID_INDEX;
-            g.sampler[k] = sampler_count;
-            if (img[k] < tex_count) {
-                g.tex[k] = img[k];
-                if (smp[k] < sampler_count) g.sampler[k] = smp[k];
-            }
-        }
-        gm[i] = g;
-    }
-    // textures: one RGBA8 pool, per-level offsets
-    std::vector<TexDesc> td(tex_count);
-    uint64_t total_texels = 0;
-    for (uint32_t i = 0; i < tex_count; ++i) {
-        const rz_texture& t = textures[i];
-        if (t.width == 0 || t.height == 0 || t.levels == 0 || t.levels > 16 || !t.texels)
-            return fail(c, RZ_INVALID_ARGUMENT, "texture " + std::to_string(i) + " is malformed");
-        uint32_t max_levels = 1;
-        while ((t.width >> max_levels) || (t.height >> max_levels)) ++max_levels;
-        if (t.levels > max_levels) return fail(c, RZ_INVALID_ARGUMENT, "texture has too many levels");
-        TexDesc d{};
-        d.width = t.width;
-        d.height = t.height;
-        d.levels = t.levels;
-        d.srgb = t.image_type == RZ_IMAGE_NORMAL_MAP ? 0u : 1u;
-        d.base = total_texels;
-        uint64_t off = 0;
-        for (uint32_t l = 0; l < t.levels; ++l) {
-            d.level_off[l] = (uint32_t)off;
-            off += (uint64_t)std::max(1u, t.width >> l) * std::max(1u, t.height >> l);
-        }
-        if (off >= 0xFFFFFFFFull) return fail(c, RZ_OVERFLOW, "texture too large");
-        td[i] = d;
-        total_texels += off;
-    }
-    std::vector<SamplerBits> sb(sampler_count + 1);
-    for (uint32_t i = 0; i < sampler_count; ++i) sb[i] = sampler_bits(samplers[i]);
-    // default sampler: linear/linear, nearest mip, repeat (src/Engine/Graphics.cpp:3421-3438)
-    sb[sampler_count] = 1u | 2u | (2u << 4) | (2u << 6);
-
-    dfree(c->d_vertices);
-    dfree(c->d_pos);
-    dfree(c->d_indices);
-    dfree(c->d_materials);
-    dfree(c->d_textures);
-    dfree(c->d_texels);
-    dfree(c->d_samplers);
-    RZ_CUDA(c, dalloc(&c->d_vertices, nv), "vertex buffer");
-    RZ_CUDA(c, dalloc(&c->d_pos, nv), "position stream");
-    RZ_CUDA(c, dalloc(&c->d_indices, std::max<uint64_t>(ni, 1)), "index buffer");
-    RZ_CUDA(c, dalloc(&c->d_materials, std::max<uint32_t>(mat_count, 1)), "material buffer");
-    RZ_CUDA(c, dalloc(&c->d_textures, std::max<uint32_t>(tex_count, 1)), "texture table");
-    RZ_CUDA(c, dalloc(&c->d_texels, std::max<uint64_t>(total_texels, 1)), "texel pool");
-    RZ_CUDA(c, dalloc(&c->d_samplers, sb.size()), "sampler table");
-    RZ_CUDA(c, cudaMemcpy(c->d_vertices, verts.data(), nv * sizeof(rz_vertex), cudaMemcpyHostToDevice), "upload vertices");
-    RZ_CUDA(c, cudaMemcpy(c->d_pos, pos.data(), nv * sizeof(float4), cudaMemcpyHostToDevice), "upload positions");
-    if (ni) RZ_CUDA(c, cudaMemcpy(c->d_indices, idx.data(), ni * 4, cudaMemcpyHostToDevice), "upload indices");
-    if (mat_count)
-        RZ_CUDA(c, cudaMemcpy(c->d_materials, gm.data(), mat_count * sizeof(GpuMaterial), cudaMemcpyHostToDevice), "upload materials");
-    if (tex_count)
-        RZ_CUDA(c, cudaMemcpy(c->d_textures, td.data(), tex_count * sizeof(TexDesc), cudaMemcpyHostToDevice), "upload texture table");
-    for (uint32_t i = 0; i < tex_count; ++i) {
-        const uint64_t n = (i + 1 < tex_count ? td[i + 1].base : total_texels) - td[i].base;
-        RZ_CUDA(c, cudaMemcpy(c->d_texels + td[i].base, textures[i].texels, n * 4, cudaMemcpyHostToDevice), "upload texels");
-    }
-    RZ_CUDA(c, cudaMemcpy(c->d_samplers, sb.data(), sb.size() * sizeof(SamplerBits), cudaMemcpyHostToDevice), "upload samplers");
-    c->vertex_count = (uint32_t)nv;
-    c->index_count = (uint32_t)ni;
-    c->materials = gm;
-    c->texture_count = tex_count;
-    c->sampler_count = sampler_count;
-    c->have_asset = true;
-    c->have_objects = false;  // draw lists refer to the old meshes
-    return RZ_OK;
+    c->scenes.push_back(sh);
+    return upload_asset(c);
 }
 
 int rz_set_objects(rz_ctx* c, const rz_object* objects, uint32_t object_count, const rz_surface* surfaces,
                    uint32_t surface_count) {
     if (!c) return RZ_INVALID_ARGUMENT;
-    if (!c->have_asset) return fail(c, RZ_INVALID_STATE, "rz_set_asset has not been called");
+    if (c->scenes.empty()) return fail(c, RZ_INVALID_STATE, "rz_set_asset has not been called");
     // src/Engine/Graphics.cpp:4693-4697: an empty scene is an invalid argument
-    if (object_count == 0 || !objects || surface_count == 0 || !surfaces)
-        return fail(c, RZ_INVALID_ARGUMENT, "empty scene");
-    std::vector<DrawRec> shadow, opaque, blended;
-    uint32_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0, blended_draws = 0, varyings = 0;
-    const uint32_t mesh_count = (uint32_t)(c->mesh_table.size() / 4);
-    for (uint32_t i = 0; i < surface_count; ++i) {
-        const rz_surface& s = surfaces[i];
-        if (s.mesh_index >= mesh_count) return fail(c, RZ_INVALID_ARGUMENT, "surface mesh index out of range");
-        const uint64_t obj = (uint64_t)s.graphic_objects_offset + s.graphics_object_index;
-        if (obj >= object_count) return fail(c, RZ_INVALID_ARGUMENT, "surface object index out of range");
-        const uint32_t* mt = &c->mesh_table[4 * s.mesh_index];
-        if ((uint64_t)s.start_index + s.index_count > mt[3])
-            return fail(c, RZ_INVALID_ARGUMENT, "surface index range outside its mesh");
-        const bool has_mat = s.material_index < c->materials.size();
-        if (!s.blended && has_mat && c->materials[s.material_index].alpha_mode != 0)
-            return fail(c, RZ_INVALID_ARGUMENT, "opaque surface with a non-opaque material");
-        DrawRec d{};
-        d.vertex_base = mt[0];
-        d.first_index = mt[2] + s.start_index;
-        d.tri_count = s.index_count / 3;
-        d.object = (uint32_t)obj;
-        d.material = has_mat ? (int32_t)s.material_index : -1;
-        d.tri_base = shadow_tris;
-        shadow.push_back(d);
-        if ((uint64_t)shadow_tris + d.tri_count >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many triangles");
-        shadow_tris += d.tri_count;
-        if (s.blended) {
-            d.tri_base = blended_tris;
-            d.vertex_count = mt[1];
-            blended_tris += d.tri_count;
-            ++blended_draws;
-            blended.push_back(d);
-        } else {
-            d.tri_base = opaque_tris;
-            d.varying_base = varyings;
-            d.vertex_count = mt[1];
-            if ((uint64_t)varyings + mt[1] >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many vertices");
-            varyings += mt[1];
-            opaque.push_back(d);
-            opaque_tris += d.tri_count;
-        }
-    }
-    // varying records of the blended draws follow the opaque ones
-    const uint32_t blended_varying_base = varyings;
-    for (DrawRec& d : blended) {
-        if ((uint64_t)varyings + d.vertex_count >= 0xFFFFFFF0ull) return fail(c, RZ_OVERFLOW, "too many vertices");
-        d.varying_base = varyings;
-        varyings += d.vertex_count;
-    }
+    if (object_count == 0 || !objects || surface_count == 0 || !surfaces) return fail(c, RZ_INVALID_ARGUMENT, "empty scene");
+    if (c->scenes.size() != 1) return fail(c, RZ_INVALID_STATE, "rz_set_objects applies to a single-scene context");
+    SceneHost& sh = c->scenes[0];
+    const int rc = check_surfaces(c, sh, object_count, surfaces, surface_count);
+    if (rc != RZ_OK) return rc;
+    cudaSetDevice(c->device);
+    c->objects.assign(objects, objects + object_count);
+    sh.object_base = 0;
+    sh.object_count = object_count;
+    sh.surfaces.assign(surfaces, surfaces + surface_count);
+    sh.has_objects = true;
+    return upload_objects(c);
+}
+
+int rz_add_scene(rz_ctx* c, const rz_mesh* meshes, uint32_t mesh_count, const rz_material* mats, uint32_t mat_count,
+                 const rz_texture* textures, uint32_t tex_count, const rz_sampler* samplers, uint32_t sampler_count,
+                 const rz_object* objects, uint32_t object_count, const rz_surface* surfaces, uint32_t surface_count,
+                 uint32_t* scene_index) {
+    if (!c) return RZ_INVALID_ARGUMENT;
+    if (object_count == 0 || !objects || surface_count == 0 || !surfaces) return fail(c, RZ_INVALID_ARGUMENT, "empty scene");
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graph(c);
-    dfree(c->d_objects);
-    dfree(c->d_shadow_draws);
-    dfree(c->d_opaque_draws);
-    dfree(c->d_shadow_mvp);
-    dfree(c->d_camera_consts);
-    dfree(c->d_varyings);
-    dfree(c->d_blended_draws);
-    dfree(c->d_blended_consts);
-    dfree(c->d_color16);
-    if (c->h_objects) cudaFreeHost(c->h_objects);
-    c->h_objects = nullptr;
-    RZ_CUDA(c, dalloc(&c->d_objects, object_count), "object buffer");
-    RZ_CUDA(c, cudaMallocHost(&c->h_objects, (size_t)object_count * sizeof(rz_object)), "object staging");
-    RZ_CUDA(c, dalloc(&c->d_shadow_draws, std::max<size_t>(shadow.size(), 1)), "shadow draw list");
-    RZ_CUDA(c, dalloc(&c->d_opaque_draws, std::max<size_t>(opaque.size(), 1)), "opaque draw list");
-    RZ_CUDA(c, dalloc(&c->d_shadow_mvp, std::max<size_t>(shadow.size(), 1) * 16), "shadow matrices");
-    RZ_CUDA(c, dalloc(&c->d_camera_consts, std::max<size_t>(opaque.size(), 1)), "camera constants");
-    RZ_CUDA(c, dalloc(&c->d_blended_draws, std::max<size_t>(blended.size(), 1)), "blended draw list");
-    RZ_CUDA(c, dalloc(&c->d_blended_consts, std::max<size_t>(blended.size(), 1)), "blended constants");
-    if (!blended.empty())
-        RZ_CUDA(c, dalloc(&c->d_color16, (size_t)c->width * c->height), "RGBA16F draw image");
-    RZ_CUDA(c, dalloc(&c->d_varyings, std::max<size_t>(varyings, 1) * 8), "varying records");
-    RZ_CUDA(c, cudaMemcpy(c->d_objects, objects, (size_t)object_count * sizeof(rz_object), cudaMemcpyHostToDevice), "upload objects");
-    if (!shadow.empty())
-        RZ_CUDA(c, cudaMemcpy(c->d_shadow_draws, shadow.data(), shadow.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
-    if (!opaque.empty())
-        RZ_CUDA(c, cudaMemcpy(c->d_opaque_draws, opaque.data(), opaque.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
-    if (!blended.empty())
-        RZ_CUDA(c, cudaMemcpy(c->d_blended_draws, blended.data(), blended.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
-    c->object_count = object_count;
-    c->shadow_draw_count = (uint32_t)shadow.size();
-    c->opaque_draw_count = (uint32_t)opaque.size();
-    c->blended_draw_count = blended_draws;
-    c->shadow_tris = shadow_tris;
-    c->opaque_tris = opaque_tris;
-    c->blended_tris = blended_tris;
-    c->varying_count = varyings;
-    c->blended_varying_base = blended_varying_base;
-    if (blended_tris) {
-        const int rb = size_pass(c, c->blended_pass, blended_tris, default_stamp_hint(blended_tris, c->width, c->height));
-        if (rb != RZ_OK) return rb;
+    // roll back the host arrays if the asset or its surfaces are rejected
+    const size_t nv = c->verts.size(), ni = c->idx.size(), nm = c->mesh_table.size(), nmat = c->materials.size();
+    const size_t ntex = c->tex_descs.size(), nsmp = c->samplers.size();
+    auto rollback = [&]() {
+        for (size_t i = ntex; i < c->tex_allocs.size(); ++i) cudaFree(c->tex_allocs[i]);
+        c->tex_allocs.resize(ntex);
+        c->verts.resize(nv);
+        c->pos.resize(nv);
+        c->idx.resize(ni);
+        c->mesh_table.resize(nm);
+        c->materials.resize(nmat);
+        c->tex_descs.resize(ntex);
+        c->samplers.resize(nsmp);
+    };
+    SceneHost sh;
+    int rc = append_asset(c, meshes, mesh_count, mats, mat_count, textures, tex_count, samplers, sampler_count, sh);
+    if (rc == RZ_OK) rc = check_surfaces(c, sh, object_count, surfaces, surface_count);
+    if (rc != RZ_OK) {
+        rollback();
+        return rc;
     }
-    int rc = size_pass(c, c->shadow_pass, shadow_tris, default_stamp_hint(shadow_tris, c->shadow_size, c->shadow_size));
+    sh.object_base = (uint32_t)c->objects.size();
+    sh.object_count = object_count;
+    c->objects.insert(c->objects.end(), objects, objects + object_count);
+    sh.surfaces.assign(surfaces, surfaces + surface_count);
+    sh.has_objects = true;
+    c->scenes.push_back(sh);
+    if (scene_index) *scene_index = (uint32_t)(c->scenes.size() - 1);
+    rc = upload_asset(c);
+    if (rc == RZ_OK) rc = upload_objects(c);
+    return rc;
+}
+
+int rz_set_views(rz_ctx* c, const rz_view* views, uint32_t count) {
+    if (!c || !views || count == 0) return RZ_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < count; ++i) {
+        const rz_view& v = views[i];
+        if (v.width == 0 || v.height == 0 || v.width > 16384 || v.height > 16384 || v.shadow_map_size == 0 ||
+            v.shadow_map_size > 16384)
+            return fail(c, RZ_INVALID_ARGUMENT, "bad view extent");
+        if (v.draw_config.pcf_mode > RZ_PCF_3X3) return fail(c, RZ_INVALID_ARGUMENT, "unknown pcf mode");
+        if (v.scene >= c->scenes.size()) return fail(c, RZ_INVALID_ARGUMENT, "view refers to a missing scene");
+    }
+    cudaSetDevice(c->device);
+    const int rc = ensure_scene_data(c, count);
     if (rc != RZ_OK) return rc;
-    rc = size_pass(c, c->camera_pass, opaque_tris, default_stamp_hint(opaque_tris, c->width, c->height));
-    if (rc != RZ_OK) return rc;
-    c->have_objects = true;
+    std::vector<ViewHost> vs(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        vs[i].scene = views[i].scene;
+        vs[i].width = views[i].width;
+        vs[i].height = views[i].height;
+        vs[i].shadow = views[i].shadow_map_size;
+        vs[i].dc = views[i].draw_config;
+        vs[i].has_scene_data = i < c->views.size() ? c->views[i].has_scene_data : false;
+    }
+    c->views = vs;
+    c->layout_dirty = true;
     return RZ_OK;
 }
 
 int rz_update_objects(rz_ctx* c, uint32_t offset, const rz_object* objects, uint32_t count) {
     if (!c) return RZ_INVALID_ARGUMENT;
-    if (!c->have_objects) return fail(c, RZ_INVALID_STATE, "rz_set_objects has not been called");
+    if (c->scenes.empty() || !c->scenes[0].has_objects) return fail(c, RZ_INVALID_STATE, "rz_set_objects has not been called");
     if (count == 0) return RZ_OK;
-    if (!objects || (uint64_t)offset + count > c->object_count) return fail(c, RZ_INVALID_ARGUMENT, "object range");
+    const SceneHost& sh = c->scenes[0];
+    if (!objects || (uint64_t)offset + count > sh.object_count) return fail(c, RZ_INVALID_ARGUMENT, "object range");
     cudaSetDevice(c->device);
     RZ_CUDA(c, cudaEventSynchronize(c->objects_copied), "wait staging");
-    std::memcpy(c->h_objects + offset, objects, (size_t)count * sizeof(rz_object));
-    RZ_CUDA(c, cudaMemcpyAsync(c->d_objects + offset, c->h_objects + offset, (size_t)count * sizeof(rz_object),
+    const uint32_t at = sh.object_base + offset;
+    std::memcpy(c->h_objects + at, objects, (size_t)count * sizeof(rz_object));
+    std::memcpy(c->objects.data() + at, objects, (size_t)count * sizeof(rz_object));
+    RZ_CUDA(c, cudaMemcpyAsync(c->d_objects + at, c->h_objects + at, (size_t)count * sizeof(rz_object),
                                cudaMemcpyHostToDevice, c->stream), "upload objects");
     RZ_CUDA(c, cudaEventRecord(c->objects_copied, c->stream), "record");
     return RZ_OK;
@@ -856,63 +1105,40 @@ int rz_update_objects(rz_ctx* c, uint32_t offset, const rz_object* objects, uint
 int rz_set_draw_config(rz_ctx* c, const rz_draw_config* cfg) {
     if (!c || !cfg) return RZ_INVALID_ARGUMENT;
     if (cfg->pcf_mode > RZ_PCF_3X3) return fail(c, RZ_INVALID_ARGUMENT, "unknown pcf mode");
-    c->draw_config = *cfg;
-    drop_graph(c);
+    c->views[0].dc = *cfg;
+    c->layout_dirty = true;
     return RZ_OK;
 }
 
-int rz_update(rz_ctx* c, const rz_scene_data* scene) {
+int rz_update_view(rz_ctx* c, uint32_t view, const rz_scene_data* scene) {
     if (!c || !scene) return RZ_INVALID_ARGUMENT;
+    if (view >= c->views.size()) return fail(c, RZ_INVALID_ARGUMENT, "no such view");
     cudaSetDevice(c->device);
     RZ_CUDA(c, cudaEventSynchronize(c->scene_copied), "wait staging");
-    std::memcpy(c->h_scene, scene, sizeof(rz_scene_data));
-    RZ_CUDA(c, cudaMemcpyAsync(c->d_scene, c->h_scene, sizeof(rz_scene_data), cudaMemcpyHostToDevice, c->stream),
-            "upload scene");
+    std::memcpy(c->h_scene_data + view, scene, sizeof(rz_scene_data));
+    RZ_CUDA(c, cudaMemcpyAsync(c->d_scene_data + view, c->h_scene_data + view, sizeof(rz_scene_data),
+                               cudaMemcpyHostToDevice, c->stream), "upload scene");
     RZ_CUDA(c, cudaEventRecord(c->scene_copied, c->stream), "record");
-    c->have_scene = true;
+    c->views[view].has_scene_data = true;
     return RZ_OK;
 }
+
+int rz_update(rz_ctx* c, const rz_scene_data* scene) { return rz_update_view(c, 0, scene); }
 
 int rz_render(rz_ctx* c) {
     const int ready = check_ready(c);
     if (ready != RZ_OK) return ready;
     cudaSetDevice(c->device);
+    if (c->asset_dirty) {
+        const int rc = upload_asset(c);
+        if (rc != RZ_OK) return rc;
+    }
+    if (c->layout_dirty) {
+        const int rc = build_layout(c);
+        if (rc != RZ_OK) return rc;
+    }
     if (c->grow_records || c->grow_chunks) {
-        // Size the queues from what the overflowing frame needed (exact counts
-        // from the device), with 25% headroom.
-        cudaStreamSynchronize(c->stream);
-        drop_graph(c);
-        c->queue_chunks = 0;
-        auto grow = [&](PassBuffers& p, const PassHeader& h) -> int {
-            const uint64_t want_chunks = (h.stamps + kChunkStamps - 1) / kChunkStamps;
-            const uint64_t want_recs = h.records_needed;
-            if (want_chunks > p.chunk_capacity) {
-                const uint64_t n = std::min<uint64_t>(want_chunks + want_chunks / 4 + 1024, 0xFFFFFFFFull);
-                dfree(p.chunk_map);
-                p.chunk_capacity = 0;
-                RZ_CUDA(c, dalloc(&p.chunk_map, (size_t)n), "chunk map");
-                p.chunk_capacity = (uint32_t)n;
-            }
-            if (want_recs > p.record_capacity) {
-                const uint64_t n = std::min<uint64_t>(want_recs + want_recs / 4 + 1024, 0xFFFFFFull);
-                dfree(p.records);
-                p.record_capacity = 0;
-                RZ_CUDA(c, dalloc(&p.records, (size_t)n), "raster records");
-                p.record_capacity = (uint32_t)n;
-            }
-            if (h.small_records > p.small_capacity) {
-                const uint64_t n = std::min<uint64_t>((uint64_t)h.small_records + h.small_records / 4 + 1024, 0xFFFFFFFFull);
-                dfree(p.small_records);
-                p.small_capacity = 0;
-                RZ_CUDA(c, dalloc(&p.small_records, (size_t)n), "small raster records");
-                p.small_capacity = (uint32_t)n;
-            }
-            return RZ_OK;
-        };
-        int rc = grow(c->shadow_pass, c->h_report->shadow);
-        if (rc == RZ_OK) rc = grow(c->camera_pass, c->h_report->camera);
-        if (rc == RZ_OK && c->blended_tris) rc = grow(c->blended_pass, c->h_report->blended);
-        c->grow_records = c->grow_chunks = false;
+        const int rc = grow_queues(c);
         if (rc != RZ_OK) return rc;
     }
     // Stage timing records events between the stages and enqueues directly.
@@ -979,29 +1205,27 @@ int rz_sync(rz_ctx* c, uint32_t timeout_ms) {
     return RZ_OK;
 }
 
-int rz_get_frame(rz_ctx* c, rz_frame_out* out) {
+int rz_get_view_frame(rz_ctx* c, uint32_t view, rz_frame_out* out) {
     if (!c || !out) return RZ_INVALID_ARGUMENT;
-    out->color_rgba8 = c->d_color;
-    out->depth_f32 = c->d_depth;
-    out->visibility_u64 = c->d_vis;
-    out->shadow_map_f32 = c->d_shadow;
-    out->width = c->width;
-    out->height = c->height;
-    out->shadow_map_size = c->shadow_size;
-    out->reserved = 0;
+    if (c->layout_dirty || view >= c->view_recs.size()) return fail(c, RZ_INVALID_STATE, "no rendered frame for this view");
+    *out = frame_of(c, view);
     return RZ_OK;
 }
 
+int rz_get_frame(rz_ctx* c, rz_frame_out* out) { return rz_get_view_frame(c, 0, out); }
+
 int rz_read_frame(rz_ctx* c, void* color_host, size_t color_bytes, void* depth_host, size_t depth_bytes) {
     if (!c) return RZ_INVALID_ARGUMENT;
-    const size_t need = (size_t)c->width * c->height * 4;
+    if (c->layout_dirty || c->view_recs.empty()) return fail(c, RZ_INVALID_STATE, "no rendered frame");
+    const ViewRec& r = c->view_recs[0];
+    const size_t need = (size_t)r.width * r.height * 4;
     if ((color_host && color_bytes < need) || (depth_host && depth_bytes < need))
         return fail(c, RZ_INVALID_ARGUMENT, "host buffer too small");
     cudaSetDevice(c->device);
     if (color_host)
-        RZ_CUDA(c, cudaMemcpyAsync(color_host, c->d_color, need, cudaMemcpyDeviceToHost, c->stream), "read colour");
+        RZ_CUDA(c, cudaMemcpyAsync(color_host, r.color, need, cudaMemcpyDeviceToHost, c->stream), "read colour");
     if (depth_host)
-        RZ_CUDA(c, cudaMemcpyAsync(depth_host, c->d_depth, need, cudaMemcpyDeviceToHost, c->stream), "read depth");
+        RZ_CUDA(c, cudaMemcpyAsync(depth_host, r.depth, need, cudaMemcpyDeviceToHost, c->stream), "read depth");
     return RZ_OK;
 }
 
@@ -1015,9 +1239,9 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->shadow_stamps = c->h_report->shadow.stamps;
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->error_flags;
-    // clears (2) + prep (1) + prep_camera (1) + setup/raster per pass with triangles + vertex + shade
-    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + (c->opaque_tris ? 2u : 0u) + 2u + (c->varying_count ? 1u : 0u) +
-                           (c->blended_tris ? 5u : 0u);
+    // clears (2) + shadow prep/setup/raster + camera prep/setup/raster + vertex + shade (+ blended: prep, setup, vertex, blend)
+    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + 1u + (c->opaque_tris ? 2u : 0u) +
+                           (c->varying_count ? 1u : 0u) + 1u + (c->blended_tris ? 4u : 0u);
     return RZ_OK;
 }
 

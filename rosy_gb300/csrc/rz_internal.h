@@ -19,8 +19,28 @@ struct DrawRec {
     uint32_t tri_base;     // first triangle id of this draw within the pass
     uint32_t varying_base; // camera pass: first varying record of this draw (one per mesh vertex)
     uint32_t vertex_count; // vertices of the draw's mesh
+    uint32_t view;         // the view this draw renders into
+    uint32_t pad[3];
 };
-static_assert(sizeof(DrawRec) == 32, "DrawRec layout");
+static_assert(sizeof(DrawRec) == 48, "DrawRec layout");
+
+// One view of a frame (a batch renders many): its targets, viewport sizes,
+// fixed-function state and scene constants. All views' targets live in pools.
+struct ViewRec {
+    int width, height;            // camera viewport
+    int shadow_w, shadow_h;       // shadow-map viewport
+    int cull_front, ccw_front;
+    int bias_enabled;
+    float bias_constant, bias_clamp, bias_slope;
+    uint32_t pcf_mode;
+    uint32_t shade_block_base;    // first 16x16 shading tile of this view (tiles are numbered view by view)
+    uint64_t* vis;                // width*height
+    uint32_t* color;              // width*height RGBA8
+    float* depth;                 // width*height
+    uint32_t* shadow;             // shadow_w*shadow_h depth bits
+    uint2* color16;               // width*height RGBA16F (only with blended surfaces)
+    const rz_scene_data* scene;
+};
 
 // gpu_material, src/Engine/Graphics.cpp:345-360, packed as in 4071-4150.
 struct GpuMaterial {
@@ -32,11 +52,11 @@ struct GpuMaterial {
 };
 static_assert(sizeof(GpuMaterial) == 64, "gpu_material is 64 bytes");
 
-// Bindless texture table entry. Texels are RGBA8 in one pool, level-major,
-// each level row-major (the caller's layout).
+// Bindless texture table entry. Texels are RGBA8, level-major, each level
+// row-major (the caller's layout), one device allocation per texture.
 struct TexDesc {
     uint32_t width, height, levels, srgb;
-    uint64_t base;             // first texel (u32 units) of level 0 in the pool
+    uint64_t base;             // device address of the texture's texels (level 0 first)
     uint32_t level_off[16];    // texel offset of each level from base
 };
 
@@ -61,7 +81,7 @@ struct TriRecord {
     uint32_t p0;                     // px0 | py0 << 16 (bounding box, pixels)
     uint32_t p1;                     // px1 | py1 << 16 (inclusive)
     uint32_t id;                     // camera pass: triangle id + 1
-    uint32_t stamps;                 // number of 8x4 stamps of the bounding box
+    uint32_t view;                   // view (target) of the triangle
     uint64_t stamp_offset;           // exclusive prefix of stamps over all records
 };
 static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
@@ -107,12 +127,9 @@ struct PassParams {
     const float4* pos;        // positions (x, y, z, pad)
     const uint32_t* indices;
     uint32_t vertex_count;
-    int width, height;        // viewport
-    int cull_front, ccw_front;
-    int bias_enabled;
-    float bias_constant, bias_clamp, bias_slope;
+    const ViewRec* views;
     int write_id;             // 1: camera pass (64-bit depth|id keys); 0: shadow (depth only)
-    int ordered;              // 1: keep every record in submission order (blended list)
+    int ordered;              // 1: keep every record in submission order, cull none (blended list)
     TriRecord* records;       // large records (stamp-balanced raster)
     uint32_t record_capacity;
     TriRecord* small_records; // small records (one lane each)
@@ -122,16 +139,12 @@ struct PassParams {
     uint32_t chunk_capacity;
     PassHeader* header;
     uint32_t* error_flags;
-    void* target;             // uint64_t* visibility or uint32_t* shadow depth bits
 };
 
 struct ShadeParams {
-    const uint64_t* vis;
-    const float* shadow;
-    int shadow_size;
-    uint32_t* color;          // RGBA8 out
-    float* depth;             // D32 out
-    int width, height;
+    const ViewRec* views;
+    uint32_t view_count;
+    uint32_t shade_blocks;    // 16x16 tiles over all views
     const DrawRec* draws;     // opaque list
     uint32_t draw_count;
     const DrawConsts* consts; // per opaque draw
@@ -145,11 +158,8 @@ struct ShadeParams {
     uint32_t texture_count;
     const SamplerBits* samplers;  // sampler_count + 1 entries (last = default)
     uint32_t sampler_count;
-    const uint32_t* texels;
-    const rz_scene_data* scene;
-    uint32_t pcf_mode;
     const float* srgb_table;      // 256 entries
-    uint2* color16;               // if set: k_shade stores the RGBA16F draw image here instead of RGBA8
+    int blended;                  // 1: k_shade stores the RGBA16F draw image (color16) for k_blend
 };
 
 // The blended list (src/Engine/Graphics.cpp:5654-5691) over the opaque result.
@@ -158,7 +168,6 @@ struct BlendParams {
     const TriRecord* records;     // setup records of the blended triangles, in submission order
     const PassHeader* header;
     uint32_t record_capacity;
-    const float* depth;           // opaque depth
 };
 
 // Up to four buffers to zero in one launch (16-byte stores, byte tail).
@@ -170,9 +179,9 @@ struct ClearList {
 
 // Launchers (rz_raster.cu / rz_shade.cu). All enqueue on `stream`.
 void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream);
-void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const float* proj16,
+void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
                  float* out_mvp, cudaStream_t stream);
-void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const rz_scene_data* scene,
+void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
                         DrawConsts* out, cudaStream_t stream);
 void launch_setup(const PassParams& p, cudaStream_t stream);
 void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream);

@@ -34,9 +34,10 @@ namespace rz {
 // ---------------------------------------------------------------------------
 
 __global__ void k_prep(const DrawRec* __restrict__ draws, uint32_t n, const rz_object* __restrict__ objects,
-                       const float* __restrict__ P, float* __restrict__ out) {
+                       const ViewRec* __restrict__ views, float* __restrict__ out) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
+    const float* P = views[draws[d].view].scene->shadow_projection_near;
     float A[16], B[16], C[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) A[i] = P[i];
@@ -48,10 +49,10 @@ __global__ void k_prep(const DrawRec* __restrict__ draws, uint32_t n, const rz_o
     for (int i = 0; i < 16; ++i) out[16 * d + i] = C[i];
 }
 
-void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const float* proj16, float* out_mvp,
+void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views, float* out_mvp,
                  cudaStream_t stream) {
     if (n == 0) return;
-    k_prep<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, proj16, out_mvp);
+    k_prep<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, views, out_mvp);
 }
 
 // ---------------------------------------------------------------------------
@@ -160,11 +161,25 @@ __device__ __forceinline__ int64_t area2(const SV& a, const SV& b, const SV& c) 
     return (int64_t)(b.X - a.X) * (int64_t)(c.Y - a.Y) - (int64_t)(c.X - a.X) * (int64_t)(b.Y - a.Y);
 }
 
+__device__ __forceinline__ uint32_t record_stamps(const TriRecord& r) {
+    const int px0 = r.p0 & 0xffff, py0 = r.p0 >> 16, px1 = r.p1 & 0xffff, py1 = r.p1 >> 16;
+    return (uint32_t)((px1 - px0) / kStampW + 1) * (uint32_t)((py1 - py0) / kStampH + 1);
+}
+
+// Viewport and fixed-function state of the view a triangle belongs to.
+struct ViewState {
+    int width, height;
+    int cull_front, ccw_front;
+    int bias_enabled;
+    float bias_constant, bias_clamp, bias_slope;
+    uint32_t view;
+};
+
 // Builds the record of a triangle ordered with S > 0. Returns 0 if its pixel
 // bounding box is empty, 2 for a small triangle (extent at most kSmallExtent
 // pixels each way, rasterised by one lane), 1 otherwise.
-__device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV& v2, int64_t S, const PassParams& P,
-                                           uint32_t id, TriRecord& r) {
+__device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV& v2, int64_t S, const ViewState& P,
+                                           bool ordered, uint32_t id, TriRecord& r) {
     const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
     const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
     const int px0 = max((minX + 127) >> 8, 0), px1 = min((maxX - 128) >> 8, P.width - 1);
@@ -201,11 +216,9 @@ __device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV&
     r.p0 = (uint32_t)px0 | ((uint32_t)py0 << 16);
     r.p1 = (uint32_t)px1 | ((uint32_t)py1 << 16);
     r.id = id;
-    const uint32_t nsx = (uint32_t)((px1 - px0) / kStampW + 1);
-    const uint32_t nsy = (uint32_t)((py1 - py0) / kStampH + 1);
-    r.stamps = nsx * nsy;
+    r.view = P.view;
     r.stamp_offset = 0;
-    const bool small = !P.ordered && (maxX - minX) <= kSmallExtent * 256 && (maxY - minY) <= kSmallExtent * 256;
+    const bool small = !ordered && (maxX - minX) <= kSmallExtent * 256 && (maxY - minY) <= kSmallExtent * 256;
     return small ? 2 : 1;
 }
 
@@ -223,6 +236,17 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         atomicOr(P.error_flags, kErrBadIndex);
         return;
     }
+    const ViewRec& VR = P.views[dr.view];
+    ViewState V;
+    V.view = dr.view;
+    V.width = P.write_id ? VR.width : VR.shadow_w;
+    V.height = P.write_id ? VR.height : VR.shadow_h;
+    V.cull_front = P.ordered ? 0 : VR.cull_front;
+    V.ccw_front = VR.ccw_front;
+    V.bias_enabled = P.write_id ? 0 : VR.bias_enabled;
+    V.bias_constant = VR.bias_constant;
+    V.bias_clamp = VR.bias_clamp;
+    V.bias_slope = VR.bias_slope;
     const float* M = P.mvp + (size_t)P.mvp_stride * d;
     float Mr[16];
 #pragma unroll
@@ -236,17 +260,17 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
     }
     const unsigned o0 = outcode(v[0]), o1 = outcode(v[1]), o2 = outcode(v[2]);
     if (o0 & o1 & o2) return;
-    const float hw = (float)P.width * 0.5f, hh = (float)P.height * 0.5f;
+    const float hw = (float)V.width * 0.5f, hh = (float)V.height * 0.5f;
     const uint32_t id = P.write_id ? (tri + 1u) : 0u;
     if (!(o0 | o1 | o2)) {
         if (!(v[0].w > 0.0f) || !(v[1].w > 0.0f) || !(v[2].w > 0.0f)) return;
         const SV a = to_screen(v[0], hw, hh), b = to_screen(v[1], hw, hh), c = to_screen(v[2], hw, hh);
         const int64_t S = area2(a, b, c);
         if (S == 0) return;
-        const bool front = P.ccw_front ? (S < 0) : (S > 0);
-        if (P.cull_front && front) return;
+        const bool front = V.ccw_front ? (S < 0) : (S > 0);
+        if (V.cull_front && front) return;
         TriRecord r;
-        const int kind = S > 0 ? make_record(a, b, c, S, P, id, r) : make_record(a, c, b, -S, P, id, r);
+        const int kind = S > 0 ? make_record(a, b, c, S, V, P.ordered != 0, id, r) : make_record(a, c, b, -S, V, P.ordered != 0, id, r);
         if (kind) emit(r, kind == 2);
         return;
     }
@@ -264,14 +288,14 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
     int64_t S = 0;
     for (int i = 1; i + 1 < n; ++i) S += area2(sv[0], sv[i], sv[i + 1]);
     if (S == 0) return;
-    const bool front = P.ccw_front ? (S < 0) : (S > 0);
-    if (P.cull_front && front) return;
+    const bool front = V.ccw_front ? (S < 0) : (S > 0);
+    if (V.cull_front && front) return;
     for (int i = 1; i + 1 < n; ++i) {
         const int64_t si = area2(sv[0], sv[i], sv[i + 1]);
         if (si == 0 || ((si > 0) != (S > 0))) continue;
         TriRecord r;
-        const int kind = si > 0 ? make_record(sv[0], sv[i], sv[i + 1], si, P, id, r)
-                                : make_record(sv[0], sv[i + 1], sv[i], -si, P, id, r);
+        const int kind = si > 0 ? make_record(sv[0], sv[i], sv[i + 1], si, V, P.ordered != 0, id, r)
+                                : make_record(sv[0], sv[i + 1], sv[i], -si, V, P.ordered != 0, id, r);
         if (kind) emit(r, kind == 2);
     }
 }
@@ -300,7 +324,7 @@ struct CountEmit {
             return;
         }
         ++recs;
-        stamps += r.stamps;
+        stamps += record_stamps(r);
     }
 };
 
@@ -327,7 +351,7 @@ struct WriteEmit {
         store_record(P->records + rec, r);
         // chunks whose first stamp lies inside this record start here
         uint64_t k = (stamp + kChunkStamps - 1) / kChunkStamps;
-        const uint64_t end = stamp + r.stamps;
+        const uint64_t end = stamp + record_stamps(r);
         for (; k * kChunkStamps < end; ++k) {
             if (k >= P->chunk_capacity) {
                 atomicOr(P->error_flags, kErrStampOverflow);
@@ -519,16 +543,29 @@ void launch_setup(const PassParams& p, cudaStream_t stream) {
 // With the top-left decision folded into the constant (E' = E - 1 on the other
 // edges) the test is E' >= 0 on all three edges.
 
+// The target of a view: visibility (camera pass) or shadow map, and its row pitch.
+struct Target {
+    void* ptr;
+    int pitch;
+};
+
 template <bool kWriteId>
-__device__ __forceinline__ void write_fragment(const PassParams& P, int px, int py, float z, uint32_t id) {
+__device__ __forceinline__ Target view_target(const PassParams& P, uint32_t view) {
+    const ViewRec& V = P.views[view];
+    if (kWriteId) return Target{V.vis, V.width};
+    return Target{V.shadow, V.shadow_w};
+}
+
+template <bool kWriteId>
+__device__ __forceinline__ void write_fragment(const Target& T, int px, int py, float z, uint32_t id) {
     if (!(z > 0.0f)) z = 0.0f;
     if (z > 1.0f) z = 1.0f;
-    const size_t p = (size_t)py * (size_t)P.width + (size_t)px;
+    const size_t p = (size_t)py * (size_t)T.pitch + (size_t)px;
     if (kWriteId) {
         const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
-        atomicMax(reinterpret_cast<unsigned long long*>(P.target) + p, key);
+        atomicMax(reinterpret_cast<unsigned long long*>(T.ptr) + p, key);
     } else {
-        atomicMax(reinterpret_cast<unsigned int*>(P.target) + p, __float_as_uint(z));
+        atomicMax(reinterpret_cast<unsigned int*>(T.ptr) + p, __float_as_uint(z));
     }
 }
 
@@ -543,6 +580,7 @@ __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecor
     const float bias = __int_as_float(q2.y);
     const int px0 = q2.z & 0xffff, py0 = (uint32_t)q2.z >> 16, px1 = q2.w & 0xffff, py1 = (uint32_t)q2.w >> 16;
     const uint32_t id = (uint32_t)q3.x;
+    const Target T = view_target<kWriteId>(P, (uint32_t)q3.y);
     // edge constants relative to vertex 0 (all values < 2^12 sub-pixels, products < 2^24)
     int32_t dx[3], dy[3], c[3];
 #pragma unroll
@@ -564,7 +602,7 @@ __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecor
             if ((e0 | e1 | e2) >= 0) {
                 float z = fmaf(dzdx, (float)rx, fmaf(dzdy, (float)ry, z0));
                 if (!kWriteId) z = z + bias;
-                write_fragment<kWriteId>(P, px, py, z, id);
+                write_fragment<kWriteId>(T, px, py, z, id);
             }
         }
     }
@@ -584,7 +622,7 @@ struct LargeRecord {
     int32_t X0, Y0;
     float z0, dzdx, dzdy, bias;
     int px0, py0, px1, py1;
-    uint32_t id, nsx;
+    uint32_t id, nsx, view;
     uint64_t begin, end;
 };
 
@@ -608,9 +646,10 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L)
     L.px1 = q2.w & 0xffff;
     L.py1 = (uint32_t)q2.w >> 16;
     L.id = (uint32_t)q3.x;
+    L.view = (uint32_t)q3.y;
     L.begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
-    L.end = L.begin + (uint32_t)q3.y;
     L.nsx = (uint32_t)((L.px1 - L.px0) / kStampW + 1);
+    L.end = L.begin + (uint64_t)L.nsx * (uint32_t)((L.py1 - L.py0) / kStampH + 1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const int a = (i + 1) % 3, b = (i + 2) % 3;
@@ -650,7 +689,7 @@ __device__ __forceinline__ void generic_edges(const LargeRecord& L, GenericEdges
 
 // Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
 template <bool kWriteId>
-__device__ __forceinline__ void raster_stamp(const PassParams& P, const LargeRecord& L, const GenericEdges& G, uint32_t sx,
+__device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord& L, const GenericEdges& G, uint32_t sx,
                                              uint32_t sy, int lx, int ly) {
     const int sx0 = L.px0 + (int)sx * kStampW, sy0 = L.py0 + (int)sy * kStampH;
     const int32_t PXo = sx0 * 256 + 128, PYo = sy0 * 256 + 128;
@@ -698,7 +737,7 @@ __device__ __forceinline__ void raster_stamp(const PassParams& P, const LargeRec
     }
     float z = fmaf(L.dzdx, fx, fmaf(L.dzdy, fy, L.z0));
     if (!kWriteId) z = z + L.bias;
-    write_fragment<kWriteId>(P, px, py, z, L.id);
+    write_fragment<kWriteId>(T, px, py, z, L.id);
 }
 
 // Incremental walk over the stamps of a medium record in raster order. Each
@@ -740,11 +779,11 @@ __device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, 
 }
 
 template <bool kWriteId>
-__device__ __forceinline__ void medium_step(const PassParams& P, const LargeRecord& L, MediumWalk& w) {
+__device__ __forceinline__ void medium_step(const Target& T, const LargeRecord& L, MediumWalk& w) {
     if (((w.e[0] | w.e[1] | w.e[2]) >= 0) && w.px <= L.px1 && w.py <= L.py1) {
         float z = fmaf(L.dzdx, w.fx, w.zrow);
         if (!kWriteId) z = z + L.bias;
-        write_fragment<kWriteId>(P, w.px, w.py, z, L.id);
+        write_fragment<kWriteId>(T, w.px, w.py, z, L.id);
     }
     if (++w.sx == L.nsx) {
         w.sx = 0;
@@ -802,16 +841,17 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
             const uint32_t n = (uint32_t)(seg_end - s);
             const uint32_t i = (uint32_t)(s - L.begin);
             const uint32_t sy = i / L.nsx, sx = i - sy * L.nsx;
+            const Target T = view_target<kWriteId>(P, L.view);
             if (L.medium) {
                 MediumWalk w;
                 medium_start(L, sx, sy, lx, ly, w);
-                for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId>(P, L, w);
+                for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId>(T, L, w);
             } else {
                 GenericEdges G;
                 generic_edges(L, G);
                 uint32_t x = sx, y = sy;
                 for (uint32_t j = 0; j < n; ++j) {
-                    raster_stamp<kWriteId>(P, L, G, x, y, lx, ly);
+                    raster_stamp<kWriteId>(T, L, G, x, y, lx, ly);
                     if (++x == L.nsx) {
                         x = 0;
                         ++y;

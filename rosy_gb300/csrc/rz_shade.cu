@@ -59,9 +59,10 @@ __device__ __forceinline__ V3 mulm3v(const float* N, V3 v) {
 // ---------------------------------------------------------------------------
 
 __global__ void k_prep_camera(const DrawRec* __restrict__ draws, uint32_t n, const rz_object* __restrict__ objects,
-                              const rz_scene_data* __restrict__ sd, DrawConsts* __restrict__ out) {
+                              const ViewRec* __restrict__ views, DrawConsts* __restrict__ out) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
+    const rz_scene_data* sd = views[draws[d].view].scene;
     const rz_object& gd = objects[draws[d].object];
     float W[16], VP[16], C[16];
 #pragma unroll
@@ -100,10 +101,10 @@ __global__ void k_prep_camera(const DrawRec* __restrict__ draws, uint32_t n, con
     }
 }
 
-void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const rz_scene_data* scene,
+void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
                         DrawConsts* out, cudaStream_t stream) {
     if (n == 0) return;
-    k_prep_camera<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, scene, out);
+    k_prep_camera<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, views, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -313,7 +314,7 @@ struct Sampler {
     const float* unorm;  // shared-memory table: byte -> byte / 255
 
     __device__ __forceinline__ void texel(const TexDesc& t, uint32_t off, int w, int i, int j, float out[4]) const {
-        const uint32_t v = __ldg(&P->texels[t.base + off + (uint32_t)j * (uint32_t)w + (uint32_t)i]);
+        const uint32_t v = __ldg(reinterpret_cast<const uint32_t*>(t.base) + off + (uint32_t)j * (uint32_t)w + (uint32_t)i);
         const uint32_t r = v & 0xffu, g = (v >> 8) & 0xffu, b = (v >> 16) & 0xffu, a = v >> 24;
         if (t.srgb) {
             out[0] = srgb[r];
@@ -473,7 +474,7 @@ __device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughnes
 }
 
 // fragmentMain, src/shaders/basic.slang:137-344. Returns false on discard.
-__device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, const GpuMaterial* md, const Frag& bv,
+__device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const GpuMaterial* md, const Frag& bv,
                               const Sampler& smp, float out[4]) {
     const V3 ambientLight{sd.ambient_color[0], sd.ambient_color[1], sd.ambient_color[2]};
     float outFragColor[4] = {bv.color[0], bv.color[1], bv.color[2], bv.color[3]};
@@ -548,7 +549,8 @@ __device__ bool fragment_main(const ShadeParams& P, const rz_scene_data& sd, con
     }
     if (sd.light_enabled > 0) {
         float shadowFactor = 1.0f;
-        if (sd.shadows_enabled == 1) shadowFactor = pcf(P.shadow, P.shadow_size, bv.csm, P.pcf_mode);
+        if (sd.shadows_enabled == 1)
+            shadowFactor = pcf(reinterpret_cast<const float*>(VR.shadow), VR.shadow_w, bv.csm, VR.pcf_mode);
         if (sd.brdf_lighting_enabled == 0) {
             const float ml = fmaxf(cosTheta, 0.0f);
             const V3 sunLight{sd.sunlight_color[0] * ml, sd.sunlight_color[1] * ml, sd.sunlight_color[2] * ml};
@@ -642,7 +644,7 @@ __global__ void __launch_bounds__(256) k_vertex(ShadeParams P, uint32_t first) {
     v.color[0] = q2.z; v.color[1] = q2.w; v.color[2] = q3.x; v.color[3] = q3.y;
     v.uv[0] = q3.z; v.uv[1] = q3.w;
     VsOut o;
-    vertex_main(*P.scene, gd, dc, md != nullptr, has_nm, v, o);
+    vertex_main(*P.views[dr.view].scene, gd, dc, md != nullptr, has_nm, v, o);
     const float4 clip = transform_point(dc.mvp, v.position[0], v.position[1], v.position[2]);
     float4* dst = P.varyings + (size_t)i * kVaryingF4;
     dst[0] = make_float4(o.normal.x, o.normal.y, o.normal.z, o.viewDir.x);
@@ -667,8 +669,8 @@ void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stre
 
 // Shade triangle `tri` (pass-global id) at pixel (px, py) from the varying
 // records of its three vertices.
-__device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const Sampler& smp, uint32_t tri, int px, int py,
-                            float out[4]) {
+__device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_scene_data& sd, const Sampler& smp, uint32_t tri,
+                            int px, int py, float out[4]) {
     const uint32_t d = find_draw(P.draws, P.draw_count, tri);
     const DrawRec dr = P.draws[d];
     const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
@@ -684,11 +686,11 @@ __device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const
         clip[k] = make_float4(q.y, q.z, 0.0f, q.w);
     }
     float b[3], bq0[3], bqx[3], bqy[3];
-    barycentrics(clip[0], clip[1], clip[2], px, py, P.width, P.height, b);
+    barycentrics(clip[0], clip[1], clip[2], px, py, VR.width, VR.height, b);
     const int qx = px & ~1, qy = py & ~1;
-    barycentrics(clip[0], clip[1], clip[2], qx, qy, P.width, P.height, bq0);
-    barycentrics(clip[0], clip[1], clip[2], qx + 1, qy, P.width, P.height, bqx);
-    barycentrics(clip[0], clip[1], clip[2], qx, qy + 1, P.width, P.height, bqy);
+    barycentrics(clip[0], clip[1], clip[2], qx, qy, VR.width, VR.height, bq0);
+    barycentrics(clip[0], clip[1], clip[2], qx + 1, qy, VR.width, VR.height, bqx);
+    barycentrics(clip[0], clip[1], clip[2], qx, qy + 1, VR.width, VR.height, bqy);
     const bool debug_extra = sd.fragment_output == 1 || sd.fragment_output == 7;
     Frag f;
     float u0[2], ux[2], uy[2];
@@ -753,49 +755,64 @@ __device__ bool shade_pixel(const ShadeParams& P, const rz_scene_data& sd, const
         f.duvdx[i] = ux[i] - u0[i];
         f.duvdy[i] = uy[i] - u0[i];
     }
-    return fragment_main(P, sd, md, f, smp, out);
+    return fragment_main(VR, sd, md, f, smp, out);
+}
+
+// The view a 16x16 shading tile belongs to (tiles are numbered view by view).
+__device__ __forceinline__ uint32_t tile_view(const ViewRec* __restrict__ views, uint32_t n, uint32_t tile) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&views[mid].shade_block_base) <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
 __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
         s_srgb[t] = P.srgb_table[t];
         s_unorm[t] = (float)t / 255.0f;
+        if (t == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x);
     }
     __syncthreads();
-    const int px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int py = blockIdx.y * blockDim.y + threadIdx.y;
-    if (px >= P.width || py >= P.height) return;
-    const size_t p = (size_t)py * P.width + px;
-    const unsigned long long key = P.vis[p];
+    const ViewRec& VR = P.views[s_view];
+    const uint32_t lt = blockIdx.x - VR.shade_block_base;
+    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
+    const int px = (int)(lt % tiles_x) * 16 + threadIdx.x;
+    const int py = (int)(lt / tiles_x) * 16 + threadIdx.y;
+    if (px >= VR.width || py >= VR.height) return;
+    const size_t p = (size_t)py * VR.width + px;
+    const unsigned long long key = VR.vis[p];
     const uint32_t id = (uint32_t)key;
     float col[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // clear colour, src/Engine/Graphics.cpp:5416-5419
     if (id != 0) {
         const Sampler smp{&P, s_srgb, s_unorm};
         float o[4];
-        if (shade_pixel(P, *P.scene, smp, id - 1u, px, py, o)) {
+        if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o)) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) col[k] = o[k];
         }
     }
-    P.depth[p] = __uint_as_float((uint32_t)(key >> 32));
-    if (P.color16) {  // blended surfaces follow: keep the RGBA16F draw image
+    VR.depth[p] = __uint_as_float((uint32_t)(key >> 32));
+    if (P.blended) {  // blended surfaces follow: keep the RGBA16F draw image
         const __half2 rg = __floats2half2_rn(col[0], col[1]), ba = __floats2half2_rn(col[2], col[3]);
-        P.color16[p] = make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&ba));
+        VR.color16[p] = make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&ba));
         return;
     }
     const uint32_t r = encode_srgb8(half_round(col[0]));
     const uint32_t g = encode_srgb8(half_round(col[1]));
     const uint32_t b = encode_srgb8(half_round(col[2]));
     const uint32_t a = encode_unorm8(half_round(col[3]));
-    P.color[p] = r | (g << 8) | (b << 16) | (a << 24);
+    VR.color[p] = r | (g << 8) | (b << 16) | (a << 24);
 }
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
-    const dim3 block(16, 16);
-    const dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
-    k_shade<<<grid, block, 0, stream>>>(p);
+    if (p.shade_blocks == 0) return;
+    k_shade<<<p.shade_blocks, dim3(16, 16), 0, stream>>>(p);
 }
 
 // ---------------------------------------------------------------------------
@@ -815,24 +832,31 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
     __shared__ float s_srgb[256], s_unorm[256];
     __shared__ uint32_t s_list[kBlendBatch];
     __shared__ uint32_t s_count[256 / 32 + 1];
+    __shared__ uint32_t s_view;
     const ShadeParams& P = B.sh;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     s_srgb[tid] = P.srgb_table[tid];
     s_unorm[tid] = (float)tid / 255.0f;
-    const int tx0 = blockIdx.x * 16, ty0 = blockIdx.y * 16;
+    if (tid == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x);
+    __syncthreads();
+    const uint32_t view = s_view;
+    const ViewRec& VR = P.views[view];
+    const uint32_t lt = blockIdx.x - VR.shade_block_base;
+    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
+    const int tx0 = (int)(lt % tiles_x) * 16, ty0 = (int)(lt / tiles_x) * 16;
     const int px = tx0 + threadIdx.x, py = ty0 + threadIdx.y;
-    const bool inside = px < P.width && py < P.height;
-    const size_t p = inside ? (size_t)py * P.width + px : 0;
+    const bool inside = px < VR.width && py < VR.height;
+    const size_t p = inside ? (size_t)py * VR.width + px : 0;
     float col[4] = {0.f, 0.f, 0.f, 0.f};
     float dst_depth = 0.f;
     if (inside) {
-        const uint2 c = P.color16[p];
+        const uint2 c = VR.color16[p];
         const __half2 rg = *reinterpret_cast<const __half2*>(&c.x), ba = *reinterpret_cast<const __half2*>(&c.y);
         col[0] = __low2float(rg);
         col[1] = __high2float(rg);
         col[2] = __low2float(ba);
         col[3] = __high2float(ba);
-        dst_depth = B.depth[p];
+        dst_depth = VR.depth[p];
     }
     const Sampler smp{&P, s_srgb, s_unorm};
     const uint32_t n = min(B.header->records, B.record_capacity);
@@ -846,7 +870,7 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
             if (r < n) {
                 const TriRecord& rec = B.records[r];
                 const int bx0 = rec.p0 & 0xffff, by0 = rec.p0 >> 16, bx1 = rec.p1 & 0xffff, by1 = rec.p1 >> 16;
-                if (bx1 >= tx0 && bx0 <= tx0 + 15 && by1 >= ty0 && by0 <= ty0 + 15) mask |= 1u << k;
+                if (rec.view == view && bx1 >= tx0 && bx0 <= tx0 + 15 && by1 >= ty0 && by0 <= ty0 + 15) mask |= 1u << k;
             }
         }
         const uint32_t cnt = __popc(mask);
@@ -891,7 +915,7 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
                 if (z > 1.0f) z = 1.0f;
                 if (!(z >= dst_depth)) continue;
                 float s4[4];
-                if (!shade_pixel(P, *P.scene, smp, rec.id - 1u, px, py, s4)) continue;
+                if (!shade_pixel(P, VR, *VR.scene, smp, rec.id - 1u, px, py, s4)) continue;
                 const float a = s4[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) col[k] = half_round(s4[k] * a + col[k] * (1.0f - a));
@@ -905,13 +929,12 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
     const uint32_t g = encode_srgb8(col[1]);
     const uint32_t b = encode_srgb8(col[2]);
     const uint32_t a = encode_unorm8(col[3]);
-    P.color[p] = r | (g << 8) | (b << 16) | (a << 24);
+    VR.color[p] = r | (g << 8) | (b << 16) | (a << 24);
 }
 
 void launch_blend(const BlendParams& p, cudaStream_t stream) {
-    const dim3 block(16, 16);
-    const dim3 grid((p.sh.width + 15) / 16, (p.sh.height + 15) / 16);
-    k_blend<<<grid, block, 0, stream>>>(p);
+    if (p.sh.shade_blocks == 0) return;
+    k_blend<<<p.sh.shade_blocks, dim3(16, 16), 0, stream>>>(p);
 }
 
 }  // namespace rz

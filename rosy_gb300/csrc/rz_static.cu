@@ -40,7 +40,9 @@ constexpr size_t kOffHeader = kOffTiles + ((kStaticTiles * sizeof(uint64_t) + 25
 constexpr size_t kOffDraw = kOffHeader + 256;
 constexpr size_t kOffMvp = kOffDraw + 256;
 constexpr size_t kOffFlags = kOffMvp + 256;
-constexpr size_t kStaticBytes = kOffFlags + 256;
+constexpr size_t kOffView = kOffFlags + 256;
+constexpr size_t kStaticBytes = kOffView + 256;
+static_assert(sizeof(ViewRec) <= 256, "view record fits its slot");
 static_assert(kOffSmall % 256 == 0 && kOffChunks % 256 == 0 && kOffTiles % 256 == 0, "scratch parts are 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
@@ -50,6 +52,7 @@ struct StaticPrepArgs {
     float world[16];
     uint32_t tri_count;
     uint32_t vertex_count;
+    ViewRec view;  // the target and fixed-function state of the call
 };
 
 // Clears the parts of the shared scratch that must start at zero, and writes the
@@ -72,6 +75,7 @@ __global__ void k_static_prep(StaticPrepArgs a) {
         mat4_mul(a.proj, a.world, C);
         float* mvp = reinterpret_cast<float*>(base + kOffMvp);
         for (int i = 0; i < 16; ++i) mvp[i] = C[i];
+        *reinterpret_cast<ViewRec*>(base + kOffView) = a.view;
     }
 }
 
@@ -123,6 +127,17 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
     }
     a.tri_count = tris;
     a.vertex_count = vertex_count;
+    a.view.shadow_w = (int)width;
+    a.view.shadow_h = (int)height;
+    a.view.width = (int)width;
+    a.view.height = (int)height;
+    a.view.cull_front = cfg->cull_enabled ? 1 : 0;
+    a.view.ccw_front = cfg->reverse_winding_order_enabled ? 1 : 0;
+    a.view.bias_enabled = cfg->depth_bias_enabled ? 1 : 0;
+    a.view.bias_constant = cfg->depth_bias_constant;
+    a.view.bias_clamp = cfg->depth_bias_clamp;
+    a.view.bias_slope = cfg->depth_bias_slope_factor;
+    a.view.shadow = reinterpret_cast<uint32_t*>(depth_out);
     k_static_prep<<<1, 128, 0, s>>>(a);
     if (tris) {
         PassParams p{};
@@ -134,14 +149,7 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.pos = static_cast<const float4*>(positions);
         p.indices = indices;
         p.vertex_count = vertex_count;
-        p.width = (int)width;
-        p.height = (int)height;
-        p.cull_front = cfg->cull_enabled ? 1 : 0;
-        p.ccw_front = cfg->reverse_winding_order_enabled ? 1 : 0;
-        p.bias_enabled = cfg->depth_bias_enabled ? 1 : 0;
-        p.bias_constant = cfg->depth_bias_constant;
-        p.bias_clamp = cfg->depth_bias_clamp;
-        p.bias_slope = cfg->depth_bias_slope_factor;
+        p.views = reinterpret_cast<const ViewRec*>(scratch + kOffView);
         p.write_id = 0;
         p.records = reinterpret_cast<TriRecord*>(scratch + kOffRecords);
         p.record_capacity = kStaticRecords;
@@ -152,7 +160,6 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.chunk_capacity = kStaticChunks;
         p.header = reinterpret_cast<PassHeader*>(scratch + kOffHeader);
         p.error_flags = reinterpret_cast<uint32_t*>(scratch + kOffFlags);
-        p.target = depth_out;
         launch_setup(p, s);
         launch_raster(p, sms, s);
     }

@@ -58,6 +58,47 @@ class Graphics:
         self._check(self._lib.rz_set_objects(self._ctx, _abi.ptr(objects), len(objects),
                                              _abi.ptr(surfaces), len(surfaces)), "rz_set_objects")
 
+    # -- batched views -------------------------------------------------------------
+    def add_scene(self, scene: Scene) -> int:
+        """Appends a scene (asset + objects + surfaces); returns its index."""
+        m = _abi.Marshalled(scene)
+        self._batch_keep = getattr(self, "_batch_keep", []) + [m]
+        idx = C.c_uint32()
+        self._check(self._lib.rz_add_scene(
+            self._ctx, C.cast(m.meshes, C.c_void_p), len(scene.meshes), _abi.ptr(m.materials), len(m.materials),
+            C.cast(m.textures, C.c_void_p), m.n_textures, _abi.ptr(m.samplers), len(m.samplers),
+            _abi.ptr(m.objects), len(m.objects), _abi.ptr(m.surfaces), len(m.surfaces), C.byref(idx)), "rz_add_scene")
+        return int(idx.value)
+
+    def set_views(self, views) -> None:
+        """views: sequence of (scene_index, width, height, shadow_map_size, draw_config record)."""
+        arr = (_abi.RzView * len(views))()
+        for i, (sc_i, w, h, sz, dc) in enumerate(views):
+            arr[i].scene, arr[i].width, arr[i].height, arr[i].shadow_map_size = sc_i, w, h, sz
+            C.memmove(C.byref(arr[i].draw_config), np.ascontiguousarray(dc).ctypes.data, 32)
+        self._views = list(views)
+        self._check(self._lib.rz_set_views(self._ctx, arr, len(views)), "rz_set_views")
+
+    def update_view(self, view: int, scene_data: np.ndarray) -> None:
+        sd = np.ascontiguousarray(scene_data)
+        self._check(self._lib.rz_update_view(self._ctx, view, _abi.ptr(sd)), "rz_update_view")
+
+    def download_view(self, view: int) -> dict:
+        """Colour, depth, ids and shadow map of one view of the last frame."""
+        f = _abi.RzFrameOut()
+        self._check(self._lib.rz_get_view_frame(self._ctx, view, C.byref(f)), "rz_get_view_frame")
+        self.sync()
+        W, H, S = f.width, f.height, f.shadow_map_size
+        out = {
+            "vis": device_array(f.visibility_u64, (H, W), np.uint64),
+            "shadow": device_array(f.shadow_map_f32, (S, S), np.float32),
+            "color": device_array(f.color_rgba8, (H, W, 4), np.uint8),
+            "depth": device_array(f.depth_f32, (H, W), np.float32),
+        }
+        ids = (out["vis"] & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        out["ids"] = np.where(ids > 0, ids - np.uint32(f.triangle_id_base), 0).astype(np.uint32)
+        return out
+
     def update_objects(self, offset: int, objects: np.ndarray) -> None:
         """The go_update upload (mob transforms) of src/Engine/Graphics.cpp:5120-5138."""
         objects = np.ascontiguousarray(objects, np.float32)

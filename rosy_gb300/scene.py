@@ -582,3 +582,49 @@ def with_blended(s: Scene, fraction: float = 0.5, alpha: float = 0.6, mask_cutof
     out.textures = textures
     out.name = s.name + ("_mask" if mask_cutoff is not None else "_blended")
     return out
+
+
+def view_of(s: Scene, width: int, height: int, shadow_size: int, camera: int = 0, fov_deg: float = 60.0) -> Scene:
+    """The scene seen through camera `camera` at another extent and shadow-map size."""
+    out = Scene(**{k: getattr(s, k) for k in s.__dataclass_fields__})
+    src = s.cameras[camera % len(s.cameras)]
+    view = src["view"][0].reshape(4, 4).T.astype(np.float64)
+    cam = np.linalg.inv(view)[:3, 3]
+    sun = src["sun_position"][0]
+    spn = src["shadow_projection_near"][0].reshape(4, 4).T.astype(np.float64)
+    proj = projection(width / height, math.radians(fov_deg))
+    rec = scene_record(view, proj, sun, spn, cam, width, height)
+    for k in ("fragment_output", "light_enabled", "tangent_space_enabled", "shadows_enabled", "normal_maps_enabled",
+              "brdf_lighting_enabled", "flip_lights", "flip_tangents"):
+        rec[k] = src[k]
+    out.scene = rec
+    out.cameras = [rec]
+    out.width, out.height, out.shadow_size = width, height, shadow_size
+    return out
+
+
+def batch_views(seed: int = 0, views: int = 256, scenes: int = 16, min_tris: int = 1000, max_tris: int = 200000,
+                min_size: int = 64, max_size: int = 1024, min_shadow: int = 512, max_shadow: int = 2048,
+                texture_size: int = 256):
+    """Many views of uneven size over several scenes: `scenes` seeded scenes with
+    log-uniform triangle counts in [min_tris, max_tris], and `views` views with
+    log-uniform extents in [min_size, max_size]^2 and log-uniform shadow maps in
+    [min_shadow, max_shadow]^2, each on a random scene and spline camera.
+    Returns (scene list, [(scene index, view Scene)])."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    scene_list = []
+    for k in range(scenes):
+        tris = int(round(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris)))))
+        meshes = int(max(1, min(64, tris // 2048)))
+        per = max(128, (tris // meshes) // 128 * 128)
+        scene_list.append(scene_scale(seed=seed * 1000 + k, meshes=meshes, triangles_per_mesh=per,
+                                      materials=max(1, min(8, meshes)), texture_size=texture_size, width=512,
+                                      height=512, shadow_size=min_shadow, frames=8))
+    out = []
+    for v in range(views):
+        k = int(rng.integers(0, scenes))
+        w = int(round(math.exp(rng.uniform(math.log(min_size), math.log(max_size)))))
+        h = int(round(math.exp(rng.uniform(math.log(min_size), math.log(max_size)))))
+        sz = int(round(math.exp(rng.uniform(math.log(min_shadow), math.log(max_shadow)))))
+        out.append((k, view_of(scene_list[k], w, h, sz, camera=int(rng.integers(0, 8)))))
+    return scene_list, out
