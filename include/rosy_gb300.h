@@ -344,6 +344,25 @@ int rz_update_view(struct rz_ctx* ctx, uint32_t view, const rz_scene_data* scene
 /* Device pointers of one view's frame buffers (rz_get_frame is view 0). */
 int rz_get_view_frame(struct rz_ctx* ctx, uint32_t view, rz_frame_out* out);
 
+/* Raster work distribution and batching (see rz_autotune). */
+typedef struct rz_tuning {
+    uint32_t chunk_stamps;  /* stamps (8x4 pixels) per raster work chunk, the unit a warp takes: 8..256 */
+    uint32_t small_extent;  /* triangles up to this extent (pixels, each way) are rasterised one per lane: 1..16 */
+    uint32_t queue_chunks;  /* raster work-queue depth per pass in chunks (0 = sized from the scene) */
+    uint32_t batched;       /* 1: each stage is one launch over all views; 0: per-view sequential launches */
+} rz_tuning;
+
+/* Sets / reads the tuning of the following frames. */
+int rz_set_tuning(struct rz_ctx* ctx, const rz_tuning* tuning);
+int rz_get_tuning(struct rz_ctx* ctx, rz_tuning* tuning);
+
+/* Autotuner: renders the current views `frames` times (after one warm-up
+ * frame) with every candidate of chunk_stamps in {16, 32, 64} x small_extent in
+ * {4, 8, 12}, measures device time with CUDA events, applies the fastest and
+ * returns it; `ms` (optional) receives the mean frame time of each candidate in
+ * that order. The views need their scene constants (rz_update_view) first. */
+int rz_autotune(struct rz_ctx* ctx, uint32_t frames, rz_tuning* chosen, float* ms, uint32_t capacity);
+
 /* Frame stages timed by rz_get_stage_times (CUDA events on the context's stream). */
 #define RZ_STAGE_SHADOW_CLEAR 0u  /* shadow-map clear */
 #define RZ_STAGE_SHADOW_SETUP 1u  /* shadow draw matrices + triangle setup */

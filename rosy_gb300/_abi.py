@@ -41,6 +41,11 @@ class RzView(C.Structure):
                 ("shadow_map_size", C.c_uint32), ("draw_config", RzDrawConfig)]
 
 
+class RzTuning(C.Structure):
+    _fields_ = [("chunk_stamps", C.c_uint32), ("small_extent", C.c_uint32), ("queue_chunks", C.c_uint32),
+                ("batched", C.c_uint32)]
+
+
 class RzFrameOut(C.Structure):
     _fields_ = [("color_rgba8", C.c_void_p), ("depth_f32", C.c_void_p), ("visibility_u64", C.c_void_p),
                 ("shadow_map_f32", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),

@@ -26,7 +26,7 @@ EXPORTS = [
     "rz_set_draw_config", "rz_update", "rz_render", "rz_sync", "rz_get_frame", "rz_read_frame",
     "rz_get_stats", "rz_get_stream", "rz_last_error", "rz_abi_version", "rz_set_stage_timing",
     "rz_get_stage_times", "rz_shadow_depth_static", "rz_add_scene", "rz_set_views", "rz_update_view",
-    "rz_get_view_frame",
+    "rz_get_view_frame", "rz_set_tuning", "rz_get_tuning", "rz_autotune",
 ]
 
 _lib = None
@@ -79,7 +79,11 @@ def load(build_if_missing: bool = False):
     lib.rz_set_views.argtypes = [P, P, u32]
     lib.rz_update_view.argtypes = [P, u32, P]
     lib.rz_get_view_frame.argtypes = [P, u32, C.POINTER(_abi.RzFrameOut)]
-    for name in ("rz_add_scene", "rz_set_views", "rz_update_view", "rz_get_view_frame"):
+    lib.rz_set_tuning.argtypes = [P, C.POINTER(_abi.RzTuning)]
+    lib.rz_get_tuning.argtypes = [P, C.POINTER(_abi.RzTuning)]
+    lib.rz_autotune.argtypes = [P, u32, C.POINTER(_abi.RzTuning), C.POINTER(C.c_float), u32]
+    for name in ("rz_add_scene", "rz_set_views", "rz_update_view", "rz_get_view_frame", "rz_set_tuning",
+                 "rz_get_tuning", "rz_autotune"):
         getattr(lib, name).restype = C.c_int
     lib.rz_abi_version.argtypes = []
     lib.rz_abi_version.restype = u32

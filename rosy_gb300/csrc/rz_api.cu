@@ -88,6 +88,9 @@ struct rz_ctx {
     cudaStream_t side = nullptr;  // shadow pass branch of the frame graph
     cudaEvent_t fork = nullptr, join = nullptr;
     uint32_t queue_chunks = 0;    // fixed work-queue depth (0 = sized from the scene)
+    uint32_t chunk_stamps = kChunkStamps;
+    uint32_t small_extent = kSmallExtent;
+    bool batched = true;          // false: per-view sequential launches
     std::string last_error;
 
     // asset of all scenes, concatenated (host copies of the small arrays, device arrays)
@@ -123,6 +126,13 @@ struct rz_ctx {
     ViewRec* d_views = nullptr;
     std::vector<ViewRec> view_recs;
     std::vector<uint32_t> view_id_base;  // first opaque triangle id of each view
+    // per-view ranges for sequential launches
+    struct ViewRange {
+        uint32_t shadow_tri_base, shadow_tris, opaque_tri_base, opaque_tris;
+        uint32_t varying_begin, varying_end, block_base, blocks;
+        size_t pix_off, pix, shadow_off, shadow;
+    };
+    std::vector<ViewRange> ranges;
     uint64_t* d_vis = nullptr;
     uint32_t* d_color = nullptr;
     float* d_depth = nullptr;
@@ -200,7 +210,7 @@ void free_pass(PassBuffers& p) {
 int size_pass(rz_ctx* c, PassBuffers& p, uint32_t tris, uint64_t stamps_hint) {
     const uint32_t rec_cap = tris + tris / 4 + 4096;
     const uint32_t tiles = (uint32_t)setup_ctas(tris) + 1;
-    uint64_t chunks = (stamps_hint + kChunkStamps - 1) / kChunkStamps + 1024;
+    uint64_t chunks = (stamps_hint + c->chunk_stamps - 1) / c->chunk_stamps + 1024;
     if (c->queue_chunks) chunks = c->queue_chunks;
     if (chunks > 0xFFFFFFFFull) chunks = 0xFFFFFFFFull;
     if (rec_cap > p.record_capacity) {
@@ -475,9 +485,20 @@ int build_layout(rz_ctx* c) {
     std::vector<DrawRec> shadow_list, opaque, blended;
     uint64_t shadow_tris = 0, opaque_tris = 0, blended_tris = 0, varyings = 0;
     c->view_id_base.assign(c->views.size(), 0);
+    c->ranges.assign(c->views.size(), rz_ctx::ViewRange{});
     for (uint32_t vi = 0; vi < c->views.size(); ++vi) {
         const ViewHost& v = c->views[vi];
         c->view_id_base[vi] = (uint32_t)opaque_tris;
+        rz_ctx::ViewRange& rg = c->ranges[vi];
+        rg.shadow_tri_base = (uint32_t)shadow_tris;
+        rg.opaque_tri_base = (uint32_t)opaque_tris;
+        rg.varying_begin = (uint32_t)varyings;
+        rg.block_base = block_base[vi];
+        rg.blocks = ((v.width + 15) / 16) * ((v.height + 15) / 16);
+        rg.pix_off = pix_off[vi];
+        rg.pix = (size_t)v.width * v.height;
+        rg.shadow_off = shadow_off[vi];
+        rg.shadow = (size_t)v.shadow * v.shadow;
         if (v.scene >= c->scenes.size()) return fail(c, RZ_INVALID_STATE, "view refers to a missing scene");
         const SceneHost& sh = c->scenes[v.scene];
         if (!sh.has_objects) return fail(c, RZ_INVALID_STATE, "scene has no objects (rz_set_objects)");
@@ -507,6 +528,9 @@ int build_layout(rz_ctx* c) {
                 opaque_tris += d.tri_count;
             }
         }
+        rg.shadow_tris = (uint32_t)(shadow_tris - rg.shadow_tri_base);
+        rg.opaque_tris = (uint32_t)(opaque_tris - rg.opaque_tri_base);
+        rg.varying_end = (uint32_t)varyings;
     }
     const uint64_t blended_varying_base = varyings;
     for (DrawRec& d : blended) {
@@ -612,6 +636,8 @@ PassParams pass_params(rz_ctx* c, int kind) {
     p.vertex_count = (uint32_t)c->verts.size();
     p.views = c->d_views;
     p.error_flags = c->d_error;
+    p.chunk_stamps = c->chunk_stamps;
+    p.small_extent = c->small_extent;
     PassBuffers* pb;
     if (kind == 2) {  // blended list: cull none, records kept in submission order
         p.draws = c->d_blended_draws;
@@ -749,6 +775,56 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
     }
 }
 
+// Per-view sequential launches: the same kernels, restricted to one view at a
+// time (its draws, its pixels, its targets), view after view. This is what the
+// batched frame is measured against.
+void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
+    for (uint32_t vi = 0; vi < c->views.size(); ++vi) {
+        const rz_ctx::ViewRange& rg = c->ranges[vi];
+        ClearList cl{};
+        cl.ptr[0] = c->d_shadow + rg.shadow_off;
+        cl.bytes[0] = rg.shadow * 4;
+        cl.ptr[1] = c->d_vis + rg.pix_off;
+        cl.bytes[1] = rg.pix * 8;
+        cl.ptr[2] = c->d_headers;
+        cl.bytes[2] = 2 * sizeof(PassHeader);
+        cl.count = 3;
+        if (c->shadow_tris) {
+            cl.ptr[3] = c->shadow_pass.tile_status;
+            cl.bytes[3] = (size_t)setup_ctas(rg.shadow_tris) * 8;
+            cl.count = 4;
+        }
+        launch_clear(cl, c->sm_count, s);
+        if (c->opaque_tris) {
+            ClearList c2{};
+            c2.ptr[0] = c->camera_pass.tile_status;
+            c2.bytes[0] = (size_t)setup_ctas(rg.opaque_tris) * 8;
+            c2.count = 1;
+            launch_clear(c2, c->sm_count, s);
+        }
+        if (rg.shadow_tris) {
+            PassParams sp = pass_params(c, 0);
+            sp.tri_offset = rg.shadow_tri_base;
+            sp.tri_total = rg.shadow_tris;
+            launch_setup(sp, s);
+            launch_raster(sp, c->sm_count, s);
+        }
+        if (rg.opaque_tris) {
+            PassParams cp = pass_params(c, 1);
+            cp.tri_offset = rg.opaque_tri_base;
+            cp.tri_total = rg.opaque_tris;
+            launch_setup(cp, s);
+            launch_raster(cp, c->sm_count, s);
+        }
+        ShadeParams v = sh;
+        v.varying_count = rg.varying_end;
+        launch_vertex_range(v, rg.varying_begin, s);
+        v.block_offset = rg.block_base;
+        v.shade_blocks = rg.blocks;
+        launch_shade(v, s);
+    }
+}
+
 // Enqueues one frame (everything after the scene/object uploads). With stage
 // timing the stages run one after the other on the main stream between
 // events; otherwise the shadow passes run on a side stream concurrently with
@@ -757,7 +833,11 @@ int enqueue_frame(rz_ctx* c) {
     cudaStream_t s = c->stream;
     const ShadeParams sh = shade_params(c);
     RZ_CUDA(c, cudaMemsetAsync(c->d_error, 0, sizeof(uint32_t), s), "clear error flags");
-    if (c->timing) {
+    if (!c->batched && !c->blended_tris && !c->timing) {
+        launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s);
+        launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s);
+        enqueue_sequential(c, s, sh);
+    } else if (c->timing) {
         stamp(c, 0);
         enqueue_shadow(c, s, true);
         stamp(c, 3);
@@ -771,7 +851,7 @@ int enqueue_frame(rz_ctx* c) {
         RZ_CUDA(c, cudaEventRecord(c->join, c->side), "join");
         RZ_CUDA(c, cudaStreamWaitEvent(s, c->join, 0), "join");
     }
-    launch_shade(sh, s);
+    if (c->batched || c->blended_tris || c->timing) launch_shade(sh, s);
     if (c->blended_tris) {
         BlendParams bp{};
         bp.sh = sh;
@@ -810,7 +890,7 @@ int grow_queues(rz_ctx* c) {
     drop_graph(c);
     c->queue_chunks = 0;
     auto grow = [&](PassBuffers& p, const PassHeader& h) -> int {
-        const uint64_t want_chunks = (h.stamps + kChunkStamps - 1) / kChunkStamps;
+        const uint64_t want_chunks = (h.stamps + c->chunk_stamps - 1) / c->chunk_stamps;
         const uint64_t want_recs = h.records_needed;
         if (want_chunks > p.chunk_capacity) {
             const uint64_t n = std::min<uint64_t>(want_chunks + want_chunks / 4 + 1024, 0xFFFFFFFFull);
@@ -1267,6 +1347,89 @@ int rz_get_stage_times(rz_ctx* c, float* ms, uint32_t capacity, uint32_t* count)
     }
     if (count) *count = n;
     return RZ_OK;
+}
+
+int rz_set_tuning(rz_ctx* c, const rz_tuning* t) {
+    if (!c || !t) return RZ_INVALID_ARGUMENT;
+    if (t->chunk_stamps < 8 || t->chunk_stamps > 256 || t->small_extent < 1 || t->small_extent > (uint32_t)kMaxSmallExtent)
+        return fail(c, RZ_INVALID_ARGUMENT, "tuning out of range");
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    const bool resize = t->chunk_stamps != c->chunk_stamps || t->queue_chunks != c->queue_chunks;
+    c->chunk_stamps = t->chunk_stamps;
+    c->small_extent = t->small_extent;
+    c->queue_chunks = t->queue_chunks;
+    c->batched = t->batched != 0;
+    if (resize) {
+        // re-size the chunk maps for the new chunk size / depth
+        free_pass(c->shadow_pass);
+        free_pass(c->camera_pass);
+        free_pass(c->blended_pass);
+        c->layout_dirty = true;
+    }
+    drop_graph(c);
+    return RZ_OK;
+}
+
+int rz_get_tuning(rz_ctx* c, rz_tuning* t) {
+    if (!c || !t) return RZ_INVALID_ARGUMENT;
+    t->chunk_stamps = c->chunk_stamps;
+    t->small_extent = c->small_extent;
+    t->queue_chunks = c->queue_chunks;
+    t->batched = c->batched ? 1u : 0u;
+    return RZ_OK;
+}
+
+int rz_autotune(rz_ctx* c, uint32_t frames, rz_tuning* chosen, float* ms, uint32_t capacity) {
+    if (!c || frames == 0) return RZ_INVALID_ARGUMENT;
+    const uint32_t chunk_opts[3] = {16, 32, 64};
+    const uint32_t small_opts[3] = {4, 8, 12};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    RZ_CUDA(c, cudaEventCreate(&e0), "event");
+    RZ_CUDA(c, cudaEventCreate(&e1), "event");
+    rz_tuning base{};
+    rz_get_tuning(c, &base);
+    float best = 1e30f;
+    rz_tuning best_t = base;
+    int rc = RZ_OK;
+    uint32_t n = 0;
+    for (uint32_t a = 0; a < 3 && rc == RZ_OK; ++a) {
+        for (uint32_t b = 0; b < 3 && rc == RZ_OK; ++b) {
+            rz_tuning t = base;
+            t.chunk_stamps = chunk_opts[a];
+            t.small_extent = small_opts[b];
+            t.queue_chunks = 0;
+            rc = rz_set_tuning(c, &t);
+            if (rc != RZ_OK) break;
+            // warm-up (also grows the queues if they overflow)
+            for (int w = 0; w < 2 && rc == RZ_OK; ++w) {
+                rc = rz_render(c);
+                if (rc == RZ_OK) {
+                    const int s = rz_sync(c, 0);
+                    if (s != RZ_OK && s != RZ_OVERFLOW) rc = s;
+                }
+            }
+            if (rc != RZ_OK) break;
+            cudaEventRecord(e0, c->stream);
+            for (uint32_t f = 0; f < frames && rc == RZ_OK; ++f) rc = rz_render(c);
+            cudaEventRecord(e1, c->stream);
+            if (rc == RZ_OK) rc = rz_sync(c, 0);
+            float t_ms = 0.0f;
+            cudaEventElapsedTime(&t_ms, e0, e1);
+            t_ms /= (float)frames;
+            if (ms && n < capacity) ms[n] = t_ms;
+            ++n;
+            if (rc == RZ_OK && t_ms < best) {
+                best = t_ms;
+                best_t = t;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const int r2 = rz_set_tuning(c, &best_t);
+    if (chosen) *chosen = best_t;
+    return rc != RZ_OK ? rc : r2;
 }
 
 void* rz_get_stream(rz_ctx* c) { return c ? (void*)c->stream : nullptr; }

@@ -88,7 +88,7 @@ static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
 
 constexpr int kStampW = 8;
 constexpr int kStampH = 4;
-constexpr int kChunkStamps = 32;      // stamps per raster work chunk
+constexpr int kChunkStamps = 32;      // default stamps per raster work chunk
 constexpr int kSetupThreads = 256;    // triangles per setup CTA
 constexpr float kGuardBand = 64.0f;
 
@@ -115,13 +115,17 @@ static_assert(sizeof(PassHeader) == 48, "PassHeader layout");
 
 // A record is "small" when the triangle's own extent (not its clamped bounding
 // box) is at most kSmallExtent pixels in x and y: one lane rasterises it.
-constexpr int kSmallExtent = 8;
+constexpr int kSmallExtent = 8;       // default
+constexpr int kMaxSmallExtent = 16;   // edge values of a lane-rasterised triangle stay below 2^26
 
 // Pass description handed to the setup/raster launchers.
 struct PassParams {
     const DrawRec* draws;
     uint32_t draw_count;
-    uint32_t tri_total;
+    uint32_t tri_total;       // triangles to set up: ids tri_offset .. tri_offset + tri_total - 1
+    uint32_t tri_offset;
+    uint32_t chunk_stamps;    // stamps per raster work chunk (tuning)
+    uint32_t small_extent;    // largest extent (pixels) of a lane-rasterised triangle (tuning)
     const float* mvp;         // MVP of draw d at mvp + mvp_stride * d
     uint32_t mvp_stride;
     const float4* pos;        // positions (x, y, z, pad)
@@ -144,7 +148,8 @@ struct PassParams {
 struct ShadeParams {
     const ViewRec* views;
     uint32_t view_count;
-    uint32_t shade_blocks;    // 16x16 tiles over all views
+    uint32_t shade_blocks;    // 16x16 tiles to shade: block_offset .. block_offset + shade_blocks - 1
+    uint32_t block_offset;
     const DrawRec* draws;     // opaque list
     uint32_t draw_count;
     const DrawConsts* consts; // per opaque draw

@@ -59,15 +59,22 @@ void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, con
 // clears (the load-op CLEAR of the depth attachments, scratch headers)
 // ---------------------------------------------------------------------------
 
+// Zeroes each buffer with 16-byte stores on its 16-byte-aligned body and byte
+// stores on the unaligned head and tail, so any start address and size is safe.
 __global__ void __launch_bounds__(256) k_clear(ClearList L) {
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (int b = 0; b < L.count; ++b) {
-        uint4* p = static_cast<uint4*>(L.ptr[b]);
-        const size_t n16 = L.bytes[b] / 16;
-        for (size_t i = tid; i < n16; i += stride) p[i] = make_uint4(0u, 0u, 0u, 0u);
-        const size_t tail = L.bytes[b] - n16 * 16;
-        if (tid < tail) reinterpret_cast<unsigned char*>(L.ptr[b])[n16 * 16 + tid] = 0;
+        unsigned char* base = static_cast<unsigned char*>(L.ptr[b]);
+        const size_t n = L.bytes[b];
+        size_t head = (16 - ((size_t)base & 15)) & 15;
+        if (head > n) head = n;
+        if (tid < head) base[tid] = 0;
+        const size_t n16 = (n - head) / 16;
+        uint4* body = reinterpret_cast<uint4*>(base + head);
+        for (size_t i = tid; i < n16; i += stride) body[i] = make_uint4(0u, 0u, 0u, 0u);
+        const size_t done = head + n16 * 16;
+        if (tid < n - done) base[done + tid] = 0;
     }
 }
 
@@ -179,7 +186,7 @@ struct ViewState {
 // bounding box is empty, 2 for a small triangle (extent at most kSmallExtent
 // pixels each way, rasterised by one lane), 1 otherwise.
 __device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV& v2, int64_t S, const ViewState& P,
-                                           bool ordered, uint32_t id, TriRecord& r) {
+                                           bool ordered, uint32_t small_extent, uint32_t id, TriRecord& r) {
     const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
     const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
     const int px0 = max((minX + 127) >> 8, 0), px1 = min((maxX - 128) >> 8, P.width - 1);
@@ -218,7 +225,7 @@ __device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV&
     r.id = id;
     r.view = P.view;
     r.stamp_offset = 0;
-    const bool small = !ordered && (maxX - minX) <= kSmallExtent * 256 && (maxY - minY) <= kSmallExtent * 256;
+    const bool small = !ordered && (maxX - minX) <= (int32_t)small_extent * 256 && (maxY - minY) <= (int32_t)small_extent * 256;
     return small ? 2 : 1;
 }
 
@@ -270,7 +277,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         const bool front = V.ccw_front ? (S < 0) : (S > 0);
         if (V.cull_front && front) return;
         TriRecord r;
-        const int kind = S > 0 ? make_record(a, b, c, S, V, P.ordered != 0, id, r) : make_record(a, c, b, -S, V, P.ordered != 0, id, r);
+        const int kind = S > 0 ? make_record(a, b, c, S, V, P.ordered != 0, P.small_extent, id, r) : make_record(a, c, b, -S, V, P.ordered != 0, P.small_extent, id, r);
         if (kind) emit(r, kind == 2);
         return;
     }
@@ -294,8 +301,8 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         const int64_t si = area2(sv[0], sv[i], sv[i + 1]);
         if (si == 0 || ((si > 0) != (S > 0))) continue;
         TriRecord r;
-        const int kind = si > 0 ? make_record(sv[0], sv[i], sv[i + 1], si, V, P.ordered != 0, id, r)
-                                : make_record(sv[0], sv[i + 1], sv[i], -si, V, P.ordered != 0, id, r);
+        const int kind = si > 0 ? make_record(sv[0], sv[i], sv[i + 1], si, V, P.ordered != 0, P.small_extent, id, r)
+                                : make_record(sv[0], sv[i + 1], sv[i], -si, V, P.ordered != 0, P.small_extent, id, r);
         if (kind) emit(r, kind == 2);
     }
 }
@@ -350,9 +357,10 @@ struct WriteEmit {
         r.stamp_offset = stamp;
         store_record(P->records + rec, r);
         // chunks whose first stamp lies inside this record start here
-        uint64_t k = (stamp + kChunkStamps - 1) / kChunkStamps;
+        const uint64_t cs = P->chunk_stamps;
+        uint64_t k = (stamp + cs - 1) / cs;
         const uint64_t end = stamp + record_stamps(r);
-        for (; k * kChunkStamps < end; ++k) {
+        for (; k * cs < end; ++k) {
             if (k >= P->chunk_capacity) {
                 atomicOr(P->error_flags, kErrStampOverflow);
                 break;
@@ -387,10 +395,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     if (threadIdx.x == 0) s_tile = atomicAdd(&P.header->ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
-    const uint32_t tri = tile * kSetupThreads + threadIdx.x;
+    const uint32_t local = tile * kSetupThreads + threadIdx.x;
+    const uint32_t tri = P.tri_offset + local;
 
     CountEmit cnt;
-    if (tri < P.tri_total) setup_triangle(P, tri, cnt);
+    if (local < P.tri_total) setup_triangle(P, tri, cnt);
 
     // CTA-wide inclusive scan of (records, stamps) packed in one 64-bit word.
     const uint64_t mine = ((uint64_t)cnt.recs << kStampBits) | cnt.stamps;
@@ -442,7 +451,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
                 // last CTA: publish the totals for the raster and the host
                 const uint64_t fin = atomicAdd(reinterpret_cast<unsigned long long*>(&P.header->alloc), 0ull);
                 const uint64_t recs = fin >> kStampBits, st = fin & kStampMask;
-                uint64_t chunks = (st + kChunkStamps - 1) / kChunkStamps;
+                uint64_t chunks = (st + P.chunk_stamps - 1) / P.chunk_stamps;
                 if (chunks > P.chunk_capacity) {
                     chunks = P.chunk_capacity;
                     atomicOr(P.error_flags, kErrStampOverflow);
@@ -506,7 +515,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
             s_base_stamps = pre_stamps;
             if (tile == gridDim.x - 1) {
                 const uint64_t st = pre_stamps + agg_stamps;
-                uint64_t chunks = (st + kChunkStamps - 1) / kChunkStamps;
+                uint64_t chunks = (st + P.chunk_stamps - 1) / P.chunk_stamps;
                 if (chunks > P.chunk_capacity) chunks = P.chunk_capacity;
                 P.header->records = (uint32_t)((pre_recs + agg_recs) < (uint64_t)P.record_capacity
                                                    ? (pre_recs + agg_recs) : (uint64_t)P.record_capacity);
@@ -569,8 +578,9 @@ __device__ __forceinline__ void write_fragment(const Target& T, int px, int py, 
     }
 }
 
-// One lane rasterises one small triangle: its extent is at most kSmallExtent
-// pixels each way (2048 sub-pixels), so every edge value and product fits in 32 bits.
+// One lane rasterises one small triangle: its extent is at most the pass's
+// small_extent (<= kMaxSmallExtent = 16 pixels = 4096 sub-pixels) each way, so
+// every edge value and product stays below 2^26 and fits in 32 bits.
 template <bool kWriteId>
 __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecord* rec) {
     const int4* src = reinterpret_cast<const int4*>(rec);
@@ -826,8 +836,8 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
     const uint64_t total = P.header->stamps;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < chunks; k += warps) {
-        uint64_t s = (uint64_t)k * kChunkStamps;
-        const uint64_t s_end = (s + kChunkStamps < total) ? (s + kChunkStamps) : total;
+        uint64_t s = (uint64_t)k * P.chunk_stamps;
+        const uint64_t s_end = (s + P.chunk_stamps < total) ? (s + P.chunk_stamps) : total;
         uint32_t r = P.chunk_map[k];
         while (s < s_end) {
             if (r >= P.record_capacity) break;

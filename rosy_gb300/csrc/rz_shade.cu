@@ -776,11 +776,11 @@ __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
         s_srgb[t] = P.srgb_table[t];
         s_unorm[t] = (float)t / 255.0f;
-        if (t == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x);
+        if (t == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
     }
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
-    const uint32_t lt = blockIdx.x - VR.shade_block_base;
+    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
     const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
     const int px = (int)(lt % tiles_x) * 16 + threadIdx.x;
     const int py = (int)(lt / tiles_x) * 16 + threadIdx.y;
@@ -837,11 +837,11 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     s_srgb[tid] = P.srgb_table[tid];
     s_unorm[tid] = (float)tid / 255.0f;
-    if (tid == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x);
+    if (tid == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
     __syncthreads();
     const uint32_t view = s_view;
     const ViewRec& VR = P.views[view];
-    const uint32_t lt = blockIdx.x - VR.shade_block_base;
+    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
     const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
     const int tx0 = (int)(lt % tiles_x) * 16, ty0 = (int)(lt / tiles_x) * 16;
     const int px = tx0 + threadIdx.x, py = ty0 + threadIdx.y;

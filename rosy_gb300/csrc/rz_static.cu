@@ -144,6 +144,8 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.draws = reinterpret_cast<const DrawRec*>(scratch + kOffDraw);
         p.draw_count = 1;
         p.tri_total = tris;
+        p.chunk_stamps = kChunkStamps;
+        p.small_extent = kSmallExtent;
         p.mvp = reinterpret_cast<const float*>(scratch + kOffMvp);
         p.mvp_stride = 16;
         p.pos = static_cast<const float4*>(positions);

@@ -79,6 +79,24 @@ class Graphics:
         self._views = list(views)
         self._check(self._lib.rz_set_views(self._ctx, arr, len(views)), "rz_set_views")
 
+    def set_tuning(self, chunk_stamps: int = 32, small_extent: int = 8, queue_chunks: int = 0,
+                   batched: bool = True) -> None:
+        t = _abi.RzTuning(chunk_stamps, small_extent, queue_chunks, 1 if batched else 0)
+        self._check(self._lib.rz_set_tuning(self._ctx, C.byref(t)), "rz_set_tuning")
+
+    def tuning(self) -> dict:
+        t = _abi.RzTuning()
+        self._check(self._lib.rz_get_tuning(self._ctx, C.byref(t)), "rz_get_tuning")
+        return {"chunk_stamps": t.chunk_stamps, "small_extent": t.small_extent, "queue_chunks": t.queue_chunks,
+                "batched": bool(t.batched)}
+
+    def autotune(self, frames: int = 5) -> tuple[dict, list]:
+        """Tries chunk_stamps in {16,32,64} x small_extent in {4,8,12}; applies the fastest."""
+        t = _abi.RzTuning()
+        ms = (C.c_float * 9)()
+        self._check(self._lib.rz_autotune(self._ctx, frames, C.byref(t), ms, 9), "rz_autotune")
+        return self.tuning(), [float(x) for x in ms]
+
     def update_view(self, view: int, scene_data: np.ndarray) -> None:
         sd = np.ascontiguousarray(scene_data)
         self._check(self._lib.rz_update_view(self._ctx, view, _abi.ptr(sd)), "rz_update_view")

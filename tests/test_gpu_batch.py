@@ -49,3 +49,40 @@ def test_batch_with_blended_and_mixed_state(gpu, oracle):
     outs = render_batch([a, b], [(0, v1), (1, v2), (0, v3)])
     for v, out in zip((v1, v2, v3), outs):
         check_parity(v, oracle.render(v), out)
+
+
+@pytest.mark.gpu
+def test_sequential_launches_equal_batched_and_autotune(gpu, oracle):
+    scenes, views = sc.batch_views(seed=5, views=6, scenes=2, min_tris=400, max_tris=4000, min_size=40,
+                                   max_size=200, min_shadow=128, max_shadow=384, texture_size=32)
+    g = Graphics()
+    g.init(64, 64, 64)
+    try:
+        idx = [g.add_scene(s) for s in scenes]
+        g.set_views([(idx[k], v.width, v.height, v.shadow_size, v.draw_config) for k, v in views])
+        for i, (_, v) in enumerate(views):
+            g.update_view(i, v.scene)
+        g.render()
+        if g.sync_code() == 14:
+            g.render()
+        g.sync()
+        batched = [g.download_view(i) for i in range(len(views))]
+        g.set_tuning(batched=False)
+        g.render()
+        g.sync()
+        seq = [g.download_view(i) for i in range(len(views))]
+        for a, b in zip(batched, seq):
+            for k in ("ids", "color"):
+                assert np.array_equal(a[k], b[k])
+            for k in ("depth", "shadow"):
+                assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32))
+        g.set_tuning(batched=True)
+        chosen, ms = g.autotune(frames=2)
+        assert chosen["chunk_stamps"] in (16, 32, 64) and chosen["small_extent"] in (4, 8, 12)
+        assert all(m > 0 for m in ms)
+        g.render()
+        g.sync()
+        for (k, v), i in zip(views, range(len(views))):
+            check_parity(v, oracle.render(v), g.download_view(i))
+    finally:
+        g.deinit()
