@@ -414,6 +414,100 @@ const char* rz_last_error(struct rz_ctx* ctx);
 /* RZ_ABI_VERSION of the loaded library. */
 uint32_t rz_abi_version(void);
 
+/* ---- G-buffer ------------------------------------------------------------
+ * Inputs of the learned upsampler. The reference has no G-buffer (it shades
+ * forward into its draw image); these are extra outputs of the same shading
+ * pass. With rz_set_gbuffer(ctx, 1) every following frame also writes, per
+ * pixel of every view: the albedo (the sampled base colour of fragmentMain,
+ * rounded to f16 and sRGB-encoded; alpha = 255 where a triangle covers the
+ * pixel, else 0) and the interpolated world-space normal, octahedral-encoded as
+ * two f16 (x in the low half). */
+typedef struct rz_gbuffer {
+    const void* color_rgba8;      /* width*height RGBA8 sRGB (the frame's colour) */
+    const void* depth_f32;        /* width*height f32 (reverse-Z, 0 = background) */
+    const void* albedo_rgba8;     /* width*height RGBA8 */
+    const void* normal_oct_f16x2; /* width*height u32 */
+    uint32_t width;
+    uint32_t height;
+} rz_gbuffer;
+
+int rz_set_gbuffer(struct rz_ctx* ctx, uint32_t enable);
+
+/* Device pointers of one view's G-buffer (valid after rz_sync of a frame
+ * rendered with the G-buffer on). */
+int rz_get_view_gbuffer(struct rz_ctx* ctx, uint32_t view, rz_gbuffer* out);
+
+/* ---- Learned upsampler ---------------------------------------------------
+ * Reconstructs a 2W x 2H RGBA8 sRGB frame from a W x H G-buffer. The network is
+ * four 3x3 convolutions with zero padding, 16 -> 32 -> 32 -> 32 -> 12 channels,
+ * ReLU after the first three, BF16 weights and activations with FP32
+ * accumulation on the tensor cores; its 12 output channels are pixel-shuffled
+ * (x2) into RGB and added to the bilinear x2 upsampling of the input colour
+ * (sRGB values / 255), then clamped and rounded to 8 bits. The input channels
+ * are: colour rgb / 255, albedo rgb / 255, normal (octahedral u, v), coverage
+ * (albedo alpha / 255), min(16 * depth, 4), and six zeros.
+ *
+ * Parameters are one f32 array of RZ_UPSAMPLER_PARAM_COUNT values: for each
+ * layer l = 0..3 its weights [cout_l][9][cin_l] (tap = 3 * ky + kx, ky, kx in
+ * 0..2 for offsets -1..1) followed by its biases [cout_l], with (cin, cout) =
+ * (16, 32), (32, 32), (32, 32), (32, 16); the weights of input channels 10..15
+ * of layer 0 and of output channels 12..15 of layer 3 should be zero (their
+ * gradients are zero).
+ *
+ * Training: rz_upsampler_accumulate runs the network on one G-buffer, the loss
+ * sum over the 2W x 2H x 3 output values of (prediction - target / 255)^2
+ * (prediction before clamping), and the backward pass, adding the gradients of
+ * that sum to the gradient buffer; rz_upsampler_adam_step applies Adam with
+ * the gradient multiplied by grad_scale and clears the gradient buffer. Every
+ * call runs on `stream` (a cudaStream_t; NULL = default stream) without
+ * waiting, except the get functions, which synchronise it. One upsampler is
+ * used by one host thread at a time. */
+#define RZ_UPSAMPLER_PARAM_COUNT 27760u
+
+struct rz_upsampler;
+typedef struct rz_upsampler rz_upsampler;
+
+/* Allocates the weights and activation buffers for inputs up to max_width x
+ * max_height on `device`; parameters start at zero. */
+int rz_upsampler_create(struct rz_upsampler** out, int device, uint32_t max_width, uint32_t max_height);
+void rz_upsampler_destroy(struct rz_upsampler* u);
+
+/* Copies `count` (= RZ_UPSAMPLER_PARAM_COUNT) host f32 parameters in / out and
+ * resets the Adam moments (set only). */
+int rz_upsampler_set_params(struct rz_upsampler* u, const float* params, uint32_t count, void* stream);
+int rz_upsampler_get_params(struct rz_upsampler* u, float* params, uint32_t count, void* stream);
+
+/* Inference: out_rgba8 is a device array of (2 * in->width) * (2 * in->height) u32. */
+int rz_upsampler_infer(struct rz_upsampler* u, const rz_gbuffer* in, void* out_rgba8, void* stream);
+
+/* Forward + loss + backward on one frame; target_rgba8 is the full-resolution
+ * (2W x 2H) frame on the device. out_rgba8 (optional, may be NULL) receives the
+ * prediction as in rz_upsampler_infer. */
+int rz_upsampler_accumulate(struct rz_upsampler* u, const rz_gbuffer* in, const void* target_rgba8, void* out_rgba8,
+                            void* stream);
+
+/* Copies the accumulated gradients (count = RZ_UPSAMPLER_PARAM_COUNT, may be
+ * NULL), the accumulated loss sum and the number of accumulated output values
+ * to the host. */
+int rz_upsampler_get_grads(struct rz_upsampler* u, float* grads, uint32_t count, double* loss_sum,
+                           uint64_t* values, void* stream);
+
+/* p -= lr * m_hat / (sqrt(v_hat) + eps) with g = grad_scale * gradient; then
+ * clears the gradients and the loss sum. */
+int rz_upsampler_adam_step(struct rz_upsampler* u, float lr, float beta1, float beta2, float eps, float grad_scale,
+                           void* stream);
+
+/* Device-side error bits of the upsampler's kernels so far (a tensor-core wait
+ * that ran out of its iteration limit sets bit 0); synchronises `stream`. */
+int rz_upsampler_status(struct rz_upsampler* u, uint32_t* flags, void* stream);
+
+/* Tensor-core self-test: D (128 x n, f32) = A (128 x k, bf16, row-major) *
+ * B (n x k, bf16, row-major)^T with one CTA, the MMA layout the convolutions
+ * use; n in {16, 32}, k in {16, 32, 48, 64}. All pointers are device arrays.
+ * Synchronises `stream`. */
+int rz_upsampler_selftest_gemm(const void* a_bf16, const void* b_bf16, float* d_f32, uint32_t n, uint32_t k,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,11 @@ class RzFrameOut(C.Structure):
                 ("shadow_map_size", C.c_uint32), ("triangle_id_base", C.c_uint32)]
 
 
+class RzGbuffer(C.Structure):
+    _fields_ = [("color_rgba8", C.c_void_p), ("depth_f32", C.c_void_p), ("albedo_rgba8", C.c_void_p),
+                ("normal_oct_f16x2", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 class RzStats(C.Structure):
     _fields_ = [("draw_call_count", C.c_uint32), ("triangle_count", C.c_uint32),
                 ("shadow_setup_records", C.c_uint32), ("camera_setup_records", C.c_uint32),

@@ -26,7 +26,10 @@ EXPORTS = [
     "rz_set_draw_config", "rz_update", "rz_render", "rz_sync", "rz_get_frame", "rz_read_frame",
     "rz_get_stats", "rz_get_stream", "rz_last_error", "rz_abi_version", "rz_set_stage_timing",
     "rz_get_stage_times", "rz_shadow_depth_static", "rz_add_scene", "rz_set_views", "rz_update_view",
-    "rz_get_view_frame", "rz_set_tuning", "rz_get_tuning", "rz_autotune",
+    "rz_get_view_frame", "rz_set_tuning", "rz_get_tuning", "rz_autotune", "rz_set_gbuffer", "rz_get_view_gbuffer",
+    "rz_upsampler_create", "rz_upsampler_destroy", "rz_upsampler_set_params", "rz_upsampler_get_params",
+    "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads", "rz_upsampler_adam_step",
+    "rz_upsampler_status", "rz_upsampler_selftest_gemm",
 ]
 
 _lib = None
@@ -84,6 +87,25 @@ def load(build_if_missing: bool = False):
     lib.rz_autotune.argtypes = [P, u32, C.POINTER(_abi.RzTuning), C.POINTER(C.c_float), u32]
     for name in ("rz_add_scene", "rz_set_views", "rz_update_view", "rz_get_view_frame", "rz_set_tuning",
                  "rz_get_tuning", "rz_autotune"):
+        getattr(lib, name).restype = C.c_int
+    G = C.POINTER(_abi.RzGbuffer)
+    lib.rz_set_gbuffer.argtypes = [P, u32]
+    lib.rz_get_view_gbuffer.argtypes = [P, u32, G]
+    lib.rz_upsampler_create.argtypes = [C.POINTER(P), C.c_int, u32, u32]
+    lib.rz_upsampler_destroy.argtypes = [P]
+    lib.rz_upsampler_destroy.restype = None
+    lib.rz_upsampler_set_params.argtypes = [P, C.POINTER(C.c_float), u32, P]
+    lib.rz_upsampler_get_params.argtypes = [P, C.POINTER(C.c_float), u32, P]
+    lib.rz_upsampler_infer.argtypes = [P, G, P, P]
+    lib.rz_upsampler_accumulate.argtypes = [P, G, P, P, P]
+    lib.rz_upsampler_get_grads.argtypes = [P, C.POINTER(C.c_float), u32, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_uint64), P]
+    lib.rz_upsampler_adam_step.argtypes = [P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P]
+    lib.rz_upsampler_status.argtypes = [P, C.POINTER(u32), P]
+    lib.rz_upsampler_selftest_gemm.argtypes = [P, P, P, u32, u32, P]
+    for name in ("rz_set_gbuffer", "rz_get_view_gbuffer", "rz_upsampler_create", "rz_upsampler_set_params",
+                 "rz_upsampler_get_params", "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads",
+                 "rz_upsampler_adam_step", "rz_upsampler_status", "rz_upsampler_selftest_gemm"):
         getattr(lib, name).restype = C.c_int
     lib.rz_abi_version.argtypes = []
     lib.rz_abi_version.restype = u32

@@ -138,6 +138,10 @@ struct rz_ctx {
     float* d_depth = nullptr;
     uint32_t* d_shadow = nullptr;
     uint2* d_color16 = nullptr;
+    bool gbuffer = false;             // shading also writes albedo + normal (rz_set_gbuffer)
+    uint32_t* d_gb_albedo = nullptr;
+    uint32_t* d_gb_normal = nullptr;
+    size_t gb_capacity = 0;
     size_t pix_capacity = 0, shadow_capacity = 0, color16_capacity = 0;
     size_t pix_total = 0, shadow_total = 0;
     uint32_t shade_blocks = 0;
@@ -563,6 +567,14 @@ int build_layout(rz_ctx* c) {
         RZ_CUDA(c, dalloc(&c->d_color16, pix), "RGBA16F draw images");
         c->color16_capacity = pix;
     }
+    if (c->gbuffer && pix > c->gb_capacity) {
+        dfree(c->d_gb_albedo);
+        dfree(c->d_gb_normal);
+        c->gb_capacity = 0;
+        RZ_CUDA(c, dalloc(&c->d_gb_albedo, pix), "G-buffer albedo");
+        RZ_CUDA(c, dalloc(&c->d_gb_normal, pix), "G-buffer normals");
+        c->gb_capacity = pix;
+    }
     c->view_recs.resize(c->views.size());
     for (uint32_t vi = 0; vi < c->views.size(); ++vi) {
         const ViewHost& v = c->views[vi];
@@ -584,6 +596,8 @@ int build_layout(rz_ctx* c) {
         r.shadow = c->d_shadow + shadow_off[vi];
         r.color16 = c->d_color16 ? c->d_color16 + pix_off[vi] : nullptr;
         r.scene = c->d_scene_data + vi;
+        r.gb_albedo = c->gbuffer ? c->d_gb_albedo + pix_off[vi] : nullptr;
+        r.gb_normal = c->gbuffer ? c->d_gb_normal + pix_off[vi] : nullptr;
         c->view_recs[vi] = r;
     }
     dfree(c->d_views);
@@ -1026,6 +1040,8 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_depth);
     dfree(c->d_shadow);
     dfree(c->d_color16);
+    dfree(c->d_gb_albedo);
+    dfree(c->d_gb_normal);
     dfree(c->d_shadow_draws);
     dfree(c->d_opaque_draws);
     dfree(c->d_blended_draws);
@@ -1293,6 +1309,33 @@ int rz_get_view_frame(rz_ctx* c, uint32_t view, rz_frame_out* out) {
 }
 
 int rz_get_frame(rz_ctx* c, rz_frame_out* out) { return rz_get_view_frame(c, 0, out); }
+
+int rz_set_gbuffer(rz_ctx* c, uint32_t enable) {
+    if (!c) return RZ_INVALID_ARGUMENT;
+    if (c->frame_pending) return fail(c, RZ_INVALID_STATE, "a frame is in flight; call rz_sync first");
+    if ((enable != 0) != c->gbuffer) {
+        c->gbuffer = enable != 0;
+        c->layout_dirty = true;
+        drop_graph(c);
+    }
+    return RZ_OK;
+}
+
+int rz_get_view_gbuffer(rz_ctx* c, uint32_t view, rz_gbuffer* out) {
+    if (!c || !out) return RZ_INVALID_ARGUMENT;
+    if (!c->gbuffer) return fail(c, RZ_INVALID_STATE, "G-buffer output is off (rz_set_gbuffer)");
+    if (c->layout_dirty || view >= c->view_recs.size()) return fail(c, RZ_INVALID_STATE, "no rendered frame for this view");
+    const ViewRec& r = c->view_recs[view];
+    rz_gbuffer g{};
+    g.color_rgba8 = r.color;
+    g.depth_f32 = r.depth;
+    g.albedo_rgba8 = r.gb_albedo;
+    g.normal_oct_f16x2 = r.gb_normal;
+    g.width = (uint32_t)r.width;
+    g.height = (uint32_t)r.height;
+    *out = g;
+    return RZ_OK;
+}
 
 int rz_read_frame(rz_ctx* c, void* color_host, size_t color_bytes, void* depth_host, size_t depth_bytes) {
     if (!c) return RZ_INVALID_ARGUMENT;

@@ -40,6 +40,8 @@ struct ViewRec {
     uint32_t* shadow;             // shadow_w*shadow_h depth bits
     uint2* color16;               // width*height RGBA16F (only with blended surfaces)
     const rz_scene_data* scene;
+    uint32_t* gb_albedo;          // width*height RGBA8 sRGB albedo, or null (G-buffer off)
+    uint32_t* gb_normal;          // width*height world normal, octahedral 2 x f16, or null
 };
 
 // gpu_material, src/Engine/Graphics.cpp:345-360, packed as in 4071-4150.

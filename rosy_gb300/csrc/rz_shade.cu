@@ -475,7 +475,7 @@ __device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughnes
 
 // fragmentMain, src/shaders/basic.slang:137-344. Returns false on discard.
 __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const GpuMaterial* md, const Frag& bv,
-                              const Sampler& smp, float out[4]) {
+                              const Sampler& smp, float out[4], float* albedo = nullptr) {
     const V3 ambientLight{sd.ambient_color[0], sd.ambient_color[1], sd.ambient_color[2]};
     float outFragColor[4] = {bv.color[0], bv.color[1], bv.color[2], bv.color[3]};
     float imageTextureColor[4] = {outFragColor[0], outFragColor[1], outFragColor[2], outFragColor[3]};
@@ -510,6 +510,10 @@ __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const 
         else smp.sample(md->tex[2], md->sampler[2], bv, cache, s);
         sampledRoughness = s[1];
         sampledMetallic = s[2];
+    }
+    if (albedo) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) albedo[k] = imageTextureColor[k];
     }
     const V3 V = fnormalize(bv.viewDir);
     const V3 L = lightDir;
@@ -669,8 +673,10 @@ void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stre
 
 // Shade triangle `tri` (pass-global id) at pixel (px, py) from the varying
 // records of its three vertices.
+// With `aux` non-null it also returns the G-buffer values: albedo (the sampled
+// base colour, rgb) and the interpolated world-space normal (normalised, xyz).
 __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_scene_data& sd, const Sampler& smp, uint32_t tri,
-                            int px, int py, float out[4]) {
+                            int px, int py, float out[4], float* aux = nullptr) {
     const uint32_t d = find_draw(P.draws, P.draw_count, tri);
     const DrawRec dr = P.draws[d];
     const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
@@ -691,7 +697,7 @@ __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_sc
     barycentrics(clip[0], clip[1], clip[2], qx, qy, VR.width, VR.height, bq0);
     barycentrics(clip[0], clip[1], clip[2], qx + 1, qy, VR.width, VR.height, bqx);
     barycentrics(clip[0], clip[1], clip[2], qx, qy + 1, VR.width, VR.height, bqy);
-    const bool debug_extra = sd.fragment_output == 1 || sd.fragment_output == 7;
+    const bool debug_extra = sd.fragment_output == 1 || sd.fragment_output == 7 || aux != nullptr;
     Frag f;
     float u0[2], ux[2], uy[2];
 #pragma unroll
@@ -755,7 +761,30 @@ __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_sc
         f.duvdx[i] = ux[i] - u0[i];
         f.duvdy[i] = uy[i] - u0[i];
     }
-    return fragment_main(VR, sd, md, f, smp, out);
+    if (aux) {
+        const V3 n = fnormalize(f.worldNormal);
+        aux[3] = n.x;
+        aux[4] = n.y;
+        aux[5] = n.z;
+    }
+    return fragment_main(VR, sd, md, f, smp, out, aux);
+}
+
+// Octahedral encoding of a unit vector into two f16 (x in the low half).
+__device__ __forceinline__ uint32_t encode_octahedral(float x, float y, float z) {
+    const float s = fabsf(x) + fabsf(y) + fabsf(z);
+    float u = 0.0f, v = 0.0f;
+    if (s > 0.0f) {
+        u = x / s;
+        v = y / s;
+        if (z < 0.0f) {
+            const float au = 1.0f - fabsf(v), av = 1.0f - fabsf(u);
+            u = u >= 0.0f ? au : -au;
+            v = v >= 0.0f ? av : -av;
+        }
+    }
+    const __half2 h = __floats2half2_rn(u, v);
+    return *reinterpret_cast<const uint32_t*>(&h);
 }
 
 // The view a 16x16 shading tile belongs to (tiles are numbered view by view).
@@ -789,13 +818,20 @@ __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
     const unsigned long long key = VR.vis[p];
     const uint32_t id = (uint32_t)key;
     float col[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // clear colour, src/Engine/Graphics.cpp:5416-5419
+    const bool gbuffer = VR.gb_albedo != nullptr;
+    float aux[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     if (id != 0) {
         const Sampler smp{&P, s_srgb, s_unorm};
         float o[4];
-        if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o)) {
+        if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o, gbuffer ? aux : nullptr)) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) col[k] = o[k];
         }
+    }
+    if (gbuffer) {
+        VR.gb_albedo[p] = encode_srgb8(half_round(aux[0])) | (encode_srgb8(half_round(aux[1])) << 8) |
+                          (encode_srgb8(half_round(aux[2])) << 16) | ((id != 0 ? 255u : 0u) << 24);
+        VR.gb_normal[p] = encode_octahedral(aux[3], aux[4], aux[5]);
     }
     VR.depth[p] = __uint_as_float((uint32_t)(key >> 32));
     if (P.blended) {  // blended surfaces follow: keep the RGBA16F draw image

@@ -1,0 +1,957 @@
+// Learned upsampler: a W x H G-buffer (colour, depth, albedo, normal) to a
+// 2W x 2H RGBA8 sRGB frame, trained and run with this file's own kernels.
+//
+// Network: four 3x3 convolutions (zero padding) 16 -> 32 -> 32 -> 32 -> 12
+// channels, ReLU after the first three; the 12 output channels are the 2x2
+// sub-pixels (s = 2 i + j for full-resolution pixel (2x + j, 2y + i)) times RGB,
+// added to the bilinear x2 upsampling of the input colour. Weights and
+// activations are BF16, accumulation FP32.
+//
+// Every convolution is an implicit GEMM on the 5th-generation tensor cores
+// (tcgen05.mma, kind::f16, M = 128, accumulators in tensor memory):
+//   forward / input gradient:  D[pixel, cout] = sum over (tap, cin) of
+//     X[pixel + offset(tap), cin] * W[cout, tap, cin]
+//   One CTA owns a 128-pixel x 4-row output tile. It stages the input halo (6
+//   rows x 130 pixels) in shared memory once, as one plane per group of 8
+//   channels with each pixel's 8 channels in 16 bytes; a tap's A operand is the
+//   same planes at a start address shifted by whole pixels (16 bytes), so no
+//   im2col copy is made. The input gradient is the same kernel with the
+//   weights transposed and the taps mirrored.
+//   weight gradient: D[(tap, cin), cout] = sum over pixels of
+//     X[pixel + offset(tap), cin] * dY[pixel, cout]
+//   One persistent CTA per half SM walks 64-pixel x 4-row tiles; it stages X
+//   transposed (8 pixels of one channel per 16 bytes) for the three horizontal
+//   shifts, laid out so that the (tap, channel) rows of an M block sit at a
+//   uniform stride, and accumulates D in tensor memory over all its tiles.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8 x 16-byte core matrices; the descriptor's leading byte offset is the
+// distance between core matrices along K and the stride byte offset the
+// distance between 8-row groups along M (or N).
+//
+// Every wait on a tensor-core completion barrier has a time limit; a wait that
+// runs out sets kErrMmaTimeout, skips the epilogue, frees the tensor memory and
+// returns.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rz_internal.h"
+
+namespace rz {
+namespace up {
+
+constexpr int kThreads = 128;
+constexpr int kTileW = 128;  // conv: output pixels per MMA tile (M = 128), one row segment
+constexpr int kTileRows = 4; // conv: output rows per CTA
+constexpr int kHaloW = kTileW + 2;
+constexpr int kWgKP = 64;    // weight gradient: pixels per tile row (K chunk)
+constexpr int kWgRows = 4;   // weight gradient: rows per tile
+constexpr long long kWaitCycles = 2000000000ll;  // about one second at 2 GHz
+constexpr uint32_t kErrMmaTimeout = 1u << 0;
+
+enum { kEpiRelu = 0, kEpiMask = 1, kEpiFinal = 2 };
+
+// Parameter layout: per layer weights [cout][9][cin] then biases [cout].
+__host__ __device__ constexpr int layer_cin(int l) { return l == 0 ? 16 : 32; }
+__host__ __device__ constexpr int layer_cout(int l) { return l == 3 ? 16 : 32; }
+__host__ __device__ constexpr int layer_wcount(int l) { return 9 * layer_cin(l) * layer_cout(l); }
+__host__ __device__ constexpr int layer_woff(int l) {
+    return l == 0 ? 0 : layer_woff(l - 1) + layer_wcount(l - 1) + layer_cout(l - 1);
+}
+__host__ __device__ constexpr int layer_boff(int l) { return layer_woff(l) + layer_wcount(l); }
+constexpr int kParamCount = layer_boff(3) + layer_cout(3);
+static_assert(kParamCount == (int)RZ_UPSAMPLER_PARAM_COUNT, "parameter count");
+// BF16 operand images: forward for layers 0..3, input gradient for layers 1..3.
+__host__ __device__ constexpr int fwd_img_off(int l) { return l == 0 ? 0 : fwd_img_off(l - 1) + layer_wcount(l - 1); }
+__host__ __device__ constexpr int dgrad_img_off(int l) {
+    return l == 1 ? fwd_img_off(3) + layer_wcount(3) : dgrad_img_off(l - 1) + layer_wcount(l - 1);
+}
+constexpr int kImgCount = dgrad_img_off(3) + layer_wcount(3);
+constexpr int kOutChannels = 12;
+constexpr int kFeatChannels = 16;
+
+// ---- PTX helpers ------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory matrix descriptor, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;  // descriptor version 1 (tcgen05)
+    return d;                 // base offset 0, absolute LBO mode, layout type 0 = no swizzle
+}
+
+// Instruction descriptor, kind::f16: D f32, A and B bf16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the barrier phase of `parity`; false if the time limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t cols) {  // one full warp
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols) {  // one full warp
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive f32 columns of the warp's 32 lanes (one lane per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__host__ __device__ constexpr uint32_t tmem_cols_for(int cols) { return cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : 256u; }
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t v) { return __uint_as_float(v & 0xFFFF0000u); }
+
+// ---- features -----------------------------------------------------------------
+
+// One pixel's 16 input channels from the G-buffer (see rz_upsampler_* in the header).
+__global__ void k_features(rz_gbuffer g, __nv_bfloat16* __restrict__ feat) {
+    const int n = (int)(g.width * g.height);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t c = __ldg(static_cast<const uint32_t*>(g.color_rgba8) + i);
+    const uint32_t a = __ldg(static_cast<const uint32_t*>(g.albedo_rgba8) + i);
+    const uint32_t nn = __ldg(static_cast<const uint32_t*>(g.normal_oct_f16x2) + i);
+    const float d = __ldg(static_cast<const float*>(g.depth_f32) + i);
+    const __half2 h = *reinterpret_cast<const __half2*>(&nn);
+    const float2 oct = __half22float2(h);
+    float f[16];
+    f[0] = (float)(c & 255u) / 255.0f;
+    f[1] = (float)((c >> 8) & 255u) / 255.0f;
+    f[2] = (float)((c >> 16) & 255u) / 255.0f;
+    f[3] = (float)(a & 255u) / 255.0f;
+    f[4] = (float)((a >> 8) & 255u) / 255.0f;
+    f[5] = (float)((a >> 16) & 255u) / 255.0f;
+    f[6] = oct.x;
+    f[7] = oct.y;
+    f[8] = (float)(a >> 24) / 255.0f;
+    f[9] = fminf(d * 16.0f, 4.0f);
+#pragma unroll
+    for (int k = 10; k < 16; ++k) f[k] = 0.0f;
+    uint4* dst = reinterpret_cast<uint4*>(feat + (size_t)i * kFeatChannels);
+    dst[0] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+    dst[1] = make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]), pack_bf16(f[14], f[15]));
+}
+
+// ---- convolution (forward and input gradient) ---------------------------------
+
+struct ConvArgs {
+    const __nv_bfloat16* in;        // H x W x CIN
+    const __nv_bfloat16* wimg;      // B operand image [9 * CIN / 8][N][8]
+    const float* bias;              // N (relu, final)
+    int W, H;
+    __nv_bfloat16* out;             // H x W x N (relu, mask)
+    const __nv_bfloat16* mask_src;  // H x W x N: out = acc where mask_src > 0, else 0 (mask)
+    const uint32_t* color_lr;       // H x W RGBA8: bilinear base (final)
+    uint32_t* out_rgba8;            // 2H x 2W, or null (final)
+    const uint32_t* target;         // 2H x 2W RGBA8, or null (final, training)
+    __nv_bfloat16* dy;              // H x W x 16: gradient of the loss sum (final, training)
+    double* loss;                   // loss sum accumulator (final, training)
+    uint32_t* err;
+};
+
+template <int CIN, int N>
+struct ConvSmem {
+    static constexpr int G = CIN / 8;
+    static constexpr uint32_t S_G = kHaloW * 16;  // between channel planes (K direction)
+    static constexpr uint32_t S_R = G * S_G;      // between halo rows
+    static constexpr uint32_t A_BYTES = (kTileRows + 2) * S_R;
+    static constexpr uint32_t B_OFF = (A_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t B_BYTES = 9 * CIN * N * 2;
+    static constexpr uint32_t BAR_OFF = (B_OFF + B_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t BYTES = BAR_OFF + 16;
+    static constexpr uint32_t TMEM_COLS = tmem_cols_for(kTileRows * N);
+};
+
+__device__ __forceinline__ float rgba_channel(uint32_t v, int k) { return (float)((v >> (8 * k)) & 255u) / 255.0f; }
+
+template <int N, int EPI>
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss) {
+    const bool inside = x < a.W && y < a.H;
+    if (EPI == kEpiRelu) {
+        if (!inside) return;
+        uint32_t pk[N / 2];
+#pragma unroll
+        for (int c = 0; c < N / 2; ++c)
+            pk[c] = pack_bf16(fmaxf(acc[2 * c] + __ldg(a.bias + 2 * c), 0.0f), fmaxf(acc[2 * c + 1] + __ldg(a.bias + 2 * c + 1), 0.0f));
+        uint4* dst = reinterpret_cast<uint4*>(a.out + ((size_t)y * a.W + x) * N);
+#pragma unroll
+        for (int q = 0; q < N / 8; ++q) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+    } else if (EPI == kEpiMask) {
+        if (!inside) return;
+        const uint4* ms = reinterpret_cast<const uint4*>(a.mask_src + ((size_t)y * a.W + x) * N);
+        uint4* dst = reinterpret_cast<uint4*>(a.out + ((size_t)y * a.W + x) * N);
+#pragma unroll
+        for (int q = 0; q < N / 8; ++q) {
+            const uint4 m = __ldg(ms + q);
+            const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
+            uint32_t o[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const int c = 8 * q + 2 * h;
+                o[h] = pack_bf16(bf16_lo(mw[h]) > 0.0f ? acc[c] : 0.0f, bf16_hi(mw[h]) > 0.0f ? acc[c + 1] : 0.0f);
+            }
+            dst[q] = make_uint4(o[0], o[1], o[2], o[3]);
+        }
+    } else {  // final: pixel shuffle + bilinear base (+ loss gradient)
+        if (!inside) return;
+        float net[kOutChannels];
+#pragma unroll
+        for (int c = 0; c < kOutChannels; ++c) net[c] = acc[c] + __ldg(a.bias + c);
+        const int W = a.W, H = a.H;
+        const uint32_t c00 = __ldg(a.color_lr + (size_t)y * W + x);
+        float g[kOutChannels];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int ys = i == 0 ? max(y - 1, 0) : min(y + 1, H - 1);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int xs = j == 0 ? max(x - 1, 0) : min(x + 1, W - 1);
+                const uint32_t c01 = __ldg(a.color_lr + (size_t)y * W + xs);
+                const uint32_t c10 = __ldg(a.color_lr + (size_t)ys * W + x);
+                const uint32_t c11 = __ldg(a.color_lr + (size_t)ys * W + xs);
+                const size_t op = (size_t)(2 * y + i) * (2 * W) + (2 * x + j);
+                uint32_t t = 0;
+                if (a.target) t = __ldg(a.target + op);
+                uint32_t o = 255u << 24;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float base = 0.5625f * rgba_channel(c00, k);
+                    base = base + 0.1875f * rgba_channel(c01, k);
+                    base = base + 0.1875f * rgba_channel(c10, k);
+                    base = base + 0.0625f * rgba_channel(c11, k);
+                    const float v = base + net[(2 * i + j) * 3 + k];
+                    const float q = fminf(fmaxf(v, 0.0f), 1.0f);
+                    o |= (uint32_t)floorf(q * 255.0f + 0.5f) << (8 * k);
+                    if (a.target) {
+                        const float d = v - rgba_channel(t, k);
+                        g[(2 * i + j) * 3 + k] = 2.0f * d;
+                        loss += d * d;
+                    }
+                }
+                if (a.out_rgba8) a.out_rgba8[op] = o;
+            }
+        }
+        if (a.target) {
+            uint4* dst = reinterpret_cast<uint4*>(a.dy + ((size_t)y * W + x) * 16);
+            dst[0] = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]), pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
+            dst[1] = make_uint4(pack_bf16(g[8], g[9]), pack_bf16(g[10], g[11]), 0u, 0u);
+        }
+    }
+}
+
+template <int CIN, int N, int EPI>
+__global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a) {
+    using L = ConvSmem<CIN, N>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;
+    unsigned char* sB = smem + L::B_OFF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int x0 = blockIdx.x * kTileW, y0 = blockIdx.y * kTileRows;
+
+    if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
+    if (tid == 0) mbar_init(bar, 1);
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(a.wimg);
+        uint4* dst = reinterpret_cast<uint4*>(sB);
+        for (int i = tid; i < (int)(L::B_BYTES / 16); i += kThreads) dst[i] = __ldg(src + i);
+    }
+    {
+        constexpr int n = (kTileRows + 2) * kHaloW * L::G;
+        for (int i = tid; i < n; i += kThreads) {
+            const int g = i % L::G;
+            const int px = (i / L::G) % kHaloW;
+            const int r = i / (L::G * kHaloW);
+            const int x = x0 - 1 + px, y = y0 - 1 + r;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (x >= 0 && x < a.W && y >= 0 && y < a.H)
+                v = __ldg(reinterpret_cast<const uint4*>(a.in + ((size_t)y * a.W + x) * CIN) + g);
+            *reinterpret_cast<uint4*>(sA + r * L::S_R + g * L::S_G + px * 16) = v;
+        }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    if (tid == 0) {
+        constexpr uint32_t idesc = idesc_bf16(128, N);
+        constexpr uint32_t lbo_b = N * 16;
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+        for (int t = 0; t < kTileRows; ++t) {
+            uint32_t acc = 0;
+            for (int tap = 0; tap < 9; ++tap) {
+                const int ky = tap / 3, kx = tap % 3;
+#pragma unroll
+                for (int s = 0; s < CIN / 16; ++s) {
+                    const uint64_t da = umma_desc(a0 + (t + ky) * L::S_R + kx * 16 + 2 * s * L::S_G, L::S_G, 128);
+                    const uint64_t db = umma_desc(b0 + (tap * L::G + 2 * s) * lbo_b, lbo_b, 128);
+                    mma_bf16(tmem + t * N, da, db, idesc, acc);
+                    acc = 1;
+                }
+            }
+        }
+        mma_commit(bar);
+    }
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0) ? 1 : 0) != 0;
+    tc_fence_after();
+    float loss = 0.0f;
+    if (ok) {
+        for (int t = 0; t < kTileRows; ++t) {
+            float acc[N];
+#pragma unroll
+            for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + t * N + c, acc + c);
+            conv_epilogue<N, EPI>(a, acc, x0 + warp * 32 + lane, y0 + t, loss);
+        }
+    } else if (tid == 0) {
+        atomicOr(a.err, kErrMmaTimeout);
+    }
+    if (EPI == kEpiFinal && a.target) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, o);
+        if (lane == 0 && loss != 0.0f) atomicAdd(a.loss, (double)loss);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, L::TMEM_COLS);
+}
+
+// ---- weight gradient ------------------------------------------------------------
+
+struct WgradArgs {
+    const __nv_bfloat16* x;   // H x W x CIN: the layer's input
+    const __nv_bfloat16* dy;  // H x W x N: gradient of the loss sum w.r.t. the layer's pre-activation output
+    float* dw;                // [N][9][CIN], accumulated
+    float* db;                // [N], accumulated
+    int W, H;
+    uint32_t* err;
+};
+
+template <int CIN, int N>
+struct WgSmem {
+    static constexpr int G = CIN / 8;
+    static constexpr int NB = (9 * CIN + 127) / 128;         // M blocks of 128 (tap, channel) rows
+    static constexpr uint32_t S_CG = kWgKP * 16;              // between 8-channel groups (M direction)
+    static constexpr uint32_t S_KX = G * S_CG;                // between horizontal shifts
+    static constexpr uint32_t S_ROW = 3 * S_KX;               // between halo rows
+    static constexpr uint32_t XT_USED = (kWgRows + 2) * S_ROW;
+    static constexpr uint32_t XT_READ = (kWgRows - 1) * S_ROW + 16 * NB * S_CG;  // end of the furthest M block read
+    static constexpr uint32_t XT_BYTES = XT_USED > XT_READ ? XT_USED : XT_READ;
+    static constexpr uint32_t S_COG = kWgKP * 16;             // between 8-channel groups of dY (N direction)
+    static constexpr uint32_t S_DYROW = (N / 8) * S_COG;
+    static constexpr uint32_t DY_OFF = (XT_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t DY_BYTES = kWgRows * S_DYROW;
+    static constexpr uint32_t BAR_OFF = (DY_OFF + DY_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t BYTES = BAR_OFF + 16;
+    static constexpr uint32_t TMEM_COLS = tmem_cols_for(NB * N);
+};
+
+template <int CIN, int N>
+__global__ void __launch_bounds__(kThreads) k_wgrad(WgradArgs a) {
+    using L = WgSmem<CIN, N>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sX = smem;
+    unsigned char* sD = smem + L::DY_OFF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
+    if (tid == 0) mbar_init(bar, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int tiles_x = (a.W + kWgKP - 1) / kWgKP, tiles_y = (a.H + kWgRows - 1) / kWgRows;
+    const int ntiles = tiles_x * tiles_y;
+    const int ci = tid % CIN, xgroups = kThreads / CIN;
+    const int co = tid % N, dgroups = kThreads / N;
+    float dbsum = 0.0f;
+    bool ok = true;
+    int iter = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++iter) {
+        if (iter > 0) ok = ok && mbar_wait(bar, (uint32_t)(iter - 1) & 1u);
+        if (!__syncthreads_and(ok ? 1 : 0)) {
+            ok = false;
+            break;
+        }
+        const int x0 = (tile % tiles_x) * kWgKP, y0 = (tile / tiles_x) * kWgRows;
+        // X transposed, three horizontal shifts: 16 bytes = 8 pixels of one channel
+        for (int task = tid / CIN; task < (kWgRows + 2) * (kWgKP / 8); task += xgroups) {
+            const int r = task / (kWgKP / 8), pxg = task % (kWgKP / 8);
+            const int y = y0 - 1 + r;
+            const int xs = x0 + 8 * pxg - 1;
+            float v[10];
+#pragma unroll
+            for (int j = 0; j < 10; ++j) {
+                const int x = xs + j;
+                v[j] = (y >= 0 && y < a.H && x >= 0 && x < a.W)
+                           ? __bfloat162float(a.x[((size_t)y * a.W + x) * CIN + ci])
+                           : 0.0f;
+            }
+#pragma unroll
+            for (int kx = 0; kx < 3; ++kx) {
+                const uint4 w = make_uint4(pack_bf16(v[kx], v[kx + 1]), pack_bf16(v[kx + 2], v[kx + 3]),
+                                           pack_bf16(v[kx + 4], v[kx + 5]), pack_bf16(v[kx + 6], v[kx + 7]));
+                *reinterpret_cast<uint4*>(sX + r * L::S_ROW + kx * L::S_KX + (ci / 8) * L::S_CG + pxg * 128 +
+                                          (ci % 8) * 16) = w;
+            }
+        }
+        // dY transposed: 16 bytes = 8 pixels of one output channel
+        for (int task = tid / N; task < kWgRows * (kWgKP / 8); task += dgroups) {
+            const int r = task / (kWgKP / 8), pxg = task % (kWgKP / 8);
+            const int y = y0 + r;
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int x = x0 + 8 * pxg + j;
+                v[j] = (y < a.H && x < a.W) ? __bfloat162float(a.dy[((size_t)y * a.W + x) * N + co]) : 0.0f;
+                dbsum += v[j];
+            }
+            *reinterpret_cast<uint4*>(sD + r * L::S_DYROW + (co / 8) * L::S_COG + pxg * 128 + (co % 8) * 16) =
+                make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            constexpr uint32_t idesc = idesc_bf16(128, N);
+            const uint32_t xa = smem_u32(sX), da0 = smem_u32(sD);
+            for (int r = 0; r < kWgRows; ++r) {
+#pragma unroll
+                for (int s = 0; s < kWgKP / 16; ++s) {
+                    const uint64_t db = umma_desc(da0 + r * L::S_DYROW + s * 256, 128, L::S_COG);
+                    const uint32_t accum = (iter > 0 || r > 0 || s > 0) ? 1u : 0u;
+#pragma unroll
+                    for (int b = 0; b < L::NB; ++b) {
+                        const uint64_t dx = umma_desc(xa + r * L::S_ROW + 16 * b * L::S_CG + s * 256, 128, L::S_CG);
+                        mma_bf16(tmem + b * N, dx, db, idesc, accum);
+                    }
+                }
+            }
+            mma_commit(bar);
+        }
+    }
+    if (ok && iter > 0) ok = mbar_wait(bar, (uint32_t)(iter - 1) & 1u);
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    tc_fence_after();
+    if (ok && iter > 0) {
+        for (int b = 0; b < L::NB; ++b) {
+            float acc[N];
+#pragma unroll
+            for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + b * N + c, acc + c);
+            const int m = 128 * b + 32 * warp + lane;
+            const int tap = m / CIN, c_in = m % CIN;
+            if (tap < 9) {
+#pragma unroll
+                for (int c = 0; c < N; ++c)
+                    if (acc[c] != 0.0f) atomicAdd(a.dw + ((size_t)c * 9 + tap) * CIN + c_in, acc[c]);
+            }
+        }
+        if (dbsum != 0.0f) atomicAdd(a.db + co, dbsum);
+    } else if (!ok && tid == 0) {
+        atomicOr(a.err, kErrMmaTimeout);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, L::TMEM_COLS);
+}
+
+// ---- optimizer and operand images --------------------------------------------------
+
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v, int n,
+                       float lr, float b1, float b2, float eps, float scale, float bc1, float bc2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * scale;
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    g[i] = 0.0f;
+}
+
+// BF16 operand images of every layer from the f32 parameters: the forward image
+// of layer l at element ((k / 8) * cout + co) * 8 + k % 8 with k = tap * cin + ci,
+// and (l >= 1) the input-gradient image: rows ci, k' = (8 - tap) * cout + co.
+__global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* __restrict__ img) {
+    constexpr int kWoff[4] = {layer_woff(0), layer_woff(1), layer_woff(2), layer_woff(3)};
+    constexpr int kFwd[4] = {fwd_img_off(0), fwd_img_off(1), fwd_img_off(2), fwd_img_off(3)};
+    constexpr int kDgrad[4] = {0, dgrad_img_off(1), dgrad_img_off(2), dgrad_img_off(3)};
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParamCount) return;
+    const int l = i >= kWoff[3] ? 3 : i >= kWoff[2] ? 2 : i >= kWoff[1] ? 1 : 0;
+    const int local = i - kWoff[l];
+    const int cin = l == 0 ? 16 : 32, cout = l == 3 ? 16 : 32;
+    if (local >= 9 * cin * cout) return;  // biases
+    const int c_in = local % cin, tap = (local / cin) % 9, co = local / (9 * cin);
+    const __nv_bfloat16 w = __float2bfloat16_rn(p[i]);
+    const int k = tap * cin + c_in;
+    img[kFwd[l] + ((k / 8) * cout + co) * 8 + (k % 8)] = w;
+    if (l >= 1) {
+        const int k2 = (8 - tap) * cout + co;
+        img[kDgrad[l] + ((k2 / 8) * cin + c_in) * 8 + (k2 % 8)] = w;
+    }
+}
+
+// ---- self-test GEMM ------------------------------------------------------------------
+
+// D (128 x n) = A (128 x k) * B (n x k)^T with the layouts the convolutions use.
+// The operand regions are sized so that every address either descriptor field
+// could reach stays inside them.
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_selftest(const __nv_bfloat16* A, const __nv_bfloat16* B, float* D, int K,
+                                                      uint32_t* err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    constexpr uint32_t kA = 65536, kB = 16384;
+    unsigned char* sA = smem;
+    unsigned char* sB = smem + kA;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kA + kB);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kA + kB + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tmem_alloc(slot, 32);
+    if (tid == 0) mbar_init(bar, 1);
+    for (uint32_t i = tid; i < (kA + kB) / 16; i += kThreads) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    // A: core matrix (m / 8, k / 8) at (k / 8) * 2048 + (m / 8) * 128; B: (k / 8) * (N * 16) + (n / 8) * 128
+    for (int i = tid; i < 128 * K; i += kThreads) {
+        const int m = i / K, k = i % K;
+        *reinterpret_cast<__nv_bfloat16*>(sA + (k / 8) * 2048 + m * 16 + (k % 8) * 2) = A[i];
+    }
+    for (int i = tid; i < N * K; i += kThreads) {
+        const int n = i / K, k = i % K;
+        *reinterpret_cast<__nv_bfloat16*>(sB + (k / 8) * (N * 16) + n * 16 + (k % 8) * 2) = B[i];
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    if (tid == 0) {
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+        for (int s = 0; s < K / 16; ++s)
+            mma_bf16(tmem, umma_desc(a0 + s * 2 * 2048, 2048, 128), umma_desc(b0 + s * 2 * N * 16, N * 16, 128),
+                     idesc_bf16(128, N), s > 0 ? 1u : 0u);
+        mma_commit(bar);
+    }
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0) ? 1 : 0) != 0;
+    tc_fence_after();
+    if (ok) {
+        float acc[N];
+#pragma unroll
+        for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c, acc + c);
+        const int m = warp * 32 + lane;
+#pragma unroll
+        for (int c = 0; c < N; ++c) D[m * N + c] = acc[c];
+    } else if (tid == 0) {
+        atomicOr(err, kErrMmaTimeout);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 32);
+}
+
+}  // namespace up
+}  // namespace rz
+
+using namespace rz::up;
+
+struct rz_upsampler {
+    int device = 0;
+    int sms = 0;
+    uint32_t max_w = 0, max_h = 0;
+    float* d_params = nullptr;
+    float* d_grads = nullptr;
+    float* d_m = nullptr;
+    float* d_v = nullptr;
+    __nv_bfloat16* d_img = nullptr;
+    __nv_bfloat16* d_feat = nullptr;
+    __nv_bfloat16* d_act[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* d_dy3 = nullptr;
+    __nv_bfloat16* d_dyA = nullptr;
+    __nv_bfloat16* d_dyB = nullptr;
+    double* d_loss = nullptr;
+    uint32_t* d_err = nullptr;
+    uint64_t values = 0;
+    int adam_t = 0;
+};
+
+namespace {
+
+template <class T>
+cudaError_t ualloc(T** p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+void ufree_all(rz_upsampler* u) {
+    cudaFree(u->d_params);
+    cudaFree(u->d_grads);
+    cudaFree(u->d_m);
+    cudaFree(u->d_v);
+    cudaFree(u->d_img);
+    cudaFree(u->d_feat);
+    for (auto* p : u->d_act) cudaFree(p);
+    cudaFree(u->d_dy3);
+    cudaFree(u->d_dyA);
+    cudaFree(u->d_dyB);
+    cudaFree(u->d_loss);
+    cudaFree(u->d_err);
+}
+
+template <class K>
+cudaError_t allow_smem(K kernel, uint32_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+std::once_flag g_attr_once;
+cudaError_t g_attr_status = cudaSuccess;
+
+void set_attributes() {
+    cudaError_t e = cudaSuccess;
+    auto keep = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+    };
+    keep(allow_smem(k_conv<16, 32, kEpiRelu>, ConvSmem<16, 32>::BYTES));
+    keep(allow_smem(k_conv<32, 32, kEpiRelu>, ConvSmem<32, 32>::BYTES));
+    keep(allow_smem(k_conv<32, 16, kEpiFinal>, ConvSmem<32, 16>::BYTES));
+    keep(allow_smem(k_conv<16, 32, kEpiMask>, ConvSmem<16, 32>::BYTES));
+    keep(allow_smem(k_conv<32, 32, kEpiMask>, ConvSmem<32, 32>::BYTES));
+    keep(allow_smem(k_wgrad<32, 16>, WgSmem<32, 16>::BYTES));
+    keep(allow_smem(k_wgrad<32, 32>, WgSmem<32, 32>::BYTES));
+    keep(allow_smem(k_wgrad<16, 32>, WgSmem<16, 32>::BYTES));
+    keep(allow_smem(k_selftest<16>, 65536 + 16384 + 16));
+    keep(allow_smem(k_selftest<32>, 65536 + 16384 + 16));
+    g_attr_status = e;
+}
+
+cudaError_t ensure_attributes() {
+    std::call_once(g_attr_once, set_attributes);
+    return g_attr_status;
+}
+
+template <int CIN, int N, int EPI>
+void launch_conv(const ConvArgs& a, cudaStream_t s) {
+    const dim3 grid((a.W + kTileW - 1) / kTileW, (a.H + kTileRows - 1) / kTileRows);
+    k_conv<CIN, N, EPI><<<grid, kThreads, ConvSmem<CIN, N>::BYTES, s>>>(a);
+}
+
+template <int CIN, int N>
+void launch_wgrad(const rz_upsampler* u, const WgradArgs& a, cudaStream_t s) {
+    const int tiles = ((a.W + kWgKP - 1) / kWgKP) * ((a.H + kWgRows - 1) / kWgRows);
+    const int grid = std::min(tiles, 2 * std::max(u->sms, 1));
+    k_wgrad<CIN, N><<<grid, kThreads, WgSmem<CIN, N>::BYTES, s>>>(a);
+}
+
+bool gbuffer_ok(const rz_upsampler* u, const rz_gbuffer* g) {
+    return g && g->color_rgba8 && g->depth_f32 && g->albedo_rgba8 && g->normal_oct_f16x2 && g->width > 0 &&
+           g->height > 0 && g->width <= u->max_w && g->height <= u->max_h;
+}
+
+ConvArgs conv_args(const rz_upsampler* u, int W, int H) {
+    ConvArgs a{};
+    a.W = W;
+    a.H = H;
+    a.err = u->d_err;
+    return a;
+}
+
+// Forward pass; with `target` it also writes the loss gradient and sum.
+void forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out, cudaStream_t s) {
+    const int W = (int)g->width, H = (int)g->height;
+    const int n = W * H;
+    k_features<<<(n + 255) / 256, 256, 0, s>>>(*g, u->d_feat);
+    ConvArgs a = conv_args(u, W, H);
+    a.in = u->d_feat;
+    a.wimg = u->d_img + fwd_img_off(0);
+    a.bias = u->d_params + layer_boff(0);
+    a.out = u->d_act[0];
+    launch_conv<16, 32, kEpiRelu>(a, s);
+    for (int l = 1; l <= 2; ++l) {
+        a.in = u->d_act[l - 1];
+        a.wimg = u->d_img + fwd_img_off(l);
+        a.bias = u->d_params + layer_boff(l);
+        a.out = u->d_act[l];
+        launch_conv<32, 32, kEpiRelu>(a, s);
+    }
+    ConvArgs f = conv_args(u, W, H);
+    f.in = u->d_act[2];
+    f.wimg = u->d_img + fwd_img_off(3);
+    f.bias = u->d_params + layer_boff(3);
+    f.color_lr = static_cast<const uint32_t*>(g->color_rgba8);
+    f.out_rgba8 = static_cast<uint32_t*>(out);
+    f.target = static_cast<const uint32_t*>(target);
+    f.dy = u->d_dy3;
+    f.loss = u->d_loss;
+    launch_conv<32, 16, kEpiFinal>(f, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rz_upsampler_create(rz_upsampler** out, int device, uint32_t max_width, uint32_t max_height) {
+    if (!out || max_width == 0 || max_height == 0 || max_width > 8192 || max_height > 8192) return RZ_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return RZ_ERROR;
+    if (ensure_attributes() != cudaSuccess) return RZ_ERROR;
+    rz_upsampler* u = new rz_upsampler();
+    u->device = device;
+    u->max_w = max_width;
+    u->max_h = max_height;
+    cudaDeviceGetAttribute(&u->sms, cudaDevAttrMultiProcessorCount, device);
+    const size_t px = (size_t)max_width * max_height;
+    bool ok = ualloc(&u->d_params, kParamCount) == cudaSuccess && ualloc(&u->d_grads, kParamCount) == cudaSuccess &&
+              ualloc(&u->d_m, kParamCount) == cudaSuccess && ualloc(&u->d_v, kParamCount) == cudaSuccess &&
+              ualloc(&u->d_img, kImgCount) == cudaSuccess && ualloc(&u->d_feat, px * kFeatChannels) == cudaSuccess &&
+              ualloc(&u->d_act[0], px * 32) == cudaSuccess && ualloc(&u->d_act[1], px * 32) == cudaSuccess &&
+              ualloc(&u->d_act[2], px * 32) == cudaSuccess && ualloc(&u->d_dy3, px * 16) == cudaSuccess &&
+              ualloc(&u->d_dyA, px * 32) == cudaSuccess && ualloc(&u->d_dyB, px * 32) == cudaSuccess &&
+              ualloc(&u->d_loss, 1) == cudaSuccess && ualloc(&u->d_err, 1) == cudaSuccess;
+    if (ok) {
+        ok = cudaMemset(u->d_params, 0, kParamCount * sizeof(float)) == cudaSuccess &&
+             cudaMemset(u->d_grads, 0, kParamCount * sizeof(float)) == cudaSuccess &&
+             cudaMemset(u->d_m, 0, kParamCount * sizeof(float)) == cudaSuccess &&
+             cudaMemset(u->d_v, 0, kParamCount * sizeof(float)) == cudaSuccess &&
+             cudaMemset(u->d_img, 0, kImgCount * sizeof(__nv_bfloat16)) == cudaSuccess &&
+             cudaMemset(u->d_loss, 0, sizeof(double)) == cudaSuccess && cudaMemset(u->d_err, 0, 4) == cudaSuccess &&
+             cudaDeviceSynchronize() == cudaSuccess;
+    }
+    if (!ok) {
+        ufree_all(u);
+        delete u;
+        return RZ_ERROR;
+    }
+    *out = u;
+    return RZ_OK;
+}
+
+void rz_upsampler_destroy(rz_upsampler* u) {
+    if (!u) return;
+    cudaSetDevice(u->device);
+    cudaDeviceSynchronize();
+    ufree_all(u);
+    delete u;
+}
+
+int rz_upsampler_set_params(rz_upsampler* u, const float* params, uint32_t count, void* stream) {
+    if (!u || !params || count != (uint32_t)kParamCount) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(u->d_params, params, kParamCount * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(u->d_m, 0, kParamCount * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(u->d_v, 0, kParamCount * sizeof(float), s) != cudaSuccess)
+        return RZ_ERROR;
+    u->adam_t = 0;
+    k_pack<<<(kParamCount + 255) / 256, 256, 0, s>>>(u->d_params, u->d_img);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return RZ_ERROR;  // the host array may be freed after return
+    return cudaGetLastError() == cudaSuccess ? RZ_OK : RZ_ERROR;
+}
+
+int rz_upsampler_get_params(rz_upsampler* u, float* params, uint32_t count, void* stream) {
+    if (!u || !params || count != (uint32_t)kParamCount) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(params, u->d_params, kParamCount * sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return RZ_ERROR;
+    return RZ_OK;
+}
+
+int rz_upsampler_infer(rz_upsampler* u, const rz_gbuffer* in, void* out_rgba8, void* stream) {
+    if (!u || !gbuffer_ok(u, in) || !out_rgba8) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    forward(u, in, nullptr, out_rgba8, static_cast<cudaStream_t>(stream));
+    return cudaGetLastError() == cudaSuccess ? RZ_OK : RZ_ERROR;
+}
+
+int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* target_rgba8, void* out_rgba8,
+                            void* stream) {
+    if (!u || !gbuffer_ok(u, in) || !target_rgba8) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int W = (int)in->width, H = (int)in->height;
+    forward(u, in, target_rgba8, out_rgba8, s);
+    WgradArgs w{};
+    w.W = W;
+    w.H = H;
+    w.err = u->d_err;
+    ConvArgs d = conv_args(u, W, H);
+    // layer 3
+    w.x = u->d_act[2];
+    w.dy = u->d_dy3;
+    w.dw = u->d_grads + layer_woff(3);
+    w.db = u->d_grads + layer_boff(3);
+    launch_wgrad<32, 16>(u, w, s);
+    d.in = u->d_dy3;
+    d.wimg = u->d_img + dgrad_img_off(3);
+    d.mask_src = u->d_act[2];
+    d.out = u->d_dyA;
+    launch_conv<16, 32, kEpiMask>(d, s);
+    // layer 2
+    w.x = u->d_act[1];
+    w.dy = u->d_dyA;
+    w.dw = u->d_grads + layer_woff(2);
+    w.db = u->d_grads + layer_boff(2);
+    launch_wgrad<32, 32>(u, w, s);
+    d.in = u->d_dyA;
+    d.wimg = u->d_img + dgrad_img_off(2);
+    d.mask_src = u->d_act[1];
+    d.out = u->d_dyB;
+    launch_conv<32, 32, kEpiMask>(d, s);
+    // layer 1
+    w.x = u->d_act[0];
+    w.dy = u->d_dyB;
+    w.dw = u->d_grads + layer_woff(1);
+    w.db = u->d_grads + layer_boff(1);
+    launch_wgrad<32, 32>(u, w, s);
+    d.in = u->d_dyB;
+    d.wimg = u->d_img + dgrad_img_off(1);
+    d.mask_src = u->d_act[0];
+    d.out = u->d_dyA;
+    launch_conv<32, 32, kEpiMask>(d, s);
+    // layer 0
+    w.x = u->d_feat;
+    w.dy = u->d_dyA;
+    w.dw = u->d_grads + layer_woff(0);
+    w.db = u->d_grads + layer_boff(0);
+    launch_wgrad<16, 32>(u, w, s);
+    u->values += (uint64_t)4 * W * H * 3;
+    return cudaGetLastError() == cudaSuccess ? RZ_OK : RZ_ERROR;
+}
+
+int rz_upsampler_get_grads(rz_upsampler* u, float* grads, uint32_t count, double* loss_sum, uint64_t* values,
+                           void* stream) {
+    if (!u || (grads && count != (uint32_t)kParamCount)) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (grads && cudaMemcpyAsync(grads, u->d_grads, kParamCount * sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return RZ_ERROR;
+    double l = 0.0;
+    if (cudaMemcpyAsync(&l, u->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return RZ_ERROR;
+    if (loss_sum) *loss_sum = l;
+    if (values) *values = u->values;
+    return RZ_OK;
+}
+
+int rz_upsampler_adam_step(rz_upsampler* u, float lr, float beta1, float beta2, float eps, float grad_scale,
+                           void* stream) {
+    if (!u || !(lr >= 0.0f) || !(beta1 >= 0.0f && beta1 < 1.0f) || !(beta2 >= 0.0f && beta2 < 1.0f) || !(eps > 0.0f))
+        return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    u->adam_t += 1;
+    const float bc1 = 1.0f - (float)std::pow((double)beta1, (double)u->adam_t);
+    const float bc2 = 1.0f - (float)std::pow((double)beta2, (double)u->adam_t);
+    k_adam<<<(kParamCount + 255) / 256, 256, 0, s>>>(u->d_params, u->d_grads, u->d_m, u->d_v, kParamCount, lr, beta1,
+                                                      beta2, eps, grad_scale, bc1, bc2);
+    k_pack<<<(kParamCount + 255) / 256, 256, 0, s>>>(u->d_params, u->d_img);
+    if (cudaMemsetAsync(u->d_loss, 0, sizeof(double), s) != cudaSuccess) return RZ_ERROR;
+    u->values = 0;
+    return cudaGetLastError() == cudaSuccess ? RZ_OK : RZ_ERROR;
+}
+
+int rz_upsampler_status(rz_upsampler* u, uint32_t* flags, void* stream) {
+    if (!u || !flags) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(u->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(flags, u->d_err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        return RZ_ERROR;
+    return RZ_OK;
+}
+
+int rz_upsampler_selftest_gemm(const void* a_bf16, const void* b_bf16, float* d_f32, uint32_t n, uint32_t k, void* stream) {
+    if (!a_bf16 || !b_bf16 || !d_f32 || (n != 16 && n != 32) || k == 0 || k > 64 || k % 16 != 0) return RZ_INVALID_ARGUMENT;
+    if (ensure_attributes() != cudaSuccess) return RZ_ERROR;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t* err = nullptr;
+    if (cudaMalloc(&err, 4) != cudaSuccess) return RZ_ERROR;
+    cudaMemsetAsync(err, 0, 4, s);
+    const auto* A = static_cast<const __nv_bfloat16*>(a_bf16);
+    const auto* B = static_cast<const __nv_bfloat16*>(b_bf16);
+    if (n == 16) k_selftest<16><<<1, kThreads, 65536 + 16384 + 16, s>>>(A, B, d_f32, (int)k, err);
+    else k_selftest<32><<<1, kThreads, 65536 + 16384 + 16, s>>>(A, B, d_f32, (int)k, err);
+    uint32_t flags = 0;
+    const bool ok = cudaGetLastError() == cudaSuccess &&
+                    cudaMemcpyAsync(&flags, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                    cudaStreamSynchronize(s) == cudaSuccess;
+    cudaFree(err);
+    if (!ok) return RZ_ERROR;
+    return flags ? RZ_TIMEOUT : RZ_OK;
+}
+
+}  // extern "C"

@@ -117,6 +117,29 @@ class Graphics:
         out["ids"] = np.where(ids > 0, ids - np.uint32(f.triangle_id_base), 0).astype(np.uint32)
         return out
 
+    def set_gbuffer(self, enable: bool) -> None:
+        """Makes the shading pass also write albedo and octahedral normals (the upsampler's inputs)."""
+        self._check(self._lib.rz_set_gbuffer(self._ctx, 1 if enable else 0), "rz_set_gbuffer")
+
+    def gbuffer(self, view: int = 0) -> _abi.RzGbuffer:
+        """Device pointers of one view's G-buffer (after sync)."""
+        g = _abi.RzGbuffer()
+        self._check(self._lib.rz_get_view_gbuffer(self._ctx, view, C.byref(g)), "rz_get_view_gbuffer")
+        return g
+
+    def download_gbuffer(self, view: int = 0) -> dict:
+        """Host copies of one view's G-buffer: colour and albedo (H, W, 4) u8, depth (H, W) f32,
+        normal (H, W, 2) f16."""
+        self.sync()
+        g = self.gbuffer(view)
+        H, W = g.height, g.width
+        return {
+            "color": device_array(g.color_rgba8, (H, W, 4), np.uint8),
+            "depth": device_array(g.depth_f32, (H, W), np.float32),
+            "albedo": device_array(g.albedo_rgba8, (H, W, 4), np.uint8),
+            "normal": device_array(g.normal_oct_f16x2, (H, W, 2), np.float16),
+        }
+
     def update_objects(self, offset: int, objects: np.ndarray) -> None:
         """The go_update upload (mob transforms) of src/Engine/Graphics.cpp:5120-5138."""
         objects = np.ascontiguousarray(objects, np.float32)

@@ -1,0 +1,182 @@
+"""GPU tests of the learned upsampler's tensor-core kernels against the numpy
+oracle (oracle/upsampler_ref.py): the tcgen05 GEMM layout, the G-buffer the
+shading pass writes, the forward pass, the gradients of every parameter, the
+Adam step, and that a few training steps lower the loss."""
+import numpy as np
+import pytest
+
+from oracle import upsampler_ref as U
+from rosy_gb300 import scene as sc
+from rosy_gb300 import upsampler as up
+from rosy_gb300.graphics import Graphics
+
+pytestmark = pytest.mark.gpu
+
+
+def _render(s, gbuffer=True):
+    g = Graphics()
+    g.init(s.width, s.height, s.shadow_size)
+    g.set_asset(s)
+    g.set_graphic_objects(s.objects, s.surfaces)
+    g.set_draw_config(s.draw_config)
+    if gbuffer:
+        g.set_gbuffer(True)
+    g.update(s.scene)
+    g.render()
+    if g.sync_code() == 14:
+        g.render()
+    g.sync()
+    return g
+
+
+def _pair(w, h, camera=0, seed=0):
+    """Half-resolution G-buffer renderer and the full-resolution target of one camera."""
+    base = sc.tiny(seed)
+    lo = _render(sc.view_of(base, w, h, 128, camera=camera))
+    hi = _render(sc.view_of(base, 2 * w, 2 * h, 128, camera=camera), gbuffer=False)
+    return lo, hi
+
+
+def _params(seed, last_scale=0.2):
+    rng = np.random.default_rng(seed)
+    p = U.init_params(seed, last_scale=last_scale)
+    for (wo, bo), (cin, cout) in zip(U.OFFSETS, U.LAYERS):
+        real = 12 if cout == 16 else cout
+        p[bo:bo + real] = rng.normal(0.0, 0.05, real).astype(np.float32)
+    return p
+
+
+def test_tcgen05_selftest_gemm(gpu):
+    import torch
+
+    for n in (16, 32):
+        for k in (16, 64):
+            gen = torch.Generator().manual_seed(100 * n + k)
+            A = torch.randn(128, k, generator=gen).to(torch.bfloat16)
+            B = torch.randn(n, k, generator=gen).to(torch.bfloat16)
+            a, b = A.cuda(), B.cuda()
+            d = torch.full((128, n), float("nan"), device="cuda")
+            torch.cuda.synchronize()
+            assert up.selftest_gemm(a.data_ptr(), b.data_ptr(), d.data_ptr(), n, k) == 0
+            want = A.double() @ B.double().T
+            err = (d.cpu().double() - want).abs().max().item()
+            assert err < 1e-3 * max(1.0, want.abs().max().item()), (n, k, err)
+
+
+def test_gbuffer_albedo_and_normal(gpu):
+    s = sc.tiny(0)
+    s.scene = s.scene.copy()
+    s.scene["light_enabled"] = 0
+    s.scene["fragment_output"] = 0
+    g = _render(s)
+    gb = g.download_gbuffer()
+    fr = g.download()
+    covered = fr["ids"] > 0
+    assert covered.any() and (~covered).any()
+    assert np.array_equal(gb["albedo"][..., 3], np.where(covered, 255, 0).astype(np.uint8))
+    # unlit, debug output 0: the colour is the sampled albedo
+    assert np.array_equal(gb["albedo"][covered][:, :3], fr["color"][covered][:, :3])
+    assert np.array_equal(gb["color"], fr["color"])
+    # debug output 1 shows the world normal * 0.5 + 0.5; compare with the decoded octahedral normal
+    s.scene["fragment_output"] = 1
+    g.update(s.scene)
+    g.render()
+    g.sync()
+    col = g.download()["color"][..., :3].astype(np.float64) / 255.0
+    lin = np.where(col <= 0.04045, col / 12.92, ((col + 0.055) / 1.055) ** 2.4)
+    n_dbg = lin[covered] * 2.0 - 1.0
+    o = gb["normal"][covered].astype(np.float64)
+    z = 1.0 - np.abs(o[:, 0]) - np.abs(o[:, 1])
+    x, y = o[:, 0].copy(), o[:, 1].copy()
+    neg = z < 0
+    x[neg] = (1.0 - np.abs(o[neg, 1])) * np.sign(o[neg, 0])
+    y[neg] = (1.0 - np.abs(o[neg, 0])) * np.sign(o[neg, 1])
+    n = np.stack([x, y, z], 1)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    err = np.abs(n - n_dbg)
+    assert err.mean() < 0.01 and err.max() < 0.06, (err.mean(), err.max())
+    g.deinit()
+
+
+@pytest.mark.parametrize("w,h", [(96, 64), (200, 70)])
+def test_upsampler_forward_matches_oracle(gpu, w, h):
+    import torch
+
+    lo, hi = _pair(w, h)
+    gbh = lo.download_gbuffer()
+    p = _params(5)
+    u = up.Upsampler(0, w, h)
+    u.set_params(p)
+    out = torch.zeros((2 * h, 2 * w), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    u.infer(lo.gbuffer(), out.data_ptr())
+    assert u.status() == 0
+    got = out.cpu().numpy().view(np.uint8).reshape(2 * h, 2 * w, 4)
+    ref = U.forward(p, gbh)["rgba8"]
+    d = np.abs(got.astype(np.int32) - ref.astype(np.int32))
+    assert d.max() <= 2 and (d > 0).mean() < 0.01, (d.max(), (d > 0).mean())
+    # the prediction differs from plain bilinear (the network did something)
+    assert not np.array_equal(ref, U.to_rgba8(U.bilinear_base(gbh["color"])))
+    u.close()
+    lo.deinit()
+    hi.deinit()
+
+
+@pytest.mark.parametrize("w,h", [(96, 64), (200, 70)])
+def test_upsampler_gradients_match_oracle(gpu, w, h):
+    import torch
+
+    lo, hi = _pair(w, h, camera=1)
+    gbh = lo.download_gbuffer()
+    target = hi.download()["color"]
+    p = _params(9)
+    u = up.Upsampler(0, w, h)
+    u.set_params(p)
+    tgt = torch.from_numpy(target.reshape(2 * h, 2 * w, 4).view(np.int32).reshape(2 * h, 2 * w).copy()).cuda()
+    torch.cuda.synchronize()
+    u.accumulate(lo.gbuffer(), tgt.data_ptr())
+    grads, loss, values = u.grads()
+    assert u.status() == 0
+    assert values == 2 * h * 2 * w * 3
+    ref, ref_loss = U.gradients(p, gbh, target)
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss, (loss, ref_loss)
+    for l, ((wo, bo), (cin, cout)) in enumerate(zip(U.OFFSETS, U.LAYERS)):
+        for name, sl in (("w", slice(wo, bo)), ("b", slice(bo, bo + cout))):
+            a, r = grads[sl].astype(np.float64), ref[sl]
+            rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-12)
+            assert rel < 2e-2, (l, name, rel)
+    # Adam, first step: p - lr * g / (|g| + eps) with bias-corrected moments
+    lr = 1e-3
+    u.adam_step(lr, 0.9, 0.999, 1e-8, 1.0)
+    p1 = u.params()
+    g64 = grads.astype(np.float64)
+    want = p - lr * g64 / (np.abs(g64) + 1e-8)
+    assert np.allclose(p1, want, rtol=1e-5, atol=1e-6)
+    _, l2, v2 = u.grads()
+    assert l2 == 0.0 and v2 == 0
+    u.close()
+    lo.deinit()
+    hi.deinit()
+
+
+def test_training_steps_lower_the_loss(gpu):
+    import torch
+
+    w, h = 96, 64
+    lo, hi = _pair(w, h, camera=2)
+    target = hi.download()["color"]
+    u = up.Upsampler(0, w, h)
+    u.set_params(up.init_params(0))
+    tgt = torch.from_numpy(target.view(np.int32).reshape(2 * h, 2 * w).copy()).cuda()
+    torch.cuda.synchronize()
+    losses = []
+    for _ in range(40):
+        u.accumulate(lo.gbuffer(), tgt.data_ptr())
+        loss, values = u.loss()
+        losses.append(loss / values)
+        u.adam_step(2e-3, grad_scale=1.0 / values)
+    assert u.status() == 0
+    assert losses[-1] < 0.8 * losses[0], losses
+    u.close()
+    lo.deinit()
+    hi.deinit()
