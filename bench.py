@@ -45,6 +45,45 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops, burst)"
+    return 1900.0, "fallback 1.9 PFLOP/s"
+
+
+def learned_block(frames: int = 64, cameras: int = 256) -> dict:
+    """The learned half-resolution path against the plain path at 1920x1080 on the
+    random-triangles scene: device frames/s of both, held-out PSNR and max error per
+    frame against the plain render, and the upsampler's tensor-core roofline."""
+    from rosy_gb300 import learned
+
+    params, meta = learned.load_weights()
+    t = learned.time_paths(params, frames=frames)
+    ev = learned.evaluate(params, cameras)
+    peak, src = bf16_peak()
+    per = ev.pop("per_frame")
+    return {
+        "workload": "random_triangles (4,096 triangles, 256^2 texture, 1024^2 shadow map): plain 1920x1080 vs "
+                    "960x540 render + upsampler to 1920x1080; L2 flushed between frames",
+        "plain_fps": round(t["plain_fps"], 2), "learned_fps": round(t["learned_fps"], 2),
+        "speedup": round(t["speedup"], 3), "plain_ms": round(t["plain_ms"], 5), "learned_ms": round(t["learned_ms"], 5),
+        "heldout": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in ev.items()},
+        "psnr_floor_db": learned.PSNR_FLOOR_DB,
+        "fallback_to_plain": ev["psnr_db_mean"] < learned.PSNR_FLOOR_DB,
+        "per_frame_psnr_db": [round(f["psnr_db"], 2) for f in per],
+        "per_frame_max_abs_error": [f["max_abs_error"] for f in per],
+        "upsampler_roofline": {"bound": "tensor", "achieved": round(t["upsampler_tflops"], 2), "peak": peak,
+                               "unit": "TFLOP/s", "frac": round(t["upsampler_tflops"] / peak, 4),
+                               "peak_source": src, "ms_per_frame": round(t["upsampler_ms"], 5),
+                               "flops_per_frame": t["upsampler_flops"],
+                               "flops_note": "2 x 9 x cin x cout x 960 x 540 over the real channels "
+                                             "(10-32-32-32-12)"},
+        "weights": {k: meta.get(k) for k in ("steps", "batch", "lr", "train_cameras", "train_seconds")},
+    }
+
+
 def measured_traffic(stage: str):
     """DRAM bytes per launch of a kernel from the committed ncu summary of this
     workload (profiles/dram_traffic_scene_scale_1080p.json), or None."""
@@ -356,6 +395,8 @@ def run_rz(args):
             "visibility_matches_oracle_frame0": parity,
             "algorithmic_bytes": {k: (int(v) if v is not None else None) for k, v in algo.items()},
         }
+        if not args.no_learned:
+            line["learned_upsample"] = learned_block()
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
@@ -481,6 +522,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="timed frames only (for ncu captures)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-path comparison")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "rz":
         args.warmup = 3

@@ -145,6 +145,13 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols) {  /
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
 }
 
+// 16-byte asynchronous global -> shared copy; valid == false writes zeros (src must still be a mapped address).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -233,10 +240,9 @@ struct ConvSmem {
     static constexpr uint32_t TMEM_COLS = tmem_cols_for(kTileRows * N);
 };
 
-__device__ __forceinline__ float rgba_channel(uint32_t v, int k) { return (float)((v >> (8 * k)) & 255u) / 255.0f; }
-
 template <int N, int EPI>
-__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss) {
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss,
+                                              const float* lut) {
     const bool inside = x < a.W && y < a.H;
     if (EPI == kEpiRelu) {
         if (!inside) return;
@@ -269,38 +275,50 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
 #pragma unroll
         for (int c = 0; c < kOutChannels; ++c) net[c] = acc[c] + __ldg(a.bias + c);
         const int W = a.W, H = a.H;
-        const uint32_t c00 = __ldg(a.color_lr + (size_t)y * W + x);
+        // the 3x3 neighbourhood of low-resolution colours (edges clamped), as byte / 255
+        float f[3][3][3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const int yy = min(max(y + r - 1, 0), H - 1);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const int xx = min(max(x + q - 1, 0), W - 1);
+                const uint32_t c = __ldg(a.color_lr + (size_t)yy * W + xx);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) f[r][q][k] = lut[(c >> (8 * k)) & 255u];
+            }
+        }
         float g[kOutChannels];
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
-            const int ys = i == 0 ? max(y - 1, 0) : min(y + 1, H - 1);
+            const int rs = i == 0 ? 0 : 2;
+            const size_t op = (size_t)(2 * y + i) * (2 * W) + 2 * x;
+            uint2 t = make_uint2(0u, 0u);
+            if (a.target) t = __ldg(reinterpret_cast<const uint2*>(a.target + op));
+            uint32_t o[2];
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-                const int xs = j == 0 ? max(x - 1, 0) : min(x + 1, W - 1);
-                const uint32_t c01 = __ldg(a.color_lr + (size_t)y * W + xs);
-                const uint32_t c10 = __ldg(a.color_lr + (size_t)ys * W + x);
-                const uint32_t c11 = __ldg(a.color_lr + (size_t)ys * W + xs);
-                const size_t op = (size_t)(2 * y + i) * (2 * W) + (2 * x + j);
-                uint32_t t = 0;
-                if (a.target) t = __ldg(a.target + op);
-                uint32_t o = 255u << 24;
+                const int qs = j == 0 ? 0 : 2;
+                const uint32_t tj = j == 0 ? t.x : t.y;
+                uint32_t ov = 255u << 24;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    float base = 0.5625f * rgba_channel(c00, k);
-                    base = base + 0.1875f * rgba_channel(c01, k);
-                    base = base + 0.1875f * rgba_channel(c10, k);
-                    base = base + 0.0625f * rgba_channel(c11, k);
+                    float base = 0.5625f * f[1][1][k];
+                    base = base + 0.1875f * f[1][qs][k];
+                    base = base + 0.1875f * f[rs][1][k];
+                    base = base + 0.0625f * f[rs][qs][k];
                     const float v = base + net[(2 * i + j) * 3 + k];
-                    const float q = fminf(fmaxf(v, 0.0f), 1.0f);
-                    o |= (uint32_t)floorf(q * 255.0f + 0.5f) << (8 * k);
+                    const float qv = fminf(fmaxf(v, 0.0f), 1.0f);
+                    ov |= (uint32_t)floorf(qv * 255.0f + 0.5f) << (8 * k);
                     if (a.target) {
-                        const float d = v - rgba_channel(t, k);
+                        const float d = v - lut[(tj >> (8 * k)) & 255u];
                         g[(2 * i + j) * 3 + k] = 2.0f * d;
                         loss += d * d;
                     }
                 }
-                if (a.out_rgba8) a.out_rgba8[op] = o;
+                o[j] = ov;
             }
+            if (a.out_rgba8) *reinterpret_cast<uint2*>(a.out_rgba8 + op) = make_uint2(o[0], o[1]);
         }
         if (a.target) {
             uint4* dst = reinterpret_cast<uint4*>(a.dy + ((size_t)y * W + x) * 16);
@@ -321,26 +339,30 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int x0 = blockIdx.x * kTileW, y0 = blockIdx.y * kTileRows;
 
+    __shared__ float s_lut[EPI == kEpiFinal ? 256 : 1];
     if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
     if (tid == 0) mbar_init(bar, 1);
+    if (EPI == kEpiFinal) {
+        for (int i = tid; i < 256; i += kThreads) s_lut[i] = (float)i / 255.0f;
+    }
     {
         const uint4* src = reinterpret_cast<const uint4*>(a.wimg);
-        uint4* dst = reinterpret_cast<uint4*>(sB);
-        for (int i = tid; i < (int)(L::B_BYTES / 16); i += kThreads) dst[i] = __ldg(src + i);
+        for (int i = tid; i < (int)(L::B_BYTES / 16); i += kThreads) cp_async16(sB + 16 * i, src + i, true);
     }
     {
         constexpr int n = (kTileRows + 2) * kHaloW * L::G;
+#pragma unroll 4
         for (int i = tid; i < n; i += kThreads) {
             const int g = i % L::G;
             const int px = (i / L::G) % kHaloW;
             const int r = i / (L::G * kHaloW);
             const int x = x0 - 1 + px, y = y0 - 1 + r;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (x >= 0 && x < a.W && y >= 0 && y < a.H)
-                v = __ldg(reinterpret_cast<const uint4*>(a.in + ((size_t)y * a.W + x) * CIN) + g);
-            *reinterpret_cast<uint4*>(sA + r * L::S_R + g * L::S_G + px * 16) = v;
+            const bool valid = x >= 0 && x < a.W && y >= 0 && y < a.H;
+            const __nv_bfloat16* src = valid ? a.in + ((size_t)y * a.W + x) * CIN + 8 * g : a.in;
+            cp_async16(sA + r * L::S_R + g * L::S_G + px * 16, src, valid);
         }
     }
+    cp_async_wait_all();
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -373,7 +395,7 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a) {
             float acc[N];
 #pragma unroll
             for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + t * N + c, acc + c);
-            conv_epilogue<N, EPI>(a, acc, x0 + warp * 32 + lane, y0 + t, loss);
+            conv_epilogue<N, EPI>(a, acc, x0 + warp * 32 + lane, y0 + t, loss, s_lut);
         }
     } else if (tid == 0) {
         atomicOr(a.err, kErrMmaTimeout);

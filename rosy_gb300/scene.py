@@ -603,6 +603,26 @@ def view_of(s: Scene, width: int, height: int, shadow_size: int, camera: int = 0
     return out
 
 
+def orbit_view(s: Scene, cam_dir, width: int, height: int, fov_deg: float = 60.0) -> np.ndarray:
+    """Scene constants of a camera at 3 * cam_dir looking at the origin (the
+    random-triangles camera), keeping the scene's sun and feature switches."""
+    src = s.scene
+    cam = 3.0 * np.asarray(cam_dir, np.float64) / np.linalg.norm(cam_dir)
+    view = camera_look_at_origin(cam)
+    spn = src["shadow_projection_near"][0].reshape(4, 4).T.astype(np.float64)
+    rec = scene_record(view, projection(width / height, math.radians(fov_deg)), src["sun_position"][0], spn, cam,
+                       width, height)
+    for k in ("fragment_output", "light_enabled", "tangent_space_enabled", "shadows_enabled", "normal_maps_enabled",
+              "brdf_lighting_enabled", "flip_lights", "flip_tangents"):
+        rec[k] = src[k]
+    return rec
+
+
+def camera_dirs(count: int, seed: int) -> np.ndarray:
+    """`count` seeded unit vectors (camera directions on the orbit sphere)."""
+    return _unit(np.random.Generator(np.random.PCG64(seed)), count)
+
+
 def batch_views(seed: int = 0, views: int = 256, scenes: int = 16, min_tris: int = 1000, max_tris: int = 200000,
                 min_size: int = 64, max_size: int = 1024, min_shadow: int = 512, max_shadow: int = 2048,
                 texture_size: int = 256):
