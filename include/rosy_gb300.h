@@ -414,6 +414,53 @@ const char* rz_last_error(struct rz_ctx* ctx);
 /* RZ_ABI_VERSION of the loaded library. */
 uint32_t rz_abi_version(void);
 
+/* ---- .rsy asset files ------------------------------------------------------
+ * Reader for the asset format of rosy_asset::asset (src/Asset/Asset.h:10-148,
+ * read by src/Asset/Asset.cpp:409-848), so that Rosy's own assets feed
+ * rz_set_asset / rz_set_objects. rz_rsy_read replaces asset::read (fopen_s and
+ * all): RZ_OPEN_FAILED if the file cannot be opened, RZ_READ_FAILED if it is
+ * truncated, has the wrong magic, version or endianness, or a count larger than
+ * the file. Images are named, not embedded (the engine loads them as separate
+ * files), so textures are supplied by the caller. */
+struct rz_rsy;
+typedef struct rz_rsy rz_rsy;
+
+typedef struct rz_rsy_info {
+    uint32_t mesh_count;
+    uint32_t material_count;
+    uint32_t sampler_count;
+    uint32_t image_count;
+    uint32_t node_count;
+    uint32_t scene_count;
+    uint32_t root_scene;
+    uint32_t object_count;        /* graphics objects of the root scene (statics first, then mobs) */
+    uint32_t surface_count;       /* surfaces of those objects, in scene order */
+    uint32_t static_object_count; /* objects before the first mob */
+    float coordinate_system[16];  /* the asset's coordinate system (column-major) */
+} rz_rsy_info;
+
+int rz_rsy_read(const char* path, struct rz_rsy** out);
+void rz_rsy_free(struct rz_rsy* asset);
+int rz_rsy_get_info(const struct rz_rsy* asset, rz_rsy_info* out);
+
+/* Meshes as rz_mesh records whose pointers stay valid until rz_rsy_free;
+ * materials and samplers copied out. RZ_OVERFLOW if capacity is too small. */
+int rz_rsy_get_meshes(const struct rz_rsy* asset, rz_mesh* out, uint32_t capacity);
+int rz_rsy_get_materials(const struct rz_rsy* asset, rz_material* out, uint32_t capacity);
+int rz_rsy_get_samplers(const struct rz_rsy* asset, rz_sampler* out, uint32_t capacity);
+
+/* Type and name of image `index` (name NUL-terminated, truncated to name_capacity - 1). */
+int rz_rsy_get_image(const struct rz_rsy* asset, uint32_t index, uint32_t* image_type, char* name,
+                     uint32_t name_capacity, uint32_t* name_length);
+
+/* The root scene flattened as the level flattens a new asset
+ * (src/Engine/Level.cpp:922-1160, node transforms src/Engine/Node.cpp:96-103):
+ * one graphics object per node with a mesh, breadth first, static nodes first
+ * and nodes under a node named "mobs" after them; one surface per mesh surface.
+ * RZ_INVALID_ARGUMENT if the root scene or a node index is out of range. */
+int rz_rsy_get_scene(const struct rz_rsy* asset, rz_object* objects, uint32_t object_capacity, rz_surface* surfaces,
+                     uint32_t surface_capacity);
+
 /* ---- G-buffer ------------------------------------------------------------
  * Inputs of the learned upsampler. The reference has no G-buffer (it shades
  * forward into its draw image); these are extra outputs of the same shading

@@ -57,6 +57,13 @@ class RzGbuffer(C.Structure):
                 ("normal_oct_f16x2", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
 
 
+class RzRsyInfo(C.Structure):
+    _fields_ = [("mesh_count", C.c_uint32), ("material_count", C.c_uint32), ("sampler_count", C.c_uint32),
+                ("image_count", C.c_uint32), ("node_count", C.c_uint32), ("scene_count", C.c_uint32),
+                ("root_scene", C.c_uint32), ("object_count", C.c_uint32), ("surface_count", C.c_uint32),
+                ("static_object_count", C.c_uint32), ("coordinate_system", C.c_float * 16)]
+
+
 class RzStats(C.Structure):
     _fields_ = [("draw_call_count", C.c_uint32), ("triangle_count", C.c_uint32),
                 ("shadow_setup_records", C.c_uint32), ("camera_setup_records", C.c_uint32),

@@ -29,7 +29,8 @@ EXPORTS = [
     "rz_get_view_frame", "rz_set_tuning", "rz_get_tuning", "rz_autotune", "rz_set_gbuffer", "rz_get_view_gbuffer",
     "rz_upsampler_create", "rz_upsampler_destroy", "rz_upsampler_set_params", "rz_upsampler_get_params",
     "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads", "rz_upsampler_adam_step",
-    "rz_upsampler_status", "rz_upsampler_selftest_gemm",
+    "rz_upsampler_status", "rz_upsampler_selftest_gemm", "rz_rsy_read", "rz_rsy_free", "rz_rsy_get_info",
+    "rz_rsy_get_meshes", "rz_rsy_get_materials", "rz_rsy_get_samplers", "rz_rsy_get_image", "rz_rsy_get_scene",
 ]
 
 _lib = None
@@ -106,6 +107,18 @@ def load(build_if_missing: bool = False):
     for name in ("rz_set_gbuffer", "rz_get_view_gbuffer", "rz_upsampler_create", "rz_upsampler_set_params",
                  "rz_upsampler_get_params", "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads",
                  "rz_upsampler_adam_step", "rz_upsampler_status", "rz_upsampler_selftest_gemm"):
+        getattr(lib, name).restype = C.c_int
+    lib.rz_rsy_read.argtypes = [C.c_char_p, C.POINTER(P)]
+    lib.rz_rsy_free.argtypes = [P]
+    lib.rz_rsy_free.restype = None
+    lib.rz_rsy_get_info.argtypes = [P, C.POINTER(_abi.RzRsyInfo)]
+    lib.rz_rsy_get_meshes.argtypes = [P, P, u32]
+    lib.rz_rsy_get_materials.argtypes = [P, P, u32]
+    lib.rz_rsy_get_samplers.argtypes = [P, P, u32]
+    lib.rz_rsy_get_image.argtypes = [P, u32, C.POINTER(u32), C.c_char_p, u32, C.POINTER(u32)]
+    lib.rz_rsy_get_scene.argtypes = [P, P, u32, P, u32]
+    for name in ("rz_rsy_read", "rz_rsy_get_info", "rz_rsy_get_meshes", "rz_rsy_get_materials", "rz_rsy_get_samplers",
+                 "rz_rsy_get_image", "rz_rsy_get_scene"):
         getattr(lib, name).restype = C.c_int
     lib.rz_abi_version.argtypes = []
     lib.rz_abi_version.restype = u32

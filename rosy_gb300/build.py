@@ -18,7 +18,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "librosy_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["rz_api.cu", "rz_raster.cu", "rz_shade.cu", "rz_static.cu", "rz_upsample.cu"]
+SOURCES = ["rz_api.cu", "rz_raster.cu", "rz_shade.cu", "rz_static.cu", "rz_upsample.cu", "rz_rsy.cpp"]
 HEADERS = ["rz_internal.h", "rz_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
@@ -46,7 +46,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             cmd = [nvcc()] + ARCH + NVCC_FLAGS + (extra or []) + ["-c", s, "-o", o]
