@@ -198,8 +198,17 @@ typedef struct rz_draw_config {
     float depth_bias_clamp;
     float depth_bias_slope_factor;
     uint32_t pcf_mode;                      /* RZ_PCF_* */
-    uint32_t reserved;
+    uint32_t shadow_cascades;               /* 0 or 1: the reference's single "near" map; 2..4: nested
+                                               cascades (see below) */
 } rz_draw_config;
+
+/* Shadow cascades (the reference allocates three layers and renders only the
+ * "near" one, src/Engine/Graphics.cpp:2545, 5203). With shadow_cascades = n > 1
+ * the shadow pass renders n maps of shadow_map_size^2, stored one after the
+ * other: cascade k uses shadowProjNear with clip x and y scaled by 2^-k (the
+ * light's orthographic extent times 2^k). A fragment uses the finest cascade k
+ * whose coordinates (csm.xy - 0.5) * 2^-k + 0.5 (csm.xy itself for k = 0) lie in
+ * [2 / size, 1 - 2 / size], else the coarsest. */
 
 /* Context creation: the headless analogue of graphics::init's config
  * (src/Engine/Types.h:33-37). */

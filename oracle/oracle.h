@@ -48,7 +48,7 @@ typedef struct oracle_out {
     uint8_t* color;      /* width*height*4, RGBA8 sRGB (may be NULL) */
     float* depth;        /* width*height (may be NULL) */
     uint32_t* ids;       /* width*height, triangle id + 1, 0 = background (may be NULL) */
-    float* shadow;       /* shadow_size^2 (may be NULL) */
+    float* shadow;       /* cascades * shadow_size^2: one map per shadow cascade (may be NULL) */
     double* color_f64;   /* width*height*4, FP64 shading, sRGB-encoded in [0,1] before 8-bit rounding (may be NULL) */
     uint64_t* texel_bytes; /* if non-NULL: compulsory texture + shadow-map bytes the shading touched */
 } oracle_out;

@@ -98,6 +98,19 @@ def _scene_struct(m: Marshalled) -> OracleScene:
     return o
 
 
+def cascades(s) -> int:
+    """Shadow cascades of the scene's draw config (1..4)."""
+    n = int(s.draw_config["shadow_cascades"][0]) if "shadow_cascades" in s.draw_config.dtype.names else 1
+    return min(max(n, 1), 4)
+
+
+def _shadow_array(s) -> np.ndarray:
+    """(S, S) for one shadow map, (cascades, S, S) for several."""
+    n = cascades(s)
+    shape = (s.shadow_size, s.shadow_size) if n == 1 else (n, s.shadow_size, s.shadow_size)
+    return np.zeros(shape, np.float32)
+
+
 def render(s, threads: int = 0, fp64: bool = False, texel_bytes: bool = False) -> dict:
     """Full frame: colour (H,W,4) u8, depth (H,W) f32, ids (H,W) u32, shadow (S,S) f32,
     optionally color_f64 (H,W,4) and the compulsory texel bytes of the shading."""
@@ -107,7 +120,7 @@ def render(s, threads: int = 0, fp64: bool = False, texel_bytes: bool = False) -
         "color": np.zeros((s.height, s.width, 4), np.uint8),
         "depth": np.zeros((s.height, s.width), np.float32),
         "ids": np.zeros((s.height, s.width), np.uint32),
-        "shadow": np.zeros((s.shadow_size, s.shadow_size), np.float32),
+        "shadow": _shadow_array(s),
     }
     oo = OracleOut(ptr(out["color"]), ptr(out["depth"]), ptr(out["ids"]), ptr(out["shadow"]), None, None)
     if fp64:
@@ -131,7 +144,7 @@ def raster(s, threads: int = 0) -> dict:
     out = {
         "depth": np.zeros((s.height, s.width), np.float32),
         "ids": np.zeros((s.height, s.width), np.uint32),
-        "shadow": np.zeros((s.shadow_size, s.shadow_size), np.float32),
+        "shadow": _shadow_array(s),
     }
     oo = OracleOut(None, ptr(out["depth"]), ptr(out["ids"]), ptr(out["shadow"]), None, None)
     rc = lib().oracle_raster(C.byref(o), C.byref(oo), int(threads))

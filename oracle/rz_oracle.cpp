@@ -361,13 +361,37 @@ void parallel_rows(int rows, int threads, F&& f) {
 }
 
 // Shadow pass: src/Engine/Graphics.cpp:5195-5292 with shadow.slang:6-19.
+void shadow_cascade(const Ctx& c, const float* P, float* shadow, int threads);
+
+// Shadow cascades: draw_config.shadow_cascades clamped to 1..4 (0 = 1, the reference's single map).
+int cascades_of(const oracle_scene* s) {
+    const uint32_t n = s->draw_config->shadow_cascades;
+    return n < 1 ? 1 : (n > 4 ? 4 : (int)n);
+}
+
+// One shadow map per cascade, S x S each, consecutive. Cascade k rasterises with
+// shadowProjNear whose clip x and y rows are scaled by 2^-k (exactly).
 void shadow_pass(const Ctx& c, float* shadow, int threads) {
+    const oracle_scene* s = c.s;
+    const int S = (int)s->shadow_size;
+    for (int k = 0; k < cascades_of(s); ++k) {
+        float P[16];
+        for (int i = 0; i < 16; ++i) P[i] = s->scene->shadow_projection_near[i];
+        const float sc = std::ldexp(1.0f, -k);
+        for (int col = 0; col < 4; ++col) {
+            P[col * 4 + 0] *= sc;
+            P[col * 4 + 1] *= sc;
+        }
+        shadow_cascade(c, P, shadow + (size_t)k * S * S, threads);
+    }
+}
+
+void shadow_cascade(const Ctx& c, const float* P, float* shadow, int threads) {
     const oracle_scene* s = c.s;
     const int S = (int)s->shadow_size;
     std::fill(shadow, shadow + (size_t)S * S, 0.0f);  // clear depth to 0 (5213)
     std::vector<float> mvps(c.shadow.size() * 16);
-    for (size_t i = 0; i < c.shadow.size(); ++i)
-        draw_mvp(c, c.shadow[i], s->scene->shadow_projection_near, &mvps[16 * i]);
+    for (size_t i = 0; i < c.shadow.size(); ++i) draw_mvp(c, c.shadow[i], P, &mvps[16 * i]);
     parallel_rows(S, threads, [&](int r0, int r1) {
         RasterState rs;
         rs.width = S;
@@ -908,7 +932,32 @@ bool fragment_main(const Ctx& c, const Draw& d, const Frag<T>& bv, const float* 
     if (sd.light_enabled > 0) {
         T shadowFactor = T(1);
         if (sd.shadows_enabled == 1)
-            shadowFactor = pcf<T>(shadow, (int)c.s->shadow_size, bv.csm, c.s->draw_config->pcf_mode, shadow_marks);
+        {
+            // the finest cascade whose coordinates keep the PCF footprint inside the map
+            const int S = (int)c.s->shadow_size;
+            const int n = cascades_of(c.s);
+            T cc[4] = {bv.csm[0], bv.csm[1], bv.csm[2], bv.csm[3]};
+            int k = 0;
+            if (n > 1) {
+                const T m = (T)(2.0f / (float)S);
+                const T hi = T(1) - m;
+                for (k = 0; k < n; ++k) {
+                    T x = bv.csm[0], y = bv.csm[1];
+                    if (k > 0) {
+                        const T sc = (T)std::ldexp(1.0f, -k);
+                        x = (bv.csm[0] - T(0.5)) * sc + T(0.5);
+                        y = (bv.csm[1] - T(0.5)) * sc + T(0.5);
+                    }
+                    if ((x >= m && x <= hi && y >= m && y <= hi) || k == n - 1) {
+                        cc[0] = x;
+                        cc[1] = y;
+                        break;
+                    }
+                }
+            }
+            shadowFactor = pcf<T>(shadow + (size_t)k * S * S, S, cc, c.s->draw_config->pcf_mode,
+                                  shadow_marks);
+        }
         if (sd.brdf_lighting_enabled == 0) {
             const T ml = fmaxT<T>(cosTheta, T(0));
             const V3<T> sunLight{(T)sd.sunlight_color[0] * ml, (T)sd.sunlight_color[1] * ml, (T)sd.sunlight_color[2] * ml};
@@ -1143,7 +1192,7 @@ extern "C" int oracle_raster(const oracle_scene* s, oracle_out* out, int threads
     std::vector<uint32_t> ids_local;
     float* shadow = out->shadow;
     if (!shadow) {
-        shadow_local.resize((size_t)s->shadow_size * s->shadow_size);
+        shadow_local.resize((size_t)cascades_of(s) * s->shadow_size * s->shadow_size);
         shadow = shadow_local.data();
     }
     float* depth = out->depth;
@@ -1167,7 +1216,7 @@ extern "C" int oracle_render(const oracle_scene* s, oracle_out* out, int threads
     Ctx c;
     build_ctx(s, c);
     const size_t np = (size_t)s->width * s->height;
-    std::vector<float> shadow((size_t)s->shadow_size * s->shadow_size), depth(np);
+    std::vector<float> shadow((size_t)cascades_of(s) * s->shadow_size * s->shadow_size), depth(np);
     std::vector<uint32_t> ids(np);
     shadow_pass(c, shadow.data(), threads);
     camera_pass(c, depth.data(), ids.data(), threads);

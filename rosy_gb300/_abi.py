@@ -33,7 +33,7 @@ class RzDrawConfig(C.Structure):
     _fields_ = [("cull_enabled", C.c_uint32), ("reverse_winding_order_enabled", C.c_uint32),
                 ("depth_bias_enabled", C.c_uint32), ("depth_bias_constant", C.c_float),
                 ("depth_bias_clamp", C.c_float), ("depth_bias_slope_factor", C.c_float),
-                ("pcf_mode", C.c_uint32), ("reserved", C.c_uint32)]
+                ("pcf_mode", C.c_uint32), ("shadow_cascades", C.c_uint32)]
 
 
 class RzView(C.Structure):

@@ -467,6 +467,12 @@ int ensure_scene_data(rz_ctx* c, uint32_t n) {
     return RZ_OK;
 }
 
+// Shadow cascades of a view: draw_config.shadow_cascades clamped to 1..kMaxCascades (0 = 1).
+uint32_t cascades_of(const ViewHost& v) {
+    const uint32_t n = v.dc.shadow_cascades;
+    return n < 1 ? 1u : (n > (uint32_t)kMaxCascades ? (uint32_t)kMaxCascades : n);
+}
+
 // Rebuilds the draw lists over all views, the target pools and the view table.
 int build_layout(rz_ctx* c) {
     if (c->views.empty()) return fail(c, RZ_INVALID_STATE, "no views");
@@ -482,7 +488,7 @@ int build_layout(rz_ctx* c) {
         shadow_off.push_back(shadow);
         block_base.push_back(blocks);
         pix += (size_t)v.width * v.height;
-        shadow += (size_t)v.shadow * v.shadow;
+        shadow += (size_t)cascades_of(v) * v.shadow * v.shadow;
         blocks += ((v.width + 15) / 16) * ((v.height + 15) / 16);
     }
     // draw lists, view-major, each view's surfaces in scene order (src/Engine/Graphics.cpp:4715-4735)
@@ -502,7 +508,7 @@ int build_layout(rz_ctx* c) {
         rg.pix_off = pix_off[vi];
         rg.pix = (size_t)v.width * v.height;
         rg.shadow_off = shadow_off[vi];
-        rg.shadow = (size_t)v.shadow * v.shadow;
+        rg.shadow = (size_t)cascades_of(v) * v.shadow * v.shadow;
         if (v.scene >= c->scenes.size()) return fail(c, RZ_INVALID_STATE, "view refers to a missing scene");
         const SceneHost& sh = c->scenes[v.scene];
         if (!sh.has_objects) return fail(c, RZ_INVALID_STATE, "scene has no objects (rz_set_objects)");
@@ -517,9 +523,13 @@ int build_layout(rz_ctx* c) {
             d.material = s.material_index < sh.material_count ? (int32_t)(sh.material_base + s.material_index) : -1;
             d.vertex_count = mt[1];
             d.view = vi;
-            d.tri_base = (uint32_t)shadow_tris;
-            shadow_list.push_back(d);
-            shadow_tris += d.tri_count;
+            for (uint32_t k = 0; k < cascades_of(v); ++k) {
+                d.cascade = k;
+                d.tri_base = (uint32_t)shadow_tris;
+                shadow_list.push_back(d);
+                shadow_tris += d.tri_count;
+            }
+            d.cascade = 0;
             if (s.blended) {
                 d.tri_base = (uint32_t)blended_tris;
                 blended.push_back(d);
@@ -589,6 +599,7 @@ int build_layout(rz_ctx* c) {
         r.bias_clamp = v.dc.depth_bias_clamp;
         r.bias_slope = v.dc.depth_bias_slope_factor;
         r.pcf_mode = v.dc.pcf_mode;
+        r.cascades = (int)cascades_of(v);
         r.shade_block_base = block_base[vi];
         r.vis = c->d_vis + pix_off[vi];
         r.color = c->d_color + pix_off[vi];

@@ -20,7 +20,8 @@ struct DrawRec {
     uint32_t varying_base; // camera pass: first varying record of this draw (one per mesh vertex)
     uint32_t vertex_count; // vertices of the draw's mesh
     uint32_t view;         // the view this draw renders into
-    uint32_t pad[3];
+    uint32_t cascade;      // shadow pass: the shadow cascade of the view this draw renders into
+    uint32_t pad[2];
 };
 static_assert(sizeof(DrawRec) == 48, "DrawRec layout");
 
@@ -40,6 +41,7 @@ struct ViewRec {
     uint32_t* shadow;             // shadow_w*shadow_h depth bits
     uint2* color16;               // width*height RGBA16F (only with blended surfaces)
     const rz_scene_data* scene;
+    int cascades;                 // shadow cascades (1..kMaxCascades), each shadow_w*shadow_h, consecutive
     uint32_t* gb_albedo;          // width*height RGBA8 sRGB albedo, or null (G-buffer off)
     uint32_t* gb_normal;          // width*height world normal, octahedral 2 x f16, or null
 };
@@ -87,6 +89,11 @@ struct TriRecord {
     uint64_t stamp_offset;           // exclusive prefix of stamps over all records
 };
 static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
+
+// Records of the shadow pass carry the cascade in the top bits of their view field.
+constexpr uint32_t kViewBits = 24;
+constexpr uint32_t kViewMask = (1u << kViewBits) - 1u;
+constexpr int kMaxCascades = 4;
 
 constexpr int kStampW = 8;
 constexpr int kStampH = 4;

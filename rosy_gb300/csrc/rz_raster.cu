@@ -41,6 +41,13 @@ __global__ void k_prep(const DrawRec* __restrict__ draws, uint32_t n, const rz_o
     float A[16], B[16], C[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) A[i] = P[i];
+    // cascade k: the light's orthographic extent times 2^k, i.e. clip x and y scaled by 2^-k (exact)
+    const float s = ldexpf(1.0f, -(int)draws[d].cascade);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        A[c * 4 + 0] *= s;
+        A[c * 4 + 1] *= s;
+    }
     const float* W = objects[draws[d].object].transform;
 #pragma unroll
     for (int i = 0; i < 16; ++i) B[i] = W[i];
@@ -245,7 +252,7 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
     }
     const ViewRec& VR = P.views[dr.view];
     ViewState V;
-    V.view = dr.view;
+    V.view = dr.view | (dr.cascade << kViewBits);
     V.width = P.write_id ? VR.width : VR.shadow_w;
     V.height = P.write_id ? VR.height : VR.shadow_h;
     V.cull_front = P.ordered ? 0 : VR.cull_front;
@@ -560,9 +567,9 @@ struct Target {
 
 template <bool kWriteId>
 __device__ __forceinline__ Target view_target(const PassParams& P, uint32_t view) {
-    const ViewRec& V = P.views[view];
+    const ViewRec& V = P.views[view & kViewMask];
     if (kWriteId) return Target{V.vis, V.width};
-    return Target{V.shadow, V.shadow_w};
+    return Target{V.shadow + (size_t)(view >> kViewBits) * (size_t)V.shadow_w * (size_t)V.shadow_h, V.shadow_w};
 }
 
 template <bool kWriteId>

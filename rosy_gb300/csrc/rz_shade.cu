@@ -473,6 +473,35 @@ __device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughnes
     return geometry_schlick_ggx(NdotL, roughness) * geometry_schlick_ggx(NdotV, roughness);
 }
 
+// The shadow map a fragment samples: with one cascade the view's map and csm
+// unchanged; with n > 1 the finest cascade k whose coordinates
+// (csm.xy - 0.5) * 2^-k + 0.5 keep the PCF footprint (2 texels) inside the map,
+// else the coarsest. Writes the coordinates in that cascade to cc.
+__device__ __forceinline__ const float* select_cascade(const ViewRec& VR, const float csm[4], float cc[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) cc[i] = csm[i];
+    const float* base = reinterpret_cast<const float*>(VR.shadow);
+    const int n = VR.cascades;
+    if (n <= 1) return base;
+    const float m = 2.0f / (float)VR.shadow_w;
+    const float hi = 1.0f - m;
+    int k = 0;
+    for (; k < n; ++k) {
+        float x = csm[0], y = csm[1];
+        if (k > 0) {
+            const float sc = ldexpf(1.0f, -k);
+            x = (csm[0] - 0.5f) * sc + 0.5f;
+            y = (csm[1] - 0.5f) * sc + 0.5f;
+        }
+        if ((x >= m && x <= hi && y >= m && y <= hi) || k == n - 1) {
+            cc[0] = x;
+            cc[1] = y;
+            break;
+        }
+    }
+    return base + (size_t)k * (size_t)VR.shadow_w * (size_t)VR.shadow_h;
+}
+
 // fragmentMain, src/shaders/basic.slang:137-344. Returns false on discard.
 __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const GpuMaterial* md, const Frag& bv,
                               const Sampler& smp, float out[4], float* albedo = nullptr) {
@@ -554,7 +583,11 @@ __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const 
     if (sd.light_enabled > 0) {
         float shadowFactor = 1.0f;
         if (sd.shadows_enabled == 1)
-            shadowFactor = pcf(reinterpret_cast<const float*>(VR.shadow), VR.shadow_w, bv.csm, VR.pcf_mode);
+        {
+            float cc[4];
+            const float* map = select_cascade(VR, bv.csm, cc);
+            shadowFactor = pcf(map, VR.shadow_w, cc, VR.pcf_mode);
+        }
         if (sd.brdf_lighting_enabled == 0) {
             const float ml = fmaxf(cosTheta, 0.0f);
             const V3 sunLight{sd.sunlight_color[0] * ml, sd.sunlight_color[1] * ml, sd.sunlight_color[2] * ml};

@@ -138,6 +138,7 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
     a.view.bias_clamp = cfg->depth_bias_clamp;
     a.view.bias_slope = cfg->depth_bias_slope_factor;
     a.view.shadow = reinterpret_cast<uint32_t*>(depth_out);
+    a.view.cascades = 1;
     k_static_prep<<<1, 128, 0, s>>>(a);
     if (tris) {
         PassParams p{};

@@ -107,9 +107,11 @@ class Graphics:
         self._check(self._lib.rz_get_view_frame(self._ctx, view, C.byref(f)), "rz_get_view_frame")
         self.sync()
         W, H, S = f.width, f.height, f.shadow_map_size
+        v = getattr(self, "_views", None)
+        n = min(max(int(v[view][4]["shadow_cascades"][0]), 1), 4) if v else 1
         out = {
             "vis": device_array(f.visibility_u64, (H, W), np.uint64),
-            "shadow": device_array(f.shadow_map_f32, (S, S), np.float32),
+            "shadow": device_array(f.shadow_map_f32, (S, S) if n == 1 else (n, S, S), np.float32),
             "color": device_array(f.color_rgba8, (H, W, 4), np.uint8),
             "depth": device_array(f.depth_f32, (H, W), np.float32),
         }
@@ -148,6 +150,7 @@ class Graphics:
 
     def set_draw_config(self, draw_config: np.ndarray) -> None:
         dc = np.ascontiguousarray(draw_config)
+        self._cascades = min(max(int(dc["shadow_cascades"][0]), 1), 4)
         self._check(self._lib.rz_set_draw_config(self._ctx, _abi.ptr(dc)), "rz_set_draw_config")
 
     def update(self, scene_data: np.ndarray) -> None:
@@ -215,9 +218,10 @@ class Graphics:
         f = self.frame()
         W, H, S = self.viewport_width, self.viewport_height, self.shadow_size
         self.sync()
+        n = getattr(self, "_cascades", 1)
         out = {
             "vis": device_array(f.visibility_u64, (H, W), np.uint64),
-            "shadow": device_array(f.shadow_map_f32, (S, S), np.float32),
+            "shadow": device_array(f.shadow_map_f32, (S, S) if n == 1 else (n, S, S), np.float32),
         }
         color = np.empty((H, W, 4), np.uint8)
         depth = np.empty((H, W), np.float32)

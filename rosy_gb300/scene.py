@@ -79,7 +79,7 @@ DRAW_CONFIG_DTYPE = np.dtype([
     ("cull_enabled", "<u4"), ("reverse_winding_order_enabled", "<u4"),
     ("depth_bias_enabled", "<u4"), ("depth_bias_constant", "<f4"),
     ("depth_bias_clamp", "<f4"), ("depth_bias_slope_factor", "<f4"),
-    ("pcf_mode", "<u4"), ("reserved", "<u4"),
+    ("pcf_mode", "<u4"), ("shadow_cascades", "<u4"),
 ])
 
 IMAGE_COLOR, IMAGE_NORMAL_MAP, IMAGE_METALLIC_ROUGHNESS, IMAGE_MIXMAP = 0, 1, 2, 3

@@ -98,6 +98,20 @@ def variants():
     v["alpha_mask"] = lambda: sc.with_blended(
         sc.random_triangles(seed=13, triangles=400, width=200, height=120, shadow_size=256, texture_size=32), 0.5,
         alpha=1.0, mask_cutoff=0.5)
+    def cascades(n, seed):
+        def make():
+            s = sc.random_triangles(seed=seed, triangles=800, width=256, height=160, shadow_size=256,
+                                    texture_size=64)
+            s.scene = s.scene.copy()
+            P = s.scene["shadow_projection_near"][0].reshape(4, 4).copy()  # rows of the column-major array = columns
+            P[:, 0:2] *= 16.0  # light extent 36 / 16 units: the cube spans several cascades
+            s.scene["shadow_projection_near"] = P.reshape(1, 16)
+            s.cameras = [s.scene]
+            s.draw_config["shadow_cascades"] = n
+            return s
+        return make
+    v["cascades_4"] = cascades(4, 14)
+    v["cascades_2"] = cascades(2, 15)
     return v
 
 

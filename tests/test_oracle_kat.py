@@ -238,3 +238,35 @@ def test_blended_list_order_and_depth(oracle):
     after_g = f16(np.float32(1.0) * np.float32(0.5) + red * np.float32(0.5))  # white-ish (1) over 1
     assert px[3] == int(math.floor(f16(0.5) * np.float32(255) + np.float32(0.5)))  # alpha = last passing blend (0.5)
     assert px[0] == srgb8(after_g)
+
+
+def test_shadow_cascades_are_scaled_projections(oracle):
+    """Cascade k of an n-cascade render is the single-map render with the light's
+    clip x and y scaled by 2^-k; fragments inside the finest cascade shade as the
+    single-map render with that cascade as its map."""
+    from rosy_gb300 import scene as sc
+
+    s = sc.random_triangles(seed=14, triangles=300, width=96, height=64, shadow_size=128, texture_size=32)
+    s.scene = s.scene.copy()
+    P = s.scene["shadow_projection_near"][0].reshape(4, 4).copy()
+    P[:, 0:2] *= 16.0
+    s.scene["shadow_projection_near"] = P.reshape(1, 16)
+    s.cameras = [s.scene]
+    s.draw_config = s.draw_config.copy()
+    s.draw_config["shadow_cascades"] = 4
+    multi = oracle.raster(s)
+    assert multi["shadow"].shape == (4, 128, 128)
+    for k in range(4):
+        t = sc.Scene(**{f: getattr(s, f) for f in s.__dataclass_fields__})
+        t.draw_config = s.draw_config.copy()
+        t.draw_config["shadow_cascades"] = 1
+        t.scene = s.scene.copy()
+        Pk = P.copy()
+        Pk[:, 0:2] *= np.float32(2.0 ** -k)
+        t.scene["shadow_projection_near"] = Pk.reshape(1, 16)
+        single = oracle.raster(t)
+        assert np.array_equal(single["shadow"].view(np.uint32), multi["shadow"][k].view(np.uint32)), k
+        assert (single["shadow"] > 0).any()
+    # coverage grows with the extent
+    cov = [(multi["shadow"][k] > 0).mean() for k in range(4)]
+    assert cov[0] > cov[1] > cov[2] > cov[3]
