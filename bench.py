@@ -478,6 +478,103 @@ def run_batch(args):
     }))
 
 
+def run_stress(args):
+    """The combined stress workload (1,048,576 triangles, 256 meshes, 64 materials with
+    2048^2 textures, 4 shadow cascades of 4096^2, 3x3 PCF): a batch of 8 views along
+    the camera spline rendered at 3840x2160 by the plain path, against the same 8 views
+    rendered at 1920x1080 (G-buffer on) and upsampled to 3840x2160 by the learned
+    upsampler. Reports views/s of both, per-view PSNR and max error of the learned
+    views against the plain ones."""
+    import torch
+
+    from rosy_gb300 import build as rzbuild
+    from rosy_gb300 import learned
+    from rosy_gb300 import scene as sc
+    from rosy_gb300.upsampler import Upsampler, psnr
+
+    rzbuild.build()
+    from rosy_gb300.graphics import Graphics
+
+    views = 8
+    s = sc.stress(frames=views)
+    lo_recs = [sc.view_of(s, 1920, 1080, 4096, camera=i).scene for i in range(views)]
+    params, meta = learned.load_weights()
+
+    def ctx(w, h, gbuffer):
+        g = Graphics()
+        g.init(w, h, 4096)
+        g.set_asset(s)
+        g.set_graphic_objects(s.objects, s.surfaces)
+        g.set_draw_config(s.draw_config)
+        g.set_views([(0, w, h, 4096, s.draw_config)] * views)
+        if gbuffer:
+            g.set_gbuffer(True)
+        return g
+
+    plain = ctx(3840, 2160, False)
+    for i in range(views):
+        plain.update_view(i, s.cameras[i])
+    low = ctx(1920, 1080, True)
+    for i in range(views):
+        low.update_view(i, lo_recs[i])
+    net = Upsampler(0, 1920, 1080)
+    net.set_params(params)
+    outs = [torch.zeros((2160, 3840), dtype=torch.int32, device="cuda") for _ in range(views)]
+    for g in (plain, low):  # grow the queues, build the graphs
+        for _ in range(3):
+            g.render()
+            if g.sync_code() != 14:
+                break
+        g.sync()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timed(kind, steps):
+        g = plain if kind == "plain" else low
+        st = torch.cuda.ExternalStream(g.stream)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(st):
+            for i in range(steps + args.warmup):
+                flush.fill_(float(i))
+                if i >= args.warmup:
+                    ev[i - args.warmup][0].record(st)
+                g.render()
+                if kind == "learned":
+                    for v in range(views):
+                        net.infer(low.gbuffer(v), outs[v].data_ptr(), low.stream)
+                if i >= args.warmup:
+                    ev[i - args.warmup][1].record(st)
+        st.synchronize()
+        return float(np.mean([a.elapsed_time(b) for a, b in ev]))
+
+    steps = max(3, min(args.steps, 20))
+    plain_ms = timed("plain", steps)
+    learned_ms = timed("learned", steps)
+    per = []
+    for v in range(views):
+        ref = plain.download_view(v)["color"]
+        got = outs[v].cpu().numpy().view(np.uint8).reshape(2160, 3840, 4)
+        d = np.abs(got[..., :3].astype(np.int32) - ref[..., :3].astype(np.int32))
+        per.append({"psnr_db": round(psnr(got, ref), 3), "max_abs_error": int(d.max())})
+    if net.status() != 0:
+        raise RuntimeError("upsampler kernels reported an error")
+    net.close()
+    plain.deinit()
+    low.deinit()
+    print(json.dumps({
+        "metric": "stress: 3840x2160 views/s, plain vs 1920x1080 + learned upsampler", "unit": "views/s",
+        "value": round(views / (learned_ms / 1e3), 2), "plain_value": round(views / (plain_ms / 1e3), 2),
+        "speedup": round(plain_ms / learned_ms, 3), "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_batch": {"plain": round(plain_ms, 4), "learned": round(learned_ms, 4)},
+        "higher_is_better": True, "dtype": "f32 raster/shading, bf16 upsampler", "data": "synthetic (seeded)",
+        "config": {"workload": "stress", "triangles": s.triangle_count, "meshes": 256, "materials": 64,
+                   "textures": len(s.textures), "texture_size": 2048, "shadow_cascades": 4, "shadow_map": 4096,
+                   "views_per_batch": views, "plain_extent": [3840, 2160], "render_extent": [1920, 1080],
+                   "l2": "flushed between batches (256 MiB write)"},
+        "per_view": per, "psnr_db_mean": round(float(np.mean([p["psnr_db"] for p in per])), 3),
+        "weights": {k: meta.get(k) for k in ("steps", "train_cameras")},
+    }))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -517,7 +614,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="rz", choices=["rz", "reference"])
-    ap.add_argument("--config", default="scene_scale", choices=["scene_scale", "random_triangles", "batch_views"])
+    ap.add_argument("--config", default="scene_scale",
+                    choices=["scene_scale", "random_triangles", "batch_views", "stress"])
     ap.add_argument("--views", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -530,6 +628,8 @@ def main():
         run_reference(args)
     elif args.config == "batch_views":
         run_batch(args)
+    elif args.config == "stress":
+        run_stress(args)
     else:
         run_rz(args)
 

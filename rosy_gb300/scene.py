@@ -292,6 +292,32 @@ def value_noise(rng, size: int, cells: int, channels: int, octaves: int = 3) -> 
     return out / total
 
 
+def value_noise_separable(rng, size: int, cells: int, channels: int, octaves: int = 3) -> np.ndarray:
+    """The same tileable smoothstep value noise as value_noise, evaluated as
+    W @ lattice @ W^T per octave (W: size x cells interpolation weights), which
+    is fast for large textures; values agree with value_noise to float rounding."""
+    out = np.zeros((channels, size, size), np.float32)
+    amp, total = 1.0, 0.0
+    c = cells
+    for _ in range(octaves):
+        c = max(1, min(c, size))
+        lattice = rng.random((channels, c, c), dtype=np.float32)
+        x = (np.arange(size, dtype=np.float32) + 0.5) * (c / size)
+        i0 = np.floor(x).astype(np.int64)
+        f = x - i0
+        f = f * f * (3.0 - 2.0 * f)
+        i0 %= c
+        i1 = (i0 + 1) % c
+        Wm = np.zeros((size, c), np.float32)
+        np.add.at(Wm, (np.arange(size), i0), 1.0 - f)
+        np.add.at(Wm, (np.arange(size), i1), f)
+        out += amp * (Wm[None] @ lattice @ Wm.T[None])
+        total += amp
+        amp *= 0.5
+        c *= 2
+    return np.ascontiguousarray((out / total).transpose(1, 2, 0))
+
+
 def build_mips(level0: np.ndarray) -> tuple[np.ndarray, int]:
     """Full box-filtered mip chain of an (h, w, 4) uint8 image (power-of-two sizes)."""
     h, w, _ = level0.shape
@@ -312,19 +338,20 @@ def build_mips(level0: np.ndarray) -> tuple[np.ndarray, int]:
     return flat, len(levels)
 
 
-def make_texture(rng, size: int, image_type: int, cells: int = 16) -> Texture:
+def make_texture(rng, size: int, image_type: int, cells: int = 16, separable: bool = False) -> Texture:
+    noise = value_noise_separable if separable else value_noise
     if image_type == IMAGE_NORMAL_MAP:
-        n = value_noise(rng, size, cells, 2) * 0.8 - 0.4
+        n = noise(rng, size, cells, 2) * 0.8 - 0.4
         nz = np.sqrt(np.maximum(0.0, 1.0 - n[..., 0] ** 2 - n[..., 1] ** 2))
         rgb = np.stack([n[..., 0], n[..., 1], nz], -1) * 0.5 + 0.5
         a = np.ones(rgb.shape[:2] + (1,), np.float32)
         img = np.concatenate([rgb, a], -1)
     elif image_type == IMAGE_METALLIC_ROUGHNESS or image_type == IMAGE_MIXMAP:
-        n = value_noise(rng, size, cells, 2)
+        n = noise(rng, size, cells, 2)
         img = np.stack([np.ones_like(n[..., 0]), 0.15 + 0.85 * n[..., 0],
                         np.clip(n[..., 1] * 1.6 - 0.5, 0, 1), np.ones_like(n[..., 0])], -1)
     else:
-        n = value_noise(rng, size, cells, 3)
+        n = noise(rng, size, cells, 3)
         rgb = 0.1 + 0.85 * n
         img = np.concatenate([rgb, np.ones(rgb.shape[:2] + (1,), np.float32)], -1)
     img8 = np.clip(np.floor(img * 255.0 + 0.5), 0, 255).astype(np.uint8)
@@ -451,11 +478,13 @@ def catmull_rom(p0, p1, p2, p3, t):
 def scene_scale(seed: int = 0, meshes: int = 64, triangles_per_mesh: int = 4096, materials: int = 32,
                 texture_size: int = 1024, width: int = 1920, height: int = 1080, shadow_size: int = 4096,
                 frames: int = 8, fov_deg: float = 60.0, median_area_px: float = 4.0, sigma: float = 1.5,
-                pcf_mode: int = PCF_3X3) -> Scene:
+                pcf_mode: int = PCF_3X3, texture_workers: int = 0) -> Scene:
     """Meshes (UV spheres) whose per-mesh triangle screen area at the first camera
     is log-normal(median, sigma); each material has albedo (sRGB), normal (UNORM)
     and metal-roughness (sRGB) textures with full mips; per-draw material IDs;
-    camera frames along a seeded Catmull-Rom spline."""
+    camera frames along a seeded Catmull-Rom spline. With texture_workers > 0 the
+    textures come from per-texture seeds on that many threads with the separable
+    noise (a different, faster stream of the same kind of noise)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     segs = 64
     rings = max(1, triangles_per_mesh // (2 * segs))
@@ -502,11 +531,25 @@ def scene_scale(seed: int = 0, meshes: int = 64, triangles_per_mesh: int = 4096,
         mesh_list.append((v0, nv, i0, len(sidx)))
         objects.append(object_record(node_world(center, r, rng.uniform(0, 2 * math.pi))))
     textures, mats = [], []
+    kinds = [(IMAGE_COLOR, 16), (IMAGE_NORMAL_MAP, 32), (IMAGE_METALLIC_ROUGHNESS, 8)]
+    if texture_workers > 0:
+        from concurrent.futures import ThreadPoolExecutor
+
+        base = int(rng.integers(0, 2 ** 63))
+
+        def one(i):
+            kind, cells = kinds[i % 3]
+            trng = np.random.Generator(np.random.PCG64([base, i]))
+            return make_texture(trng, texture_size, kind, cells=cells, separable=True)
+
+        with ThreadPoolExecutor(texture_workers) as ex:
+            textures = list(ex.map(one, range(3 * materials)))
+    else:
+        for k in range(materials):
+            for kind, cells in kinds:
+                textures.append(make_texture(rng, texture_size, kind, cells=cells))
     for k in range(materials):
-        t0 = len(textures)
-        textures.append(make_texture(rng, texture_size, IMAGE_COLOR, cells=16))
-        textures.append(make_texture(rng, texture_size, IMAGE_NORMAL_MAP, cells=32))
-        textures.append(make_texture(rng, texture_size, IMAGE_METALLIC_ROUGHNESS, cells=8))
+        t0 = 3 * k
         mats.append(material(color_image=t0, normal_image=t0 + 1, metallic_image=t0 + 2, sampler=0))
     surf = np.zeros(meshes, SURFACE_DTYPE)
     surf["mesh_index"] = np.arange(meshes)
@@ -529,6 +572,30 @@ def scene_scale(seed: int = 0, meshes: int = 64, triangles_per_mesh: int = 4096,
         objects=np.stack(objects), surfaces=surf,
         materials=np.concatenate(mats), textures=textures, samplers=linear_sampler(),
         scene=cams[0], draw_config=default_draw_config(pcf_mode), cameras=cams)
+
+
+def stress(seed: int = 0, width: int = 3840, height: int = 2160, frames: int = 8, texture_size: int = 2048,
+           texture_workers: int = 16) -> Scene:
+    """The combined stress workload: 1,048,576 triangles over 256 meshes, 64
+    materials with three texture_size^2 textures each (full mips), 4 nested
+    shadow cascades of 4096^2 (the light's near extent 9 units, then 18, 36, 72),
+    3x3 PCF, `frames` spline cameras (one view each)."""
+    s = scene_scale(seed=seed, meshes=256, triangles_per_mesh=4096, materials=64, texture_size=texture_size,
+                    width=width, height=height, shadow_size=4096, frames=frames, pcf_mode=PCF_3X3,
+                    texture_workers=texture_workers)
+    s.name = f"stress_s{seed}_{width}x{height}"
+    cams = []
+    for c in s.cameras:
+        c = c.copy()
+        P = c["shadow_projection_near"][0].reshape(4, 4).copy()
+        P[:, 0:2] *= 4.0  # near cascade: 36 / 4 = 9 units
+        c["shadow_projection_near"] = P.reshape(1, 16)
+        cams.append(c)
+    s.cameras = cams
+    s.scene = cams[0]
+    s.draw_config = s.draw_config.copy()
+    s.draw_config["shadow_cascades"] = 4
+    return s
 
 
 def tiny(seed: int = 0) -> Scene:
