@@ -47,7 +47,9 @@
 namespace rz {
 namespace up {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 128;      // weight-gradient and self-test kernels
+constexpr int kConvThreads = 288;  // convolution: warps 0-7 epilogue (two per TMEM lane quadrant), warp 8 issues MMAs
+constexpr int kMmaThread = 256;
 constexpr int kTileW = 128;  // conv: output pixels per MMA tile (M = 128), one row segment
 constexpr int kTileRows = 4; // conv: output rows per CTA
 constexpr int kHaloW = kTileW + 2;
@@ -151,6 +153,11 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool vali
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int kPending>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory");
+}
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -168,6 +175,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 32 consecutive f32 columns of the warp's 32 lanes.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __host__ __device__ constexpr uint32_t tmem_cols_for(int cols) { return cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : 256u; }
@@ -227,29 +251,33 @@ struct ConvArgs {
     uint32_t* err;
 };
 
+// Shared memory of the persistent convolution: the weights (B operand) once,
+// then two halo buffers (A operand) that alternate between tiles.
 template <int CIN, int N>
 struct ConvSmem {
     static constexpr int G = CIN / 8;
     static constexpr uint32_t S_G = kHaloW * 16;  // between channel planes (K direction)
     static constexpr uint32_t S_R = G * S_G;      // between halo rows
     static constexpr uint32_t A_BYTES = (kTileRows + 2) * S_R;
-    static constexpr uint32_t B_OFF = (A_BYTES + 127) / 128 * 128;
     static constexpr uint32_t B_BYTES = 9 * CIN * N * 2;
-    static constexpr uint32_t BAR_OFF = (B_OFF + B_BYTES + 127) / 128 * 128;
-    static constexpr uint32_t BYTES = BAR_OFF + 16;
-    static constexpr uint32_t TMEM_COLS = tmem_cols_for(kTileRows * N);
+    static constexpr uint32_t A_OFF0 = (B_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t A_OFF1 = A_OFF0 + (A_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t BAR_OFF = A_OFF1 + (A_BYTES + 127) / 128 * 128;
+    static constexpr uint32_t BYTES = BAR_OFF + 32;     // two barriers, the TMEM address
+    static constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * kTileRows * N);  // two accumulators
 };
+static_assert(ConvSmem<32, 32>::BYTES <= 227 * 1024, "conv shared memory");
 
 template <int N, int EPI>
 __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss,
-                                              const float* lut) {
+                                              const float* lut, const float* bias) {
     const bool inside = x < a.W && y < a.H;
     if (EPI == kEpiRelu) {
         if (!inside) return;
         uint32_t pk[N / 2];
 #pragma unroll
         for (int c = 0; c < N / 2; ++c)
-            pk[c] = pack_bf16(fmaxf(acc[2 * c] + __ldg(a.bias + 2 * c), 0.0f), fmaxf(acc[2 * c + 1] + __ldg(a.bias + 2 * c + 1), 0.0f));
+            pk[c] = pack_bf16(fmaxf(acc[2 * c] + bias[2 * c], 0.0f), fmaxf(acc[2 * c + 1] + bias[2 * c + 1], 0.0f));
         uint4* dst = reinterpret_cast<uint4*>(a.out + ((size_t)y * a.W + x) * N);
 #pragma unroll
         for (int q = 0; q < N / 8; ++q) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
@@ -273,7 +301,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
         if (!inside) return;
         float net[kOutChannels];
 #pragma unroll
-        for (int c = 0; c < kOutChannels; ++c) net[c] = acc[c] + __ldg(a.bias + c);
+        for (int c = 0; c < kOutChannels; ++c) net[c] = acc[c] + bias[c];
         const int W = a.W, H = a.H;
         // the 3x3 neighbourhood of low-resolution colours (edges clamped), as byte / 255
         float f[3][3][3];
@@ -328,78 +356,135 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
     }
 }
 
+// Issues the cp.async copies of one tile's halo: rows y0 - 1 .. y0 + kTileRows,
+// pixels x0 - 1 .. x0 + kTileW, every channel group; outside the image zeros.
+template <int CIN>
+__device__ __forceinline__ void stage_halo(const ConvArgs& a, unsigned char* sA, int x0, int y0, int tid) {
+    using L = ConvSmem<CIN, 32>;
+    constexpr int n = (kTileRows + 2) * kHaloW;
+    for (int i = tid; i < n; i += kConvThreads) {  // one halo pixel, all its channel groups
+        const int r = i / kHaloW, px = i - r * kHaloW;
+        const int x = x0 - 1 + px, y = y0 - 1 + r;
+        const bool valid = x >= 0 && x < a.W && y >= 0 && y < a.H;
+        const __nv_bfloat16* src = valid ? a.in + ((size_t)y * a.W + x) * CIN : a.in;
+        unsigned char* dst = sA + r * L::S_R + px * 16;
+#pragma unroll
+        for (int g = 0; g < L::G; ++g) cp_async16(dst + g * L::S_G, valid ? src + 8 * g : src, valid);
+    }
+}
+
+// Persistent convolution: CTA b takes tiles b, b + grid, ... (128 pixels x
+// kTileRows rows each). Iteration i waits for the MMAs of tile i - 1, prefetches
+// tile i + 1 into the halo buffer they used, issues the MMAs of tile i into one
+// TMEM accumulator (one thread of warp 8), and runs the epilogue of tile i - 1
+// from the other (warps 0-7), so the copies, the tensor cores and the epilogue
+// overlap.
 template <int CIN, int N, int EPI>
-__global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a) {
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a) {
     using L = ConvSmem<CIN, N>;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sA = smem;
-    unsigned char* sB = smem + L::B_OFF;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 8);
+    unsigned char* sB = smem;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = blockIdx.x * kTileW, y0 = blockIdx.y * kTileRows;
+    const int quad = warp & 3, half = warp >> 2;  // TMEM lane quadrant; which rows of a tile this warp writes
+    const int tiles_x = (a.W + kTileW - 1) / kTileW;
+    const int ntiles = tiles_x * ((a.H + kTileRows - 1) / kTileRows);
 
     __shared__ float s_lut[EPI == kEpiFinal ? 256 : 1];
+    __shared__ float s_bias[N];
     if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
-    if (tid == 0) mbar_init(bar, 1);
-    if (EPI == kEpiFinal) {
-        for (int i = tid; i < 256; i += kThreads) s_lut[i] = (float)i / 255.0f;
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
     }
+    if (EPI == kEpiFinal) {
+        for (int i = tid; i < 256; i += kConvThreads) s_lut[i] = (float)i / 255.0f;
+    }
+    if (tid < N) s_bias[tid] = EPI == kEpiMask ? 0.0f : a.bias[tid];
     {
         const uint4* src = reinterpret_cast<const uint4*>(a.wimg);
-        for (int i = tid; i < (int)(L::B_BYTES / 16); i += kThreads) cp_async16(sB + 16 * i, src + i, true);
+        for (int i = tid; i < (int)(L::B_BYTES / 16); i += kConvThreads) cp_async16(sB + 16 * i, src + i, true);
     }
-    {
-        constexpr int n = (kTileRows + 2) * kHaloW * L::G;
-#pragma unroll 4
-        for (int i = tid; i < n; i += kThreads) {
-            const int g = i % L::G;
-            const int px = (i / L::G) % kHaloW;
-            const int r = i / (L::G * kHaloW);
-            const int x = x0 - 1 + px, y = y0 - 1 + r;
-            const bool valid = x >= 0 && x < a.W && y >= 0 && y < a.H;
-            const __nv_bfloat16* src = valid ? a.in + ((size_t)y * a.W + x) * CIN + 8 * g : a.in;
-            cp_async16(sA + r * L::S_R + g * L::S_G + px * 16, src, valid);
-        }
-    }
-    cp_async_wait_all();
-    fence_async_smem();
+    if ((int)blockIdx.x < ntiles)
+        stage_halo<CIN>(a, smem + L::A_OFF0, (blockIdx.x % tiles_x) * kTileW, (blockIdx.x / tiles_x) * kTileRows, tid);
+    cp_async_commit();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    if (tid == 0) {
-        constexpr uint32_t idesc = idesc_bf16(128, N);
-        constexpr uint32_t lbo_b = N * 16;
-        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-        for (int t = 0; t < kTileRows; ++t) {
-            uint32_t acc = 0;
-            for (int tap = 0; tap < 9; ++tap) {
-                const int ky = tap / 3, kx = tap % 3;
+    float loss = 0.0f;
+    bool ok = true;
+    int i = 0, px0 = 0, py0 = 0;
+    auto epilogue = [&](int acc_buf, int x0, int y0) {
+        if (warp >= 8) return;
 #pragma unroll
-                for (int s = 0; s < CIN / 16; ++s) {
-                    const uint64_t da = umma_desc(a0 + (t + ky) * L::S_R + kx * 16 + 2 * s * L::S_G, L::S_G, 128);
-                    const uint64_t db = umma_desc(b0 + (tap * L::G + 2 * s) * lbo_b, lbo_b, 128);
-                    mma_bf16(tmem + t * N, da, db, idesc, acc);
-                    acc = 1;
+        for (int tt = 0; tt < kTileRows / 2; ++tt) {
+            const int t = half * (kTileRows / 2) + tt;
+            float acc[N];
+            const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (acc_buf * kTileRows + t) * N;
+            if constexpr (N == 32) tmem_ld32(ta, acc);
+            else tmem_ld16(ta, acc);
+            conv_epilogue<N, EPI>(a, acc, x0 + quad * 32 + lane, y0 + t, loss, s_lut, s_bias);
+        }
+    };
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int buf = i & 1;
+        // the MMAs of tile i - 1 are complete: their halo buffer is free and their accumulator ready
+        if (i >= 1) ok = ok && mbar_wait(&bars[(i - 1) & 1], (uint32_t)((i - 1) >> 1) & 1u);
+        if (!__syncthreads_and(ok ? 1 : 0)) {
+            ok = false;
+            break;
+        }
+        const int next = tile + gridDim.x;
+        if (next < ntiles) {
+            stage_halo<CIN>(a, smem + (buf ? L::A_OFF0 : L::A_OFF1), (next % tiles_x) * kTileW, (next / tiles_x) * kTileRows, tid);
+            cp_async_commit();
+            cp_async_wait_group<1>();
+        } else {
+            cp_async_wait_group<0>();
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == kMmaThread) {
+            // descriptors differ only in their start address (the low 14 bits, in 16-byte units), so
+            // each MMA's descriptors are the tile's base descriptors plus a compile-time offset
+            constexpr uint32_t idesc = idesc_bf16(128, N);
+            constexpr uint32_t lbo_b = N * 16;
+            const uint64_t da0 = umma_desc(smem_u32(smem + (buf ? L::A_OFF1 : L::A_OFF0)), L::S_G, 128);
+            const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
+            const uint32_t d0 = tmem + buf * kTileRows * N;
+#pragma unroll
+            for (int t = 0; t < kTileRows; ++t) {
+#pragma unroll
+                for (int tap = 0; tap < 9; ++tap) {
+#pragma unroll
+                    for (int s = 0; s < CIN / 16; ++s) {
+                        const uint32_t oa = ((t + tap / 3) * L::S_R + (tap % 3) * 16 + 2 * s * L::S_G) >> 4;
+                        const uint32_t ob = ((tap * L::G + 2 * s) * lbo_b) >> 4;
+                        mma_bf16(d0 + t * N, da0 + oa, db0 + ob, idesc, (tap | s) ? 1u : 0u);
+                    }
                 }
             }
+            mma_commit(&bars[buf]);
         }
-        mma_commit(bar);
+        if (i >= 1) epilogue(buf ^ 1, px0, py0);
+        // the accumulator just read is the target of the next tile's MMAs
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        px0 = (tile % tiles_x) * kTileW;
+        py0 = (tile / tiles_x) * kTileRows;
     }
-    const bool ok = __syncthreads_and(mbar_wait(bar, 0) ? 1 : 0) != 0;
-    tc_fence_after();
-    float loss = 0.0f;
-    if (ok) {
-        for (int t = 0; t < kTileRows; ++t) {
-            float acc[N];
-#pragma unroll
-            for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + t * N + c, acc + c);
-            conv_epilogue<N, EPI>(a, acc, x0 + warp * 32 + lane, y0 + t, loss, s_lut);
-        }
-    } else if (tid == 0) {
-        atomicOr(a.err, kErrMmaTimeout);
+    if (ok && i >= 1) {
+        ok = __syncthreads_and(mbar_wait(&bars[(i - 1) & 1], (uint32_t)((i - 1) >> 1) & 1u) ? 1 : 0) != 0;
+        tc_fence_after();
+        if (ok) epilogue((i - 1) & 1, px0, py0);
     }
+    if (!ok && tid == 0) atomicOr(a.err, kErrMmaTimeout);
+    cp_async_wait_all();
     if (EPI == kEpiFinal && a.target) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, o);
@@ -725,9 +810,10 @@ cudaError_t ensure_attributes() {
 }
 
 template <int CIN, int N, int EPI>
-void launch_conv(const ConvArgs& a, cudaStream_t s) {
-    const dim3 grid((a.W + kTileW - 1) / kTileW, (a.H + kTileRows - 1) / kTileRows);
-    k_conv<CIN, N, EPI><<<grid, kThreads, ConvSmem<CIN, N>::BYTES, s>>>(a);
+void launch_conv(const rz_upsampler* u, const ConvArgs& a, cudaStream_t s) {
+    const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileRows - 1) / kTileRows);
+    const int grid = std::min(tiles, std::max(u->sms, 1));
+    k_conv<CIN, N, EPI><<<grid, kConvThreads, ConvSmem<CIN, N>::BYTES, s>>>(a);
 }
 
 template <int CIN, int N>
@@ -760,13 +846,13 @@ void forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out
     a.wimg = u->d_img + fwd_img_off(0);
     a.bias = u->d_params + layer_boff(0);
     a.out = u->d_act[0];
-    launch_conv<16, 32, kEpiRelu>(a, s);
+    launch_conv<16, 32, kEpiRelu>(u, a, s);
     for (int l = 1; l <= 2; ++l) {
         a.in = u->d_act[l - 1];
         a.wimg = u->d_img + fwd_img_off(l);
         a.bias = u->d_params + layer_boff(l);
         a.out = u->d_act[l];
-        launch_conv<32, 32, kEpiRelu>(a, s);
+        launch_conv<32, 32, kEpiRelu>(u, a, s);
     }
     ConvArgs f = conv_args(u, W, H);
     f.in = u->d_act[2];
@@ -777,7 +863,7 @@ void forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out
     f.target = static_cast<const uint32_t*>(target);
     f.dy = u->d_dy3;
     f.loss = u->d_loss;
-    launch_conv<32, 16, kEpiFinal>(f, s);
+    launch_conv<32, 16, kEpiFinal>(u, f, s);
 }
 
 }  // namespace
@@ -881,7 +967,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     d.wimg = u->d_img + dgrad_img_off(3);
     d.mask_src = u->d_act[2];
     d.out = u->d_dyA;
-    launch_conv<16, 32, kEpiMask>(d, s);
+    launch_conv<16, 32, kEpiMask>(u, d, s);
     // layer 2
     w.x = u->d_act[1];
     w.dy = u->d_dyA;
@@ -892,7 +978,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     d.wimg = u->d_img + dgrad_img_off(2);
     d.mask_src = u->d_act[1];
     d.out = u->d_dyB;
-    launch_conv<32, 32, kEpiMask>(d, s);
+    launch_conv<32, 32, kEpiMask>(u, d, s);
     // layer 1
     w.x = u->d_act[0];
     w.dy = u->d_dyB;
@@ -903,7 +989,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     d.wimg = u->d_img + dgrad_img_off(1);
     d.mask_src = u->d_act[0];
     d.out = u->d_dyA;
-    launch_conv<32, 32, kEpiMask>(d, s);
+    launch_conv<32, 32, kEpiMask>(u, d, s);
     // layer 0
     w.x = u->d_feat;
     w.dy = u->d_dyA;
