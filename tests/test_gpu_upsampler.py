@@ -180,3 +180,17 @@ def test_training_steps_lower_the_loss(gpu):
     u.close()
     lo.deinit()
     hi.deinit()
+
+
+def test_trained_network_beats_bilinear_on_heldout_cameras(gpu):
+    """The committed weights (trained only on plain-path frames from the training
+    cameras) against the method without the network (bilinear x2, the network with a
+    zero last layer), judged by the plain full-resolution render on held-out cameras."""
+    from rosy_gb300 import learned
+
+    params, meta = learned.load_weights()
+    ev = learned.evaluate(params, cameras=16)
+    assert ev["frames"] == 16
+    gains = [f["psnr_db"] - f["bilinear_psnr_db"] for f in ev["per_frame"]]
+    assert min(gains) > 0.0, gains
+    assert ev["psnr_db_mean"] > ev["bilinear_psnr_db_mean"] + 1.0, ev
