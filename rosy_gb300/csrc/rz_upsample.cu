@@ -34,6 +34,8 @@
 // returns.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -48,8 +50,8 @@ namespace rz {
 namespace up {
 
 constexpr int kThreads = 128;      // weight-gradient and self-test kernels
-constexpr int kConvThreads = 288;  // convolution: warps 0-7 epilogue (two per TMEM lane quadrant), warp 8 issues MMAs
-constexpr int kMmaThread = 256;
+constexpr int kConvEpilogueWarps = 16;  // convolution: one epilogue warp per (TMEM lane quadrant, tile row),
+constexpr int kConvThreads = 32 * (kConvEpilogueWarps + 2);  // then a TMA warp and an MMA warp
 constexpr int kTileW = 128;  // conv: output pixels per MMA tile (M = 128), one row segment
 constexpr int kTileRows = 4; // conv: output rows per CTA
 constexpr int kHaloW = kTileW + 2;
@@ -252,18 +254,21 @@ struct ConvArgs {
 };
 
 // Shared memory of the persistent convolution: the weights (B operand) once,
-// then two halo buffers (A operand) that alternate between tiles.
+// then two halo buffers (A operand) that alternate between tiles. Each halo
+// buffer is (kTileRows + 2) rows x (CIN / 8) channel planes x 130 pixels x 16
+// bytes; a plane is padded to a multiple of 128 bytes because TMA writes it.
 template <int CIN, int N>
 struct ConvSmem {
     static constexpr int G = CIN / 8;
-    static constexpr uint32_t S_G = kHaloW * 16;  // between channel planes (K direction)
-    static constexpr uint32_t S_R = G * S_G;      // between halo rows
+    static constexpr uint32_t S_G = (kHaloW * 16 + 127) / 128 * 128;  // between channel planes (K direction)
+    static constexpr uint32_t S_R = G * S_G;                          // between halo rows
     static constexpr uint32_t A_BYTES = (kTileRows + 2) * S_R;
+    static constexpr uint32_t TX_BYTES = (kTileRows + 2) * G * kHaloW * 16;  // what one tile's TMA loads write
     static constexpr uint32_t B_BYTES = 9 * CIN * N * 2;
-    static constexpr uint32_t A_OFF0 = (B_BYTES + 127) / 128 * 128;
-    static constexpr uint32_t A_OFF1 = A_OFF0 + (A_BYTES + 127) / 128 * 128;
-    static constexpr uint32_t BAR_OFF = A_OFF1 + (A_BYTES + 127) / 128 * 128;
-    static constexpr uint32_t BYTES = BAR_OFF + 32;     // two barriers, the TMEM address
+    static constexpr uint32_t A_OFF0 = (B_BYTES + 1023) / 1024 * 1024;
+    static constexpr uint32_t A_OFF1 = A_OFF0 + (A_BYTES + 1023) / 1024 * 1024;
+    static constexpr uint32_t BAR_OFF = A_OFF1 + (A_BYTES + 1023) / 1024 * 1024;
+    static constexpr uint32_t BYTES = BAR_OFF + 80;  // 8 barriers, the TMEM address
     static constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * kTileRows * N);  // two accumulators
 };
 static_assert(ConvSmem<32, 32>::BYTES <= 227 * 1024, "conv shared memory");
@@ -356,47 +361,61 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
     }
 }
 
-// Issues the cp.async copies of one tile's halo: rows y0 - 1 .. y0 + kTileRows,
-// pixels x0 - 1 .. x0 + kTileW, every channel group; outside the image zeros.
-template <int CIN>
-__device__ __forceinline__ void stage_halo(const ConvArgs& a, unsigned char* sA, int x0, int y0, int tid) {
-    using L = ConvSmem<CIN, 32>;
-    constexpr int n = (kTileRows + 2) * kHaloW;
-    for (int i = tid; i < n; i += kConvThreads) {  // one halo pixel, all its channel groups
-        const int r = i / kHaloW, px = i - r * kHaloW;
-        const int x = x0 - 1 + px, y = y0 - 1 + r;
-        const bool valid = x >= 0 && x < a.W && y >= 0 && y < a.H;
-        const __nv_bfloat16* src = valid ? a.in + ((size_t)y * a.W + x) * CIN : a.in;
-        unsigned char* dst = sA + r * L::S_R + px * 16;
-#pragma unroll
-        for (int g = 0; g < L::G; ++g) cp_async16(dst + g * L::S_G, valid ? src + 8 * g : src, valid);
-    }
+// TMA load of one box {8 channels, 130 pixels, 1 row} of an NHWC bf16 tensor
+// into shared memory, completing on `bar` with its byte count.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
+            "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c), "r"(x), "r"(y)
+        : "memory");
 }
 
-// Persistent convolution: CTA b takes tiles b, b + grid, ... (128 pixels x
-// kTileRows rows each). Iteration i waits for the MMAs of tile i - 1, prefetches
-// tile i + 1 into the halo buffer they used, issues the MMAs of tile i into one
-// TMEM accumulator (one thread of warp 8), and runs the epilogue of tile i - 1
-// from the other (warps 0-7), so the copies, the tensor cores and the epilogue
-// overlap.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent, warp-specialised convolution. CTA b takes tiles b, b + grid, ...
+// (128 pixels x kTileRows rows each) through a two-stage ring:
+//   warp 16 (one thread) TMA-loads tile j's halo into halo buffer j % 2 once the
+//                        MMAs of tile j - 2 have released it (barrier `empty`);
+//   warp 17 (one thread) waits for the halo (`full`) and for the epilogue of
+//                        tile j - 2 to have drained accumulator j % 2 (`tempty`),
+//                        issues the tile's tcgen05.mma and commits to `empty` and
+//                        `tfull`;
+//   warps 0-15           wait for `tfull`, read the accumulator (warp w reads
+//                        TMEM lane quadrant w % 4 of tile row w / 4), run the
+//                        epilogue and arrive on `tempty`.
+// Every wait is bounded; a role whose wait runs out sets kErrMmaTimeout and
+// stops, and the others then run out in turn.
 template <int CIN, int N, int EPI>
-__global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a) {
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __grid_constant__ CUtensorMap in_map) {
     using L = ConvSmem<CIN, N>;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sB = smem;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 16);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);  // [2]
+    uint64_t* empty = full + 2;                                        // [2]
+    uint64_t* tfull = full + 4;                                        // [2]
+    uint64_t* tempty = full + 6;                                       // [2]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 64);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int quad = warp & 3, half = warp >> 2;  // TMEM lane quadrant; which rows of a tile this warp writes
     const int tiles_x = (a.W + kTileW - 1) / kTileW;
     const int ntiles = tiles_x * ((a.H + kTileRows - 1) / kTileRows);
+    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
     __shared__ float s_lut[EPI == kEpiFinal ? 256 : 1];
     __shared__ float s_bias[N];
     if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], 1);
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], kConvEpilogueWarps);
+        }
     }
     if (EPI == kEpiFinal) {
         for (int i = tid; i < 256; i += kConvThreads) s_lut[i] = (float)i / 255.0f;
@@ -406,55 +425,50 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a) {
         const uint4* src = reinterpret_cast<const uint4*>(a.wimg);
         for (int i = tid; i < (int)(L::B_BYTES / 16); i += kConvThreads) cp_async16(sB + 16 * i, src + i, true);
     }
-    if ((int)blockIdx.x < ntiles)
-        stage_halo<CIN>(a, smem + L::A_OFF0, (blockIdx.x % tiles_x) * kTileW, (blockIdx.x / tiles_x) * kTileRows, tid);
-    cp_async_commit();
+    cp_async_wait_all();
+    fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    float loss = 0.0f;
     bool ok = true;
-    int i = 0, px0 = 0, py0 = 0;
-    auto epilogue = [&](int acc_buf, int x0, int y0) {
-        if (warp >= 8) return;
+    float loss = 0.0f;
+
+    if (warp == kConvEpilogueWarps && lane == 0) {
+        // producer: TMA loads of each tile's halo
+        for (int j = 0; j < my_tiles && ok; ++j) {
+            const int buf = j & 1;
+            if (j >= 2 && !mbar_wait(&empty[buf], (uint32_t)((j - 2) >> 1) & 1u)) {
+                ok = false;
+                break;
+            }
+            const int tile = blockIdx.x + j * gridDim.x;
+            const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileRows;
+            unsigned char* A = smem + (buf ? L::A_OFF1 : L::A_OFF0);
+            mbar_expect_tx(&full[buf], L::TX_BYTES);
+            for (int r = 0; r < kTileRows + 2; ++r)
 #pragma unroll
-        for (int tt = 0; tt < kTileRows / 2; ++tt) {
-            const int t = half * (kTileRows / 2) + tt;
-            float acc[N];
-            const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (acc_buf * kTileRows + t) * N;
-            if constexpr (N == 32) tmem_ld32(ta, acc);
-            else tmem_ld16(ta, acc);
-            conv_epilogue<N, EPI>(a, acc, x0 + quad * 32 + lane, y0 + t, loss, s_lut, s_bias);
+                for (int g = 0; g < L::G; ++g) tma_load_3d(A + r * L::S_R + g * L::S_G, &in_map, &full[buf], 8 * g, x0 - 1, y0 - 1 + r);
         }
-    };
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
-        const int buf = i & 1;
-        // the MMAs of tile i - 1 are complete: their halo buffer is free and their accumulator ready
-        if (i >= 1) ok = ok && mbar_wait(&bars[(i - 1) & 1], (uint32_t)((i - 1) >> 1) & 1u);
-        if (!__syncthreads_and(ok ? 1 : 0)) {
-            ok = false;
-            break;
-        }
-        const int next = tile + gridDim.x;
-        if (next < ntiles) {
-            stage_halo<CIN>(a, smem + (buf ? L::A_OFF0 : L::A_OFF1), (next % tiles_x) * kTileW, (next / tiles_x) * kTileRows, tid);
-            cp_async_commit();
-            cp_async_wait_group<1>();
-        } else {
-            cp_async_wait_group<0>();
-        }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (tid == kMmaThread) {
-            // descriptors differ only in their start address (the low 14 bits, in 16-byte units), so
-            // each MMA's descriptors are the tile's base descriptors plus a compile-time offset
-            constexpr uint32_t idesc = idesc_bf16(128, N);
-            constexpr uint32_t lbo_b = N * 16;
+        // the copies still in flight land before the CTA exits
+        for (int j = my_tiles - 2 > 0 ? my_tiles - 2 : 0; j < my_tiles; ++j)
+            if (!mbar_wait(&full[j & 1], (uint32_t)(j >> 1) & 1u)) ok = false;
+    } else if (warp == kConvEpilogueWarps + 1 && lane == 0) {
+        // MMA issue
+        constexpr uint32_t idesc = idesc_bf16(128, N);
+        constexpr uint32_t lbo_b = N * 16;
+        const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
+        for (int j = 0; j < my_tiles; ++j) {
+            const int buf = j & 1;
+            if (!mbar_wait(&full[buf], (uint32_t)(j >> 1) & 1u) ||
+                (j >= 2 && !mbar_wait(&tempty[buf], (uint32_t)((j - 2) >> 1) & 1u))) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            // descriptors differ only in their start address (the low 14 bits, in 16-byte units), so each
+            // MMA's descriptors are the tile's base descriptors plus a compile-time offset
             const uint64_t da0 = umma_desc(smem_u32(smem + (buf ? L::A_OFF1 : L::A_OFF0)), L::S_G, 128);
-            const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
             const uint32_t d0 = tmem + buf * kTileRows * N;
 #pragma unroll
             for (int t = 0; t < kTileRows; ++t) {
@@ -468,30 +482,46 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a) {
                     }
                 }
             }
-            mma_commit(&bars[buf]);
+            mma_commit(&empty[buf]);
+            mma_commit(&tfull[buf]);
         }
-        if (i >= 1) epilogue(buf ^ 1, px0, py0);
-        // the accumulator just read is the target of the next tile's MMAs
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        px0 = (tile % tiles_x) * kTileW;
-        py0 = (tile / tiles_x) * kTileRows;
+        // the last MMAs complete before the CTA frees its tensor memory
+        if (ok && my_tiles > 0 && !mbar_wait(&empty[(my_tiles - 1) & 1], (uint32_t)((my_tiles - 1) >> 1) & 1u))
+            ok = false;
+    } else if (warp < kConvEpilogueWarps) {
+        const int quad = warp & 3, row0 = (warp >> 2) * (kTileRows * 4 / kConvEpilogueWarps);
+        for (int j = 0; j < my_tiles; ++j) {
+            const int buf = j & 1;
+            if (!mbar_wait(&tfull[buf], (uint32_t)(j >> 1) & 1u)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const int tile = blockIdx.x + j * gridDim.x;
+            const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileRows;
+#pragma unroll
+            for (int tt = 0; tt < kTileRows * 4 / kConvEpilogueWarps; ++tt) {
+                const int t = row0 + tt;
+                float acc[N];
+                const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (buf * kTileRows + t) * N;
+                if constexpr (N == 32) tmem_ld32(ta, acc);
+                else tmem_ld16(ta, acc);
+                conv_epilogue<N, EPI>(a, acc, x0 + quad * 32 + lane, y0 + t, loss, s_lut, s_bias);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[buf]);
+        }
     }
-    if (ok && i >= 1) {
-        ok = __syncthreads_and(mbar_wait(&bars[(i - 1) & 1], (uint32_t)((i - 1) >> 1) & 1u) ? 1 : 0) != 0;
-        tc_fence_after();
-        if (ok) epilogue((i - 1) & 1, px0, py0);
-    }
-    if (!ok && tid == 0) atomicOr(a.err, kErrMmaTimeout);
-    cp_async_wait_all();
-    if (EPI == kEpiFinal && a.target) {
+    if (!ok) atomicOr(a.err, kErrMmaTimeout);
+    if (EPI == kEpiFinal && a.target && warp < kConvEpilogueWarps) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, o);
         if (lane == 0 && loss != 0.0f) atomicAdd(a.loss, (double)loss);
     }
     tc_fence_before();
     __syncthreads();
+    tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, L::TMEM_COLS);
 }
 
@@ -809,11 +839,40 @@ cudaError_t ensure_attributes() {
     return g_attr_status;
 }
 
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link against libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+std::once_flag g_encode_once;
+
+void load_encode_tiled() {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+}
+
+// Tensor map of an H x W x C bf16 NHWC tensor with boxes of {8 channels, kHaloW pixels, 1 row};
+// out-of-range elements read as zero.
+bool encode_nhwc(CUtensorMap* map, const void* base, int C, int W, int H) {
+    std::call_once(g_encode_once, load_encode_tiled);
+    if (!g_encode_tiled) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H};
+    const cuuint64_t strides[2] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2};
+    const cuuint32_t box[3] = {8, (cuuint32_t)kHaloW, 1};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    return g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, elem,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int CIN, int N, int EPI>
-void launch_conv(const rz_upsampler* u, const ConvArgs& a, cudaStream_t s) {
+bool launch_conv(const rz_upsampler* u, const ConvArgs& a, cudaStream_t s) {
+    CUtensorMap map;
+    if (!encode_nhwc(&map, a.in, CIN, a.W, a.H)) return false;
     const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileRows - 1) / kTileRows);
     const int grid = std::min(tiles, std::max(u->sms, 1));
-    k_conv<CIN, N, EPI><<<grid, kConvThreads, ConvSmem<CIN, N>::BYTES, s>>>(a);
+    k_conv<CIN, N, EPI><<<grid, kConvThreads, ConvSmem<CIN, N>::BYTES, s>>>(a, map);
+    return true;
 }
 
 template <int CIN, int N>
@@ -836,8 +895,9 @@ ConvArgs conv_args(const rz_upsampler* u, int W, int H) {
     return a;
 }
 
-// Forward pass; with `target` it also writes the loss gradient and sum.
-void forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out, cudaStream_t s) {
+// Forward pass; with `target` it also writes the loss gradient and sum. False if
+// a tensor map could not be encoded.
+bool forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out, cudaStream_t s) {
     const int W = (int)g->width, H = (int)g->height;
     const int n = W * H;
     k_features<<<(n + 255) / 256, 256, 0, s>>>(*g, u->d_feat);
@@ -846,13 +906,13 @@ void forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out
     a.wimg = u->d_img + fwd_img_off(0);
     a.bias = u->d_params + layer_boff(0);
     a.out = u->d_act[0];
-    launch_conv<16, 32, kEpiRelu>(u, a, s);
+    if (!launch_conv<16, 32, kEpiRelu>(u, a, s)) return false;
     for (int l = 1; l <= 2; ++l) {
         a.in = u->d_act[l - 1];
         a.wimg = u->d_img + fwd_img_off(l);
         a.bias = u->d_params + layer_boff(l);
         a.out = u->d_act[l];
-        launch_conv<32, 32, kEpiRelu>(u, a, s);
+        if (!launch_conv<32, 32, kEpiRelu>(u, a, s)) return false;
     }
     ConvArgs f = conv_args(u, W, H);
     f.in = u->d_act[2];
@@ -863,7 +923,8 @@ void forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out
     f.target = static_cast<const uint32_t*>(target);
     f.dy = u->d_dy3;
     f.loss = u->d_loss;
-    launch_conv<32, 16, kEpiFinal>(u, f, s);
+    if (!launch_conv<32, 16, kEpiFinal>(u, f, s)) return false;
+    return true;
 }
 
 }  // namespace
@@ -941,7 +1002,7 @@ int rz_upsampler_get_params(rz_upsampler* u, float* params, uint32_t count, void
 int rz_upsampler_infer(rz_upsampler* u, const rz_gbuffer* in, void* out_rgba8, void* stream) {
     if (!u || !gbuffer_ok(u, in) || !out_rgba8) return RZ_INVALID_ARGUMENT;
     cudaSetDevice(u->device);
-    forward(u, in, nullptr, out_rgba8, static_cast<cudaStream_t>(stream));
+    if (!forward(u, in, nullptr, out_rgba8, static_cast<cudaStream_t>(stream))) return RZ_ERROR;
     return cudaGetLastError() == cudaSuccess ? RZ_OK : RZ_ERROR;
 }
 
@@ -951,7 +1012,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     cudaSetDevice(u->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int W = (int)in->width, H = (int)in->height;
-    forward(u, in, target_rgba8, out_rgba8, s);
+    if (!forward(u, in, target_rgba8, out_rgba8, s)) return RZ_ERROR;
     WgradArgs w{};
     w.W = W;
     w.H = H;
@@ -967,7 +1028,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     d.wimg = u->d_img + dgrad_img_off(3);
     d.mask_src = u->d_act[2];
     d.out = u->d_dyA;
-    launch_conv<16, 32, kEpiMask>(u, d, s);
+    if (!launch_conv<16, 32, kEpiMask>(u, d, s)) return RZ_ERROR;
     // layer 2
     w.x = u->d_act[1];
     w.dy = u->d_dyA;
@@ -978,7 +1039,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     d.wimg = u->d_img + dgrad_img_off(2);
     d.mask_src = u->d_act[1];
     d.out = u->d_dyB;
-    launch_conv<32, 32, kEpiMask>(u, d, s);
+    if (!launch_conv<32, 32, kEpiMask>(u, d, s)) return RZ_ERROR;
     // layer 1
     w.x = u->d_act[0];
     w.dy = u->d_dyB;
@@ -989,7 +1050,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     d.wimg = u->d_img + dgrad_img_off(1);
     d.mask_src = u->d_act[0];
     d.out = u->d_dyA;
-    launch_conv<32, 32, kEpiMask>(u, d, s);
+    if (!launch_conv<32, 32, kEpiMask>(u, d, s)) return RZ_ERROR;
     // layer 0
     w.x = u->d_feat;
     w.dy = u->d_dyA;
