@@ -11,7 +11,9 @@ uploaded inside the frame, everything else is resident); L2 is flushed by a
 256 MiB write between frames, outside the timed events. `e2e` is frames/s
 through the C ABI with host buffers: per frame, the scene constants and all
 object transforms go host->device from pinned memory and the RGBA8 frame comes
-back device->host into pinned memory, wall-clock timed.
+back device->host into pinned memory, wall-clock timed, with two frames in
+flight (a host buffer is reused once the frame that last filled it has landed;
+the reference's Vulkan renderer keeps up to three, src/Engine/Graphics.cpp:177).
 
 --impl reference times the CPU restatement of the reference's path (the oracle,
 oracle/rz_oracle.cpp; Rosy itself needs Vulkan on Windows and cannot run here)
@@ -318,8 +320,10 @@ def run_rz(args):
     g.sync()
     stats = g.stats()
 
-    # --- e2e through the C ABI with host buffers ---
-    color_host = torch.empty((s.height, s.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    # --- e2e through the C ABI with host buffers, two frames in flight ---
+    ring = 2
+    color_hosts = [torch.empty((s.height, s.width, 4), dtype=torch.uint8, pin_memory=True).numpy()
+                   for _ in range(ring)]
     objects_host = torch.empty(s.objects.shape, dtype=torch.float32, pin_memory=True).numpy()
     objects_host[:] = s.objects
     scene_host = [torch.empty(408, dtype=torch.uint8, pin_memory=True).numpy() for _ in cams]
@@ -328,13 +332,19 @@ def run_rz(args):
     n_e2e = min(args.steps, 200)
     g.sync()
     barrier(ws)
+    done = [None] * ring
     t0 = time.perf_counter()
     for i in range(n_e2e):
+        k = i % ring
+        if done[k] is not None:
+            done[k].synchronize()  # the frame that last used this host buffer has landed
         g.update(scene_host[i % len(cams)].view(cams[0].dtype))
         g.update_objects(0, objects_host)
         g.render()
-        g.read_frame(color_host)
-        g.sync()
+        g.read_frame(color_hosts[k])
+        done[k] = torch.cuda.Event()
+        done[k].record(stream)
+    g.sync()
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
     e2e_value = ws * n_e2e / e2e_s
 
@@ -383,7 +393,7 @@ def run_rz(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": workload_config(args.config, s),
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": 408 + int(s.objects.nbytes),
-                    "d2h_bytes_per_step": int(s.width * s.height * 4), "steps": n_e2e},
+                    "d2h_bytes_per_step": int(s.width * s.height * 4), "steps": n_e2e, "frames_in_flight": ring},
             "gpu_launches": int(stats.kernel_launches) * args.steps,
             "raster_work": {"shadow_records": int(stats.shadow_setup_records), "shadow_stamps": int(stats.shadow_stamps),
                             "camera_records": int(stats.camera_setup_records), "camera_stamps": int(stats.camera_stamps)},
