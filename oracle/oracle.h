@@ -41,13 +41,13 @@ typedef struct oracle_scene {
     uint32_t width;
     uint32_t height;
     uint32_t shadow_size;
-    uint32_t reserved;
+    uint32_t samples;               /* camera-pass samples per pixel: 0 or 1, or 4 (standard 4x positions) */
 } oracle_scene;
 
 typedef struct oracle_out {
     uint8_t* color;      /* width*height*4, RGBA8 sRGB (may be NULL) */
-    float* depth;        /* width*height (may be NULL) */
-    uint32_t* ids;       /* width*height, triangle id + 1, 0 = background (may be NULL) */
+    float* depth;        /* samples * width*height, one plane per sample (may be NULL) */
+    uint32_t* ids;       /* samples * width*height, triangle id + 1, 0 = background (may be NULL) */
     float* shadow;       /* cascades * shadow_size^2: one map per shadow cascade (may be NULL) */
     double* color_f64;   /* width*height*4, FP64 shading, sRGB-encoded in [0,1] before 8-bit rounding (may be NULL) */
     uint64_t* texel_bytes; /* if non-NULL: compulsory texture + shadow-map bytes the shading touched */

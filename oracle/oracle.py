@@ -50,7 +50,7 @@ class OracleScene(C.Structure):
         ("textures", C.c_void_p), ("texture_count", C.c_uint32), ("sampler_count", C.c_uint32),
         ("samplers", C.c_void_p), ("scene", C.c_void_p), ("draw_config", C.c_void_p),
         ("width", C.c_uint32), ("height", C.c_uint32), ("shadow_size", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("samples", C.c_uint32),
     ]
 
 
@@ -95,6 +95,7 @@ def _scene_struct(m: Marshalled) -> OracleScene:
     o.scene = ptr(m.scene_rec)
     o.draw_config = ptr(m.draw_config)
     o.width, o.height, o.shadow_size = s.width, s.height, s.shadow_size
+    o.samples = getattr(s, "samples", 1)
     return o
 
 
@@ -111,15 +112,21 @@ def _shadow_array(s) -> np.ndarray:
     return np.zeros(shape, np.float32)
 
 
+def _sample_shape(s) -> tuple:
+    """(H, W) with one sample per pixel, (4, H, W) with 4x multisampling."""
+    return (s.height, s.width) if getattr(s, "samples", 1) != 4 else (4, s.height, s.width)
+
+
 def render(s, threads: int = 0, fp64: bool = False, texel_bytes: bool = False) -> dict:
-    """Full frame: colour (H,W,4) u8, depth (H,W) f32, ids (H,W) u32, shadow (S,S) f32,
-    optionally color_f64 (H,W,4) and the compulsory texel bytes of the shading."""
+    """Full frame: colour (H,W,4) u8 (resolved), depth and ids per sample ((H,W), or (4,H,W)
+    with 4x multisampling), shadow (S,S) f32 (or (cascades,S,S)), optionally color_f64
+    (H,W,4) and the compulsory texel bytes of the shading."""
     m = Marshalled(s)
     o = _scene_struct(m)
     out = {
         "color": np.zeros((s.height, s.width, 4), np.uint8),
-        "depth": np.zeros((s.height, s.width), np.float32),
-        "ids": np.zeros((s.height, s.width), np.uint32),
+        "depth": np.zeros(_sample_shape(s), np.float32),
+        "ids": np.zeros(_sample_shape(s), np.uint32),
         "shadow": _shadow_array(s),
     }
     oo = OracleOut(ptr(out["color"]), ptr(out["depth"]), ptr(out["ids"]), ptr(out["shadow"]), None, None)
@@ -142,8 +149,8 @@ def raster(s, threads: int = 0) -> dict:
     m = Marshalled(s)
     o = _scene_struct(m)
     out = {
-        "depth": np.zeros((s.height, s.width), np.float32),
-        "ids": np.zeros((s.height, s.width), np.uint32),
+        "depth": np.zeros(_sample_shape(s), np.float32),
+        "ids": np.zeros(_sample_shape(s), np.uint32),
         "shadow": _shadow_array(s),
     }
     oo = OracleOut(None, ptr(out["depth"]), ptr(out["ids"]), ptr(out["shadow"]), None, None)

@@ -158,6 +158,7 @@ int64_t area2(const SV& a, const SV& b, const SV& c) {
 
 struct RasterState {
     int width = 0, height = 0;
+    int32_t ox = 128, oy = 128;  // coverage sample within the pixel, 1/256 pixel (centre by default)
     int row_begin = 0, row_end = 0;  // band of rows this thread owns
     bool cull_front = false;
     bool ccw_front = false;
@@ -197,8 +198,9 @@ void raster_tri(const SV& v0, const SV& v1, const SV& v2, int64_t S, const Raste
     }
     const int32_t minX = std::min({v0.X, v1.X, v2.X}), maxX = std::max({v0.X, v1.X, v2.X});
     const int32_t minY = std::min({v0.Y, v1.Y, v2.Y}), maxY = std::max({v0.Y, v1.Y, v2.Y});
-    int px0 = (minX + 127) >> 8, px1 = (maxX - 128) >> 8;
-    int py0 = (minY + 127) >> 8, py1 = (maxY - 128) >> 8;
+    // pixels whose coverage sample (256 p + o) lies within the triangle's extent
+    int px0 = (minX - rs.ox + 255) >> 8, px1 = (maxX - rs.ox) >> 8;
+    int py0 = (minY - rs.oy + 255) >> 8, py1 = (maxY - rs.oy) >> 8;
     px0 = std::max(px0, 0);
     px1 = std::min(px1, rs.width - 1);
     py0 = std::max(py0, rs.row_begin);
@@ -217,9 +219,9 @@ void raster_tri(const SV& v0, const SV& v1, const SV& v2, int64_t S, const Raste
         tl[i] = dys[i] < 0 || (dys[i] == 0 && dxs[i] > 0);
     }
     for (int py = py0; py <= py1; ++py) {
-        const int32_t PY = py * 256 + 128;
+        const int32_t PY = py * 256 + rs.oy;
         for (int px = px0; px <= px1; ++px) {
-            const int32_t PX = px * 256 + 128;
+            const int32_t PX = px * 256 + rs.ox;
             bool in = true;
             for (int i = 0; i < 3 && in; ++i) {
                 const int64_t E = (int64_t)dxs[i] * (int64_t)(PY - ey[i]) - (int64_t)dys[i] * (int64_t)(PX - ex[i]);
@@ -363,6 +365,12 @@ void parallel_rows(int rows, int threads, F&& f) {
 // Shadow pass: src/Engine/Graphics.cpp:5195-5292 with shadow.slang:6-19.
 void shadow_cascade(const Ctx& c, const float* P, float* shadow, int threads);
 
+// Camera-pass samples per pixel (1, or 4 at the standard positions (0.375, 0.125),
+// (0.875, 0.375), (0.125, 0.625), (0.625, 0.875) of Vulkan's standardSampleLocations).
+int samples_of(const oracle_scene* s) { return s->samples == 4 ? 4 : 1; }
+constexpr int32_t kSampleX[4] = {96, 224, 32, 160};
+constexpr int32_t kSampleY[4] = {32, 96, 160, 224};
+
 // Shadow cascades: draw_config.shadow_cascades clamped to 1..4 (0 = 1, the reference's single map).
 int cascades_of(const oracle_scene* s) {
     const uint32_t n = s->draw_config->shadow_cascades;
@@ -420,7 +428,17 @@ void shadow_cascade(const Ctx& c, const float* P, float* shadow, int threads) {
 }
 
 // Camera pass depth/visibility: opaque list of src/Engine/Graphics.cpp:5631-5653.
+void camera_sample(const Ctx& c, float* depth, uint32_t* ids, int threads, int32_t ox, int32_t oy);
+
+// Depth and triangle id per coverage sample: `samples` planes of W x H.
 void camera_pass(const Ctx& c, float* depth, uint32_t* ids, int threads) {
+    const int n = samples_of(c.s);
+    const size_t plane = (size_t)c.s->width * c.s->height;
+    for (int k = 0; k < n; ++k)
+        camera_sample(c, depth + k * plane, ids + k * plane, threads, n > 1 ? kSampleX[k] : 128, n > 1 ? kSampleY[k] : 128);
+}
+
+void camera_sample(const Ctx& c, float* depth, uint32_t* ids, int threads, int32_t ox, int32_t oy) {
     const oracle_scene* s = c.s;
     const int W = (int)s->width, H = (int)s->height;
     std::fill(depth, depth + (size_t)W * H, 0.0f);
@@ -431,6 +449,8 @@ void camera_pass(const Ctx& c, float* depth, uint32_t* ids, int threads) {
         RasterState rs;
         rs.width = W;
         rs.height = H;
+        rs.ox = ox;
+        rs.oy = oy;
         rs.row_begin = r0;
         rs.row_end = r1;
         rs.cull_front = s->draw_config->cull_enabled != 0;
@@ -1113,66 +1133,90 @@ template <class T>
 void shading_pass(const Ctx& c, const float* shadow, const float* depth, const uint32_t* ids, float* color16,
                   double* out64, int threads, TexMarks* marks, std::vector<uint8_t>* shadow_marks) {
     const int W = (int)c.s->width, H = (int)c.s->height;
+    const int n = samples_of(c.s);
+    const size_t plane = (size_t)W * H;
     const float clear[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // src/Engine/Graphics.cpp:5416-5419
     Sampling<T> smp{&c, marks};
+    // Opaque list. With multisampling each distinct triangle of a pixel's samples
+    // is shaded once at the pixel centre and its colour goes to the samples it covers.
     parallel_rows(H, threads, [&](int r0, int r1) {
         for (int py = r0; py < r1; ++py) {
             for (int px = 0; px < W; ++px) {
                 const size_t p = (size_t)py * W + px;
-                T col[4] = {(T)clear[0], (T)clear[1], (T)clear[2], (T)clear[3]};
-                if (ids[p] != 0) {
-                    const uint32_t tri = ids[p] - 1;
-                    const Draw& d = find_draw(c.opaque, tri);
-                    T o[4];
-                    if (shade<T>(c, d, tri - d.tri_base, px, py, shadow, smp, shadow_marks, o))
-                        for (int k = 0; k < 4; ++k) col[k] = o[k];
+                T cs[4][4];
+                for (int k = 0; k < n; ++k) {
+                    const uint32_t id = ids[k * plane + p];
+                    int same = -1;
+                    for (int j = 0; j < k && same < 0; ++j)
+                        if (ids[j * plane + p] == id) same = j;
+                    if (same >= 0) {
+                        for (int i = 0; i < 4; ++i) cs[k][i] = cs[same][i];
+                        continue;
+                    }
+                    T col[4] = {(T)clear[0], (T)clear[1], (T)clear[2], (T)clear[3]};
+                    if (id != 0) {
+                        const uint32_t tri = id - 1;
+                        const Draw& d = find_draw(c.opaque, tri);
+                        T o[4];
+                        if (shade<T>(c, d, tri - d.tri_base, px, py, shadow, smp, shadow_marks, o))
+                            for (int i = 0; i < 4; ++i) col[i] = o[i];
+                    }
+                    for (int i = 0; i < 4; ++i) cs[k][i] = col[i];
                 }
-                for (int k = 0; k < 4; ++k) {
-                    if constexpr (sizeof(T) == 4) color16[4 * p + k] = to_half_and_back((float)col[k]);
-                    else out64[4 * p + k] = (double)col[k];
-                }
+                for (int k = 0; k < n; ++k)
+                    for (int i = 0; i < 4; ++i) {
+                        if constexpr (sizeof(T) == 4) color16[4 * (k * plane + p) + i] = to_half_and_back((float)cs[k][i]);
+                        else out64[4 * (k * plane + p) + i] = (double)cs[k][i];
+                    }
             }
         }
     });
-    // Blended list, in submission order: blend on, depth write off, cull none (5654-5691).
+    // Blended list, in submission order: blend on, depth write off, cull none (5654-5691),
+    // per coverage sample against that sample's opaque depth.
     if (c.blended.empty()) return;
     std::vector<float> mvps(c.blended.size() * 16);
     for (size_t i = 0; i < c.blended.size(); ++i) draw_mvp(c, c.blended[i], c.s->scene->view_projection, &mvps[16 * i]);
-    parallel_rows(H, threads, [&](int r0, int r1) {
-        RasterState rs;
-        rs.width = W;
-        rs.height = H;
-        rs.row_begin = r0;
-        rs.row_end = r1;
-        rs.cull_front = false;
-        rs.ccw_front = c.s->draw_config->reverse_winding_order_enabled != 0;
-        for (size_t di = 0; di < c.blended.size(); ++di) {
-            const Draw& d = c.blended[di];
-            for (uint32_t t = 0; t < d.index_count / 3; ++t) {
-                CV cv[3];
-                uint32_t vi[3];
-                tri_clip(c, d, &mvps[16 * di], t, cv, vi);
-                raster_primitive(cv, rs, [&](int px, int py, float z) {
-                    const size_t p = (size_t)py * W + px;
-                    if (!(z >= depth[p])) return;
-                    T s[4];
-                    if (!shade<T>(c, d, t, px, py, shadow, smp, shadow_marks, s)) return;
-                    // SRC_ALPHA / ONE_MINUS_SRC_ALPHA on colour, ONE / ZERO on alpha
-                    const T a = s[3];
-                    if constexpr (sizeof(T) == 4) {
-                        for (int k = 0; k < 3; ++k) {
-                            const float dst = color16[4 * p + k];
-                            color16[4 * p + k] = to_half_and_back((float)(s[k] * a + (T)dst * (T(1) - a)));
+    for (int k = 0; k < n; ++k) {
+        const float* dk = depth + k * plane;
+        parallel_rows(H, threads, [&](int r0, int r1) {
+            RasterState rs;
+            rs.width = W;
+            rs.height = H;
+            rs.row_begin = r0;
+            rs.row_end = r1;
+            rs.ox = n > 1 ? kSampleX[k] : 128;
+            rs.oy = n > 1 ? kSampleY[k] : 128;
+            rs.cull_front = false;
+            rs.ccw_front = c.s->draw_config->reverse_winding_order_enabled != 0;
+            for (size_t di = 0; di < c.blended.size(); ++di) {
+                const Draw& d = c.blended[di];
+                for (uint32_t t = 0; t < d.index_count / 3; ++t) {
+                    CV cv[3];
+                    uint32_t vi[3];
+                    tri_clip(c, d, &mvps[16 * di], t, cv, vi);
+                    raster_primitive(cv, rs, [&](int px, int py, float z) {
+                        const size_t p = (size_t)py * W + px;
+                        if (!(z >= dk[p])) return;
+                        T s[4];
+                        if (!shade<T>(c, d, t, px, py, shadow, smp, shadow_marks, s)) return;
+                        // SRC_ALPHA / ONE_MINUS_SRC_ALPHA on colour, ONE / ZERO on alpha
+                        const T a = s[3];
+                        const size_t q = 4 * (k * plane + p);
+                        if constexpr (sizeof(T) == 4) {
+                            for (int i = 0; i < 3; ++i) {
+                                const float dst = color16[q + i];
+                                color16[q + i] = to_half_and_back((float)(s[i] * a + (T)dst * (T(1) - a)));
+                            }
+                            color16[q + 3] = to_half_and_back((float)a);
+                        } else {
+                            for (int i = 0; i < 3; ++i) out64[q + i] = s[i] * a + out64[q + i] * (T(1) - a);
+                            out64[q + 3] = a;
                         }
-                        color16[4 * p + 3] = to_half_and_back((float)a);
-                    } else {
-                        for (int k = 0; k < 3; ++k) out64[4 * p + k] = s[k] * a + out64[4 * p + k] * (T(1) - a);
-                        out64[4 * p + 3] = a;
-                    }
-                });
+                    });
+                }
             }
-        }
-    });
+        });
+    }
 }
 
 int threads_or_default(int threads) {
@@ -1197,12 +1241,12 @@ extern "C" int oracle_raster(const oracle_scene* s, oracle_out* out, int threads
     }
     float* depth = out->depth;
     if (!depth) {
-        depth_local.resize((size_t)s->width * s->height);
+        depth_local.resize((size_t)samples_of(s) * s->width * s->height);
         depth = depth_local.data();
     }
     uint32_t* ids = out->ids;
     if (!ids) {
-        ids_local.resize((size_t)s->width * s->height);
+        ids_local.resize((size_t)samples_of(s) * s->width * s->height);
         ids = ids_local.data();
     }
     shadow_pass(c, shadow, threads);
@@ -1216,8 +1260,9 @@ extern "C" int oracle_render(const oracle_scene* s, oracle_out* out, int threads
     Ctx c;
     build_ctx(s, c);
     const size_t np = (size_t)s->width * s->height;
-    std::vector<float> shadow((size_t)cascades_of(s) * s->shadow_size * s->shadow_size), depth(np);
-    std::vector<uint32_t> ids(np);
+    const int ns = samples_of(s);
+    std::vector<float> shadow((size_t)cascades_of(s) * s->shadow_size * s->shadow_size), depth(np * ns);
+    std::vector<uint32_t> ids(np * ns);
     shadow_pass(c, shadow.data(), threads);
     camera_pass(c, depth.data(), ids.data(), threads);
     TexMarks marks;
@@ -1236,16 +1281,29 @@ extern "C" int oracle_render(const oracle_scene* s, oracle_out* out, int threads
         mp = &marks;
         smp = &shadow_marks;
     }
-    std::vector<float> color16(np * 4);
+    std::vector<float> color16(np * 4 * ns);
     shading_pass<float>(c, shadow.data(), depth.data(), ids.data(), color16.data(), nullptr, threads, mp, smp);
+    // AVERAGE resolve of the samples into the RGBA16F draw image ((s0 + s1) + (s2 + s3)) / 4
+    // (src/Engine/Graphics.cpp:5571-5572), then the blit to sRGB 8-bit
+    auto resolved = [&](size_t p, int k) -> float {
+        if (ns == 1) return color16[4 * p + k];
+        const float* q = color16.data() + 4 * p + k;
+        return to_half_and_back(((q[0] + q[4 * np]) + (q[8 * np] + q[12 * np])) * 0.25f);
+    };
     if (out->color) {
         for (size_t p = 0; p < np; ++p) {
-            for (int k = 0; k < 3; ++k) out->color[4 * p + k] = encode_srgb8(color16[4 * p + k]);
-            out->color[4 * p + 3] = encode_unorm8(color16[4 * p + 3]);
+            for (int k = 0; k < 3; ++k) out->color[4 * p + k] = encode_srgb8(resolved(p, k));
+            out->color[4 * p + 3] = encode_unorm8(resolved(p, 3));
         }
     }
     if (out->color_f64) {
-        shading_pass<double>(c, shadow.data(), depth.data(), ids.data(), nullptr, out->color_f64, threads, nullptr, nullptr);
+        std::vector<double> c64(np * 4 * ns);
+        shading_pass<double>(c, shadow.data(), depth.data(), ids.data(), nullptr, c64.data(), threads, nullptr, nullptr);
+        for (size_t p = 0; p < np; ++p)
+            for (int k = 0; k < 4; ++k) {
+                const double* q = c64.data() + 4 * p + k;
+                out->color_f64[4 * p + k] = ns == 1 ? q[0] : ((q[0] + q[4 * np]) + (q[8 * np] + q[12 * np])) * 0.25;
+            }
         for (size_t p = 0; p < np; ++p) {
             for (int k = 0; k < 4; ++k) {
                 double v = out->color_f64[4 * p + k];

@@ -139,6 +139,7 @@ struct rz_ctx {
     uint32_t* d_shadow = nullptr;
     uint2* d_color16 = nullptr;
     bool gbuffer = false;             // shading also writes albedo + normal (rz_set_gbuffer)
+    uint32_t samples = 1;             // camera-pass samples per pixel (1 or 4)
     uint32_t* d_gb_albedo = nullptr;
     uint32_t* d_gb_normal = nullptr;
     size_t gb_capacity = 0;
@@ -558,7 +559,7 @@ int build_layout(rz_ctx* c) {
         dfree(c->d_color);
         dfree(c->d_depth);
         c->pix_capacity = 0;
-        RZ_CUDA(c, dalloc(&c->d_vis, pix), "visibility buffers");
+        RZ_CUDA(c, dalloc(&c->d_vis, pix * c->samples), "visibility buffers");
         RZ_CUDA(c, dalloc(&c->d_color, pix), "colour buffers");
         RZ_CUDA(c, dalloc(&c->d_depth, pix), "depth buffers");
         RZ_CUDA(c, cudaMemset(c->d_color, 0, pix * 4), "clear colour");
@@ -574,7 +575,7 @@ int build_layout(rz_ctx* c) {
     if (!blended.empty() && pix > c->color16_capacity) {
         dfree(c->d_color16);
         c->color16_capacity = 0;
-        RZ_CUDA(c, dalloc(&c->d_color16, pix), "RGBA16F draw images");
+        RZ_CUDA(c, dalloc(&c->d_color16, pix * c->samples), "RGBA16F draw images");
         c->color16_capacity = pix;
     }
     if (c->gbuffer && pix > c->gb_capacity) {
@@ -601,11 +602,12 @@ int build_layout(rz_ctx* c) {
         r.pcf_mode = v.dc.pcf_mode;
         r.cascades = (int)cascades_of(v);
         r.shade_block_base = block_base[vi];
-        r.vis = c->d_vis + pix_off[vi];
+        r.vis = c->d_vis + pix_off[vi] * c->samples;  // `samples` planes of width*height
         r.color = c->d_color + pix_off[vi];
         r.depth = c->d_depth + pix_off[vi];
         r.shadow = c->d_shadow + shadow_off[vi];
-        r.color16 = c->d_color16 ? c->d_color16 + pix_off[vi] : nullptr;
+        r.color16 = c->d_color16 ? c->d_color16 + pix_off[vi] * c->samples : nullptr;
+        r.samples = (int)c->samples;
         r.scene = c->d_scene_data + vi;
         r.gb_albedo = c->gbuffer ? c->d_gb_albedo + pix_off[vi] : nullptr;
         r.gb_normal = c->gbuffer ? c->d_gb_normal + pix_off[vi] : nullptr;
@@ -663,6 +665,9 @@ PassParams pass_params(rz_ctx* c, int kind) {
     p.error_flags = c->d_error;
     p.chunk_stamps = c->chunk_stamps;
     p.small_extent = c->small_extent;
+    p.sample_x = 128;  // pixel centre
+    p.sample_y = 128;
+    p.sample_plane = 0;
     PassBuffers* pb;
     if (kind == 2) {  // blended list: cull none, records kept in submission order
         p.draws = c->d_blended_draws;
@@ -707,6 +712,7 @@ ShadeParams shade_params(rz_ctx* c) {
     ShadeParams sh{};
     sh.views = c->d_views;
     sh.view_count = (uint32_t)c->views.size();
+    sh.samples = c->samples;
     sh.shade_blocks = c->shade_blocks;
     sh.draws = c->d_opaque_draws;
     sh.draw_count = c->opaque_draw_count;
@@ -759,10 +765,25 @@ void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
 
 // Camera passes of all views (5566-5653): visibility cleared to 0, opaque list,
 // then the vertex stage of the shading; the blended list's setup.
+// The camera raster: one launch per coverage sample, each into its plane of the
+// visibility buffer (the setup records are shared).
+void launch_camera_raster(rz_ctx* c, PassParams cp, cudaStream_t s) {
+    if (c->samples <= 1) {
+        launch_raster(cp, c->sm_count, s);
+        return;
+    }
+    for (int k = 0; k < kMsaaSamples; ++k) {
+        cp.sample_x = kMsaaX[k];
+        cp.sample_y = kMsaaY[k];
+        cp.sample_plane = (uint32_t)k;
+        launch_raster(cp, c->sm_count, s);
+    }
+}
+
 void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& sh) {
     ClearList cl{};
     cl.ptr[0] = c->d_vis;
-    cl.bytes[0] = c->pix_total * 8;
+    cl.bytes[0] = c->pix_total * 8 * c->samples;
     cl.ptr[1] = c->d_headers + 1;
     cl.bytes[1] = 2 * sizeof(PassHeader);  // camera and blended headers
     cl.count = 2;
@@ -783,7 +804,7 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
         const PassParams cp = pass_params(c, 1);
         launch_setup(cp, s);
         if (stamps) stamp(c, 5);
-        launch_raster(cp, c->sm_count, s);
+        launch_camera_raster(c, cp, s);
     } else if (stamps) {
         stamp(c, 5);
     }
@@ -809,8 +830,8 @@ void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
         ClearList cl{};
         cl.ptr[0] = c->d_shadow + rg.shadow_off;
         cl.bytes[0] = rg.shadow * 4;
-        cl.ptr[1] = c->d_vis + rg.pix_off;
-        cl.bytes[1] = rg.pix * 8;
+        cl.ptr[1] = c->d_vis + rg.pix_off * c->samples;
+        cl.bytes[1] = rg.pix * 8 * c->samples;
         cl.ptr[2] = c->d_headers;
         cl.bytes[2] = 2 * sizeof(PassHeader);
         cl.count = 3;
@@ -839,7 +860,7 @@ void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
             cp.tri_offset = rg.opaque_tri_base;
             cp.tri_total = rg.opaque_tris;
             launch_setup(cp, s);
-            launch_raster(cp, c->sm_count, s);
+            launch_camera_raster(c, cp, s);
         }
         ShadeParams v = sh;
         v.varying_count = rg.varying_end;
@@ -972,9 +993,10 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
     *out = nullptr;
     if (cfg->width == 0 || cfg->height == 0 || cfg->width > 16384 || cfg->height > 16384) return RZ_INVALID_ARGUMENT;
     if (cfg->shadow_map_size == 0 || cfg->shadow_map_size > 16384) return RZ_INVALID_ARGUMENT;
-    if (cfg->samples != 1) return RZ_INVALID_ARGUMENT;
+    if (cfg->samples != 1 && cfg->samples != (uint32_t)kMsaaSamples) return RZ_INVALID_ARGUMENT;
     rz_ctx* c = new rz_ctx();
     c->device = cfg->device;
+    c->samples = cfg->samples;
     c->queue_chunks = cfg->queue_chunks;
     auto bail = [&](int code) {
         rz_destroy(c);
@@ -1323,6 +1345,7 @@ int rz_get_frame(rz_ctx* c, rz_frame_out* out) { return rz_get_view_frame(c, 0, 
 
 int rz_set_gbuffer(rz_ctx* c, uint32_t enable) {
     if (!c) return RZ_INVALID_ARGUMENT;
+    if (enable && c->samples > 1) return fail(c, RZ_INVALID_STATE, "the G-buffer needs one sample per pixel");
     if (c->frame_pending) return fail(c, RZ_INVALID_STATE, "a frame is in flight; call rz_sync first");
     if ((enable != 0) != c->gbuffer) {
         c->gbuffer = enable != 0;
@@ -1374,7 +1397,7 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->error_flags;
     // clears (2) + shadow prep/setup/raster + camera prep/setup/raster + vertex + shade (+ blended: prep, setup, vertex, blend)
-    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + 1u + (c->opaque_tris ? 2u : 0u) +
+    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + 1u + (c->opaque_tris ? 1u + c->samples : 0u) +
                            (c->varying_count ? 1u : 0u) + 1u + (c->blended_tris ? 4u : 0u);
     return RZ_OK;
 }

@@ -42,6 +42,7 @@ struct ViewRec {
     uint2* color16;               // width*height RGBA16F (only with blended surfaces)
     const rz_scene_data* scene;
     int cascades;                 // shadow cascades (1..kMaxCascades), each shadow_w*shadow_h, consecutive
+    int samples;                  // camera-pass samples per pixel (1 or 4): vis holds `samples` planes of width*height
     uint32_t* gb_albedo;          // width*height RGBA8 sRGB albedo, or null (G-buffer off)
     uint32_t* gb_normal;          // width*height world normal, octahedral 2 x f16, or null
 };
@@ -94,6 +95,14 @@ static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
 constexpr uint32_t kViewBits = 24;
 constexpr uint32_t kViewMask = (1u << kViewBits) - 1u;
 constexpr int kMaxCascades = 4;
+
+// Standard sample positions of 4x multisampling (Vulkan standardSampleLocations),
+// in 1/256 pixel: (0.375, 0.125), (0.875, 0.375), (0.125, 0.625), (0.625, 0.875).
+constexpr int kMsaaSamples = 4;
+constexpr int32_t kMsaaX[kMsaaSamples] = {96, 224, 32, 160};
+constexpr int32_t kMsaaY[kMsaaSamples] = {32, 96, 160, 224};
+__host__ __device__ constexpr int32_t msaa_x(int k) { return k == 0 ? 96 : k == 1 ? 224 : k == 2 ? 32 : 160; }
+__host__ __device__ constexpr int32_t msaa_y(int k) { return k == 0 ? 32 : k == 1 ? 96 : k == 2 ? 160 : 224; }
 
 constexpr int kStampW = 8;
 constexpr int kStampH = 4;
@@ -152,6 +161,10 @@ struct PassParams {
     uint32_t chunk_capacity;
     PassHeader* header;
     uint32_t* error_flags;
+    // coverage sample of this raster launch, in 1/256 pixel: the pixel centre
+    // (128, 128) or one of the standard 4x positions; camera-pass target plane
+    int32_t sample_x, sample_y;
+    uint32_t sample_plane;
 };
 
 struct ShadeParams {
@@ -174,6 +187,7 @@ struct ShadeParams {
     uint32_t sampler_count;
     const float* srgb_table;      // 256 entries
     int blended;                  // 1: k_shade stores the RGBA16F draw image (color16) for k_blend
+    uint32_t samples;             // camera-pass samples per pixel of the views (1 or 4)
 };
 
 // The blended list (src/Engine/Graphics.cpp:5654-5691) over the opaque result.

@@ -183,6 +183,7 @@ __device__ __forceinline__ uint32_t record_stamps(const TriRecord& r) {
 // Viewport and fixed-function state of the view a triangle belongs to.
 struct ViewState {
     int width, height;
+    int bb_lo, bb_hi;  // largest and smallest sample offset (1/256 pixel) of the pass: box of pixels any sample may hit
     int cull_front, ccw_front;
     int bias_enabled;
     float bias_constant, bias_clamp, bias_slope;
@@ -196,8 +197,9 @@ __device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV&
                                            bool ordered, uint32_t small_extent, uint32_t id, TriRecord& r) {
     const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
     const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
-    const int px0 = max((minX + 127) >> 8, 0), px1 = min((maxX - 128) >> 8, P.width - 1);
-    const int py0 = max((minY + 127) >> 8, 0), py1 = min((maxY - 128) >> 8, P.height - 1);
+    // pixels p with minX <= 256 p + o <= maxX for some sample offset o in [bb_hi, bb_lo]
+    const int px0 = max((minX - P.bb_lo + 255) >> 8, 0), px1 = min((maxX - P.bb_hi) >> 8, P.width - 1);
+    const int py0 = max((minY - P.bb_lo + 255) >> 8, 0), py1 = min((maxY - P.bb_hi) >> 8, P.height - 1);
     if (px0 > px1 || py0 > py1) return 0;
     const float fX1 = (float)(v1.X - v0.X), fY1 = (float)(v1.Y - v0.Y);
     const float fX2 = (float)(v2.X - v0.X), fY2 = (float)(v2.Y - v0.Y);
@@ -255,6 +257,9 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
     V.view = dr.view | (dr.cascade << kViewBits);
     V.width = P.write_id ? VR.width : VR.shadow_w;
     V.height = P.write_id ? VR.height : VR.shadow_h;
+    const bool msaa = P.write_id && VR.samples > 1;
+    V.bb_lo = msaa ? 224 : 128;
+    V.bb_hi = msaa ? 32 : 128;
     V.cull_front = P.ordered ? 0 : VR.cull_front;
     V.ccw_front = VR.ccw_front;
     V.bias_enabled = P.write_id ? 0 : VR.bias_enabled;
@@ -568,7 +573,7 @@ struct Target {
 template <bool kWriteId>
 __device__ __forceinline__ Target view_target(const PassParams& P, uint32_t view) {
     const ViewRec& V = P.views[view & kViewMask];
-    if (kWriteId) return Target{V.vis, V.width};
+    if (kWriteId) return Target{V.vis + (size_t)P.sample_plane * (size_t)V.width * (size_t)V.height, V.width};
     return Target{V.shadow + (size_t)(view >> kViewBits) * (size_t)V.shadow_w * (size_t)V.shadow_h, V.shadow_w};
 }
 
@@ -610,9 +615,9 @@ __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecor
         c[i] = dy[i] * (X[a] - X[0]) - dx[i] * (Y[a] - Y[0]) - (tl ? 0 : 1);
     }
     for (int py = py0; py <= py1; ++py) {
-        const int32_t ry = py * 256 + 128 - Y[0];
+        const int32_t ry = py * 256 + P.sample_y - Y[0];
         for (int px = px0; px <= px1; ++px) {
-            const int32_t rx = px * 256 + 128 - X[0];
+            const int32_t rx = px * 256 + P.sample_x - X[0];
             const int32_t e0 = c[0] + dx[0] * ry - dy[0] * rx;
             const int32_t e1 = c[1] + dx[1] * ry - dy[1] * rx;
             const int32_t e2 = c[2] + dx[2] * ry - dy[2] * rx;
@@ -674,8 +679,8 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L)
         L.dy[i] = L.Y[b] - L.Y[a];
         L.tl_bias[i] = (L.dy[i] < 0 || (L.dy[i] == 0 && L.dx[i] > 0)) ? 0u : 1u;
     }
-    const int32_t lo_x = L.px0 * 256 + 128 - L.X0, hi_x = L.px1 * 256 + 128 - L.X0 + kStampW * 256;
-    const int32_t lo_y = L.py0 * 256 + 128 - L.Y0, hi_y = L.py1 * 256 + 128 - L.Y0 + kStampH * 256;
+    const int32_t lo_x = L.px0 * 256 - L.X0, hi_x = L.px1 * 256 + 256 - L.X0 + kStampW * 256;
+    const int32_t lo_y = L.py0 * 256 - L.Y0, hi_y = L.py1 * 256 + 256 - L.Y0 + kStampH * 256;
     const int32_t lim = 1 << 23;
     L.near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
     const int32_t ex = max(L.X[0], max(L.X[1], L.X[2])) - min(L.X[0], min(L.X[1], L.X[2]));
@@ -707,9 +712,9 @@ __device__ __forceinline__ void generic_edges(const LargeRecord& L, GenericEdges
 // Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
 template <bool kWriteId>
 __device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord& L, const GenericEdges& G, uint32_t sx,
-                                             uint32_t sy, int lx, int ly) {
+                                             uint32_t sy, int lx, int ly, int32_t ox, int32_t oy) {
     const int sx0 = L.px0 + (int)sx * kStampW, sy0 = L.py0 + (int)sy * kStampH;
-    const int32_t PXo = sx0 * 256 + 128, PYo = sy0 * 256 + 128;
+    const int32_t PXo = sx0 * 256 + ox, PYo = sy0 * 256 + oy;
     int64_t eo[3];
     bool reject = false, accept = true;
 #pragma unroll
@@ -749,8 +754,8 @@ __device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord&
         fx = (float)(PXo - L.X0) + (float)(lx * 256);
         fy = (float)(PYo - L.Y0) + (float)(ly * 256);
     } else {
-        fx = (float)(px * 256 + 128 - L.X0);
-        fy = (float)(py * 256 + 128 - L.Y0);
+        fx = (float)(px * 256 + ox - L.X0);
+        fy = (float)(py * 256 + oy - L.Y0);
     }
     float z = fmaf(L.dzdx, fx, fmaf(L.dzdy, fy, L.z0));
     if (!kWriteId) z = z + L.bias;
@@ -772,13 +777,14 @@ struct MediumWalk {
 // Edge values relative to vertex 0 in wrapping 32-bit arithmetic: for a medium
 // triangle the true value at every pixel of the walk fits in int32, so the
 // wrapped result equals it.
-__device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, uint32_t sy, int lx, int ly, MediumWalk& w) {
+__device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, uint32_t sy, int lx, int ly, int32_t ox,
+                                             int32_t oy, MediumWalk& w) {
     w.sx = sx;
     w.sy = sy;
     w.pxr = L.px0 + lx;
     w.px = w.pxr + (int)sx * kStampW;
     w.py = L.py0 + (int)sy * kStampH + ly;
-    const int32_t rx = w.px * 256 + 128 - L.X0, ry = w.py * 256 + 128 - L.Y0, rxr = w.pxr * 256 + 128 - L.X0;
+    const int32_t rx = w.px * 256 + ox - L.X0, ry = w.py * 256 + oy - L.Y0, rxr = w.pxr * 256 + ox - L.X0;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const int a = (i + 1) % 3;
@@ -861,14 +867,14 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
             const Target T = view_target<kWriteId>(P, L.view);
             if (L.medium) {
                 MediumWalk w;
-                medium_start(L, sx, sy, lx, ly, w);
+                medium_start(L, sx, sy, lx, ly, P.sample_x, P.sample_y, w);
                 for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId>(T, L, w);
             } else {
                 GenericEdges G;
                 generic_edges(L, G);
                 uint32_t x = sx, y = sy;
                 for (uint32_t j = 0; j < n; ++j) {
-                    raster_stamp<kWriteId>(T, L, G, x, y, lx, ly);
+                    raster_stamp<kWriteId>(T, L, G, x, y, lx, ly, P.sample_x, P.sample_y);
                     if (++x == L.nsx) {
                         x = 0;
                         ++y;

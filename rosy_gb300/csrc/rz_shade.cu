@@ -831,6 +831,70 @@ __device__ __forceinline__ uint32_t tile_view(const ViewRec* __restrict__ views,
     return lo;
 }
 
+// Average of four RGBA16F sample values ((s0 + s1) + (s2 + s3)) / 4, rounded
+// to RGBA16F: the AVERAGE resolve of the multisampled draw image
+// (src/Engine/Graphics.cpp:5571-5572).
+__device__ __forceinline__ float resolve4(float a, float b, float c, float d) {
+    return half_round(((a + b) + (c + d)) * 0.25f);
+}
+
+// One pixel of a 4x multisampled view: each distinct triangle among its samples
+// is shaded once at the pixel centre (no sample shading, as the reference's
+// pipeline), its colour is rounded to RGBA16F and given to the samples it
+// covers; uncovered samples keep the clear colour. Without blended surfaces the
+// samples are resolved and encoded here; with them they go to the RGBA16F
+// sample planes for k_blend. The depth output is sample 0's.
+__device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& VR, const float* s_srgb,
+                                           const float* s_unorm, int px, int py, size_t p) {
+    const size_t plane = (size_t)VR.width * VR.height;
+    uint32_t ids[kMsaaSamples];
+    unsigned long long key0 = 0;
+#pragma unroll
+    for (int k = 0; k < kMsaaSamples; ++k) {
+        const unsigned long long key = VR.vis[p + k * plane];
+        if (k == 0) key0 = key;
+        ids[k] = (uint32_t)key;
+    }
+    float cs[kMsaaSamples][4];
+    const Sampler smp{&P, s_srgb, s_unorm};
+#pragma unroll
+    for (int k = 0; k < kMsaaSamples; ++k) {
+        float c[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // clear colour, src/Engine/Graphics.cpp:5416-5419
+        int same = -1;
+#pragma unroll
+        for (int j = 0; j < k; ++j)
+            if (same < 0 && ids[j] == ids[k]) same = j;
+        if (same >= 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cs[k][i] = cs[same][i];
+            continue;
+        }
+        if (ids[k] != 0) {
+            float o[4];
+            if (shade_pixel(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o)) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) c[i] = o[i];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cs[k][i] = half_round(c[i]);
+    }
+    VR.depth[p] = __uint_as_float((uint32_t)(key0 >> 32));
+    if (P.blended) {
+#pragma unroll
+        for (int k = 0; k < kMsaaSamples; ++k) {
+            const __half2 rg = __floats2half2_rn(cs[k][0], cs[k][1]), ba = __floats2half2_rn(cs[k][2], cs[k][3]);
+            VR.color16[p + k * plane] =
+                make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&ba));
+        }
+        return;
+    }
+    float r[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r[i] = resolve4(cs[0][i], cs[1][i], cs[2][i], cs[3][i]);
+    VR.color[p] = encode_srgb8(r[0]) | (encode_srgb8(r[1]) << 8) | (encode_srgb8(r[2]) << 16) | (encode_unorm8(r[3]) << 24);
+}
+
 __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
     __shared__ uint32_t s_view;
@@ -879,8 +943,32 @@ __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
     VR.color[p] = r | (g << 8) | (b << 16) | (a << 24);
 }
 
+// k_shade for 4x multisampled views.
+__global__ void __launch_bounds__(256, 2) k_shade_msaa(ShadeParams P) {
+    __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ uint32_t s_view;
+    {
+        const int t = threadIdx.y * blockDim.x + threadIdx.x;
+        s_srgb[t] = P.srgb_table[t];
+        s_unorm[t] = (float)t / 255.0f;
+        if (t == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
+    }
+    __syncthreads();
+    const ViewRec& VR = P.views[s_view];
+    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
+    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
+    const int px = (int)(lt % tiles_x) * 16 + threadIdx.x;
+    const int py = (int)(lt / tiles_x) * 16 + threadIdx.y;
+    if (px >= VR.width || py >= VR.height) return;
+    shade_msaa(P, VR, s_srgb, s_unorm, px, py, (size_t)py * VR.width + px);
+}
+
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
     if (p.shade_blocks == 0) return;
+    if (p.samples > 1) {
+        k_shade_msaa<<<p.shade_blocks, dim3(16, 16), 0, stream>>>(p);
+        return;
+    }
     k_shade<<<p.shade_blocks, dim3(16, 16), 0, stream>>>(p);
 }
 
@@ -916,16 +1004,25 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
     const int px = tx0 + threadIdx.x, py = ty0 + threadIdx.y;
     const bool inside = px < VR.width && py < VR.height;
     const size_t p = inside ? (size_t)py * VR.width + px : 0;
-    float col[4] = {0.f, 0.f, 0.f, 0.f};
-    float dst_depth = 0.f;
-    if (inside) {
-        const uint2 c = VR.color16[p];
-        const __half2 rg = *reinterpret_cast<const __half2*>(&c.x), ba = *reinterpret_cast<const __half2*>(&c.y);
-        col[0] = __low2float(rg);
-        col[1] = __high2float(rg);
-        col[2] = __low2float(ba);
-        col[3] = __high2float(ba);
-        dst_depth = VR.depth[p];
+    const size_t plane = (size_t)VR.width * VR.height;
+    const int nsamples = VR.samples > 1 ? kMsaaSamples : 1;
+    // per coverage sample: the RGBA16F value and the opaque depth it is tested against
+    float col[kMsaaSamples][4];
+    float dst_depth[kMsaaSamples];
+#pragma unroll
+    for (int k = 0; k < kMsaaSamples; ++k) {
+        dst_depth[k] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) col[k][i] = 0.f;
+        if (inside && k < nsamples) {
+            const uint2 c = VR.color16[p + k * plane];
+            const __half2 rg = *reinterpret_cast<const __half2*>(&c.x), ba = *reinterpret_cast<const __half2*>(&c.y);
+            col[k][0] = __low2float(rg);
+            col[k][1] = __high2float(rg);
+            col[k][2] = __low2float(ba);
+            col[k][3] = __high2float(ba);
+            dst_depth[k] = nsamples > 1 ? __uint_as_float((uint32_t)(VR.vis[p + k * plane] >> 32)) : VR.depth[p];
+        }
     }
     const Sampler smp{&P, s_srgb, s_unorm};
     const uint32_t n = min(B.header->records, B.record_capacity);
@@ -963,42 +1060,51 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
             if (mask & (1u << k)) s_list[pos++] = start + 4 * tid + k;
         __syncthreads();
         if (inside) {
-            const int32_t PX = px * 256 + 128, PY = py * 256 + 128;
             for (uint32_t j = 0; j < total; ++j) {
                 const TriRecord& rec = B.records[s_list[j]];
                 const int bx0 = rec.p0 & 0xffff, by0 = rec.p0 >> 16, bx1 = rec.p1 & 0xffff, by1 = rec.p1 >> 16;
                 if (px < bx0 || px > bx1 || py < by0 || py > by1) continue;
                 const int32_t X[3] = {rec.X0, rec.X1, rec.X2}, Y[3] = {rec.Y0, rec.Y1, rec.Y2};
-                bool in = true;
+                uint32_t pass = 0;  // samples covered and in front of the opaque depth
+                for (int k = 0; k < nsamples; ++k) {
+                    const int32_t PX = px * 256 + (nsamples > 1 ? msaa_x(k) : 128);
+                    const int32_t PY = py * 256 + (nsamples > 1 ? msaa_y(k) : 128);
+                    bool in = true;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const int a = (i + 1) % 3, b = (i + 2) % 3;
-                    const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
-                    const bool tl = dy < 0 || (dy == 0 && dx > 0);
-                    const int64_t E = (int64_t)dx * (int64_t)(PY - Y[a]) - (int64_t)dy * (int64_t)(PX - X[a]);
-                    in = in && (E > 0 || (E == 0 && tl));
+                    for (int i = 0; i < 3; ++i) {
+                        const int a = (i + 1) % 3, b = (i + 2) % 3;
+                        const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+                        const bool tl = dy < 0 || (dy == 0 && dx > 0);
+                        const int64_t E = (int64_t)dx * (int64_t)(PY - Y[a]) - (int64_t)dy * (int64_t)(PX - X[a]);
+                        in = in && (E > 0 || (E == 0 && tl));
+                    }
+                    if (!in) continue;
+                    float z = fmaf(rec.dzdx, (float)(PX - rec.X0), fmaf(rec.dzdy, (float)(PY - rec.Y0), rec.z0));
+                    if (!(z > 0.0f)) z = 0.0f;
+                    if (z > 1.0f) z = 1.0f;
+                    if (z >= dst_depth[k]) pass |= 1u << k;
                 }
-                if (!in) continue;
-                float z = fmaf(rec.dzdx, (float)(PX - rec.X0), fmaf(rec.dzdy, (float)(PY - rec.Y0), rec.z0));
-                if (!(z > 0.0f)) z = 0.0f;
-                if (z > 1.0f) z = 1.0f;
-                if (!(z >= dst_depth)) continue;
+                if (!pass) continue;
                 float s4[4];
                 if (!shade_pixel(P, VR, *VR.scene, smp, rec.id - 1u, px, py, s4)) continue;
                 const float a = s4[3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) col[k] = half_round(s4[k] * a + col[k] * (1.0f - a));
-                col[3] = half_round(a);
+                for (int k = 0; k < kMsaaSamples; ++k) {
+                    if (!(pass & (1u << k))) continue;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) col[k][i] = half_round(s4[i] * a + col[k][i] * (1.0f - a));
+                    col[k][3] = half_round(a);
+                }
             }
         }
         __syncthreads();
     }
     if (!inside) return;
-    const uint32_t r = encode_srgb8(col[0]);
-    const uint32_t g = encode_srgb8(col[1]);
-    const uint32_t b = encode_srgb8(col[2]);
-    const uint32_t a = encode_unorm8(col[3]);
-    VR.color[p] = r | (g << 8) | (b << 16) | (a << 24);
+    float o[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        o[i] = nsamples > 1 ? resolve4(col[0][i], col[1][i], col[2][i], col[3][i]) : col[0][i];
+    VR.color[p] = encode_srgb8(o[0]) | (encode_srgb8(o[1]) << 8) | (encode_srgb8(o[2]) << 16) | (encode_unorm8(o[3]) << 24);
 }
 
 void launch_blend(const BlendParams& p, cudaStream_t stream) {

@@ -139,6 +139,7 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
     a.view.bias_slope = cfg->depth_bias_slope_factor;
     a.view.shadow = reinterpret_cast<uint32_t*>(depth_out);
     a.view.cascades = 1;
+    a.view.samples = 1;
     k_static_prep<<<1, 128, 0, s>>>(a);
     if (tris) {
         PassParams p{};
@@ -163,6 +164,8 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.chunk_capacity = kStaticChunks;
         p.header = reinterpret_cast<PassHeader*>(scratch + kOffHeader);
         p.error_flags = reinterpret_cast<uint32_t*>(scratch + kOffFlags);
+        p.sample_x = 128;
+        p.sample_y = 128;
         launch_setup(p, s);
         launch_raster(p, sms, s);
     }

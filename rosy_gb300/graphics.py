@@ -27,11 +27,14 @@ class Graphics:
         self.shadow_size = 0
 
     # -- rosy::graphics -----------------------------------------------------------
-    def init(self, width: int, height: int, shadow_size: int = 4096, device: int = 0, queue_chunks: int = 0) -> None:
-        """graphics::init: creates the context (stream + frame buffers) on `device`."""
+    def init(self, width: int, height: int, shadow_size: int = 4096, device: int = 0, queue_chunks: int = 0,
+             samples: int = 1) -> None:
+        """graphics::init: creates the context (stream + frame buffers) on `device`; samples = 4
+        renders the camera pass with the reference's 4x multisampling."""
         self._lib = _lib.load()
-        cfg = _abi.RzConfig(width=width, height=height, shadow_map_size=shadow_size, samples=1, device=device,
+        cfg = _abi.RzConfig(width=width, height=height, shadow_map_size=shadow_size, samples=samples, device=device,
                             queue_chunks=queue_chunks)
+        self.samples = samples
         rc = self._lib.rz_create(C.byref(self._ctx), C.byref(cfg))
         if rc != 0:
             raise _lib.RzError(rc, "rz_create")
@@ -219,8 +222,9 @@ class Graphics:
         W, H, S = self.viewport_width, self.viewport_height, self.shadow_size
         self.sync()
         n = getattr(self, "_cascades", 1)
+        ns = getattr(self, "samples", 1)
         out = {
-            "vis": device_array(f.visibility_u64, (H, W), np.uint64),
+            "vis": device_array(f.visibility_u64, (H, W) if ns == 1 else (ns, H, W), np.uint64),
             "shadow": device_array(f.shadow_map_f32, (S, S) if n == 1 else (n, S, S), np.float32),
         }
         color = np.empty((H, W, 4), np.uint8)
@@ -255,7 +259,7 @@ def device_array(ptr: int, shape, dtype) -> np.ndarray:
 def render_scene(scene: Scene, device: int = 0) -> dict:
     """Convenience: one frame of `scene` through the C ABI, downloaded to host arrays."""
     g = Graphics()
-    g.init(scene.width, scene.height, scene.shadow_size, device)
+    g.init(scene.width, scene.height, scene.shadow_size, device, samples=getattr(scene, "samples", 1))
     try:
         g.set_asset(scene)
         g.set_graphic_objects(scene.objects, scene.surfaces)

@@ -129,6 +129,7 @@ class Scene:
     scene: np.ndarray  # SCENE_DTYPE, shape (1,)
     draw_config: np.ndarray  # DRAW_CONFIG_DTYPE, shape (1,)
     cameras: list = field(default_factory=list)  # extra SCENE_DTYPE records (one per frame)
+    samples: int = 1  # camera-pass samples per pixel (1, or 4: the reference's 4x MSAA)
 
     @property
     def triangle_count(self) -> int:

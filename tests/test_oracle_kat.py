@@ -270,3 +270,24 @@ def test_shadow_cascades_are_scaled_projections(oracle):
     # coverage grows with the extent
     cov = [(multi["shadow"][k] > 0).mean() for k in range(4)]
     assert cov[0] > cov[1] > cov[2] > cov[3]
+
+
+def test_msaa_interior_pixels_match_single_sample(oracle):
+    """With 4x multisampling a pixel whose four samples all see the triangle its
+    centre sees is shaded once at the centre and resolves to exactly the
+    single-sample colour ((4 h) / 4 = h in RGBA16F); edge pixels mix."""
+    from rosy_gb300 import scene as sc
+
+    s1 = sc.random_triangles(seed=21, triangles=200, width=96, height=64, shadow_size=128, texture_size=32)
+    s4 = sc.Scene(**{f: getattr(s1, f) for f in s1.__dataclass_fields__})
+    s4.samples = 4
+    r1 = oracle.render(s1)
+    r4 = oracle.render(s4)
+    assert r4["ids"].shape == (4, 64, 96) and r4["depth"].shape == (4, 64, 96)
+    same = np.all(r4["ids"] == r1["ids"][None], axis=0)
+    assert same.mean() > 0.5 and (~same).any()
+    assert np.array_equal(r4["color"][same], r1["color"][same])
+    # every sample plane is a valid raster of the same triangles: ids only from the scene
+    assert set(np.unique(r4["ids"])) <= set(np.unique(r1["ids"])) | set(range(1, s1.triangle_count + 1))
+    # depth and ids agree per sample (0 depth exactly where no triangle)
+    assert np.array_equal(r4["depth"] == 0, r4["ids"] == 0)
