@@ -776,6 +776,8 @@ void launch_camera_raster(rz_ctx* c, PassParams cp, cudaStream_t s) {
         cp.sample_x = kMsaaX[k];
         cp.sample_y = kMsaaY[k];
         cp.sample_plane = (uint32_t)k;
+        // each launch drains the small records through the header's cursor from the start
+        if (k > 0) cudaMemsetAsync(&cp.header->small_cursor, 0, sizeof(uint32_t), s);
         launch_raster(cp, c->sm_count, s);
     }
 }
