@@ -212,9 +212,11 @@ def cpu_baseline(s, seconds: float) -> tuple[dict, dict]:
             break
     dt = time.perf_counter() - t0
     extra = {}
-    r = oracle.render(s.with_camera(0), threads=threads, texel_bytes=True)
+    r = oracle.render(s.with_camera(0), threads=threads, texel_bytes=True, fp64=True)
     extra["texel_bytes"] = r["texel_bytes"]
     extra["oracle_ids"] = r["ids"]
+    extra["oracle_color"] = r["color"]
+    extra["oracle_color_f64"] = r["color_f64"]
     return ({"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
              "sample": f"{n} full frame(s) of the same workload (spline cameras cycled), {dt:.1f} s"}, extra)
 
@@ -383,8 +385,20 @@ def run_rz(args):
                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                       "profiles/dram_traffic_scene_scale_1080p.json"}
     parity = None
+    fp64 = None
     if rank == 0 and extra.get("oracle_ids") is not None:
         parity = bool(np.array_equal(out0["ids"], extra["oracle_ids"]))
+        # shading error against the oracle evaluated in float64 (sRGB value * 255, before 8-bit rounding)
+        ref = extra["oracle_color_f64"][..., :3] * 255.0
+        e_gpu = np.abs(out0["color"][..., :3].astype(np.float64) - ref)
+        e_o32 = np.abs(extra["oracle_color"][..., :3].astype(np.float64) - ref)
+        d32 = np.abs(out0["color"][..., :3].astype(np.int32) - extra["oracle_color"][..., :3].astype(np.int32))
+        fp64 = {"frame": 0, "unit": "1/255 of the sRGB value",
+                "gpu_max_abs": round(float(e_gpu.max()), 4), "gpu_mean_abs": round(float(e_gpu.mean()), 4),
+                "oracle_fp32_max_abs": round(float(e_o32.max()), 4),
+                "oracle_fp32_mean_abs": round(float(e_o32.mean()), 4),
+                "gpu_vs_oracle_fp32_max_levels": int(d32.max()),
+                "note": "8-bit rounding alone contributes up to 0.5"}
     g.deinit()
     if rank == 0:
         line = {
@@ -403,6 +417,7 @@ def run_rz(args):
             "cpu_baseline": cpu,
             "clocks": ck,
             "visibility_matches_oracle_frame0": parity,
+            "fp64_oracle_error": fp64,
             "algorithmic_bytes": {k: (int(v) if v is not None else None) for k, v in algo.items()},
         }
         if not args.no_learned:

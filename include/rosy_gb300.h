@@ -477,7 +477,9 @@ int rz_rsy_get_scene(const struct rz_rsy* asset, rz_object* objects, uint32_t ob
  * pixel of every view: the albedo (the sampled base colour of fragmentMain,
  * rounded to f16 and sRGB-encoded; alpha = 255 where a triangle covers the
  * pixel, else 0) and the interpolated world-space normal, octahedral-encoded as
- * two f16 (x in the low half). */
+ * two f16 (x in the low half). With 4x multisampling both are averaged over the
+ * pixel's samples (the normal renormalised) and the albedo's alpha is the
+ * covered fraction of the samples. */
 typedef struct rz_gbuffer {
     const void* color_rgba8;      /* width*height RGBA8 sRGB (the frame's colour) */
     const void* depth_f32;        /* width*height f32 (reverse-Z, 0 = background) */

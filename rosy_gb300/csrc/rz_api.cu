@@ -1347,7 +1347,6 @@ int rz_get_frame(rz_ctx* c, rz_frame_out* out) { return rz_get_view_frame(c, 0, 
 
 int rz_set_gbuffer(rz_ctx* c, uint32_t enable) {
     if (!c) return RZ_INVALID_ARGUMENT;
-    if (enable && c->samples > 1) return fail(c, RZ_INVALID_STATE, "the G-buffer needs one sample per pixel");
     if (c->frame_pending) return fail(c, RZ_INVALID_STATE, "a frame is in flight; call rz_sync first");
     if ((enable != 0) != c->gbuffer) {
         c->gbuffer = enable != 0;

@@ -857,9 +857,12 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
     }
     float cs[kMsaaSamples][4];
     const Sampler smp{&P, s_srgb, s_unorm};
+    const bool gbuffer = VR.gb_albedo != nullptr;
+    float gs[kMsaaSamples][6];  // G-buffer values per sample (albedo rgb, normal xyz)
 #pragma unroll
     for (int k = 0; k < kMsaaSamples; ++k) {
         float c[4] = {0.0f, 0.05f, 0.1f, 1.0f};  // clear colour, src/Engine/Graphics.cpp:5416-5419
+        float aux[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         int same = -1;
 #pragma unroll
         for (int j = 0; j < k; ++j)
@@ -867,17 +870,36 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
         if (same >= 0) {
 #pragma unroll
             for (int i = 0; i < 4; ++i) cs[k][i] = cs[same][i];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) gs[k][i] = gs[same][i];
             continue;
         }
         if (ids[k] != 0) {
             float o[4];
-            if (shade_pixel(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o)) {
+            if (shade_pixel(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr)) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) c[i] = o[i];
             }
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) cs[k][i] = half_round(c[i]);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) gs[k][i] = aux[i];
+    }
+    if (gbuffer) {
+        // G-buffer of a multisampled pixel: albedo and normal averaged over the samples,
+        // coverage = covered samples / 4 in the albedo's alpha
+        float g[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) g[i] = ((gs[0][i] + gs[1][i]) + (gs[2][i] + gs[3][i])) * 0.25f;
+        uint32_t covered = 0;
+#pragma unroll
+        for (int k = 0; k < kMsaaSamples; ++k) covered += ids[k] != 0 ? 1u : 0u;
+        VR.gb_albedo[p] = encode_srgb8(half_round(g[0])) | (encode_srgb8(half_round(g[1])) << 8) |
+                          (encode_srgb8(half_round(g[2])) << 16) | (encode_unorm8((float)covered * 0.25f) << 24);
+        const float len2 = g[3] * g[3] + g[4] * g[4] + g[5] * g[5];
+        const float inv = len2 > 0.0f ? rsqrtf(len2) : 0.0f;
+        VR.gb_normal[p] = encode_octahedral(g[3] * inv, g[4] * inv, g[5] * inv);
     }
     VR.depth[p] = __uint_as_float((uint32_t)(key0 >> 32));
     if (P.blended) {

@@ -27,6 +27,7 @@ from .upsampler import PARAM_COUNT, Upsampler, conv_flops, init_params
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "weights", "upsampler_random_triangles.npz")
+WEIGHTS_MSAA4 = os.path.join(HERE, "weights", "upsampler_random_triangles_msaa4.npz")
 TRAIN_CAMERAS = 4096
 TEST_CAMERAS = 256
 TRAIN_CAMERA_SEED = 1001
@@ -44,14 +45,15 @@ def _render(g: Graphics, sync: bool) -> None:
 
 
 class PairRenderer:
-    """Two contexts on one scene: `low` at W x H with the G-buffer on, `high` at 2W x 2H."""
+    """Two contexts on one scene: `low` at W x H with the G-buffer on, `high` at 2W x 2H,
+    both with `samples` camera-pass samples per pixel."""
 
-    def __init__(self, s: sc.Scene, width: int, height: int, device: int = 0):
+    def __init__(self, s: sc.Scene, width: int, height: int, device: int = 0, samples: int = 1):
         self.s, self.width, self.height = s, width, height
         self.low = Graphics()
-        self.low.init(width, height, s.shadow_size, device)
+        self.low.init(width, height, s.shadow_size, device, samples=samples)
         self.high = Graphics()
-        self.high.init(2 * width, 2 * height, s.shadow_size, device)
+        self.high.init(2 * width, 2 * height, s.shadow_size, device, samples=samples)
         for g in (self.low, self.high):
             g.set_asset(s)
             g.set_graphic_objects(s.objects, s.surfaces)
@@ -81,11 +83,11 @@ def _stream_sync(stream: int) -> None:
 
 
 def train(steps: int = 3000, batch: int = 4, lr: float = 2e-3, seed: int = 0, scene_seed: int = 0,
-          width: int = 960, height: int = 540, log=print) -> tuple[np.ndarray, list]:
+          width: int = 960, height: int = 540, log=print, samples: int = 1) -> tuple[np.ndarray, list]:
     """Adam on the loss sum over `batch` frames per step (cosine learning-rate decay);
     returns the parameters and the per-step mean squared error."""
     s = sc.random_triangles(seed=scene_seed, width=2 * width, height=2 * height)
-    pr = PairRenderer(s, width, height)
+    pr = PairRenderer(s, width, height, samples=samples)
     u = Upsampler(0, width, height)
     u.set_params(init_params(seed))
     dirs = sc.camera_dirs(TRAIN_CAMERAS, TRAIN_CAMERA_SEED)
@@ -125,13 +127,13 @@ def _psnr_dev(a, b) -> tuple[float, int]:
 
 
 def evaluate(params: np.ndarray, cameras: int = TEST_CAMERAS, scene_seed: int = 0, width: int = 960,
-             height: int = 540) -> dict:
+             height: int = 540, samples: int = 1) -> dict:
     """Per held-out frame: PSNR and max error of the learned reconstruction and of plain
     bilinear upsampling, both against the plain full-resolution render."""
     import torch
 
     s = sc.random_triangles(seed=scene_seed, width=2 * width, height=2 * height)
-    pr = PairRenderer(s, width, height)
+    pr = PairRenderer(s, width, height, samples=samples)
     net = Upsampler(0, width, height)
     net.set_params(params)
     bil = Upsampler(0, width, height)
@@ -170,14 +172,14 @@ def evaluate(params: np.ndarray, cameras: int = TEST_CAMERAS, scene_seed: int = 
 
 
 def time_paths(params: np.ndarray, frames: int = 64, warmup: int = 5, scene_seed: int = 0, width: int = 960,
-               height: int = 540) -> dict:
+               height: int = 540, samples: int = 1) -> dict:
     """Device time per frame of the plain 2W x 2H path and of the learned path (W x H render +
     upsampler), each frame after a 256 MiB L2 flush, cycling the held-out cameras; and the
     upsampler alone."""
     import torch
 
     s = sc.random_triangles(seed=scene_seed, width=2 * width, height=2 * height)
-    pr = PairRenderer(s, width, height)
+    pr = PairRenderer(s, width, height, samples=samples)
     net = Upsampler(0, width, height)
     net.set_params(params)
     out = torch.zeros((2 * height, 2 * width), dtype=torch.int32, device="cuda")
@@ -267,17 +269,21 @@ def main():
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cameras", type=int, default=TEST_CAMERAS)
-    ap.add_argument("--weights", default=WEIGHTS)
-    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--samples", type=int, default=1, choices=[1, 4])
+    ap.add_argument("--weights", default=None)
+    ap.add_argument("--out", default=None)
     args = ap.parse_args()
+    default = WEIGHTS if args.samples == 1 else WEIGHTS_MSAA4
+    args.weights = args.weights or default
+    args.out = args.out or default
     from . import build
 
     build.build()
     if args.cmd == "train":
         t0 = time.perf_counter()
-        p, hist = train(args.steps, args.batch, args.lr, args.seed)
-        ev = evaluate(p, args.cameras)
-        meta = {"steps": args.steps, "batch": args.batch, "lr": args.lr, "seed": args.seed,
+        p, hist = train(args.steps, args.batch, args.lr, args.seed, samples=args.samples)
+        ev = evaluate(p, args.cameras, samples=args.samples)
+        meta = {"steps": args.steps, "batch": args.batch, "lr": args.lr, "seed": args.seed, "samples": args.samples,
                 "train_cameras": TRAIN_CAMERAS, "train_camera_seed": TRAIN_CAMERA_SEED,
                 "test_cameras": args.cameras, "test_camera_seed": TEST_CAMERA_SEED,
                 "final_train_mse": float(np.mean(hist[-50:])), "train_seconds": time.perf_counter() - t0,
@@ -287,11 +293,11 @@ def main():
         print(json.dumps(meta))
     elif args.cmd == "eval":
         p, _ = load_weights(args.weights)
-        ev = evaluate(p, args.cameras)
+        ev = evaluate(p, args.cameras, samples=args.samples)
         print(json.dumps({k: v for k, v in ev.items() if k != "per_frame"}))
     else:
         p, _ = load_weights(args.weights)
-        print(json.dumps(time_paths(p)))
+        print(json.dumps(time_paths(p, samples=args.samples)))
 
 
 if __name__ == "__main__":

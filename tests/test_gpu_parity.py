@@ -219,3 +219,16 @@ def test_msaa_parity(gpu, oracle, name):
     assert d.max() <= COLOR_TOL, f"colour differs by {d.max()} at {np.count_nonzero(d > COLOR_TOL)} channels"
     # some pixels really are partially covered (the resolve mixes)
     assert (np.ptp(out["ids"], axis=0) > 0).any()
+
+
+@pytest.mark.gpu
+def test_shading_error_against_fp64_oracle(gpu, oracle):
+    """The oracle also shades in float64; the GPU's 8-bit sRGB colour stays within
+    1.5 levels of that (0.5 of it is the 8-bit rounding itself)."""
+    s = sc.scene_scale(seed=4, meshes=8, triangles_per_mesh=512, materials=4, texture_size=64, width=320,
+                       height=180, shadow_size=512, frames=1)
+    ref = oracle.render(s, fp64=True)
+    out = render_scene(s)
+    err = np.abs(out["color"][..., :3].astype(np.float64) - ref["color_f64"][..., :3] * 255.0)
+    assert err.max() <= 1.5, err.max()
+    assert err.mean() < 0.3, err.mean()
