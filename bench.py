@@ -96,13 +96,16 @@ def measured_traffic(stage: str):
         return None
 
 
-def make_scene(name: str):
+def make_scene(name: str, samples: int = 1):
     from rosy_gb300 import scene as sc
 
     if name == "scene_scale":
-        return sc.scene_scale(seed=0)
+        s = sc.scene_scale(seed=0)
+        s.samples = samples
+        return s
     if name == "random_triangles":
         s = sc.random_triangles(seed=0)
+        s.samples = samples
         return s
     raise SystemExit(f"unknown config {name}")
 
@@ -114,7 +117,7 @@ def workload_config(name: str, s) -> dict:
         "texture_size": s.textures[0].width if s.textures else 0,
         "width": s.width, "height": s.height, "shadow_map": s.shadow_size,
         "pcf": "3x3" if int(s.draw_config["pcf_mode"][0]) == 1 else "5-tap",
-        "frames_on_spline": len(s.cameras), "seed": 0, "samples_per_pixel": 1,
+        "frames_on_spline": len(s.cameras), "seed": 0, "samples_per_pixel": getattr(s, "samples", 1),
         "l2": "flushed between frames (256 MiB write)",
     }
 
@@ -238,7 +241,8 @@ def shade_bytes(s, ids: np.ndarray, texel_bytes: int | None) -> int | None:
     mt = np.asarray(s.meshes, np.int64)
     first = mt[mesh, 2] + surf["start_index"][d].astype(np.int64) + 3 * (tri - base[d])
     verts = np.unique(np.concatenate([s.indices[first + k].astype(np.int64) + mt[mesh, 0] for k in range(3)]))
-    return 8 * W * H + 4 * W * H + 4 * W * H + 64 * len(verts) + 64 * len(s.materials) + int(texel_bytes)
+    ns = getattr(s, "samples", 1)
+    return 8 * W * H * ns + 4 * W * H + 4 * W * H + 64 * len(verts) + 64 * len(s.materials) + int(texel_bytes)
 
 
 def raster_bytes(s, pass_name: str) -> int:
@@ -248,7 +252,7 @@ def raster_bytes(s, pass_name: str) -> int:
     D = len(s.surfaces)
     if pass_name == "shadow":
         return 64 * V + 12 * T + 164 * D + 4 * s.shadow_size ** 2
-    return 64 * V + 12 * T + 164 * D + 8 * s.width * s.height
+    return 64 * V + 12 * T + 164 * D + 8 * s.width * s.height * getattr(s, "samples", 1)
 
 
 def run_rz(args):
@@ -261,9 +265,9 @@ def run_rz(args):
     rzbuild.build()
     from rosy_gb300.graphics import Graphics
 
-    s = make_scene(args.config)
+    s = make_scene(args.config, args.samples)
     g = Graphics()
-    g.init(s.width, s.height, s.shadow_size, device=torch.cuda.current_device())
+    g.init(s.width, s.height, s.shadow_size, device=torch.cuda.current_device(), samples=s.samples)
     g.set_asset(s)
     g.set_graphic_objects(s.objects, s.surfaces)
     g.set_draw_config(s.draw_config)
@@ -604,7 +608,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    s = make_scene(args.config)
+    s = make_scene(args.config, args.samples)
     from oracle import oracle
 
     oracle.build()
@@ -646,6 +650,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="timed frames only (for ncu captures)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-path comparison")
+    ap.add_argument("--samples", type=int, default=1, choices=[1, 4],
+                    help="camera-pass samples per pixel (4: the reference's 4x multisampling)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "rz":
         args.warmup = 3
