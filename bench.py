@@ -55,20 +55,23 @@ def bf16_peak():
     return 1900.0, "fallback 1.9 PFLOP/s"
 
 
-def learned_block(frames: int = 64, cameras: int = 256) -> dict:
+def learned_block(frames: int = 64, cameras: int = 256, samples: int = 1) -> dict:
     """The learned half-resolution path against the plain path at 1920x1080 on the
     random-triangles scene: device frames/s of both, held-out PSNR and max error per
-    frame against the plain render, and the upsampler's tensor-core roofline."""
+    frame against the plain render, and the upsampler's tensor-core roofline. With
+    samples = 4 both renders use the reference's 4x multisampling (and the network
+    trained on such frames)."""
     from rosy_gb300 import learned
 
-    params, meta = learned.load_weights()
-    t = learned.time_paths(params, frames=frames)
-    ev = learned.evaluate(params, cameras)
+    params, meta = learned.load_weights(learned.WEIGHTS if samples == 1 else learned.WEIGHTS_MSAA4)
+    t = learned.time_paths(params, frames=frames, samples=samples)
+    ev = learned.evaluate(params, cameras, samples=samples)
     peak, src = bf16_peak()
     per = ev.pop("per_frame")
     return {
         "workload": "random_triangles (4,096 triangles, 256^2 texture, 1024^2 shadow map): plain 1920x1080 vs "
                     "960x540 render + upsampler to 1920x1080; L2 flushed between frames",
+        "samples_per_pixel": samples,
         "plain_fps": round(t["plain_fps"], 2), "learned_fps": round(t["learned_fps"], 2),
         "speedup": round(t["speedup"], 3), "plain_ms": round(t["plain_ms"], 5), "learned_ms": round(t["learned_ms"], 5),
         "heldout": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in ev.items()},
@@ -426,6 +429,7 @@ def run_rz(args):
         }
         if not args.no_learned:
             line["learned_upsample"] = learned_block()
+            line["learned_upsample_msaa4"] = learned_block(samples=4)
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
