@@ -236,10 +236,11 @@ class LearnedPath:
     """Renders 2W x 2H frames through the learned path, or through the plain path
     when the network's held-out PSNR is below the floor (the fallback)."""
 
-    def __init__(self, s: sc.Scene, width: int, height: int, params: np.ndarray, heldout_psnr_db: float):
+    def __init__(self, s: sc.Scene, width: int, height: int, params: np.ndarray, heldout_psnr_db: float,
+                 samples: int = 1):
         import torch
 
-        self.pr = PairRenderer(s, width, height)
+        self.pr = PairRenderer(s, width, height, samples=samples)
         self.net = Upsampler(0, width, height)
         self.net.set_params(params)
         self.use_network = heldout_psnr_db >= PSNR_FLOOR_DB
