@@ -531,11 +531,11 @@ def run_stress(args):
     views = 8
     s = sc.stress(frames=views)
     lo_recs = [sc.view_of(s, 1920, 1080, 4096, camera=i).scene for i in range(views)]
-    params, meta = learned.load_weights()
+    params, meta = learned.load_weights(learned.WEIGHTS if args.samples == 1 else learned.WEIGHTS_MSAA4)
 
     def ctx(w, h, gbuffer):
         g = Graphics()
-        g.init(w, h, 4096)
+        g.init(w, h, 4096, samples=args.samples)
         g.set_asset(s)
         g.set_graphic_objects(s.objects, s.surfaces)
         g.set_draw_config(s.draw_config)
@@ -599,7 +599,8 @@ def run_stress(args):
         "speedup": round(plain_ms / learned_ms, 3), "n_gpus": 1, "steps": steps, "warmup": args.warmup,
         "ms_per_batch": {"plain": round(plain_ms, 4), "learned": round(learned_ms, 4)},
         "higher_is_better": True, "dtype": "f32 raster/shading, bf16 upsampler", "data": "synthetic (seeded)",
-        "config": {"workload": "stress", "triangles": s.triangle_count, "meshes": 256, "materials": 64,
+        "config": {"workload": "stress", "samples_per_pixel": args.samples, "triangles": s.triangle_count,
+                   "meshes": 256, "materials": 64,
                    "textures": len(s.textures), "texture_size": 2048, "shadow_cascades": 4, "shadow_map": 4096,
                    "views_per_batch": views, "plain_extent": [3840, 2160], "render_extent": [1920, 1080],
                    "l2": "flushed between batches (256 MiB write)"},
