@@ -668,6 +668,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
     p.sample_x = 128;  // pixel centre
     p.sample_y = 128;
     p.sample_plane = 0;
+    p.bb_hi = (kind != 0 && c->samples > 1) ? 32 : 128;
     PassBuffers* pb;
     if (kind == 2) {  // blended list: cull none, records kept in submission order
         p.draws = c->d_blended_draws;

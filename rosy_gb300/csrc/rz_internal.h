@@ -165,6 +165,7 @@ struct PassParams {
     // (128, 128) or one of the standard 4x positions; camera-pass target plane
     int32_t sample_x, sample_y;
     uint32_t sample_plane;
+    int32_t bb_hi;  // smallest sample offset the setup boxed for (32 with 4x samples, else 128)
 };
 
 struct ShadeParams {

@@ -640,6 +640,7 @@ struct LargeRecord {
     int32_t dx[3], dy[3];
     uint32_t tl_bias[3];  // 0 on top-left edges, 1 otherwise
     bool medium;          // extent <= kMediumExtent px and near_origin: incremental 32-bit walk
+    bool clipped;         // the box was cut by the viewport: pixels past px1 / py1 may be inside the triangle
     bool near_origin;     // |PX - X0|, |PY - Y0| < 2^23 over the box: float offsets exact
     int32_t X0, Y0;
     float z0, dzdx, dzdy, bias;
@@ -648,7 +649,7 @@ struct LargeRecord {
     uint64_t begin, end;
 };
 
-__device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L) {
+__device__ __forceinline__ void load_large(const TriRecord* rec, int32_t bb_hi, LargeRecord& L) {
     const int4* src = reinterpret_cast<const int4*>(rec);
     const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
     L.X[0] = q0.x;
@@ -683,8 +684,12 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L)
     const int32_t lo_y = L.py0 * 256 - L.Y0, hi_y = L.py1 * 256 + 256 - L.Y0 + kStampH * 256;
     const int32_t lim = 1 << 23;
     L.near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
-    const int32_t ex = max(L.X[0], max(L.X[1], L.X[2])) - min(L.X[0], min(L.X[1], L.X[2]));
-    const int32_t ey = max(L.Y[0], max(L.Y[1], L.Y[2])) - min(L.Y[0], min(L.Y[1], L.Y[2]));
+    const int32_t max_x = max(L.X[0], max(L.X[1], L.X[2])), max_y = max(L.Y[0], max(L.Y[1], L.Y[2]));
+    const int32_t ex = max_x - min(L.X[0], min(L.X[1], L.X[2]));
+    const int32_t ey = max_y - min(L.Y[0], min(L.Y[1], L.Y[2]));
+    // Pixels past an uncut box edge lie outside the triangle's extent, so the edge
+    // test alone rejects the stamps' overhang there; only a cut box needs the check.
+    L.clipped = ((max_x - bb_hi) >> 8) > L.px1 || ((max_y - bb_hi) >> 8) > L.py1;
     L.medium = L.near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
 }
 
@@ -710,7 +715,7 @@ __device__ __forceinline__ void generic_edges(const LargeRecord& L, GenericEdges
 }
 
 // Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
-template <bool kWriteId>
+template <bool kWriteId, bool kBoxCheck>
 __device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord& L, const GenericEdges& G, uint32_t sx,
                                              uint32_t sy, int lx, int ly, int32_t ox, int32_t oy) {
     const int sx0 = L.px0 + (int)sx * kStampW, sy0 = L.py0 + (int)sy * kStampH;
@@ -725,7 +730,7 @@ __device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord&
     }
     if (reject) return;
     const int px = sx0 + lx, py = sy0 + ly;
-    bool in = px <= L.px1 && py <= L.py1;
+    bool in = !kBoxCheck || (px <= L.px1 && py <= L.py1);
     if (!accept) {
         if (G.short_edges) {
             // partial edges: |eo| < 2^30 and the lane offset < 2^30, so 32 bits suffice
@@ -801,9 +806,9 @@ __device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, 
     w.zrow = fmaf(L.dzdy, w.fy, L.z0);
 }
 
-template <bool kWriteId>
+template <bool kWriteId, bool kBoxCheck>
 __device__ __forceinline__ void medium_step(const Target& T, const LargeRecord& L, MediumWalk& w) {
-    if (((w.e[0] | w.e[1] | w.e[2]) >= 0) && w.px <= L.px1 && w.py <= L.py1) {
+    if (((w.e[0] | w.e[1] | w.e[2]) >= 0) && (!kBoxCheck || (w.px <= L.px1 && w.py <= L.py1))) {
         float z = fmaf(L.dzdx, w.fx, w.zrow);
         if (!kWriteId) z = z + L.bias;
         write_fragment<kWriteId>(T, w.px, w.py, z, L.id);
@@ -855,7 +860,7 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
         while (s < s_end) {
             if (r >= P.record_capacity) break;
             LargeRecord L;
-            load_large(P.records + r, L);
+            load_large(P.records + r, P.bb_hi, L);
             if (s < L.begin || s >= L.end) {  // cannot happen with a consistent chunk map
                 atomicOr(P.error_flags, kErrStampOverflow);
                 break;
@@ -868,13 +873,17 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
             if (L.medium) {
                 MediumWalk w;
                 medium_start(L, sx, sy, lx, ly, P.sample_x, P.sample_y, w);
-                for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId>(T, L, w);
+                if (L.clipped)
+                    for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId, true>(T, L, w);
+                else
+                    for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId, false>(T, L, w);
             } else {
                 GenericEdges G;
                 generic_edges(L, G);
                 uint32_t x = sx, y = sy;
                 for (uint32_t j = 0; j < n; ++j) {
-                    raster_stamp<kWriteId>(T, L, G, x, y, lx, ly, P.sample_x, P.sample_y);
+                    if (L.clipped) raster_stamp<kWriteId, true>(T, L, G, x, y, lx, ly, P.sample_x, P.sample_y);
+                    else raster_stamp<kWriteId, false>(T, L, G, x, y, lx, ly, P.sample_x, P.sample_y);
                     if (++x == L.nsx) {
                         x = 0;
                         ++y;

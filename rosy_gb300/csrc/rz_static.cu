@@ -166,6 +166,7 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.error_flags = reinterpret_cast<uint32_t*>(scratch + kOffFlags);
         p.sample_x = 128;
         p.sample_y = 128;
+        p.bb_hi = 128;
         launch_setup(p, s);
         launch_raster(p, sms, s);
     }
