@@ -112,14 +112,16 @@ class Graphics:
         W, H, S = f.width, f.height, f.shadow_map_size
         v = getattr(self, "_views", None)
         n = min(max(int(v[view][4]["shadow_cascades"][0]), 1), 4) if v else 1
+        ns = getattr(self, "samples", 1)
         out = {
-            "vis": device_array(f.visibility_u64, (H, W), np.uint64),
+            "vis": device_array(f.visibility_u64, (H, W) if ns == 1 else (ns, H, W), np.uint64),
             "shadow": device_array(f.shadow_map_f32, (S, S) if n == 1 else (n, S, S), np.float32),
             "color": device_array(f.color_rgba8, (H, W, 4), np.uint8),
             "depth": device_array(f.depth_f32, (H, W), np.float32),
         }
         ids = (out["vis"] & np.uint64(0xFFFFFFFF)).astype(np.uint32)
         out["ids"] = np.where(ids > 0, ids - np.uint32(f.triangle_id_base), 0).astype(np.uint32)
+        out["vis_depth"] = (out["vis"] >> np.uint64(32)).astype(np.uint32).view(np.float32)
         return out
 
     def set_gbuffer(self, enable: bool) -> None:
