@@ -715,16 +715,54 @@ __device__ __forceinline__ void generic_edges(const LargeRecord& L, GenericEdges
 }
 
 // Rasterises stamp (sx, sy) of a large record: lane = pixel (lane & 7, lane >> 3).
+// Walk over the stamps of a generic record in raster order: the 64-bit edge
+// values at the current stamp's origin sample, advanced by exact constant steps
+// (one stamp right, or back to the row start and one stamp down).
+struct GenericWalk {
+    int64_t e[3], er[3];  // edge values at the current stamp's / the row's first stamp's origin sample
+    int sx0, sy0;         // origin pixel of the current stamp
+    uint32_t sx;
+};
+
+__device__ __forceinline__ void generic_start(const LargeRecord& L, const GenericEdges& G, uint32_t sx, uint32_t sy,
+                                              int32_t ox, int32_t oy, GenericWalk& w) {
+    w.sx = sx;
+    w.sx0 = L.px0 + (int)sx * kStampW;
+    w.sy0 = L.py0 + (int)sy * kStampH;
+    const int32_t PXo = w.sx0 * 256 + ox, PYo = w.sy0 * 256 + oy, PXr = L.px0 * 256 + ox;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        w.e[i] = G.c[i] + (int64_t)L.dx[i] * PYo - (int64_t)L.dy[i] * PXo;
+        w.er[i] = G.c[i] + (int64_t)L.dx[i] * PYo - (int64_t)L.dy[i] * PXr;
+    }
+}
+
+__device__ __forceinline__ void generic_next(const LargeRecord& L, GenericWalk& w) {
+    if (++w.sx == L.nsx) {
+        w.sx = 0;
+        w.sx0 = L.px0;
+        w.sy0 += kStampH;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            w.er[i] += (int64_t)L.dx[i] * (kStampH * 256);
+            w.e[i] = w.er[i];
+        }
+    } else {
+        w.sx0 += kStampW;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) w.e[i] -= (int64_t)L.dy[i] * (kStampW * 256);
+    }
+}
+
 template <bool kWriteId, bool kBoxCheck>
-__device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord& L, const GenericEdges& G, uint32_t sx,
-                                             uint32_t sy, int lx, int ly, int32_t ox, int32_t oy) {
-    const int sx0 = L.px0 + (int)sx * kStampW, sy0 = L.py0 + (int)sy * kStampH;
+__device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord& L, const GenericEdges& G,
+                                             const GenericWalk& w, int lx, int ly, int32_t ox, int32_t oy) {
+    const int sx0 = w.sx0, sy0 = w.sy0;
     const int32_t PXo = sx0 * 256 + ox, PYo = sy0 * 256 + oy;
-    int64_t eo[3];
+    const int64_t* eo = w.e;
     bool reject = false, accept = true;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        eo[i] = G.c[i] + (int64_t)L.dx[i] * PYo - (int64_t)L.dy[i] * PXo;
         reject |= eo[i] + G.max_off[i] < 0;
         accept &= eo[i] + G.min_off[i] >= 0;
     }
@@ -880,13 +918,17 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
             } else {
                 GenericEdges G;
                 generic_edges(L, G);
-                uint32_t x = sx, y = sy;
-                for (uint32_t j = 0; j < n; ++j) {
-                    if (L.clipped) raster_stamp<kWriteId, true>(T, L, G, x, y, lx, ly, P.sample_x, P.sample_y);
-                    else raster_stamp<kWriteId, false>(T, L, G, x, y, lx, ly, P.sample_x, P.sample_y);
-                    if (++x == L.nsx) {
-                        x = 0;
-                        ++y;
+                GenericWalk w;
+                generic_start(L, G, sx, sy, P.sample_x, P.sample_y, w);
+                if (L.clipped) {
+                    for (uint32_t j = 0; j < n; ++j) {
+                        raster_stamp<kWriteId, true>(T, L, G, w, lx, ly, P.sample_x, P.sample_y);
+                        generic_next(L, w);
+                    }
+                } else {
+                    for (uint32_t j = 0; j < n; ++j) {
+                        raster_stamp<kWriteId, false>(T, L, G, w, lx, ly, P.sample_x, P.sample_y);
+                        generic_next(L, w);
                     }
                 }
             }
