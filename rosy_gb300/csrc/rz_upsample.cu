@@ -268,7 +268,7 @@ struct ConvSmem {
     static constexpr uint32_t A_OFF0 = (B_BYTES + 1023) / 1024 * 1024;
     static constexpr uint32_t A_OFF1 = A_OFF0 + (A_BYTES + 1023) / 1024 * 1024;
     static constexpr uint32_t BAR_OFF = A_OFF1 + (A_BYTES + 1023) / 1024 * 1024;
-    static constexpr uint32_t BYTES = BAR_OFF + 80;  // 8 barriers, the TMEM address
+    static constexpr uint32_t BYTES = BAR_OFF + 96;  // 9 barriers, the TMEM address
     static constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * kTileRows * N);  // two accumulators
 };
 static_assert(ConvSmem<32, 32>::BYTES <= 227 * 1024, "conv shared memory");
@@ -370,6 +370,14 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+// Untiled bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, completing on `bar` with its byte count.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                     "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
@@ -400,7 +408,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     uint64_t* empty = full + 2;                                        // [2]
     uint64_t* tfull = full + 4;                                        // [2]
     uint64_t* tempty = full + 6;                                       // [2]
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 64);
+    uint64_t* wbar = full + 8;                                         // the weights have landed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 80);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (a.W + kTileW - 1) / kTileW;
     const int ntiles = tiles_x * ((a.H + kTileRows - 1) / kTileRows);
@@ -416,17 +425,12 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             mbar_init(&tfull[b], 1);
             mbar_init(&tempty[b], kConvEpilogueWarps);
         }
+        mbar_init(wbar, 1);
     }
     if (EPI == kEpiFinal) {
         for (int i = tid; i < 256; i += kConvThreads) s_lut[i] = (float)i / 255.0f;
     }
     if (tid < N) s_bias[tid] = EPI == kEpiMask ? 0.0f : a.bias[tid];
-    {
-        const uint4* src = reinterpret_cast<const uint4*>(a.wimg);
-        for (int i = tid; i < (int)(L::B_BYTES / 16); i += kConvThreads) cp_async16(sB + 16 * i, src + i, true);
-    }
-    cp_async_wait_all();
-    fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -435,7 +439,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     float loss = 0.0f;
 
     if (warp == kConvEpilogueWarps && lane == 0) {
-        // producer: TMA loads of each tile's halo
+        // producer: the weights once (one bulk copy), then the TMA loads of each tile's halo
+        mbar_expect_tx(wbar, L::B_BYTES);
+        bulk_load(sB, a.wimg, L::B_BYTES, wbar);
         for (int j = 0; j < my_tiles && ok; ++j) {
             const int buf = j & 1;
             if (j >= 2 && !mbar_wait(&empty[buf], (uint32_t)((j - 2) >> 1) & 1u)) {
@@ -453,12 +459,14 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         // the copies still in flight land before the CTA exits
         for (int j = my_tiles - 2 > 0 ? my_tiles - 2 : 0; j < my_tiles; ++j)
             if (!mbar_wait(&full[j & 1], (uint32_t)(j >> 1) & 1u)) ok = false;
+        if (!mbar_wait(wbar, 0)) ok = false;
     } else if (warp == kConvEpilogueWarps + 1 && lane == 0) {
         // MMA issue
         constexpr uint32_t idesc = idesc_bf16(128, N);
         constexpr uint32_t lbo_b = N * 16;
         const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
-        for (int j = 0; j < my_tiles; ++j) {
+        if (my_tiles > 0 && !mbar_wait(wbar, 0)) ok = false;
+        for (int j = 0; j < my_tiles && ok; ++j) {
             const int buf = j & 1;
             if (!mbar_wait(&full[buf], (uint32_t)(j >> 1) & 1u) ||
                 (j >= 2 && !mbar_wait(&tempty[buf], (uint32_t)((j - 2) >> 1) & 1u))) {
