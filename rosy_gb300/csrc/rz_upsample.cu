@@ -205,6 +205,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 __device__ __forceinline__ float bf16_lo(uint32_t v) { return __uint_as_float(v << 16); }
 __device__ __forceinline__ float bf16_hi(uint32_t v) { return __uint_as_float(v & 0xFFFF0000u); }
 
+// Activations are stored planar by groups of 8 channels: [C / 8][H][W][8] bf16,
+// so a TMA box of one channel group over a row of pixels is one contiguous run.
+__device__ __forceinline__ size_t act_index(int W, int H, int x, int y, int c) {
+    return (((size_t)(c >> 3) * H + y) * W + x) * 8 + (c & 7);
+}
+
 // ---- features -----------------------------------------------------------------
 
 // One pixel's 16 input channels from the G-buffer (see rz_upsampler_* in the header).
@@ -231,24 +237,25 @@ __global__ void k_features(rz_gbuffer g, __nv_bfloat16* __restrict__ feat) {
     f[9] = fminf(d * 16.0f, 4.0f);
 #pragma unroll
     for (int k = 10; k < 16; ++k) f[k] = 0.0f;
-    uint4* dst = reinterpret_cast<uint4*>(feat + (size_t)i * kFeatChannels);
-    dst[0] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
-    dst[1] = make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]), pack_bf16(f[14], f[15]));
+    uint4* dst0 = reinterpret_cast<uint4*>(feat + (size_t)i * 8);
+    uint4* dst1 = reinterpret_cast<uint4*>(feat + (size_t)(n + i) * 8);
+    *dst0 = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+    *dst1 = make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]), pack_bf16(f[14], f[15]));
 }
 
 // ---- convolution (forward and input gradient) ---------------------------------
 
 struct ConvArgs {
-    const __nv_bfloat16* in;        // H x W x CIN
+    const __nv_bfloat16* in;        // planar [CIN / 8][H][W][8]
     const __nv_bfloat16* wimg;      // B operand image [9 * CIN / 8][N][8]
     const float* bias;              // N (relu, final)
     int W, H;
-    __nv_bfloat16* out;             // H x W x N (relu, mask)
-    const __nv_bfloat16* mask_src;  // H x W x N: out = acc where mask_src > 0, else 0 (mask)
+    __nv_bfloat16* out;             // planar [N / 8][H][W][8] (relu, mask)
+    const __nv_bfloat16* mask_src;  // planar like out: out = acc where mask_src > 0, else 0 (mask)
     const uint32_t* color_lr;       // H x W RGBA8: bilinear base (final)
     uint32_t* out_rgba8;            // 2H x 2W, or null (final)
     const uint32_t* target;         // 2H x 2W RGBA8, or null (final, training)
-    __nv_bfloat16* dy;              // H x W x 16: gradient of the loss sum (final, training)
+    __nv_bfloat16* dy;              // planar [2][H][W][8]: gradient of the loss sum (final, training)
     double* loss;                   // loss sum accumulator (final, training)
     uint32_t* err;
 };
@@ -283,16 +290,15 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
 #pragma unroll
         for (int c = 0; c < N / 2; ++c)
             pk[c] = pack_bf16(fmaxf(acc[2 * c] + bias[2 * c], 0.0f), fmaxf(acc[2 * c + 1] + bias[2 * c + 1], 0.0f));
-        uint4* dst = reinterpret_cast<uint4*>(a.out + ((size_t)y * a.W + x) * N);
 #pragma unroll
-        for (int q = 0; q < N / 8; ++q) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+        for (int q = 0; q < N / 8; ++q)
+            *reinterpret_cast<uint4*>(a.out + act_index(a.W, a.H, x, y, 8 * q)) =
+                make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
     } else if (EPI == kEpiMask) {
         if (!inside) return;
-        const uint4* ms = reinterpret_cast<const uint4*>(a.mask_src + ((size_t)y * a.W + x) * N);
-        uint4* dst = reinterpret_cast<uint4*>(a.out + ((size_t)y * a.W + x) * N);
 #pragma unroll
         for (int q = 0; q < N / 8; ++q) {
-            const uint4 m = __ldg(ms + q);
+            const uint4 m = __ldg(reinterpret_cast<const uint4*>(a.mask_src + act_index(a.W, a.H, x, y, 8 * q)));
             const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
             uint32_t o[4];
 #pragma unroll
@@ -300,7 +306,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
                 const int c = 8 * q + 2 * h;
                 o[h] = pack_bf16(bf16_lo(mw[h]) > 0.0f ? acc[c] : 0.0f, bf16_hi(mw[h]) > 0.0f ? acc[c + 1] : 0.0f);
             }
-            dst[q] = make_uint4(o[0], o[1], o[2], o[3]);
+            *reinterpret_cast<uint4*>(a.out + act_index(a.W, a.H, x, y, 8 * q)) = make_uint4(o[0], o[1], o[2], o[3]);
         }
     } else {  // final: pixel shuffle + bilinear base (+ loss gradient)
         if (!inside) return;
@@ -354,19 +360,21 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
             if (a.out_rgba8) *reinterpret_cast<uint2*>(a.out_rgba8 + op) = make_uint2(o[0], o[1]);
         }
         if (a.target) {
-            uint4* dst = reinterpret_cast<uint4*>(a.dy + ((size_t)y * W + x) * 16);
-            dst[0] = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]), pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
-            dst[1] = make_uint4(pack_bf16(g[8], g[9]), pack_bf16(g[10], g[11]), 0u, 0u);
+            *reinterpret_cast<uint4*>(a.dy + act_index(W, H, x, y, 0)) =
+                make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]), pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
+            *reinterpret_cast<uint4*>(a.dy + act_index(W, H, x, y, 8)) =
+                make_uint4(pack_bf16(g[8], g[9]), pack_bf16(g[10], g[11]), 0u, 0u);
         }
     }
 }
 
-// TMA load of one box {8 channels, 130 pixels, 1 row} of an NHWC bf16 tensor
-// into shared memory, completing on `bar` with its byte count.
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c, int x, int y) {
+// TMA load of one box {8 channels, 130 pixels, 1 row, 1 channel group} of a
+// planar [C / 8][H][W][8] bf16 tensor into shared memory, completing on `bar`
+// with its byte count.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int g) {
     asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
-            "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c), "r"(x), "r"(y)
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], [%2];" ::
+            "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(0), "r"(x), "r"(y), "r"(g)
         : "memory");
 }
 
@@ -454,7 +462,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             mbar_expect_tx(&full[buf], L::TX_BYTES);
             for (int r = 0; r < kTileRows + 2; ++r)
 #pragma unroll
-                for (int g = 0; g < L::G; ++g) tma_load_3d(A + r * L::S_R + g * L::S_G, &in_map, &full[buf], 8 * g, x0 - 1, y0 - 1 + r);
+                for (int g = 0; g < L::G; ++g) tma_load_4d(A + r * L::S_R + g * L::S_G, &in_map, &full[buf], x0 - 1, y0 - 1 + r, g);
         }
         // the copies still in flight land before the CTA exits
         for (int j = my_tiles - 2 > 0 ? my_tiles - 2 : 0; j < my_tiles; ++j)
@@ -536,8 +544,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
 // ---- weight gradient ------------------------------------------------------------
 
 struct WgradArgs {
-    const __nv_bfloat16* x;   // H x W x CIN: the layer's input
-    const __nv_bfloat16* dy;  // H x W x N: gradient of the loss sum w.r.t. the layer's pre-activation output
+    const __nv_bfloat16* x;   // planar [CIN / 8][H][W][8]: the layer's input
+    const __nv_bfloat16* dy;  // planar [N / 8][H][W][8]: gradient of the loss sum w.r.t. the pre-activation output
     float* dw;                // [N][9][CIN], accumulated
     float* db;                // [N], accumulated
     int W, H;
@@ -602,7 +610,7 @@ __global__ void __launch_bounds__(kThreads) k_wgrad(WgradArgs a) {
             for (int j = 0; j < 10; ++j) {
                 const int x = xs + j;
                 v[j] = (y >= 0 && y < a.H && x >= 0 && x < a.W)
-                           ? __bfloat162float(a.x[((size_t)y * a.W + x) * CIN + ci])
+                           ? __bfloat162float(a.x[act_index(a.W, a.H, x, y, ci)])
                            : 0.0f;
             }
 #pragma unroll
@@ -621,7 +629,7 @@ __global__ void __launch_bounds__(kThreads) k_wgrad(WgradArgs a) {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int x = x0 + 8 * pxg + j;
-                v[j] = (y < a.H && x < a.W) ? __bfloat162float(a.dy[((size_t)y * a.W + x) * N + co]) : 0.0f;
+                v[j] = (y < a.H && x < a.W) ? __bfloat162float(a.dy[act_index(a.W, a.H, x, y, co)]) : 0.0f;
                 dbsum += v[j];
             }
             *reinterpret_cast<uint4*>(sD + r * L::S_DYROW + (co / 8) * L::S_COG + pxg * 128 + (co % 8) * 16) =
@@ -859,16 +867,16 @@ void load_encode_tiled() {
         g_encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
 }
 
-// Tensor map of an H x W x C bf16 NHWC tensor with boxes of {8 channels, kHaloW pixels, 1 row};
-// out-of-range elements read as zero.
-bool encode_nhwc(CUtensorMap* map, const void* base, int C, int W, int H) {
+// Tensor map of a planar [C / 8][H][W][8] bf16 tensor with boxes of {8 channels,
+// kHaloW pixels, 1 row, 1 group}; out-of-range elements read as zero.
+bool encode_planar(CUtensorMap* map, const void* base, int C, int W, int H) {
     std::call_once(g_encode_once, load_encode_tiled);
     if (!g_encode_tiled) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H};
-    const cuuint64_t strides[2] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2};
-    const cuuint32_t box[3] = {8, (cuuint32_t)kHaloW, 1};
-    const cuuint32_t elem[3] = {1, 1, 1};
-    return g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, elem,
+    const cuuint64_t dims[4] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)(C / 8)};
+    const cuuint64_t strides[3] = {16, (cuuint64_t)W * 16, (cuuint64_t)W * H * 16};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kHaloW, 1, 1};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    return g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, elem,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -876,7 +884,7 @@ bool encode_nhwc(CUtensorMap* map, const void* base, int C, int W, int H) {
 template <int CIN, int N, int EPI>
 bool launch_conv(const rz_upsampler* u, const ConvArgs& a, cudaStream_t s) {
     CUtensorMap map;
-    if (!encode_nhwc(&map, a.in, CIN, a.W, a.H)) return false;
+    if (!encode_planar(&map, a.in, CIN, a.W, a.H)) return false;
     const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileRows - 1) / kTileRows);
     const int grid = std::min(tiles, std::max(u->sms, 1));
     k_conv<CIN, N, EPI><<<grid, kConvThreads, ConvSmem<CIN, N>::BYTES, s>>>(a, map);
