@@ -89,6 +89,59 @@ def learned_block(frames: int = 64, cameras: int = 256, samples: int = 1) -> dic
     }
 
 
+def bc7_block(size: int = 8192, reps: int = 10) -> dict:
+    """BC7 decode (rz_bc7_decode, the upload-time decode of the reference's BC7
+    images) of one size x size image whose blocks cycle through every mode:
+    device time per decode with the L2 flushed between decodes, the HBM roofline
+    over the algorithmic bytes (16 read + 64 written per 4x4 block), and the
+    scalar oracle's decode rate on one host core for comparison."""
+    import ctypes as C
+
+    import torch
+
+    from oracle import oracle
+    from rosy_gb300 import _lib, bc7
+
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    base = bc7.mixed_blocks(rng, 4096)
+    nblk = (size // 4) ** 2
+    blocks = torch.from_numpy(base[rng.integers(0, len(base), nblk)].reshape(-1)).cuda()
+    out = torch.empty(size * size, dtype=torch.int32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    for _ in range(3):
+        assert lib.rz_bc7_decode(C.c_void_p(blocks.data_ptr()), size, size, C.c_void_p(out.data_ptr()), sp) == 0
+    times = []
+    for _ in range(reps):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        lib.rz_bc7_decode(C.c_void_p(blocks.data_ptr()), size, size, C.c_void_p(out.data_ptr()), sp)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = float(np.median(times))
+    algo = nblk * (16 + 64)
+    peak, src = peaks()
+    gbs = algo / (ms * 1e-3) / 1e9
+    # the oracle on one core, a 512 x 512 sample of the same blocks
+    host = blocks[: (128 * 128) * 16].cpu().numpy()
+    t0 = time.perf_counter()
+    oracle.bc7_decode(host, 512, 512)
+    cpu_s = time.perf_counter() - t0
+    return {
+        "workload": f"{size}x{size} texels ({nblk} BC7 blocks, modes 0-7 cycling), L2 flushed between decodes",
+        "ms": round(ms, 5), "gtexels_per_s": round(size * size / (ms * 1e-3) / 1e9, 2),
+        "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(gbs / peak, 4), "peak_source": src,
+                     "algorithmic_bytes": algo, "bytes_note": "16 B read + 64 B written per block"},
+        "cpu_oracle": {"mtexels_per_s": round(512 * 512 / cpu_s / 1e6, 2), "cores": 1,
+                       "sample": "512x512 texels of the same blocks, scalar oracle"},
+    }
+
+
 def measured_traffic(stage: str):
     """DRAM bytes per launch of a kernel from the committed ncu summary of this
     workload (profiles/dram_traffic_scene_scale_1080p.json), or None."""
@@ -430,6 +483,7 @@ def run_rz(args):
         if not args.no_learned:
             line["learned_upsample"] = learned_block()
             line["learned_upsample_msaa4"] = learned_block(samples=4)
+        line["bc7_decode"] = bc7_block()
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist

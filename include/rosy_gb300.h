@@ -121,15 +121,26 @@ typedef struct rz_sampler {
 #define RZ_IMAGE_METALLIC_ROUGHNESS 2u
 #define RZ_IMAGE_MIXMAP 3u
 
-/* A texture: RGBA8 texels of `levels` mip levels, concatenated level 0 first;
- * level l is max(1, width>>l) x max(1, height>>l), rows top to bottom.
- * (The reference loads BC7 .dds mips; decoded RGBA8 stands in for them.) */
+/* Texel formats of rz_texture.format. */
+#define RZ_TEXELS_RGBA8 0u /* 4 bytes per texel */
+#define RZ_TEXELS_BC7 1u   /* BC7 blocks: what the reference's .dds images hold */
+
+/* A texture of `levels` mip levels, concatenated level 0 first; level l is
+ * max(1, width>>l) x max(1, height>>l) texels, rows top to bottom.
+ * RZ_TEXELS_RGBA8: 4 bytes per texel. RZ_TEXELS_BC7: 16-byte BC7 blocks, level
+ * l is max(1, (w_l+3)/4) x max(1, (h_l+3)/4) blocks in rows top to bottom, the
+ * layout of a .dds file's mips (src/libs/dds.hpp:550-566) — the reference
+ * uploads these as VK_FORMAT_BC7_{SRGB,UNORM}_BLOCK images
+ * (src/Engine/Graphics.cpp:3632-3647); rz_set_asset decodes them on the
+ * device into RGBA8 (rz_bc7_decode), which the shading samples. */
 typedef struct rz_texture {
     uint32_t width;
     uint32_t height;
     uint32_t levels;
     uint32_t image_type;
     const void* texels;
+    uint32_t format;   /* RZ_TEXELS_RGBA8 (0) or RZ_TEXELS_BC7 */
+    uint32_t reserved; /* 0 */
 } rz_texture;
 
 /* Per-object transforms: graphic_object_data (src/Engine/Graphics.cpp:422-427),
@@ -469,6 +480,52 @@ int rz_rsy_get_image(const struct rz_rsy* asset, uint32_t index, uint32_t* image
  * RZ_INVALID_ARGUMENT if the root scene or a node index is out of range. */
 int rz_rsy_get_scene(const struct rz_rsy* asset, rz_object* objects, uint32_t object_capacity, rz_surface* surfaces,
                      uint32_t surface_capacity);
+
+/* ---- .dds images and BC7 -----------------------------------------------------
+ * Reader for the .dds files the engine loads for every asset image
+ * (src/Engine/Graphics.cpp:3605-3647 through dds::readFile / dds::readImage,
+ * src/libs/dds.hpp:409-596). rz_dds_read replaces dds::readFile and
+ * rz_dds_parse dds::readImage, with the same checks and one more: the file
+ * must hold every mip level its header announces (dds::readImage points its
+ * mip spans past the end of a short file). Results: RZ_OPEN_FAILED (file cannot
+ * be opened); RZ_READ_FAILED (shorter than the magic and header, wrong magic:
+ * ReadResult::Failure; a DX10 file shorter than 148 bytes, a zero width or
+ * height, or mips past the end of the file: ReadResult::InvalidSize);
+ * RZ_INVALID_ARGUMENT (a format other than BC7, or an array of more than one
+ * image: ReadResult::UnsupportedFormat — the engine uploads every image as BC7,
+ * Graphics.cpp:3632-3647). */
+struct rz_dds;
+typedef struct rz_dds rz_dds;
+
+typedef struct rz_dds_info {
+    uint32_t width;
+    uint32_t height;
+    uint32_t levels;         /* max(1, mipmapCount), as dds::Image::numMips */
+    uint32_t dxgi_format;    /* the DX10 header's format: 97 BC7_TYPELESS, 98 BC7_UNORM, 99 BC7_UNORM_SRGB */
+    uint32_t supports_alpha; /* DDPF_ALPHAPIXELS of the pixel format (dds::Image::supportsAlpha) */
+    uint32_t reserved;
+    uint64_t data_bytes;     /* bytes of all levels */
+    const void* data;        /* the levels' BC7 blocks, level 0 first; valid until rz_dds_free */
+} rz_dds_info;
+
+int rz_dds_read(const char* path, struct rz_dds** out);
+int rz_dds_parse(const void* bytes, uint64_t size, struct rz_dds** out); /* copies the bytes */
+void rz_dds_free(struct rz_dds* image);
+int rz_dds_get_info(const struct rz_dds* image, rz_dds_info* out);
+
+/* Decodes one image of BC7 blocks (device memory, max(1,(w+3)/4) x
+ * max(1,(h+3)/4) blocks in rows) into width x height RGBA8 texels (device
+ * memory, rows of width * 4 bytes), enqueued on `stream` (a cudaStream_t, NULL =
+ * default stream). Decoding follows the
+ * BC7 format exactly (every texel equals what the GPU's texture unit decodes
+ * from the same block; the reserved mode decodes to 0,0,0,0). */
+int rz_bc7_decode(const void* blocks, uint32_t width, uint32_t height, void* rgba8, void* stream);
+
+/* The same image decoded by the GPU's texture unit (a BC7 CUDA array sampled
+ * at texel centres), synchronously: the hardware decoder the reference's
+ * VK_FORMAT_BC7_*_BLOCK images go through, for checking rz_bc7_decode. Width
+ * and height must be multiples of 4. */
+int rz_bc7_decode_texture_unit(const void* blocks, uint32_t width, uint32_t height, void* rgba8);
 
 /* ---- G-buffer ------------------------------------------------------------
  * Inputs of the learned upsampler. The reference has no G-buffer (it shades

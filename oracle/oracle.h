@@ -59,6 +59,12 @@ int oracle_render(const oracle_scene* scene, oracle_out* out, int threads);
 /* Only the raster passes: the shadow map and the camera pass's depth/ids. */
 int oracle_raster(const oracle_scene* scene, oracle_out* out, int threads);
 
+/* BC7 (bc7_oracle.cpp): one 16-byte block to 16 RGBA8 texels (row-major), and
+ * one image of max(1,(w+3)/4) x max(1,(h+3)/4) blocks in rows to w x h RGBA8.
+ * oracle_render decodes the scene's RZ_TEXELS_BC7 textures with it first. */
+void oracle_bc7_block(const uint8_t block[16], uint8_t out[64]);
+int oracle_bc7_decode(const uint8_t* blocks, uint32_t width, uint32_t height, uint8_t* rgba);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,7 +22,7 @@ from rosy_gb300._abi import Marshalled, ptr  # noqa: E402
 
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "librz_oracle.so")
-SOURCES = [os.path.join(HERE, "rz_oracle.cpp")]
+SOURCES = [os.path.join(HERE, "rz_oracle.cpp"), os.path.join(HERE, "bc7_oracle.cpp")]
 
 
 def build(force: bool = False) -> str:
@@ -70,6 +70,8 @@ def lib():
         for fn in (_lib.oracle_render, _lib.oracle_raster):
             fn.argtypes = [C.POINTER(OracleScene), C.POINTER(OracleOut), C.c_int]
             fn.restype = C.c_int
+        _lib.oracle_bc7_decode.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+        _lib.oracle_bc7_decode.restype = C.c_int
     return _lib
 
 
@@ -157,4 +159,16 @@ def raster(s, threads: int = 0) -> dict:
     rc = lib().oracle_raster(C.byref(o), C.byref(oo), int(threads))
     if rc != 0:
         raise RuntimeError(f"oracle_raster failed: {rc}")
+    return out
+
+
+def bc7_decode(blocks: np.ndarray, width: int, height: int) -> np.ndarray:
+    """One image of BC7 blocks (bytes, max(1,(w+3)/4) x max(1,(h+3)/4) blocks in
+    rows) decoded to (height, width, 4) RGBA8 by the scalar restatement."""
+    b = np.ascontiguousarray(blocks, np.uint8).reshape(-1)
+    need = max(1, (width + 3) // 4) * max(1, (height + 3) // 4) * 16
+    assert b.size >= need, (b.size, need)
+    out = np.zeros((height, width, 4), np.uint8)
+    rc = lib().oracle_bc7_decode(ptr(b), width, height, ptr(out))
+    assert rc == 0, rc
     return out

@@ -1254,7 +1254,40 @@ extern "C" int oracle_raster(const oracle_scene* s, oracle_out* out, int threads
     return 0;
 }
 
+static int render_rgba8(const oracle_scene* s, oracle_out* out, int threads);
+
+// BC7 textures are decoded to RGBA8 level by level first, as the renderer does
+// when it uploads them; the frame is then rendered from RGBA8 texels only.
 extern "C" int oracle_render(const oracle_scene* s, oracle_out* out, int threads) {
+    if (!s || !out) return 3;
+    bool any_bc7 = false;
+    for (uint32_t i = 0; i < s->texture_count; ++i) any_bc7 = any_bc7 || s->textures[i].format == RZ_TEXELS_BC7;
+    if (!any_bc7) return render_rgba8(s, out, threads);
+    std::vector<rz_texture> tex(s->textures, s->textures + s->texture_count);
+    std::vector<std::vector<uint8_t>> texels(s->texture_count);
+    for (uint32_t i = 0; i < s->texture_count; ++i) {
+        rz_texture& t = tex[i];
+        if (t.format != RZ_TEXELS_BC7) continue;
+        size_t n = 0;
+        for (uint32_t l = 0; l < t.levels; ++l) n += (size_t)std::max(1u, t.width >> l) * std::max(1u, t.height >> l);
+        texels[i].resize(n * 4);
+        const uint8_t* blocks = static_cast<const uint8_t*>(t.texels);
+        size_t texel_off = 0, block_off = 0;
+        for (uint32_t l = 0; l < t.levels; ++l) {
+            const uint32_t w = std::max(1u, t.width >> l), h = std::max(1u, t.height >> l);
+            oracle_bc7_decode(blocks + block_off, w, h, texels[i].data() + 4 * texel_off);
+            texel_off += (size_t)w * h;
+            block_off += (size_t)((w + 3) / 4) * ((h + 3) / 4) * 16;
+        }
+        t.texels = texels[i].data();
+        t.format = RZ_TEXELS_RGBA8;
+    }
+    oracle_scene decoded = *s;
+    decoded.textures = tex.data();
+    return render_rgba8(&decoded, out, threads);
+}
+
+static int render_rgba8(const oracle_scene* s, oracle_out* out, int threads) {
     if (!s || !out) return 3;
     threads = threads_or_default(threads);
     Ctx c;

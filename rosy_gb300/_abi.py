@@ -20,7 +20,12 @@ class RzMesh(C.Structure):
 
 class RzTexture(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32),
-                ("image_type", C.c_uint32), ("texels", C.c_void_p)]
+                ("image_type", C.c_uint32), ("texels", C.c_void_p), ("format", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+TEXELS_RGBA8 = 0
+TEXELS_BC7 = 1
 
 
 class RzConfig(C.Structure):
@@ -64,6 +69,12 @@ class RzRsyInfo(C.Structure):
                 ("static_object_count", C.c_uint32), ("coordinate_system", C.c_float * 16)]
 
 
+class RzDdsInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32),
+                ("dxgi_format", C.c_uint32), ("supports_alpha", C.c_uint32), ("reserved", C.c_uint32),
+                ("data_bytes", C.c_uint64), ("data", C.c_void_p)]
+
+
 class RzStats(C.Structure):
     _fields_ = [("draw_call_count", C.c_uint32), ("triangle_count", C.c_uint32),
                 ("shadow_setup_records", C.c_uint32), ("camera_setup_records", C.c_uint32),
@@ -74,7 +85,8 @@ class RzStats(C.Structure):
 assert C.sizeof(RzVertex) == 64
 assert C.sizeof(RzView) == 48
 assert C.sizeof(RzMesh) == 24
-assert C.sizeof(RzTexture) == 24
+assert C.sizeof(RzTexture) == 32
+assert C.sizeof(RzDdsInfo) == 40
 
 
 def ptr(a: np.ndarray) -> int:
@@ -108,6 +120,7 @@ class Marshalled:
             self.textures[i].levels = t.levels
             self.textures[i].image_type = t.image_type
             self.textures[i].texels = ptr(self.tex_data[i])
+            self.textures[i].format = getattr(t, "format", TEXELS_RGBA8)
         self.scene_rec = np.ascontiguousarray(s.scene)
         self.draw_config = np.ascontiguousarray(s.draw_config)
 

@@ -31,6 +31,7 @@ EXPORTS = [
     "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads", "rz_upsampler_adam_step",
     "rz_upsampler_status", "rz_upsampler_selftest_gemm", "rz_rsy_read", "rz_rsy_free", "rz_rsy_get_info",
     "rz_rsy_get_meshes", "rz_rsy_get_materials", "rz_rsy_get_samplers", "rz_rsy_get_image", "rz_rsy_get_scene",
+    "rz_dds_read", "rz_dds_parse", "rz_dds_free", "rz_dds_get_info", "rz_bc7_decode", "rz_bc7_decode_texture_unit",
 ]
 
 _lib = None
@@ -119,6 +120,15 @@ def load(build_if_missing: bool = False):
     lib.rz_rsy_get_scene.argtypes = [P, P, u32, P, u32]
     for name in ("rz_rsy_read", "rz_rsy_get_info", "rz_rsy_get_meshes", "rz_rsy_get_materials", "rz_rsy_get_samplers",
                  "rz_rsy_get_image", "rz_rsy_get_scene"):
+        getattr(lib, name).restype = C.c_int
+    lib.rz_dds_read.argtypes = [C.c_char_p, C.POINTER(P)]
+    lib.rz_dds_parse.argtypes = [P, C.c_uint64, C.POINTER(P)]
+    lib.rz_dds_free.argtypes = [P]
+    lib.rz_dds_free.restype = None
+    lib.rz_dds_get_info.argtypes = [P, C.POINTER(_abi.RzDdsInfo)]
+    lib.rz_bc7_decode.argtypes = [P, u32, u32, P, P]
+    lib.rz_bc7_decode_texture_unit.argtypes = [P, u32, u32, P]
+    for name in ("rz_dds_read", "rz_dds_parse", "rz_dds_get_info", "rz_bc7_decode", "rz_bc7_decode_texture_unit"):
         getattr(lib, name).restype = C.c_int
     lib.rz_abi_version.argtypes = []
     lib.rz_abi_version.restype = u32

@@ -18,7 +18,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "librosy_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["rz_api.cu", "rz_raster.cu", "rz_shade.cu", "rz_static.cu", "rz_upsample.cu", "rz_rsy.cpp"]
+SOURCES = ["rz_api.cu", "rz_raster.cu", "rz_shade.cu", "rz_static.cu", "rz_upsample.cu", "rz_bc7.cu", "rz_rsy.cpp", "rz_dds.cpp"]
 HEADERS = ["rz_internal.h", "rz_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",

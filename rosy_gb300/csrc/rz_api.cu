@@ -301,7 +301,8 @@ int append_asset(rz_ctx* c, const rz_mesh* meshes, uint32_t mesh_count, const rz
     if (nv >= 0xFFFFFFFFull || ni >= 0xFFFFFFFFull) return fail(c, RZ_OVERFLOW, "asset too large");
     for (uint32_t i = 0; i < tex_count; ++i) {
         const rz_texture& t = textures[i];
-        if (t.width == 0 || t.height == 0 || t.levels == 0 || t.levels > 16 || !t.texels)
+        if (t.width == 0 || t.height == 0 || t.levels == 0 || t.levels > 16 || !t.texels ||
+            (t.format != RZ_TEXELS_RGBA8 && t.format != RZ_TEXELS_BC7))
             return fail(c, RZ_INVALID_ARGUMENT, "texture " + std::to_string(i) + " is malformed");
         uint32_t max_levels = 1;
         while ((t.width >> max_levels) || (t.height >> max_levels)) ++max_levels;
@@ -366,7 +367,19 @@ int append_asset(rz_ctx* c, const rz_mesh* meshes, uint32_t mesh_count, const rz
         uint32_t* dp = nullptr;
         RZ_CUDA(c, dalloc(&dp, (size_t)off), "texture");
         c->tex_allocs.push_back(dp);
-        RZ_CUDA(c, cudaMemcpy(dp, t.texels, (size_t)off * 4, cudaMemcpyHostToDevice), "upload texels");
+        if (t.format == RZ_TEXELS_BC7) {
+            // the blocks go through a staging buffer and are decoded into the RGBA8 texels
+            const uint64_t nb = bc7_chain_bytes(t.width, t.height, t.levels);
+            void* staging = nullptr;
+            RZ_CUDA(c, cudaMalloc(&staging, nb), "BC7 staging");
+            cudaError_t e = cudaMemcpy(staging, t.texels, nb, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = bc7_decode_chain(staging, t.width, t.height, t.levels, d.level_off, dp, 0);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+            cudaFree(staging);
+            RZ_CUDA(c, e, "BC7 decode");
+        } else {
+            RZ_CUDA(c, cudaMemcpy(dp, t.texels, (size_t)off * 4, cudaMemcpyHostToDevice), "upload texels");
+        }
         d.base = reinterpret_cast<uint64_t>(dp);
         c->tex_descs.push_back(d);
     }

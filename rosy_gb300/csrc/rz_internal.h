@@ -220,6 +220,12 @@ void launch_vertex(const ShadeParams& p, cudaStream_t stream);
 void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stream);
 void launch_blend(const BlendParams& p, cudaStream_t stream);
 void launch_shade(const ShadeParams& p, cudaStream_t stream);
+
+// BC7 (rz_bc7.cu): bytes of a mip chain's blocks, and the decode of a chain
+// (device blocks) into RGBA8 texels (device, level l starting at level_off[l]).
+uint64_t bc7_chain_bytes(uint32_t width, uint32_t height, uint32_t levels);
+cudaError_t bc7_decode_chain(const void* blocks, uint32_t width, uint32_t height, uint32_t levels,
+                             const uint32_t* level_off, uint32_t* texels, cudaStream_t stream);
 int setup_ctas(uint32_t tri_total);
 
 }  // namespace rz

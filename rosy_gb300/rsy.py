@@ -170,13 +170,41 @@ class RsyFile:
         return objs, surfs
 
 
+def _load_images(path: str, imgs: list[tuple[int, str]]) -> tuple[list, list[str]]:
+    """One texture per asset image: the named .dds file read as BC7 (the name as
+    given, else relative to the .rsy file's folder), or, where no such file can
+    be read, a 1x1 white texture of the image's type — the engine warns and
+    skips an unreadable image (src/Engine/Graphics.cpp:3609-3613)."""
+    import os
+
+    from .dds import texture_from_dds
+
+    out, missing = [], []
+    base = os.path.dirname(os.path.abspath(path))
+    for kind, name in imgs:
+        tex = None
+        for cand in (name, os.path.join(base, name)):
+            if name and os.path.isfile(cand):
+                try:
+                    tex = texture_from_dds(cand, kind)
+                    break
+                except _lib.RzError:
+                    pass
+        if tex is None:
+            missing.append(name)
+            tex = sc.Texture(1, 1, 1, kind, np.full(4, 255, np.uint8))
+        out.append(tex)
+    return out, missing
+
+
 def scene_from_rsy(path: str, textures: list | None = None, width: int = 640, height: int = 360,
                    shadow_size: int = 1024, camera_position=(0.0, 0.0, 3.0), sun_direction=(0.3, 1.0, 0.2)) -> sc.Scene:
-    """A renderable Scene from an .rsy file. The asset's images are named files
-    the engine decodes separately (BC7 .dds), so `textures` supplies one
-    scene.Texture per image; without it every image is a 1x1 white texture of
-    its type. Camera and light are the given ones (the level supplies them in
-    the engine)."""
+    """A renderable Scene from an .rsy file. The asset's images are named .dds
+    files; without `textures` (one scene.Texture per image) they are read as BC7
+    textures (decoded on the device when the scene is uploaded), and an image
+    whose file is missing becomes a 1x1 white texture of its type (the scene's
+    `missing_images` lists them). Camera and light are the given ones (the level
+    supplies them in the engine)."""
     f = RsyFile(path)
     try:
         meshes = f.meshes()
@@ -193,15 +221,18 @@ def scene_from_rsy(path: str, textures: list | None = None, width: int = 640, he
         table.append((vo, len(p), io, len(i)))
         vo += len(p)
         io += len(i)
+    missing: list[str] = []
     if textures is None:
-        textures = [sc.Texture(1, 1, 1, t, np.full(4, 255, np.uint8)) for t, _ in imgs]
+        textures, missing = _load_images(path, imgs)
     sun_position, spn = sc.sun_matrices(np.asarray(sun_direction, np.float64))
     view = sc.camera_look_at_origin(camera_position)
     import math
 
     rec = sc.scene_record(view, sc.projection(width / height, math.radians(60.0)), sun_position, spn,
                           np.asarray(camera_position, np.float64), width, height)
-    return sc.Scene(name=f"rsy:{path}", width=width, height=height, shadow_size=shadow_size, vertices=verts,
-                    indices=idx, meshes=table, objects=objs, surfaces=surfs, materials=mats, textures=list(textures),
-                    samplers=smps if len(smps) else sc.linear_sampler(), scene=rec,
-                    draw_config=sc.default_draw_config(), cameras=[rec])
+    out = sc.Scene(name=f"rsy:{path}", width=width, height=height, shadow_size=shadow_size, vertices=verts,
+                   indices=idx, meshes=table, objects=objs, surfaces=surfs, materials=mats, textures=list(textures),
+                   samplers=smps if len(smps) else sc.linear_sampler(), scene=rec,
+                   draw_config=sc.default_draw_config(), cameras=[rec])
+    out.missing_images = missing
+    return out

@@ -103,7 +103,8 @@ class Texture:
     height: int
     levels: int
     image_type: int
-    texels: np.ndarray  # uint8, all levels concatenated (RGBA8)
+    texels: np.ndarray  # uint8, all levels concatenated (RGBA8, or BC7 blocks when format is 1)
+    format: int = 0     # 0 RGBA8, 1 BC7 blocks
 
     def level_offset(self, level: int) -> int:
         off = 0
