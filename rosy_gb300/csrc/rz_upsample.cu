@@ -52,9 +52,14 @@ namespace up {
 constexpr int kThreads = 128;      // weight-gradient and self-test kernels
 constexpr int kConvEpilogueWarps = 16;  // convolution: one epilogue warp per (TMEM lane quadrant, tile row),
 constexpr int kConvThreads = 32 * (kConvEpilogueWarps + 2);  // then a TMA warp and an MMA warp
-constexpr int kTileW = 128;  // conv: output pixels per MMA tile (M = 128), one row segment
+constexpr int kTileW = 128;  // conv: MMA rows (M = 128), one row segment of output pixels
 constexpr int kTileRows = 4; // conv: output rows per tile (8 measured 4% slower)
-constexpr int kHaloW = kTileW + 2;
+constexpr int kConvStages = 4; // conv: halo buffers in flight (TMA loads ahead of the MMAs)
+// conv: pixels of one halo row = one TMA box of 256 8-byte elements (2,048 bytes, the
+// largest box); a tile row yields kTileOut valid outputs, and MMA rows kTileOut and
+// kTileOut + 1 (whose 3x3 window runs past the halo) are computed and dropped
+constexpr int kHaloW = kTileW;
+constexpr int kTileOut = kHaloW - 2;
 constexpr int kWgKP = 64;    // weight gradient: pixels per tile row (K chunk)
 constexpr int kWgRows = 4;   // weight gradient: rows per tile
 constexpr long long kWaitCycles = 2000000000ll;  // about one second at 2 GHz
@@ -263,26 +268,30 @@ struct ConvArgs {
 };
 
 // Shared memory of the persistent convolution: the weights (B operand) once,
-// then two halo buffers (A operand) that alternate between tiles. Each halo
-// buffer is (kTileRows + 2) rows x (CIN / 8) channel planes x 130 pixels x 16
-// bytes; a plane is padded to a multiple of 128 bytes because TMA writes it.
+// then kConvStages halo buffers (A operand) that tiles take in turn. Each halo
+// buffer is (kTileRows + 2) rows x (CIN / 8) channel planes x kHaloW pixels x 16
+// bytes; a plane is padded by two pixels (read by the dropped MMA rows, never
+// written) and to a multiple of 128 bytes.
 template <int CIN, int N>
 struct ConvSmem {
     static constexpr int G = CIN / 8;
-    static constexpr uint32_t S_G = (kHaloW * 16 + 127) / 128 * 128;  // between channel planes (K direction)
+    static constexpr uint32_t S_G = ((kHaloW + 2) * 16 + 127) / 128 * 128;  // between channel planes (K direction)
     static constexpr uint32_t S_R = G * S_G;                          // between halo rows
     static constexpr uint32_t A_BYTES = (kTileRows + 2) * S_R;
     static constexpr uint32_t TX_BYTES = (kTileRows + 2) * G * kHaloW * 16;  // what one tile's TMA loads write
     static constexpr uint32_t B_BYTES = 9 * CIN * N * 2;
     static constexpr uint32_t A_OFF0 = (B_BYTES + 1023) / 1024 * 1024;
-    static constexpr uint32_t A_OFF1 = A_OFF0 + (A_BYTES + 1023) / 1024 * 1024;
-    static constexpr uint32_t BAR_OFF = A_OFF1 + (A_BYTES + 1023) / 1024 * 1024;
-    static constexpr uint32_t BYTES = BAR_OFF + 96;  // 9 barriers, the TMEM address
+    static constexpr uint32_t A_STRIDE = (A_BYTES + 1023) / 1024 * 1024;  // between halo buffers
+    static constexpr uint32_t BAR_OFF = A_OFF0 + kConvStages * A_STRIDE;
+    static constexpr uint32_t NBAR = 2 * kConvStages + 5;                // full, empty, tfull[2], tempty[2], weights
+    static constexpr uint32_t BYTES = BAR_OFF + NBAR * 8 + 16;           // the barriers, the TMEM address
     static constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * kTileRows * N);  // two accumulators
 };
-static_assert(ConvSmem<32, 32>::BYTES + 2048 <= 227 * 1024, "conv shared memory");
+static_assert(ConvSmem<32, 32>::BYTES + 2048 <= 227 * 1024, "conv shared memory (with the static arrays)");
 static_assert(2 * kTileRows * 32 <= 512, "two accumulators fit the 512 TMEM columns");
 static_assert(kTileRows * 4 % kConvEpilogueWarps == 0, "epilogue warps split the tile rows evenly");
+static_assert(2 * kHaloW <= 256, "a halo row is one TMA box (at most 256 elements)");
+static_assert(ConvSmem<32, 32>::S_G % 128 == 0 && ConvSmem<16, 32>::S_R % 128 == 0, "TMA destinations 128-byte aligned");
 
 template <int N, int EPI>
 __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss,
@@ -372,13 +381,14 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
     }
 }
 
-// TMA load of one box {8 channels, 130 pixels, 1 row, 1 channel group} of a
-// planar [C / 8][H][W][8] bf16 tensor into shared memory, completing on `bar`
-// with its byte count.
-__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int g) {
+// TMA load of one box {256 8-byte elements = kHaloW pixels x 8 channels, 1 row,
+// 1 channel group} of a planar [C / 8][H][W][8] bf16 tensor (viewed as rows of
+// 2 W 8-byte elements) into shared memory, completing on `bar` with its byte
+// count. x is in 8-byte elements and even (16-byte aligned), possibly negative.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int g) {
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], [%2];" ::
-            "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(0), "r"(x), "r"(y), "r"(g)
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
+            "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(g)
         : "memory");
 }
 
@@ -399,9 +409,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 // Persistent, warp-specialised convolution. CTA b takes tiles b, b + grid, ...
-// (128 pixels x kTileRows rows each) through a two-stage ring:
-//   warp 16 (one thread) TMA-loads tile j's halo into halo buffer j % 2 once the
-//                        MMAs of tile j - 2 have released it (barrier `empty`);
+// (128 pixels x kTileRows rows each) through a ring of kConvStages halo buffers
+// and two TMEM accumulators:
+//   warp 16 (one thread) TMA-loads tile j's halo into halo buffer j % kConvStages
+//                        once the MMAs of tile j - kConvStages have released it
+//                        (barrier `empty`);
 //   warp 17 (one thread) waits for the halo (`full`) and for the epilogue of
 //                        tile j - 2 to have drained accumulator j % 2 (`tempty`),
 //                        issues the tile's tcgen05.mma and commits to `empty` and
@@ -416,14 +428,15 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     using L = ConvSmem<CIN, N>;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sB = smem;
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);  // [2]
-    uint64_t* empty = full + 2;                                        // [2]
-    uint64_t* tfull = full + 4;                                        // [2]
-    uint64_t* tempty = full + 6;                                       // [2]
-    uint64_t* wbar = full + 8;                                         // the weights have landed
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + 80);
+    constexpr int NS = kConvStages;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);  // [NS]
+    uint64_t* empty = full + NS;                                       // [NS]
+    uint64_t* tfull = full + 2 * NS;                                   // [2]
+    uint64_t* tempty = tfull + 2;                                      // [2]
+    uint64_t* wbar = tfull + 4;                                        // the weights have landed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::BAR_OFF + L::NBAR * 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tiles_x = (a.W + kTileW - 1) / kTileW;
+    const int tiles_x = (a.W + kTileOut - 1) / kTileOut;
     const int ntiles = tiles_x * ((a.H + kTileRows - 1) / kTileRows);
     const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
@@ -431,9 +444,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     __shared__ float s_bias[N];
     if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
     if (tid == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NS; ++b) {
             mbar_init(&full[b], 1);
             mbar_init(&empty[b], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
             mbar_init(&tfull[b], 1);
             mbar_init(&tempty[b], kConvEpilogueWarps);
         }
@@ -455,22 +470,23 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         mbar_expect_tx(wbar, L::B_BYTES);
         bulk_load(sB, a.wimg, L::B_BYTES, wbar);
         for (int j = 0; j < my_tiles && ok; ++j) {
-            const int buf = j & 1;
-            if (j >= 2 && !mbar_wait(&empty[buf], (uint32_t)((j - 2) >> 1) & 1u)) {
+            const int buf = j % NS;
+            if (j >= NS && !mbar_wait(&empty[buf], (uint32_t)((j - NS) / NS) & 1u)) {
                 ok = false;
                 break;
             }
             const int tile = blockIdx.x + j * gridDim.x;
-            const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileRows;
-            unsigned char* A = smem + (buf ? L::A_OFF1 : L::A_OFF0);
+            const int x0 = (tile % tiles_x) * kTileOut, y0 = (tile / tiles_x) * kTileRows;
+            unsigned char* A = smem + L::A_OFF0 + buf * L::A_STRIDE;
             mbar_expect_tx(&full[buf], L::TX_BYTES);
             for (int r = 0; r < kTileRows + 2; ++r)
 #pragma unroll
-                for (int g = 0; g < L::G; ++g) tma_load_4d(A + r * L::S_R + g * L::S_G, &in_map, &full[buf], x0 - 1, y0 - 1 + r, g);
+                for (int g = 0; g < L::G; ++g)
+                    tma_load_3d(A + r * L::S_R + g * L::S_G, &in_map, &full[buf], 2 * (x0 - 1), y0 - 1 + r, g);
         }
         // the copies still in flight land before the CTA exits
-        for (int j = my_tiles - 2 > 0 ? my_tiles - 2 : 0; j < my_tiles; ++j)
-            if (!mbar_wait(&full[j & 1], (uint32_t)(j >> 1) & 1u)) ok = false;
+        for (int j = my_tiles - NS > 0 ? my_tiles - NS : 0; j < my_tiles; ++j)
+            if (!mbar_wait(&full[j % NS], (uint32_t)(j / NS) & 1u)) ok = false;
         if (!mbar_wait(wbar, 0)) ok = false;
     } else if (warp == kConvEpilogueWarps + 1 && lane == 0) {
         // MMA issue
@@ -479,17 +495,17 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
         if (my_tiles > 0 && !mbar_wait(wbar, 0)) ok = false;
         for (int j = 0; j < my_tiles && ok; ++j) {
-            const int buf = j & 1;
-            if (!mbar_wait(&full[buf], (uint32_t)(j >> 1) & 1u) ||
-                (j >= 2 && !mbar_wait(&tempty[buf], (uint32_t)((j - 2) >> 1) & 1u))) {
+            const int buf = j % NS, acc = j & 1;
+            if (!mbar_wait(&full[buf], (uint32_t)(j / NS) & 1u) ||
+                (j >= 2 && !mbar_wait(&tempty[acc], (uint32_t)((j - 2) >> 1) & 1u))) {
                 ok = false;
                 break;
             }
             tc_fence_after();
             // descriptors differ only in their start address (the low 14 bits, in 16-byte units), so each
             // MMA's descriptors are the tile's base descriptors plus a compile-time offset
-            const uint64_t da0 = umma_desc(smem_u32(smem + (buf ? L::A_OFF1 : L::A_OFF0)), L::S_G, 128);
-            const uint32_t d0 = tmem + buf * kTileRows * N;
+            const uint64_t da0 = umma_desc(smem_u32(smem + L::A_OFF0 + buf * L::A_STRIDE), L::S_G, 128);
+            const uint32_t d0 = tmem + acc * kTileRows * N;
 #pragma unroll
             for (int t = 0; t < kTileRows; ++t) {
 #pragma unroll
@@ -503,10 +519,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
                 }
             }
             mma_commit(&empty[buf]);
-            mma_commit(&tfull[buf]);
+            mma_commit(&tfull[acc]);
         }
         // the last MMAs complete before the CTA frees its tensor memory
-        if (ok && my_tiles > 0 && !mbar_wait(&empty[(my_tiles - 1) & 1], (uint32_t)((my_tiles - 1) >> 1) & 1u))
+        if (ok && my_tiles > 0 && !mbar_wait(&empty[(my_tiles - 1) % NS], (uint32_t)((my_tiles - 1) / NS) & 1u))
             ok = false;
     } else if (warp < kConvEpilogueWarps) {
         const int quad = warp & 3, row0 = (warp >> 2) * (kTileRows * 4 / kConvEpilogueWarps);
@@ -518,7 +534,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             }
             tc_fence_after();
             const int tile = blockIdx.x + j * gridDim.x;
-            const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileRows;
+            const int x0 = (tile % tiles_x) * kTileOut, y0 = (tile / tiles_x) * kTileRows;
+            const int col = quad * 32 + lane;
+            const int x = col < kTileOut ? x0 + col : a.W;  // the dropped MMA rows count as outside the image
 #pragma unroll
             for (int tt = 0; tt < kTileRows * 4 / kConvEpilogueWarps; ++tt) {
                 const int t = row0 + tt;
@@ -526,7 +544,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
                 const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (buf * kTileRows + t) * N;
                 if constexpr (N == 32) tmem_ld32(ta, acc);
                 else tmem_ld16(ta, acc);
-                conv_epilogue<N, EPI>(a, acc, x0 + quad * 32 + lane, y0 + t, loss, s_lut, s_bias);
+                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, s_lut, s_bias);
             }
             tc_fence_before();
             __syncwarp();
@@ -871,16 +889,19 @@ void load_encode_tiled() {
         g_encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
 }
 
-// Tensor map of a planar [C / 8][H][W][8] bf16 tensor with boxes of {8 channels,
-// kHaloW pixels, 1 row, 1 group}; out-of-range elements read as zero.
+// Tensor map of a planar [C / 8][H][W][8] bf16 tensor viewed as [C / 8][H][2 W]
+// 8-byte elements (a pixel's 8 channels are two elements), with boxes of
+// {2 kHaloW elements, 1 row, 1 group}: each box is one contiguous 2,048-byte
+// run, so TMA moves whole rows rather than 16-byte pieces. Out-of-range
+// elements read as zero.
 bool encode_planar(CUtensorMap* map, const void* base, int C, int W, int H) {
     std::call_once(g_encode_once, load_encode_tiled);
     if (!g_encode_tiled) return false;
-    const cuuint64_t dims[4] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)(C / 8)};
-    const cuuint64_t strides[3] = {16, (cuuint64_t)W * 16, (cuuint64_t)W * H * 16};
-    const cuuint32_t box[4] = {8, (cuuint32_t)kHaloW, 1, 1};
-    const cuuint32_t elem[4] = {1, 1, 1, 1};
-    return g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, elem,
+    const cuuint64_t dims[3] = {(cuuint64_t)W * 2, (cuuint64_t)H, (cuuint64_t)(C / 8)};
+    const cuuint64_t strides[2] = {(cuuint64_t)W * 16, (cuuint64_t)W * H * 16};
+    const cuuint32_t box[3] = {(cuuint32_t)(2 * kHaloW), 1, 1};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    return g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void*>(base), dims, strides, box, elem,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -889,7 +910,7 @@ template <int CIN, int N, int EPI>
 bool launch_conv(const rz_upsampler* u, const ConvArgs& a, cudaStream_t s) {
     CUtensorMap map;
     if (!encode_planar(&map, a.in, CIN, a.W, a.H)) return false;
-    const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileRows - 1) / kTileRows);
+    const int tiles = ((a.W + kTileOut - 1) / kTileOut) * ((a.H + kTileRows - 1) / kTileRows);
     const int grid = std::min(tiles, std::max(u->sms, 1));
     k_conv<CIN, N, EPI><<<grid, kConvThreads, ConvSmem<CIN, N>::BYTES, s>>>(a, map);
     return true;
