@@ -201,6 +201,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Writes zeros to `cols` (a multiple of 16) columns of this warp's 32 TMEM lanes from
+// taddr on, and waits until the stores have landed.
+__device__ __forceinline__ void tmem_zero(uint32_t taddr, int cols) {
+    const uint32_t z = 0u;
+    for (int c = 0; c < cols; c += 16)
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+            "{%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr + c), "r"(z)
+            : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __host__ __device__ constexpr uint32_t tmem_cols_for(int cols) {
     return cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : cols <= 256 ? 256u : 512u;
 }
@@ -254,7 +266,7 @@ __global__ void k_features(rz_gbuffer g, __nv_bfloat16* __restrict__ feat) {
 
 struct ConvArgs {
     const __nv_bfloat16* in;        // planar [CIN / 8][H][W][8]
-    const __nv_bfloat16* wimg;      // B operand image [9 * CIN / 8][N][8]
+    const __nv_bfloat16* wimg;      // B operand image [3 dx][CIN / 8][3 dy][N][8]
     const float* bias;              // N (relu, final)
     int W, H;
     __nv_bfloat16* out;             // planar [N / 8][H][W][8] (relu, mask)
@@ -285,10 +297,11 @@ struct ConvSmem {
     static constexpr uint32_t BAR_OFF = A_OFF0 + kConvStages * A_STRIDE;
     static constexpr uint32_t NBAR = 2 * kConvStages + 5;                // full, empty, tfull[2], tempty[2], weights
     static constexpr uint32_t BYTES = BAR_OFF + NBAR * 8 + 16;           // the barriers, the TMEM address
-    static constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * kTileRows * N);  // two accumulators
+    static constexpr uint32_t ACC_COLS = (kTileRows + 4) * N;                 // one accumulator buffer
+    static constexpr uint32_t TMEM_COLS = tmem_cols_for(2 * ACC_COLS);        // two of them
 };
 static_assert(ConvSmem<32, 32>::BYTES + 2048 <= 227 * 1024, "conv shared memory (with the static arrays)");
-static_assert(2 * kTileRows * 32 <= 512, "two accumulators fit the 512 TMEM columns");
+static_assert(2 * (kTileRows + 4) * 32 <= 512, "two accumulator buffers fit the 512 TMEM columns");
 static_assert(kTileRows * 4 % kConvEpilogueWarps == 0, "epilogue warps split the tile rows evenly");
 static_assert(2 * kHaloW <= 256, "a halo row is one TMA box (at most 256 elements)");
 static_assert(ConvSmem<32, 32>::S_G % 128 == 0 && ConvSmem<16, 32>::S_R % 128 == 0, "TMA destinations 128-byte aligned");
@@ -415,12 +428,21 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 //                        once the MMAs of tile j - kConvStages have released it
 //                        (barrier `empty`);
 //   warp 17 (one thread) waits for the halo (`full`) and for the epilogue of
-//                        tile j - 2 to have drained accumulator j % 2 (`tempty`),
-//                        issues the tile's tcgen05.mma and commits to `empty` and
-//                        `tfull`;
+//                        tile j - 2 to have drained accumulator buffer j % 2
+//                        (`tempty`), issues the tile's tcgen05.mma and commits to
+//                        `empty` and `tfull`;
 //   warps 0-15           wait for `tfull`, read the accumulator (warp w reads
-//                        TMEM lane quadrant w % 4 of tile row w / 4), run the
-//                        epilogue and arrive on `tempty`.
+//                        TMEM lane quadrant w % 4 of tile row w / 4), zero it,
+//                        run the epilogue and arrive on `tempty`.
+// One MMA takes one halo row i, one horizontal tap dx and 16 input channels, and
+// N = 3 x Cout weight columns: the three vertical taps at once. Its three column
+// blocks add halo row i's contributions to output rows i, i - 1 and i - 2, so the
+// accumulator of output row o (-2 <= o <= kTileRows + 1) sits at column
+// Cout x (kTileRows + 1 - o) and the blocks of consecutive rows are adjacent in
+// the order an MMA writes them. Rows outside 0..kTileRows - 1 collect the halo
+// rows' unused contributions and are never read; the others are zeroed by the
+// epilogue (and once at the start), and every MMA accumulates. Each activation
+// read from shared memory thus feeds 96 weight columns instead of 32.
 // Every wait is bounded; a role whose wait runs out sets kErrMmaTimeout and
 // stops, and the others then run out in turn.
 template <int CIN, int N, int EPI>
@@ -462,6 +484,15 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    if (warp < kConvEpilogueWarps) {  // the read accumulator rows of both buffers start at zero
+        const int quad = warp & 3, row0 = (warp >> 2) * (kTileRows * 4 / kConvEpilogueWarps);
+        for (int b = 0; b < 2; ++b)
+            for (int tt = 0; tt < kTileRows * 4 / kConvEpilogueWarps; ++tt)
+                tmem_zero(tmem + ((uint32_t)(quad * 32) << 16) + b * L::ACC_COLS + (kTileRows + 1 - (row0 + tt)) * N, N);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
     bool ok = true;
     float loss = 0.0f;
 
@@ -490,8 +521,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         if (!mbar_wait(wbar, 0)) ok = false;
     } else if (warp == kConvEpilogueWarps + 1 && lane == 0) {
         // MMA issue
-        constexpr uint32_t idesc = idesc_bf16(128, N);
-        constexpr uint32_t lbo_b = N * 16;
+        constexpr uint32_t idesc = idesc_bf16(128, 3 * N);
+        constexpr uint32_t lbo_b = 3 * N * 16;  // between the weight image's 8-channel groups
         const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
         if (my_tiles > 0 && !mbar_wait(wbar, 0)) ok = false;
         for (int j = 0; j < my_tiles && ok; ++j) {
@@ -505,16 +536,16 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             // descriptors differ only in their start address (the low 14 bits, in 16-byte units), so each
             // MMA's descriptors are the tile's base descriptors plus a compile-time offset
             const uint64_t da0 = umma_desc(smem_u32(smem + L::A_OFF0 + buf * L::A_STRIDE), L::S_G, 128);
-            const uint32_t d0 = tmem + acc * kTileRows * N;
+            const uint32_t d0 = tmem + acc * L::ACC_COLS;
 #pragma unroll
-            for (int t = 0; t < kTileRows; ++t) {
+            for (int i = 0; i < kTileRows + 2; ++i) {
 #pragma unroll
-                for (int tap = 0; tap < 9; ++tap) {
+                for (int dx = 0; dx < 3; ++dx) {
 #pragma unroll
                     for (int s = 0; s < CIN / 16; ++s) {
-                        const uint32_t oa = ((t + tap / 3) * L::S_R + (tap % 3) * 16 + 2 * s * L::S_G) >> 4;
-                        const uint32_t ob = ((tap * L::G + 2 * s) * lbo_b) >> 4;
-                        mma_bf16(d0 + t * N, da0 + oa, db0 + ob, idesc, (tap | s) ? 1u : 0u);
+                        const uint32_t oa = (i * L::S_R + dx * 16 + 2 * s * L::S_G) >> 4;
+                        const uint32_t ob = ((dx * L::G + 2 * s) * lbo_b) >> 4;
+                        mma_bf16(d0 + (kTileRows + 1 - i) * N, da0 + oa, db0 + ob, idesc, 1u);
                     }
                 }
             }
@@ -541,9 +572,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             for (int tt = 0; tt < kTileRows * 4 / kConvEpilogueWarps; ++tt) {
                 const int t = row0 + tt;
                 float acc[N];
-                const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (buf * kTileRows + t) * N;
+                const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + buf * L::ACC_COLS + (kTileRows + 1 - t) * N;
                 if constexpr (N == 32) tmem_ld32(ta, acc);
                 else tmem_ld16(ta, acc);
+                tmem_zero(ta, N);
                 conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, s_lut, s_bias);
             }
             tc_fence_before();
@@ -734,11 +766,13 @@ __global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* __restrict__ 
     if (local >= 9 * cin * cout) return;  // biases
     const int c_in = local % cin, tap = (local / cin) % 9, co = local / (9 * cin);
     const __nv_bfloat16 w = __float2bfloat16_rn(p[i]);
-    const int k = tap * cin + c_in;
-    img[kFwd[l] + ((k / 8) * cout + co) * 8 + (k % 8)] = w;
-    if (l >= 1) {
-        const int k2 = (8 - tap) * cout + co;
-        img[kDgrad[l] + ((k2 / 8) * cin + c_in) * 8 + (k2 % 8)] = w;
+    // image [dx][8-channel group][dy][n][8]: for one horizontal tap and group, the
+    // 3 x N rows an MMA reads are the three vertical taps' weights for every output n
+    const int dy = tap / 3, dx = tap % 3;
+    img[kFwd[l] + (((dx * (cin / 8) + c_in / 8) * 3 + dy) * cout + co) * 8 + c_in % 8] = w;
+    if (l >= 1) {  // input gradient: the mirrored tap, inputs and outputs swapped
+        const int dy2 = (8 - tap) / 3, dx2 = (8 - tap) % 3;
+        img[kDgrad[l] + (((dx2 * (cout / 8) + co / 8) * 3 + dy2) * cin + c_in) * 8 + co % 8] = w;
     }
 }
 
