@@ -557,6 +557,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             ok = false;
     } else if (warp < kConvEpilogueWarps) {
         const int quad = warp & 3, row0 = (warp >> 2) * (kTileRows * 4 / kConvEpilogueWarps);
+        // the biases live in registers: shared-memory reads would queue behind the MMAs' operand traffic
+        float bias[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) bias[c] = s_bias[c];
         for (int j = 0; j < my_tiles; ++j) {
             const int buf = j & 1;
             if (!mbar_wait(&tfull[buf], (uint32_t)(j >> 1) & 1u)) {
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
                 if constexpr (N == 32) tmem_ld32(ta, acc);
                 else tmem_ld16(ta, acc);
                 tmem_zero(ta, N);
-                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, s_lut, s_bias);
+                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, s_lut, bias);
             }
             tc_fence_before();
             __syncwarp();
