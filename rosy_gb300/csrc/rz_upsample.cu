@@ -306,9 +306,18 @@ static_assert(kTileRows * 4 % kConvEpilogueWarps == 0, "epilogue warps split the
 static_assert(2 * kHaloW <= 256, "a halo row is one TMA box (at most 256 elements)");
 static_assert(ConvSmem<32, 32>::S_G % 128 == 0 && ConvSmem<16, 32>::S_R % 128 == 0, "TMA destinations 128-byte aligned");
 
+// byte / 255, correctly rounded: the product with the rounded reciprocal and one
+// residual-correction step (Markstein's method), which gives the correctly rounded
+// quotient for every byte value (checked exhaustively against IEEE division).
+__device__ __forceinline__ float unorm8(uint32_t b) {
+    const float x = (float)b, r = 1.0f / 255.0f;
+    const float q = x * r;
+    return __fmaf_rn(__fmaf_rn(-q, 255.0f, x), r, q);
+}
+
 template <int N, int EPI>
 __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss,
-                                              const float* lut, const float* bias) {
+                                              const float* bias) {
     const bool inside = x < a.W && y < a.H;
     if (EPI == kEpiRelu) {
         if (!inside) return;
@@ -350,7 +359,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
                 const int xx = min(max(x + q - 1, 0), W - 1);
                 const uint32_t c = __ldg(a.color_lr + (size_t)yy * W + xx);
 #pragma unroll
-                for (int k = 0; k < 3; ++k) f[r][q][k] = lut[(c >> (8 * k)) & 255u];
+                for (int k = 0; k < 3; ++k) f[r][q][k] = unorm8((c >> (8 * k)) & 255u);
             }
         }
         float g[kOutChannels];
@@ -376,7 +385,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
                     const float qv = fminf(fmaxf(v, 0.0f), 1.0f);
                     ov |= (uint32_t)floorf(qv * 255.0f + 0.5f) << (8 * k);
                     if (a.target) {
-                        const float d = v - lut[(tj >> (8 * k)) & 255u];
+                        const float d = v - unorm8((tj >> (8 * k)) & 255u);
                         g[(2 * i + j) * 3 + k] = 2.0f * d;
                         loss += d * d;
                     }
@@ -462,7 +471,6 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     const int ntiles = tiles_x * ((a.H + kTileRows - 1) / kTileRows);
     const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
-    __shared__ float s_lut[EPI == kEpiFinal ? 256 : 1];
     __shared__ float s_bias[N];
     if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
     if (tid == 0) {
@@ -475,9 +483,6 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             mbar_init(&tempty[b], kConvEpilogueWarps);
         }
         mbar_init(wbar, 1);
-    }
-    if (EPI == kEpiFinal) {
-        for (int i = tid; i < 256; i += kConvThreads) s_lut[i] = (float)i / 255.0f;
     }
     if (tid < N) s_bias[tid] = EPI == kEpiMask ? 0.0f : a.bias[tid];
     tc_fence_before();
@@ -580,7 +585,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
                 if constexpr (N == 32) tmem_ld32(ta, acc);
                 else tmem_ld16(ta, acc);
                 tmem_zero(ta, N);
-                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, s_lut, bias);
+                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, bias);
             }
             tc_fence_before();
             __syncwarp();

@@ -122,6 +122,28 @@ def test_upsampler_forward_matches_oracle(gpu, w, h):
     hi.deinit()
 
 
+def test_zero_network_is_exactly_the_bilinear_base(gpu):
+    """With every parameter zero the network adds nothing, so the output is the
+    bilinear x2 base alone, and it equals the oracle's bit for bit: byte / 255,
+    the 9/16, 3/16, 3/16, 1/16 sum in order, clamping and rounding to 8 bits."""
+    import torch
+
+    w, h = 200, 70
+    lo, hi = _pair(w, h, camera=3)
+    gbh = lo.download_gbuffer()
+    u = up.Upsampler(0, w, h)
+    u.set_params(np.zeros_like(U.init_params(0)))
+    out = torch.zeros((2 * h, 2 * w), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    u.infer(lo.gbuffer(), out.data_ptr())
+    assert u.status() == 0
+    got = out.cpu().numpy().view(np.uint8).reshape(2 * h, 2 * w, 4)
+    assert np.array_equal(got, U.to_rgba8(U.bilinear_base(gbh["color"])))
+    u.close()
+    lo.deinit()
+    hi.deinit()
+
+
 @pytest.mark.parametrize("w,h", [(96, 64), (200, 70)])
 def test_upsampler_gradients_match_oracle(gpu, w, h):
     import torch
