@@ -752,23 +752,30 @@ void stamp(rz_ctx* c, int i) {
 
 // Shadow passes of all views (src/Engine/Graphics.cpp:5195-5292): clear to 0,
 // per-draw matrices, setup, raster.
+// The shadow maps are zeroed by the setup launch when there is one (the raster
+// follows it), else by the clear launch.
 void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
     ClearList cl{};
-    cl.ptr[0] = c->d_shadow;
-    cl.bytes[0] = c->shadow_total * 4;
-    cl.ptr[1] = c->d_headers + 0;
-    cl.bytes[1] = sizeof(PassHeader);
-    cl.count = 2;
+    cl.ptr[0] = c->d_headers + 0;
+    cl.bytes[0] = sizeof(PassHeader);
+    cl.count = 1;
     if (c->shadow_tris) {
-        cl.ptr[2] = c->shadow_pass.tile_status;
-        cl.bytes[2] = (size_t)setup_ctas(c->shadow_tris) * 8;
-        cl.count = 3;
+        cl.ptr[1] = c->shadow_pass.tile_status;
+        cl.bytes[1] = (size_t)setup_ctas(c->shadow_tris) * 8;
+        cl.count = 2;
+    } else {
+        cl.ptr[1] = c->d_shadow;
+        cl.bytes[1] = c->shadow_total * 4;
+        cl.count = 2;
     }
     launch_clear(cl, c->sm_count, s);
     if (stamps) stamp(c, 1);
     if (c->shadow_tris) {
         launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s);
-        const PassParams sp = pass_params(c, 0);
+        PassParams sp = pass_params(c, 0);
+        sp.clear_ptr[0] = c->d_shadow;
+        sp.clear_bytes[0] = c->shadow_total * 4;
+        sp.clear_count = 1;
         launch_setup(sp, s);
         if (stamps) stamp(c, 2);
         launch_raster(sp, c->sm_count, s);
@@ -796,13 +803,18 @@ void launch_camera_raster(rz_ctx* c, PassParams cp, cudaStream_t s) {
     }
 }
 
+// The visibility buffer is zeroed by the opaque setup launch when there is one,
+// else by the clear launch.
 void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& sh) {
     ClearList cl{};
-    cl.ptr[0] = c->d_vis;
-    cl.bytes[0] = c->pix_total * 8 * c->samples;
-    cl.ptr[1] = c->d_headers + 1;
-    cl.bytes[1] = 2 * sizeof(PassHeader);  // camera and blended headers
-    cl.count = 2;
+    cl.ptr[0] = c->d_headers + 1;
+    cl.bytes[0] = 2 * sizeof(PassHeader);  // camera and blended headers
+    cl.count = 1;
+    if (!c->opaque_tris) {
+        cl.ptr[cl.count] = c->d_vis;
+        cl.bytes[cl.count] = c->pix_total * 8 * c->samples;
+        ++cl.count;
+    }
     if (c->opaque_tris) {
         cl.ptr[cl.count] = c->camera_pass.tile_status;
         cl.bytes[cl.count] = (size_t)setup_ctas(c->opaque_tris) * 8;
@@ -817,8 +829,12 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
     launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s);
     if (stamps) stamp(c, 4);
     if (c->opaque_tris) {
-        const PassParams cp = pass_params(c, 1);
+        PassParams cp = pass_params(c, 1);
+        cp.clear_ptr[0] = c->d_vis;
+        cp.clear_bytes[0] = c->pix_total * 8 * c->samples;
+        cp.clear_count = 1;
         launch_setup(cp, s);
+        cp.clear_count = 0;
         if (stamps) stamp(c, 5);
         launch_camera_raster(c, cp, s);
     } else if (stamps) {

@@ -166,6 +166,12 @@ struct PassParams {
     int32_t sample_x, sample_y;
     uint32_t sample_plane;
     int32_t bb_hi;  // smallest sample offset the setup boxed for (32 with 4x samples, else 128)
+    // buffers the setup launch zeroes besides its own work (the depth target's
+    // CLEAR load-op, folded into the launch that precedes the raster); none when
+    // clear_count is 0
+    void* clear_ptr[2];
+    size_t clear_bytes[2];
+    uint32_t clear_count;
 };
 
 struct ShadeParams {

@@ -66,23 +66,25 @@ void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, con
 // clears (the load-op CLEAR of the depth attachments, scratch headers)
 // ---------------------------------------------------------------------------
 
-// Zeroes each buffer with 16-byte stores on its 16-byte-aligned body and byte
-// stores on the unaligned head and tail, so any start address and size is safe.
+// Thread `tid` of `stride` threads' share of zeroing n bytes at ptr: 16-byte
+// stores on the 16-byte-aligned body, byte stores on the unaligned head and
+// tail, so any start address and size is safe.
+__device__ __forceinline__ void zero_share(void* ptr, size_t n, size_t tid, size_t stride) {
+    unsigned char* base = static_cast<unsigned char*>(ptr);
+    size_t head = (16 - ((size_t)base & 15)) & 15;
+    if (head > n) head = n;
+    if (tid < head) base[tid] = 0;
+    const size_t n16 = (n - head) / 16;
+    uint4* body = reinterpret_cast<uint4*>(base + head);
+    for (size_t i = tid; i < n16; i += stride) body[i] = make_uint4(0u, 0u, 0u, 0u);
+    const size_t done = head + n16 * 16;
+    if (tid < n - done) base[done + tid] = 0;
+}
+
 __global__ void __launch_bounds__(256) k_clear(ClearList L) {
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (int b = 0; b < L.count; ++b) {
-        unsigned char* base = static_cast<unsigned char*>(L.ptr[b]);
-        const size_t n = L.bytes[b];
-        size_t head = (16 - ((size_t)base & 15)) & 15;
-        if (head > n) head = n;
-        if (tid < head) base[tid] = 0;
-        const size_t n16 = (n - head) / 16;
-        uint4* body = reinterpret_cast<uint4*>(base + head);
-        for (size_t i = tid; i < n16; i += stride) body[i] = make_uint4(0u, 0u, 0u, 0u);
-        const size_t done = head + n16 * 16;
-        if (tid < n - done) base[done + tid] = 0;
-    }
+    for (int b = 0; b < L.count; ++b) zero_share(L.ptr[b], L.bytes[b], tid, stride);
 }
 
 void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream) {
@@ -405,6 +407,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     __shared__ uint32_t s_small_warp[kSetupThreads / 32];
     __shared__ uint32_t s_small_base;
     if (threadIdx.x == 0) s_tile = atomicAdd(&P.header->ticket, 1u);
+    // the pass's depth target is zeroed by the same launch: its stores overlap the
+    // setup arithmetic, and the raster (the next launch) sees it cleared
+    for (uint32_t b = 0; b < P.clear_count; ++b)
+        zero_share(P.clear_ptr[b], P.clear_bytes[b], (size_t)blockIdx.x * blockDim.x + threadIdx.x,
+                   (size_t)gridDim.x * blockDim.x);
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t local = tile * kSetupThreads + threadIdx.x;
