@@ -17,43 +17,51 @@
 // ((64 - w) * e0 + w * e1 + 32) >> 6 with w from the 2-, 3- or 4-bit weight
 // table; anchor texels store their index with one bit fewer.
 //
-// Work: one thread per block, reading its 16 bytes with one vector load and
-// writing four rows of 16 bytes; a warp covers 32 consecutive blocks of a
-// block row, so its loads and stores are contiguous. Tables (partition maps,
-// anchor masks, mode fields, weights) are a kernel parameter copied to shared
-// memory. Bound: HBM, 16 bytes read + 64 written per block.
+// Work: one CTA per tile of 64 x 4 blocks (256 x 16 texels). Each thread reads
+// one block (a 16-byte load); the tile's blocks are counting-sorted by mode in
+// shared memory, so that a warp almost always decodes 32 blocks of one mode with
+// the code specialised for that mode: every field sits at a compile-time bit
+// position (a funnel shift and a mask), and the index streams are made uniform
+// by inserting the anchors' missing high bits. Decoded texels are staged in
+// shared memory and the tile leaves as 16 rows of 1 KB, coalesced. Tables
+// (partition maps, anchors) are a kernel parameter copied to shared memory.
+// Bound: HBM, 16 bytes read + 64 written per block.
 #include "rz_device.cuh"
 
 namespace rz {
 
 namespace {
 
-constexpr int kBc7Threads = 256;
+constexpr int kBc7Threads = 256;   // one thread per block of a tile
+constexpr int kTileBX = 64;        // a tile: 64 x 4 blocks = 256 x 16 texels
+constexpr int kTileBY = 4;
+constexpr int kStagePitch = 4 * kTileBX + 4;  // staged texel row (u32), padded against bank conflicts
 constexpr int kBc7MaxLevels = 16;
+static_assert(kTileBX * kTileBY == kBc7Threads, "one thread per block of a tile");
 
-// Subset maps (2 bits per texel, texel 0 lowest) and anchor-texel masks:
-// entries [0, 64) are the two-subset partitions, [64, 128) the three-subset ones.
+// Subset of every texel (2 bits per texel, texel 0 lowest) and the anchor texels
+// other than texel 0: entries [0, 64) are the two-subset partitions (anchor
+// index), [64, 128) the three-subset ones (lower anchor | higher anchor << 8).
 struct Bc7Tables {
     uint32_t map[128];
     uint32_t anchors[128];
-    uint32_t mode_lo[8];  // per mode: ns | pb << 4 | rb << 8 | isb << 12 | cb << 16 | ab << 20 | pbit kind << 24 | ib << 28
-    uint32_t mode_hi[8];  // per mode: secondary index bits
-    uint32_t weights[12]; // bytes: [0,4) 2-bit, [4,12) 3-bit, [16,32) 4-bit weights, 4 per word
 };
 
 struct Bc7Level {
-    uint32_t block0;  // first block of the level in the chain
-    uint32_t bw, bh;  // blocks per row, block rows
-    uint32_t w, h;    // texels
-    uint32_t texel0;  // first texel of the level in the output
-    uint32_t vec;     // rows and the level start are 16-byte aligned: full blocks store as uint4
+    uint32_t block0;   // first block of the level in the chain
+    uint32_t bw, bh;   // blocks per row, block rows
+    uint32_t w, h;     // texels
+    uint32_t texel0;   // first texel of the level in the output
+    uint32_t tile0;    // first tile of the level
+    uint32_t tiles_x;  // tiles per row of tiles
+    uint32_t vec;      // rows and the level start are 16-byte aligned: four texels store as one uint4
 };
 
 struct Bc7Job {
     const uint4* blocks;
     uint32_t* texels;
     uint32_t levels;
-    uint32_t total_blocks;
+    uint32_t total_tiles;
     Bc7Level L[kBc7MaxLevels];
 };
 
@@ -108,11 +116,6 @@ constexpr uint8_t kModeFields[8][9] = {
     {1, 0, 2, 1, 5, 6, 0, 2, 3}, {1, 0, 2, 0, 7, 8, 0, 2, 2}, {1, 0, 0, 0, 7, 7, 1, 4, 0}, {2, 6, 0, 0, 5, 5, 1, 2, 0},
 };
 
-constexpr uint8_t kWeightBytes[48] = {
-    0, 21, 43, 64, 0, 9, 18, 27, 37, 46, 55, 64, 0, 0, 0, 0,
-    0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64,
-};
-
 Bc7Tables make_tables() {
     Bc7Tables t{};
     for (int p = 0; p < 64; ++p) {
@@ -123,17 +126,10 @@ Bc7Tables make_tables() {
         }
         t.map[p] = m2;
         t.map[64 + p] = m3;
-        t.anchors[p] = 1u | (1u << kAnchorTwo[p]);
-        t.anchors[64 + p] = 1u | (1u << kAnchorThreeA[p]) | (1u << kAnchorThreeB[p]);
+        t.anchors[p] = kAnchorTwo[p];
+        const uint32_t a = kAnchorThreeA[p], b = kAnchorThreeB[p];
+        t.anchors[64 + p] = std::min(a, b) | std::max(a, b) << 8;
     }
-    for (int m = 0; m < 8; ++m) {
-        const uint8_t* f = kModeFields[m];
-        t.mode_lo[m] = f[0] | f[1] << 4 | f[2] << 8 | f[3] << 12 | f[4] << 16 | f[5] << 20 | f[6] << 24 | (uint32_t)f[7] << 28;
-        t.mode_hi[m] = f[8];
-    }
-    for (int i = 0; i < 12; ++i)
-        t.weights[i] = kWeightBytes[4 * i] | kWeightBytes[4 * i + 1] << 8 | kWeightBytes[4 * i + 2] << 16 |
-                       (uint32_t)kWeightBytes[4 * i + 3] << 24;
     return t;
 }
 
@@ -142,145 +138,232 @@ const Bc7Tables& tables() {
     return t;
 }
 
-// Takes the next n (0..8) bits of the 128-bit block held in lo:hi.
-__device__ __forceinline__ uint32_t take(uint64_t& lo, uint64_t& hi, uint32_t n) {
-    const uint32_t v = (uint32_t)lo & ((1u << n) - 1u);
-    if (n) {
-        lo = (lo >> n) | (hi << (64 - n));
-        hi >>= n;
+__device__ __forceinline__ uint32_t word_of(const uint4& q, int i) {
+    return i == 0 ? q.x : i == 1 ? q.y : i == 2 ? q.z : i == 3 ? q.w : 0u;
+}
+
+// Bits [pos, pos + n) of the block, n <= 32. The decoders call it with positions
+// and widths known at compile time, where it is a funnel shift and a mask.
+__device__ __forceinline__ uint32_t field(const uint4& q, int pos, int n) {
+    const uint32_t v = __funnelshift_r(word_of(q, pos >> 5), word_of(q, (pos >> 5) + 1), pos & 31);
+    return n >= 32 ? v : v & ((1u << n) - 1u);
+}
+
+__device__ __forceinline__ uint64_t field64(const uint4& q, int pos, int n) {  // n <= 64
+    const uint64_t lo = field(q, pos, n < 32 ? n : 32);
+    return n <= 32 ? lo : lo | (uint64_t)field(q, pos + 32, n - 32) << 32;
+}
+
+// x with a zero bit inserted at position p (the bits from p up move up one).
+__device__ __forceinline__ uint64_t insert_zero(uint64_t x, uint32_t p) {
+    const uint64_t low = x & ((1ull << p) - 1ull);
+    return low | ((x ^ low) << 1);
+}
+
+// Interpolation weight (out of 64) of a 2-, 3- or 4-bit index: the format's
+// tables {0, 21, 43, 64}, {0, 9, 18, 27, 37, 46, 55, 64} and {0, 4, 9, ..., 60, 64}
+// are floor((64 i + c) / (2^IB - 1)) with c = 1, 3, 7; the division is a
+// multiply by a rounded-up 2^16 / (2^IB - 1), exact for these small numerators
+// (checked against every table entry).
+template <int IB>
+__device__ __forceinline__ uint32_t weight_of(uint32_t i) {
+    constexpr uint32_t c = IB == 2 ? 1u : IB == 3 ? 3u : 7u;
+    constexpr uint32_t m = IB == 2 ? 21846u : IB == 3 ? 9363u : 4370u;
+    return ((64u * i + c) * m) >> 16;
+}
+
+// Widens the three colour bytes of a packed endpoint from N (5..8) bits to 8 by
+// replicating their high bits; each byte holds a value below 2^N.
+template <int N>
+__device__ __forceinline__ uint32_t widen3(uint32_t e) {
+    if constexpr (N >= 8) {
+        return e;
+    } else {
+        constexpr uint32_t hi_mask = ((0xFFu << (8 - N)) & 0xFFu) * 0x010101u;
+        constexpr uint32_t lo_mask = ((1u << (8 - N)) - 1u) * 0x010101u;
+        return ((e << (8 - N)) & hi_mask) | ((e >> (2 * N - 8)) & lo_mask);
     }
-    return v;
 }
 
-// Widens the three colour bytes of a packed endpoint from n (5..8) bits to 8 by
-// replicating their high bits; each byte holds a value below 2^n.
-__device__ __forceinline__ uint32_t widen3(uint32_t e, uint32_t n) {
-    if (n >= 8) return e;
-    const uint32_t hi_mask = ((0xFFu << (8 - n)) & 0xFFu) * 0x010101u;
-    const uint32_t lo_mask = ((1u << (8 - n)) - 1u) * 0x010101u;
-    return ((e << (8 - n)) & hi_mask) | ((e >> (2 * n - 8)) & lo_mask);
+template <int N>
+__device__ __forceinline__ uint32_t widen1(uint32_t v) {
+    if constexpr (N >= 8) return v;
+    else return (v << (8 - N)) | (v >> (2 * N - 8));
 }
 
-__device__ __forceinline__ uint32_t widen1(uint32_t v, uint32_t n) { return n >= 8 ? v : (v << (8 - n)) | (v >> (2 * n - 8)); }
-
-__device__ __forceinline__ uint32_t weight(const uint8_t* w, uint32_t bits, uint32_t idx) {
-    return w[(bits == 2 ? 0 : bits == 3 ? 4 : 16) + idx];
-}
-
-// Decodes one block into 16 RGBA8 texels (row-major).
-__device__ void bc7_block(uint4 q, const Bc7Tables& T, uint32_t px[16]) {
-    const uint32_t m8 = q.x & 0xFFu;
-    if (m8 == 0) {
-#pragma unroll
-        for (int t = 0; t < 16; ++t) px[t] = 0u;
-        return;
-    }
-    const uint32_t mode = __ffs(m8) - 1;
-    const uint32_t f = T.mode_lo[mode];
-    const uint32_t ns = f & 15, pb = (f >> 4) & 15, rb = (f >> 8) & 15, isbits = (f >> 12) & 15;
-    const uint32_t cb = (f >> 16) & 15, ab = (f >> 20) & 15, pkind = (f >> 24) & 15, ib = f >> 28;
-    const uint32_t ib2 = T.mode_hi[mode];
-    uint64_t lo = q.x | (uint64_t)q.y << 32, hi = q.z | (uint64_t)q.w << 32;
-    take(lo, hi, mode + 1);
-    const uint32_t part = take(lo, hi, pb);
-    const uint32_t rot = take(lo, hi, rb);
-    const uint32_t isb = take(lo, hi, isbits);
+// One block of mode M to its 4 x 4 RGBA8 texels, row r at out + r * pitch (16-byte
+// aligned). The layout follows the mode: partition, rotation and index-selection
+// fields after the mode bits, colour endpoints channel-major, alpha endpoints,
+// P-bits, then the primary and (modes 4, 5) secondary index streams. Rows are a
+// loop (the streams and the subset map shift down after each), the four texels
+// of a row unrolled: the eight decoders stay small enough for the instruction cache.
+template <int M>
+__device__ __forceinline__ void decode_mode(const uint4& q, const Bc7Tables& T, uint32_t* out, int pitch) {
+    constexpr int NS = kModeFields[M][0], PB = kModeFields[M][1], RB = kModeFields[M][2], ISB = kModeFields[M][3];
+    constexpr int CB = kModeFields[M][4], AB = kModeFields[M][5], PK = kModeFields[M][6];
+    constexpr int IB = kModeFields[M][7], IB2 = kModeFields[M][8];
+    constexpr int P0 = M + 1, R0 = P0 + PB, S0 = R0 + RB, E0 = S0 + ISB;
+    constexpr int A0 = E0 + 3 * 2 * NS * CB, B0 = A0 + 2 * NS * AB;
+    constexpr int I0 = B0 + (PK == 1 ? 2 * NS : PK == 2 ? NS : 0);
+    constexpr int L1 = 16 * IB - NS, L2 = IB2 ? 16 * IB2 - 1 : 0;
+    static_assert(I0 + L1 + L2 == 128, "the mode's fields fill the block");
+    constexpr int NC = CB + (PK ? 1 : 0), NA = AB ? AB + (PK ? 1 : 0) : 0;
+    const uint32_t part = PB ? field(q, P0, PB) : 0u;
+    const uint32_t rot = RB ? field(q, R0, RB) : 0u;
+    const uint32_t isb = ISB ? field(q, S0, ISB) : 0u;
     // endpoint k = 2 * subset + end, channels packed R | G << 8 | B << 16 | A << 24
-    uint32_t E[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+    uint32_t E[2 * NS];
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch)
+    for (int k = 0; k < 2 * NS; ++k) {
+        uint32_t e = 0;
 #pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k < (int)(2 * ns)) E[k] |= take(lo, hi, cb) << (8 * ch);
-    if (ab) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k < (int)(2 * ns)) E[k] |= take(lo, hi, ab) << 24;
+        for (int ch = 0; ch < 3; ++ch) e |= field(q, E0 + (ch * 2 * NS + k) * CB, CB) << (8 * ch);
+        if constexpr (AB != 0) e |= field(q, A0 + k * AB, AB) << 24;
+        if constexpr (PK == 1) e = (e << 1) | field(q, B0 + k, 1) * 0x01010101u;  // bytes < 128: no carries
+        if constexpr (PK == 2) e = (e << 1) | field(q, B0 + k / 2, 1) * 0x01010101u;
+        uint32_t a = 255u;
+        if constexpr (NA != 0) a = widen1<NA>(e >> 24);
+        E[k] = widen3<NC>(e & 0x00FFFFFFu) | a << 24;
     }
-    if (pkind == 1) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k < (int)(2 * ns)) E[k] = (E[k] << 1) | (take(lo, hi, 1) * 0x01010101u);
-    } else if (pkind == 2) {
-#pragma unroll
-        for (int s = 0; s < 3; ++s)
-            if (s < (int)ns) {
-                const uint32_t p = take(lo, hi, 1) * 0x01010101u;
-                E[2 * s] = (E[2 * s] << 1) | p;
-                E[2 * s + 1] = (E[2 * s + 1] << 1) | p;
-            }
+    // index streams, made uniform (IB bits per texel) by inserting the anchors' missing high bits
+    uint64_t s1 = insert_zero(field64(q, I0, L1), IB - 1);
+    uint32_t map = 0;
+    if constexpr (NS == 2) {
+        map = T.map[part];
+        s1 = insert_zero(s1, T.anchors[part] * IB + IB - 1);
+    } else if constexpr (NS == 3) {
+        map = T.map[64 + part];
+        const uint32_t an = T.anchors[64 + part];
+        s1 = insert_zero(s1, (an & 255u) * IB + IB - 1);
+        s1 = insert_zero(s1, (an >> 8) * IB + IB - 1);
     }
-    const uint32_t nc = cb + (pkind ? 1u : 0u), na = ab ? ab + (pkind ? 1u : 0u) : 0u;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const uint32_t a = na ? widen1(E[k] >> 24, na) : 255u;
-        E[k] = widen3(E[k] & 0x00FFFFFFu, nc) | a << 24;
-    }
-    const uint32_t table = ns == 3 ? 64u + part : part;
-    const uint32_t map = ns == 1 ? 0u : T.map[table];
-    const uint32_t amask = ns == 1 ? 1u : T.anchors[table];
-    uint64_t i1 = 0, i2 = 0;
-#pragma unroll
-    for (int t = 0; t < 16; ++t) i1 |= (uint64_t)take(lo, hi, ib - ((amask >> t) & 1u)) << (4 * t);
-    if (ib2) {
-#pragma unroll
-        for (int t = 0; t < 16; ++t) i2 |= (uint64_t)take(lo, hi, ib2 - (t == 0 ? 1u : 0u)) << (4 * t);
-    }
-    // colour and alpha index sets: one set for both, or (modes 4, 5) the index-selection bit picks
-    const bool swap = ib2 && isb;
-    const uint64_t ci = swap ? i2 : i1, ai = ib2 ? (isb ? i1 : i2) : i1;
-    const uint32_t cbits = swap ? ib2 : ib, abits = ib2 ? (isb ? ib : ib2) : ib;
-    const uint8_t* W = reinterpret_cast<const uint8_t*>(T.weights);
+    uint64_t s2 = 0;
+    if constexpr (IB2 != 0) s2 = insert_zero(field64(q, I0 + L1, L2), IB2 - 1);
     const uint32_t sel = rot == 0 ? 0x3210u : rot == 1 ? 0x0213u : rot == 2 ? 0x1230u : 0x2310u;
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r) {
+        uint32_t v[4];
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-        const uint32_t s = (map >> (2 * t)) & 3u;
-        const uint32_t e0 = s == 0 ? E[0] : s == 1 ? E[2] : E[4];
-        const uint32_t e1 = s == 0 ? E[1] : s == 1 ? E[3] : E[5];
-        const uint32_t wc = weight(W, cbits, (uint32_t)(ci >> (4 * t)) & 15u);
-        const uint32_t wa = weight(W, abits, (uint32_t)(ai >> (4 * t)) & 15u);
-        // R and B in two 16-bit lanes: (64 - w) * 255 + w * 255 + 32 < 2^16, so the lanes never carry
-        const uint32_t rb2 = (((64u - wc) * (e0 & 0x00FF00FFu) + wc * (e1 & 0x00FF00FFu) + 0x00200020u) >> 6) & 0x00FF00FFu;
-        const uint32_t g = ((64u - wc) * ((e0 >> 8) & 0xFFu) + wc * ((e1 >> 8) & 0xFFu) + 32u) >> 6;
-        const uint32_t a = ((64u - wa) * (e0 >> 24) + wa * (e1 >> 24) + 32u) >> 6;
-        px[t] = __byte_perm(rb2 | g << 8 | a << 24, 0u, sel);
+        for (int c = 0; c < 4; ++c) {
+            uint32_t e0 = E[0], e1 = E[1];
+            if constexpr (NS >= 2) {
+                const uint32_t s = (map >> (2 * c)) & 3u;
+                if constexpr (NS == 2) {
+                    e0 = s ? E[2] : E[0];
+                    e1 = s ? E[3] : E[1];
+                } else {
+                    e0 = s == 0 ? E[0] : s == 1 ? E[2] : E[4];
+                    e1 = s == 0 ? E[1] : s == 1 ? E[3] : E[5];
+                }
+            }
+            const uint32_t w1 = weight_of<IB>((uint32_t)(s1 >> (IB * c)) & ((1u << IB) - 1u));
+            uint32_t wc = w1, wa = w1;
+            if constexpr (IB2 != 0) {
+                const uint32_t w2 = weight_of<IB2>((uint32_t)(s2 >> (IB2 * c)) & ((1u << IB2) - 1u));
+                wc = isb ? w2 : w1;  // the index-selection bit (mode 4) gives the colour the secondary set
+                wa = isb ? w1 : w2;
+            }
+            // R and B in two 16-bit lanes: (64 - w) * 255 + w * 255 + 32 < 2^16, so the lanes never carry
+            const uint32_t rb = (((64u - wc) * (e0 & 0x00FF00FFu) + wc * (e1 & 0x00FF00FFu) + 0x00200020u) >> 6) & 0x00FF00FFu;
+            const uint32_t g = ((64u - wc) * ((e0 >> 8) & 0xFFu) + wc * ((e1 >> 8) & 0xFFu) + 32u) >> 6;
+            const uint32_t a = ((64u - wa) * (e0 >> 24) + wa * (e1 >> 24) + 32u) >> 6;
+            const uint32_t t = rb | g << 8 | a << 24;
+            v[c] = RB ? __byte_perm(t, 0u, sel) : t;
+        }
+        *reinterpret_cast<uint4*>(out + r * pitch) = make_uint4(v[0], v[1], v[2], v[3]);
+        map >>= 8;
+        s1 >>= 4 * IB;
+        if constexpr (IB2 != 0) s2 >>= 4 * IB2;
+    }
+}
+
+__device__ __forceinline__ void decode_block(const uint4& q, const Bc7Tables& T, uint32_t* out, int pitch) {
+    const uint32_t m8 = q.x & 0xFFu;
+    switch (m8 ? __ffs(m8) - 1 : 8) {
+        case 0: decode_mode<0>(q, T, out, pitch); break;
+        case 1: decode_mode<1>(q, T, out, pitch); break;
+        case 2: decode_mode<2>(q, T, out, pitch); break;
+        case 3: decode_mode<3>(q, T, out, pitch); break;
+        case 4: decode_mode<4>(q, T, out, pitch); break;
+        case 5: decode_mode<5>(q, T, out, pitch); break;
+        case 6: decode_mode<6>(q, T, out, pitch); break;
+        case 7: decode_mode<7>(q, T, out, pitch); break;
+        default:  // the reserved mode
+            for (int r = 0; r < 4; ++r) *reinterpret_cast<uint4*>(out + r * pitch) = make_uint4(0u, 0u, 0u, 0u);
     }
 }
 
 __global__ void __launch_bounds__(kBc7Threads) k_bc7_decode(const Bc7Job job, const Bc7Tables tables) {
     __shared__ Bc7Tables T;
     __shared__ Bc7Level L[kBc7MaxLevels];
+    __shared__ uint4 s_blk[kBc7Threads];
+    __shared__ uint16_t s_src[kBc7Threads];
+    __shared__ uint32_t s_count[10], s_off[10];
+    __shared__ __align__(16) uint32_t s_out[4 * kTileBY][kStagePitch];
+    const int tid = threadIdx.x;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(&tables);
         uint32_t* dst = reinterpret_cast<uint32_t*>(&T);
-        for (uint32_t i = threadIdx.x; i < sizeof(Bc7Tables) / 4; i += blockDim.x) dst[i] = src[i];
+        for (uint32_t i = tid; i < sizeof(Bc7Tables) / 4; i += blockDim.x) dst[i] = src[i];
         const uint32_t* ls = reinterpret_cast<const uint32_t*>(job.L);
         uint32_t* ld = reinterpret_cast<uint32_t*>(L);
-        for (uint32_t i = threadIdx.x; i < sizeof(job.L) / 4; i += blockDim.x) ld[i] = ls[i];
+        for (uint32_t i = tid; i < sizeof(job.L) / 4; i += blockDim.x) ld[i] = ls[i];
+        if (tid < 10) s_count[tid] = 0;
     }
     __syncthreads();
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < job.total_blocks; b += stride) {
-        uint32_t l = 0;
-        while (l + 1 < job.levels && b >= L[l + 1].block0) ++l;
-        const Bc7Level& lv = L[l];
-        const uint32_t local = b - lv.block0, bx = local % lv.bw, by = local / lv.bw;
-        uint32_t px[16];
-        bc7_block(__ldg(job.blocks + b), T, px);
-        const uint32_t x0 = 4 * bx, y0 = 4 * by;
-        uint32_t* out = job.texels + lv.texel0;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const uint32_t y = y0 + r;
-            if (y >= lv.h) break;
-            uint32_t* row = out + (size_t)y * lv.w + x0;
-            if (lv.vec && x0 + 4 <= lv.w) {
-                *reinterpret_cast<uint4*>(row) = make_uint4(px[4 * r], px[4 * r + 1], px[4 * r + 2], px[4 * r + 3]);
-            } else {
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    if (x0 + c < lv.w) row[c] = px[4 * r + c];
-            }
+    const uint32_t tile = blockIdx.x;
+    uint32_t l = 0;
+    while (l + 1 < job.levels && tile >= L[l + 1].tile0) ++l;
+    const Bc7Level& lv = L[l];
+    const uint32_t lt = tile - lv.tile0;
+    const uint32_t tbx = (lt % lv.tiles_x) * kTileBX, tby = (lt / lv.tiles_x) * kTileBY;
+    // this thread's block, and its mode (9: outside the level)
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t mode = 9;
+    {
+        const uint32_t bx = tbx + tid % kTileBX, by = tby + tid / kTileBX;
+        if (bx < lv.bw && by < lv.bh) {
+            q = __ldg(job.blocks + lv.block0 + (size_t)by * lv.bw + bx);
+            const uint32_t m8 = q.x & 0xFFu;
+            mode = m8 ? __ffs(m8) - 1 : 8;
+        }
+    }
+    // counting sort of the tile's blocks by mode
+    const uint32_t rank = atomicAdd(&s_count[mode], 1u);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t acc = 0;
+        for (int m = 0; m < 10; ++m) {
+            s_off[m] = acc;
+            acc += s_count[m];
+        }
+    }
+    __syncthreads();
+    const uint32_t pos = s_off[mode] + rank;
+    s_blk[pos] = q;
+    s_src[pos] = (uint16_t)tid;
+    __syncthreads();
+    // decode the sorted blocks into the staged tile
+    {
+        const uint32_t src = s_src[tid];
+        const uint32_t sbx = src % kTileBX, sby = src / kTileBX;
+        if (tbx + sbx < lv.bw && tby + sby < lv.bh) decode_block(s_blk[tid], T, &s_out[4 * sby][4 * sbx], kStagePitch);
+    }
+    __syncthreads();
+    // the tile's texel rows, four texels per thread, consecutive threads on consecutive texels
+    for (int i = tid; i < 4 * kTileBY * kTileBX; i += kBc7Threads) {
+        const int r = i / kTileBX, g = i % kTileBX;
+        const uint32_t y = 4 * tby + r, x = 4 * (tbx + g);
+        if (y >= lv.h || x >= lv.w) continue;
+        uint32_t* dst = job.texels + lv.texel0 + (size_t)y * lv.w + x;
+        const uint4 v = *reinterpret_cast<const uint4*>(&s_out[r][4 * g]);
+        if (lv.vec && x + 4 <= lv.w) {
+            *reinterpret_cast<uint4*>(dst) = v;
+        } else {
+            dst[0] = v.x;
+            if (x + 1 < lv.w) dst[1] = v.y;
+            if (x + 2 < lv.w) dst[2] = v.z;
+            if (x + 3 < lv.w) dst[3] = v.w;
         }
     }
 }
@@ -314,26 +397,24 @@ cudaError_t bc7_decode_chain(const void* blocks, uint32_t width, uint32_t height
     job.blocks = static_cast<const uint4*>(blocks);
     job.texels = texels;
     job.levels = levels;
-    uint64_t total = 0;
+    uint64_t blocks_total = 0, tiles = 0;
     for (uint32_t l = 0; l < levels; ++l) {
         Bc7Level& lv = job.L[l];
         lv.w = std::max(1u, width >> l);
         lv.h = std::max(1u, height >> l);
         lv.bw = (lv.w + 3) / 4;
         lv.bh = (lv.h + 3) / 4;
-        lv.block0 = (uint32_t)total;
+        lv.block0 = (uint32_t)blocks_total;
         lv.texel0 = level_off[l];
         lv.vec = (lv.w % 4 == 0 && lv.texel0 % 4 == 0 && reinterpret_cast<uintptr_t>(texels) % 16 == 0) ? 1u : 0u;
-        total += (uint64_t)lv.bw * lv.bh;
+        lv.tiles_x = (lv.bw + kTileBX - 1) / kTileBX;
+        lv.tile0 = (uint32_t)tiles;
+        blocks_total += (uint64_t)lv.bw * lv.bh;
+        tiles += (uint64_t)lv.tiles_x * ((lv.bh + kTileBY - 1) / kTileBY);
     }
-    if (total >= 0xFFFFFFFFull) return cudaErrorInvalidValue;
-    job.total_blocks = (uint32_t)total;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint64_t want = (total + kBc7Threads - 1) / kBc7Threads;
-    const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)std::max(sms, 1) * 8));
-    k_bc7_decode<<<grid, kBc7Threads, 0, stream>>>(job, tables());
+    if (blocks_total >= 0xFFFFFFFFull || tiles >= 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    job.total_tiles = (uint32_t)tiles;
+    k_bc7_decode<<<(uint32_t)tiles, kBc7Threads, 0, stream>>>(job, tables());
     return cudaGetLastError();
 }
 
