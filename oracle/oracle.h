@@ -6,7 +6,9 @@
  * Parity status: unpinned by the reference. Rosy has no tests, golden images or
  * known-answer vectors, and it cannot be built or run here (Windows/VS2022,
  * Vulkan SDK, empty submodules, no graphics stack on either machine), so this
- * restatement is pinned by hand-derived known-answer tests instead.
+ * restatement is pinned by hand-derived known-answer tests instead. The BC7
+ * decoder (bc7_oracle.cpp) is pinned against the GPU texture unit's own BC7
+ * decoding, the decoder behind the reference's images (tests/golden/bc7_hw.npz).
  */
 #ifndef RZ_ORACLE_H
 #define RZ_ORACLE_H

@@ -2,7 +2,9 @@
 bench). ctypes binding of the scalar C++ restatement in rz_oracle.cpp.
 
 Parity is unpinned by the reference: Rosy has no tests or golden data and cannot
-run here; hand-derived known-answer tests pin the restatement instead.
+run here; hand-derived known-answer tests pin the restatement instead. The BC7
+decoder (bc7_oracle.cpp) is pinned against the GPU texture unit's own BC7
+decoding, the decoder behind the reference's images (tests/golden/bc7_hw.npz).
 """
 from __future__ import annotations
 
