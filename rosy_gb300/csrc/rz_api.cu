@@ -50,14 +50,22 @@ void dfree(T*& p) {
     p = nullptr;
 }
 
-// Host mirror of the device-side frame report (copied back at the end of each frame).
+// The frame report: pass headers and device error words, one block on the
+// device and its pinned host mirror, copied back in one copy at the end of each
+// frame. Each branch of the frame graph zeroes (with one clear range) and writes
+// its own error word next to its own headers, so that the clears of the two
+// concurrent branches never touch the other's flags.
 struct FrameReport {
-    uint32_t error_flags;
-    uint32_t pad;
     PassHeader shadow;
+    uint32_t shadow_errors;  // shadow pass
+    uint32_t pad0;
     PassHeader camera;
     PassHeader blended;
+    uint32_t camera_errors;  // camera and blended passes
+    uint32_t pad1;
+    uint32_t errors() const { return shadow_errors | camera_errors; }
 };
+static_assert(sizeof(FrameReport) == 160 && offsetof(FrameReport, camera) == 56, "frame report layout");
 
 // A scene: its slice of the concatenated asset and object arrays, and its surfaces.
 struct SceneHost {
@@ -162,8 +170,7 @@ struct rz_ctx {
 
     // raster scratch
     PassBuffers shadow_pass, camera_pass, blended_pass;
-    PassHeader* d_headers = nullptr;  // [0] shadow, [1] camera, [2] blended
-    uint32_t* d_error = nullptr;
+    FrameReport* d_report = nullptr;  // device frame report (pass headers, error words)
     FrameReport* h_report = nullptr;  // pinned
     bool grow_records = false, grow_chunks = false;
 
@@ -675,7 +682,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
     p.indices = c->d_indices;
     p.vertex_count = (uint32_t)c->verts.size();
     p.views = c->d_views;
-    p.error_flags = c->d_error;
+    p.error_flags = kind == 0 ? &c->d_report->shadow_errors : &c->d_report->camera_errors;
     p.chunk_stamps = c->chunk_stamps;
     p.small_extent = c->small_extent;
     p.sample_x = 128;  // pixel centre
@@ -691,7 +698,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
         p.mvp_stride = sizeof(DrawConsts) / sizeof(float);
         p.write_id = 1;
         p.ordered = 1;
-        p.header = c->d_headers + 2;
+        p.header = &c->d_report->blended;
         pb = &c->blended_pass;
     } else if (kind == 1) {
         p.draws = c->d_opaque_draws;
@@ -700,7 +707,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
         p.mvp = reinterpret_cast<const float*>(c->d_camera_consts);
         p.mvp_stride = sizeof(DrawConsts) / sizeof(float);
         p.write_id = 1;
-        p.header = c->d_headers + 1;
+        p.header = &c->d_report->camera;
         pb = &c->camera_pass;
     } else {
         p.draws = c->d_shadow_draws;
@@ -709,7 +716,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
         p.mvp = c->d_shadow_mvp;
         p.mvp_stride = 16;
         p.write_id = 0;
-        p.header = c->d_headers + 0;
+        p.header = &c->d_report->shadow;
         pb = &c->shadow_pass;
     }
     p.records = pb->records;
@@ -756,8 +763,8 @@ void stamp(rz_ctx* c, int i) {
 // follows it), else by the clear launch.
 void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
     ClearList cl{};
-    cl.ptr[0] = c->d_headers + 0;
-    cl.bytes[0] = sizeof(PassHeader);
+    cl.ptr[0] = &c->d_report->shadow;  // the shadow header and error word
+    cl.bytes[0] = offsetof(FrameReport, camera);
     cl.count = 1;
     if (c->shadow_tris) {
         cl.ptr[1] = c->shadow_pass.tile_status;
@@ -807,8 +814,8 @@ void launch_camera_raster(rz_ctx* c, PassParams cp, cudaStream_t s) {
 // else by the clear launch.
 void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& sh) {
     ClearList cl{};
-    cl.ptr[0] = c->d_headers + 1;
-    cl.bytes[0] = 2 * sizeof(PassHeader);  // camera and blended headers
+    cl.ptr[0] = &c->d_report->camera;  // the camera and blended headers and their error word
+    cl.bytes[0] = sizeof(FrameReport) - offsetof(FrameReport, camera);
     cl.count = 1;
     if (!c->opaque_tris) {
         cl.ptr[cl.count] = c->d_vis;
@@ -864,13 +871,15 @@ void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
         cl.bytes[0] = rg.shadow * 4;
         cl.ptr[1] = c->d_vis + rg.pix_off * c->samples;
         cl.bytes[1] = rg.pix * 8 * c->samples;
-        cl.ptr[2] = c->d_headers;
-        cl.bytes[2] = 2 * sizeof(PassHeader);
-        cl.count = 3;
+        cl.ptr[2] = &c->d_report->shadow;  // headers only: the error words hold the whole frame's flags
+        cl.bytes[2] = sizeof(PassHeader);
+        cl.ptr[3] = &c->d_report->camera;
+        cl.bytes[3] = sizeof(PassHeader);
+        cl.count = 4;
         if (c->shadow_tris) {
-            cl.ptr[3] = c->shadow_pass.tile_status;
-            cl.bytes[3] = (size_t)setup_ctas(rg.shadow_tris) * 8;
-            cl.count = 4;
+            cl.ptr[4] = c->shadow_pass.tile_status;
+            cl.bytes[4] = (size_t)setup_ctas(rg.shadow_tris) * 8;
+            cl.count = 5;
         }
         launch_clear(cl, c->sm_count, s);
         if (c->opaque_tris) {
@@ -910,8 +919,9 @@ void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
 int enqueue_frame(rz_ctx* c) {
     cudaStream_t s = c->stream;
     const ShadeParams sh = shade_params(c);
-    RZ_CUDA(c, cudaMemsetAsync(c->d_error, 0, sizeof(uint32_t), s), "clear error flags");
     if (!c->batched && !c->blended_tris && !c->timing) {
+        // per-view launches clear the pass headers view by view; the error words once per frame
+        RZ_CUDA(c, cudaMemsetAsync(c->d_report, 0, sizeof(FrameReport), s), "clear frame report");
         launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s);
         launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s);
         enqueue_sequential(c, s, sh);
@@ -937,16 +947,14 @@ int enqueue_frame(rz_ctx* c) {
         bp.sh.draw_count = c->blended_draw_count;
         bp.sh.consts = c->d_blended_consts;
         bp.records = c->blended_pass.records;
-        bp.header = c->d_headers + 2;
+        bp.header = &c->d_report->blended;
         bp.record_capacity = c->blended_pass.record_capacity;
         launch_blend(bp, s);
     }
     if (c->timing) stamp(c, 7);
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
-    RZ_CUDA(c, cudaMemcpyAsync(&c->h_report->error_flags, c->d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
-            "read error flags");
-    RZ_CUDA(c, cudaMemcpyAsync(&c->h_report->shadow, c->d_headers, 3 * sizeof(PassHeader), cudaMemcpyDeviceToHost, s),
-            "read pass headers");
+    RZ_CUDA(c, cudaMemcpyAsync(c->h_report, c->d_report, sizeof(FrameReport), cudaMemcpyDeviceToHost, s),
+            "read frame report");
     return RZ_OK;
 }
 
@@ -1046,7 +1054,7 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->objects_copied, cudaEventDisableTiming) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
-    if (dalloc(&c->d_headers, 3) != cudaSuccess || dalloc(&c->d_error, 1) != cudaSuccess ||
+    if (dalloc(&c->d_report, 1) != cudaSuccess || cudaMemset(c->d_report, 0, sizeof(FrameReport)) != cudaSuccess ||
         dalloc(&c->d_srgb, 256) != cudaSuccess)
         return bail(RZ_ALLOCATION_FAILURE);
     if (cudaMallocHost(&c->h_report, sizeof(FrameReport)) != cudaSuccess) return bail(RZ_ALLOCATION_FAILURE);
@@ -1114,8 +1122,7 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_camera_consts);
     dfree(c->d_blended_consts);
     dfree(c->d_varyings);
-    dfree(c->d_headers);
-    dfree(c->d_error);
+    dfree(c->d_report);
     if (c->h_scene_data) cudaFreeHost(c->h_scene_data);
     if (c->h_report) cudaFreeHost(c->h_report);
     if (c->h_objects) cudaFreeHost(c->h_objects);
@@ -1357,7 +1364,7 @@ int rz_sync(rz_ctx* c, uint32_t timeout_ms) {
     }
     if (!c->frame_pending) return RZ_OK;
     c->frame_pending = false;
-    const uint32_t e = c->h_report->error_flags;
+    const uint32_t e = c->h_report->errors();
     if (e & (kErrRecordOverflow)) c->grow_records = true;
     if (e & (kErrStampOverflow)) c->grow_chunks = true;
     if (e & (kErrRecordOverflow | kErrStampOverflow))
@@ -1426,7 +1433,7 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->camera_setup_records = c->h_report->camera.records + c->h_report->camera.small_records;
     out->shadow_stamps = c->h_report->shadow.stamps;
     out->camera_stamps = c->h_report->camera.stamps;
-    out->error_flags = c->h_report->error_flags;
+    out->error_flags = c->h_report->errors();
     // clears (2) + shadow prep/setup/raster + camera prep/setup/raster + vertex + shade (+ blended: prep, setup, vertex, blend)
     out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + 1u + (c->opaque_tris ? 1u + c->samples : 0u) +
                            (c->varying_count ? 1u : 0u) + 1u + (c->blended_tris ? 4u : 0u);

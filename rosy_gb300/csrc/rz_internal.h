@@ -207,8 +207,8 @@ struct BlendParams {
 
 // Up to four buffers to zero in one launch (16-byte stores, byte tail).
 struct ClearList {
-    void* ptr[4];
-    size_t bytes[4];
+    void* ptr[6];
+    size_t bytes[6];
     int count;
 };
 
