@@ -917,7 +917,7 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
     VR.color[p] = encode_srgb8(r[0]) | (encode_srgb8(r[1]) << 8) | (encode_srgb8(r[2]) << 16) | (encode_unorm8(r[3]) << 24);
 }
 
-__global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
+__global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
     __shared__ uint32_t s_view;
     {
@@ -966,7 +966,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(ShadeParams P) {
 }
 
 // k_shade for 4x multisampled views.
-__global__ void __launch_bounds__(256, 2) k_shade_msaa(ShadeParams P) {
+__global__ void __launch_bounds__(256, 3) k_shade_msaa(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
     __shared__ uint32_t s_view;
     {
