@@ -966,7 +966,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
 }
 
 // k_shade for 4x multisampled views.
-__global__ void __launch_bounds__(256, 3) k_shade_msaa(ShadeParams P) {
+__global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
     __shared__ uint32_t s_view;
     {
