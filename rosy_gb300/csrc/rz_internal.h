@@ -93,6 +93,15 @@ static_assert(sizeof(TriRecord) == 64, "TriRecord is 64 bytes");
 
 // Records of the shadow pass carry the cascade in the top bits of their view field.
 constexpr uint32_t kViewBits = 24;
+constexpr uint32_t kCascadeMask = 3u;     // cascade = (view >> kViewBits) & kCascadeMask
+// Large records also carry raster facts the setup computed once, so that the
+// raster decodes them instead of recomputing them for every chunk a record
+// meets: view bits 26-28 the top-left bias of edges 0-2 (1: not a top-left
+// edge), 29 medium, 30 box cut by the viewport, 31 near origin; stamp_offset
+// bits 40-63 the stamps per row of the record's box.
+constexpr uint32_t kRecFlagShift = 26;
+constexpr uint32_t kRecViewMask = (1u << kRecFlagShift) - 1u;  // view index and cascade
+constexpr int kStampOffsetBits = 40;
 constexpr uint32_t kViewMask = (1u << kViewBits) - 1u;
 constexpr int kMaxCascades = 4;
 

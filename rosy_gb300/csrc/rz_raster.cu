@@ -182,6 +182,42 @@ __device__ __forceinline__ uint32_t record_stamps(const TriRecord& r) {
     return (uint32_t)((px1 - px0) / kStampW + 1) * (uint32_t)((py1 - py0) / kStampH + 1);
 }
 
+// Triangles up to this extent (pixels, each way) take the incremental 32-bit
+// path: every edge value over the bounding box plus a stamp of overhang is
+// below 2 * ((90 + 8) * 256)^2 < 2^31.
+constexpr int kMediumExtent = 90;
+
+// The raster facts of a large record (packed by the setup, decoded by
+// load_large): the edges' top-left bias, whether the 32-bit incremental walk
+// applies (medium), whether the viewport cut its box (clipped), whether float
+// offsets from vertex 0 are exact over the box (near_origin), and its stamps per row.
+__device__ __forceinline__ uint32_t large_facts(const TriRecord& r, int32_t bb_hi, uint32_t& nsx) {
+    const int32_t X[3] = {r.X0, r.X1, r.X2}, Y[3] = {r.Y0, r.Y1, r.Y2};
+    const int px0 = (int)(r.p0 & 0xffff), py0 = (int)(r.p0 >> 16), px1 = (int)(r.p1 & 0xffff), py1 = (int)(r.p1 >> 16);
+    uint32_t flags = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, b = (i + 2) % 3;
+        const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+        if (!(dy < 0 || (dy == 0 && dx > 0))) flags |= 1u << i;
+    }
+    const int32_t lo_x = px0 * 256 - X[0], hi_x = px1 * 256 + 256 - X[0] + kStampW * 256;
+    const int32_t lo_y = py0 * 256 - Y[0], hi_y = py1 * 256 + 256 - Y[0] + kStampH * 256;
+    const int32_t lim = 1 << 23;
+    const bool near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
+    const int32_t max_x = max(X[0], max(X[1], X[2])), max_y = max(Y[0], max(Y[1], Y[2]));
+    const int32_t ex = max_x - min(X[0], min(X[1], X[2]));
+    const int32_t ey = max_y - min(Y[0], min(Y[1], Y[2]));
+    // Pixels past an uncut box edge lie outside the triangle's extent, so the edge
+    // test alone rejects the stamps' overhang there; only a cut box needs the check.
+    const bool clipped = ((max_x - bb_hi) >> 8) > px1 || ((max_y - bb_hi) >> 8) > py1;
+    const bool medium = near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
+    flags |= (medium ? 8u : 0u) | (clipped ? 16u : 0u) | (near_origin ? 32u : 0u);
+    nsx = (uint32_t)((px1 - px0) / kStampW + 1);
+    return flags;
+}
+
+
 // Viewport and fixed-function state of the view a triangle belongs to.
 struct ViewState {
     int width, height;
@@ -368,7 +404,9 @@ struct WriteEmit {
             atomicOr(P->error_flags, kErrRecordOverflow);
             return;
         }
-        r.stamp_offset = stamp;
+        uint32_t nsx;
+        r.view |= large_facts(r, P->bb_hi, nsx) << kRecFlagShift;
+        r.stamp_offset = stamp | ((uint64_t)nsx << kStampOffsetBits);
         store_record(P->records + rec, r);
         // chunks whose first stamp lies inside this record start here
         const uint64_t cs = P->chunk_stamps;
@@ -581,7 +619,8 @@ template <bool kWriteId>
 __device__ __forceinline__ Target view_target(const PassParams& P, uint32_t view) {
     const ViewRec& V = P.views[view & kViewMask];
     if (kWriteId) return Target{V.vis + (size_t)P.sample_plane * (size_t)V.width * (size_t)V.height, V.width};
-    return Target{V.shadow + (size_t)(view >> kViewBits) * (size_t)V.shadow_w * (size_t)V.shadow_h, V.shadow_w};
+    return Target{V.shadow + (size_t)((view >> kViewBits) & kCascadeMask) * (size_t)V.shadow_w * (size_t)V.shadow_h,
+                  V.shadow_w};
 }
 
 template <bool kWriteId>
@@ -637,10 +676,6 @@ __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecor
     }
 }
 
-// Triangles up to this extent (pixels, each way) take the incremental 32-bit
-// path: every edge value over the bounding box plus a stamp of overhang is
-// below 2 * ((90 + 8) * 256)^2 < 2^31.
-constexpr int kMediumExtent = 90;
 
 struct LargeRecord {
     int32_t X[3], Y[3];
@@ -656,7 +691,7 @@ struct LargeRecord {
     uint64_t begin, end;
 };
 
-__device__ __forceinline__ void load_large(const TriRecord* rec, int32_t bb_hi, LargeRecord& L) {
+__device__ __forceinline__ void load_large(const TriRecord* rec, int32_t, LargeRecord& L) {
     const int4* src = reinterpret_cast<const int4*>(rec);
     const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
     L.X[0] = q0.x;
@@ -676,28 +711,21 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, int32_t bb_hi, 
     L.px1 = q2.w & 0xffff;
     L.py1 = (uint32_t)q2.w >> 16;
     L.id = (uint32_t)q3.x;
-    L.view = (uint32_t)q3.y;
-    L.begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)(uint32_t)q3.w << 32);
-    L.nsx = (uint32_t)((L.px1 - L.px0) / kStampW + 1);
+    const uint32_t flags = (uint32_t)q3.y >> kRecFlagShift;
+    L.view = (uint32_t)q3.y & kRecViewMask;
+    L.begin = (uint64_t)(uint32_t)q3.z | ((uint64_t)((uint32_t)q3.w & 0xffu) << 32);
+    L.nsx = (uint32_t)q3.w >> (kStampOffsetBits - 32);
     L.end = L.begin + (uint64_t)L.nsx * (uint32_t)((L.py1 - L.py0) / kStampH + 1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const int a = (i + 1) % 3, b = (i + 2) % 3;
         L.dx[i] = L.X[b] - L.X[a];
         L.dy[i] = L.Y[b] - L.Y[a];
-        L.tl_bias[i] = (L.dy[i] < 0 || (L.dy[i] == 0 && L.dx[i] > 0)) ? 0u : 1u;
+        L.tl_bias[i] = (flags >> i) & 1u;
     }
-    const int32_t lo_x = L.px0 * 256 - L.X0, hi_x = L.px1 * 256 + 256 - L.X0 + kStampW * 256;
-    const int32_t lo_y = L.py0 * 256 - L.Y0, hi_y = L.py1 * 256 + 256 - L.Y0 + kStampH * 256;
-    const int32_t lim = 1 << 23;
-    L.near_origin = lo_x > -lim && hi_x < lim && lo_y > -lim && hi_y < lim;
-    const int32_t max_x = max(L.X[0], max(L.X[1], L.X[2])), max_y = max(L.Y[0], max(L.Y[1], L.Y[2]));
-    const int32_t ex = max_x - min(L.X[0], min(L.X[1], L.X[2]));
-    const int32_t ey = max_y - min(L.Y[0], min(L.Y[1], L.Y[2]));
-    // Pixels past an uncut box edge lie outside the triangle's extent, so the edge
-    // test alone rejects the stamps' overhang there; only a cut box needs the check.
-    L.clipped = ((max_x - bb_hi) >> 8) > L.px1 || ((max_y - bb_hi) >> 8) > L.py1;
-    L.medium = L.near_origin && ex <= kMediumExtent * 256 && ey <= kMediumExtent * 256;
+    L.medium = (flags & 8u) != 0;
+    L.clipped = (flags & 16u) != 0;
+    L.near_origin = (flags & 32u) != 0;
 }
 
 // Edge constants of the generic (64-bit) path.
@@ -898,6 +926,8 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
     const uint32_t chunks = P.header->chunks;
     const uint64_t total = P.header->stamps;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t cur_view = 0xffffffffu;  // the view whose target T holds
+    Target T{nullptr, 0};
     for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < chunks; k += warps) {
         uint64_t s = (uint64_t)k * P.chunk_stamps;
         const uint64_t s_end = (s + P.chunk_stamps < total) ? (s + P.chunk_stamps) : total;
@@ -913,8 +943,11 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
             const uint64_t seg_end = s_end < L.end ? s_end : L.end;
             const uint32_t n = (uint32_t)(seg_end - s);
             const uint32_t i = (uint32_t)(s - L.begin);
-            const uint32_t sy = i / L.nsx, sx = i - sy * L.nsx;
-            const Target T = view_target<kWriteId>(P, L.view);
+            const uint32_t sy = i ? i / L.nsx : 0u, sx = i - sy * L.nsx;  // a segment mostly starts at its record's first stamp
+            if (L.view != cur_view) {
+                T = view_target<kWriteId>(P, L.view);
+                cur_view = L.view;
+            }
             if (L.medium) {
                 MediumWalk w;
                 medium_start(L, sx, sy, lx, ly, P.sample_x, P.sample_y, w);

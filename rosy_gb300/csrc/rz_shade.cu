@@ -1058,7 +1058,8 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
             if (r < n) {
                 const TriRecord& rec = B.records[r];
                 const int bx0 = rec.p0 & 0xffff, by0 = rec.p0 >> 16, bx1 = rec.p1 & 0xffff, by1 = rec.p1 >> 16;
-                if (rec.view == view && bx1 >= tx0 && bx0 <= tx0 + 15 && by1 >= ty0 && by0 <= ty0 + 15) mask |= 1u << k;
+                if ((rec.view & kViewMask) == view && bx1 >= tx0 && bx0 <= tx0 + 15 && by1 >= ty0 && by0 <= ty0 + 15)
+                    mask |= 1u << k;
             }
         }
         const uint32_t cnt = __popc(mask);
