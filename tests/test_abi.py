@@ -71,3 +71,18 @@ def test_create_rejects_bad_config_without_touching_the_gpu(renderer_lib):
     assert renderer_lib.rz_create(C.byref(out), C.byref(cfg)) == 3
     cfg = _abi.RzConfig(width=10, height=10, shadow_map_size=16, samples=3, device=0)
     assert renderer_lib.rz_create(C.byref(out), C.byref(cfg)) == 3
+
+
+def test_texture_entry_points_reject_bad_arguments_without_touching_the_gpu(renderer_lib):
+    """BC7 decode and .dds entry points validate their arguments before any CUDA call."""
+    buf = C.create_string_buffer(64)
+    assert renderer_lib.rz_bc7_decode(None, 4, 4, buf, None) == 3
+    assert renderer_lib.rz_bc7_decode(buf, 4, 4, None, None) == 3
+    assert renderer_lib.rz_bc7_decode(buf, 0, 4, buf, None) == 3
+    assert renderer_lib.rz_bc7_decode_texture_unit(buf, 6, 4, buf) == 3  # not a multiple of 4
+    assert renderer_lib.rz_bc7_decode_texture_unit(None, 4, 4, buf) == 3
+    out = C.c_void_p()
+    assert renderer_lib.rz_dds_read(None, C.byref(out)) == 3
+    assert renderer_lib.rz_dds_parse(None, 16, C.byref(out)) == 3
+    assert renderer_lib.rz_dds_get_info(None, None) == 3
+    renderer_lib.rz_dds_free(None)
