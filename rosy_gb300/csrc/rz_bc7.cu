@@ -25,7 +25,8 @@
 // by inserting the anchors' missing high bits. Decoded texels are staged in
 // shared memory and the tile leaves as 16 rows of 1 KB, coalesced. Tables
 // (partition maps, anchors) are a kernel parameter copied to shared memory.
-// Bound: HBM, 16 bytes read + 64 written per block.
+// Algorithmic traffic: 16 bytes read + 64 written per block (the HBM roofline);
+// the decode arithmetic (integer ALU issue) bounds it before HBM does.
 #include "rz_device.cuh"
 
 namespace rz {
