@@ -199,7 +199,7 @@ extern "C" void oracle_bc7_block(const uint8_t block[16], uint8_t out[64]) {
 
 extern "C" int oracle_bc7_decode(const uint8_t* blocks, uint32_t width, uint32_t height, uint8_t* rgba) {
     if (!blocks || !rgba || width == 0 || height == 0) return 3;
-    const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
+    const uint32_t bw = (uint32_t)(((uint64_t)width + 3) / 4), bh = (uint32_t)(((uint64_t)height + 3) / 4);
     uint8_t px[64];
     for (uint32_t by = 0; by < bh; ++by)
         for (uint32_t bx = 0; bx < bw; ++bx) {

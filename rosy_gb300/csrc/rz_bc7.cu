@@ -384,7 +384,7 @@ uint64_t bc7_chain_bytes(uint32_t width, uint32_t height, uint32_t levels) {
     uint64_t n = 0;
     for (uint32_t l = 0; l < levels; ++l) {
         const uint32_t w = std::max(1u, width >> l), h = std::max(1u, height >> l);
-        n += (uint64_t)((w + 3) / 4) * ((h + 3) / 4) * 16;
+        n += (((uint64_t)w + 3) / 4) * (((uint64_t)h + 3) / 4) * 16;
     }
     return n;
 }
@@ -403,8 +403,8 @@ cudaError_t bc7_decode_chain(const void* blocks, uint32_t width, uint32_t height
         Bc7Level& lv = job.L[l];
         lv.w = std::max(1u, width >> l);
         lv.h = std::max(1u, height >> l);
-        lv.bw = (lv.w + 3) / 4;
-        lv.bh = (lv.h + 3) / 4;
+        lv.bw = (uint32_t)(((uint64_t)lv.w + 3) / 4);  // 64-bit: no wrap near 2^32
+        lv.bh = (uint32_t)(((uint64_t)lv.h + 3) / 4);
         lv.block0 = (uint32_t)blocks_total;
         lv.texel0 = level_off[l];
         lv.vec = (lv.w % 4 == 0 && lv.texel0 % 4 == 0 && reinterpret_cast<uintptr_t>(texels) % 16 == 0) ? 1u : 0u;

@@ -57,7 +57,8 @@ int parse(const std::vector<unsigned char>& b, rz_dds_info& info) {
     uint64_t total = 0;
     uint32_t w = width, h = height;
     for (uint32_t l = 0; l < levels; ++l) {
-        total += (uint64_t)((w + 3) / 4 > 1 ? (w + 3) / 4 : 1) * ((h + 3) / 4 > 1 ? (h + 3) / 4 : 1) * 16;
+        const uint64_t bw = ((uint64_t)w + 3) / 4, bh = ((uint64_t)h + 3) / 4;  // 64-bit: no wrap near 2^32
+        total += (bw > 1 ? bw : 1) * (bh > 1 ? bh : 1) * 16;
         if (total > avail) return RZ_READ_FAILED;                 // a level past the end of the file
         w = w / 2 > 1 ? w / 2 : 1;
         h = h / 2 > 1 ? h / 2 : 1;

@@ -130,7 +130,7 @@ def test_dds_round_trip(tmp_path):
 
 @pytest.mark.parametrize("case,code", [
     ("short", 11), ("magic", 11), ("dx10_short", 11), ("legacy_fourcc", 3), ("not_bc7", 3),
-    ("array", 3), ("truncated_mips", 11), ("zero_width", 11), ("array_zero", 11),
+    ("array", 3), ("truncated_mips", 11), ("zero_width", 11), ("array_zero", 11), ("huge_width", 11),
 ])
 def test_dds_rejects_malformed(case, code):
     blocks = np.zeros((bc7.chain_bytes(16, 16, 3) // 16, 16), np.uint8)
@@ -145,6 +145,8 @@ def test_dds_rejects_malformed(case, code):
         "truncated_mips": good[:-1],
         "zero_width": dds.dds_bytes(0, 16, 1, blocks[:4]),
         "array_zero": dds.dds_bytes(16, 16, 3, blocks, array_size=0),
+        # (width + 3) / 4 must not wrap in 32 bits: 2^32 - 1 texels wide needs far more than the file holds
+        "huge_width": good[:16] + (0xFFFFFFFF).to_bytes(4, "little") + good[20:],
     }[case]
     with pytest.raises(_lib.RzError) as e:
         dds.DdsImage(data=data)
@@ -174,3 +176,41 @@ def test_rsy_scene_loads_dds_images(tmp_path):
     assert s.textures[0].format == 1 and (s.textures[0].width, s.textures[0].height) == (8, 8)
     assert s.textures[1].format == 0 and s.textures[1].width == 1
     assert s.missing_images == ["missing.dds"]
+
+
+def test_dds_parser_survives_random_and_mutated_files():
+    """Random bytes and random byte edits of a valid file: the parser returns a
+    result code (or parses) and never reads out of bounds or crashes."""
+    hypothesis = pytest.importorskip("hypothesis")
+    from hypothesis import given, settings
+    from hypothesis import strategies as st
+
+    blocks = bc7.mixed_blocks(np.random.default_rng(9), bc7.chain_bytes(12, 8, 3) // 16)
+    good = dds.dds_bytes(12, 8, 3, blocks)
+
+    @settings(max_examples=300, deadline=None, derandomize=True)
+    @given(st.binary(max_size=400))
+    def random_bytes(data):
+        try:
+            im = dds.DdsImage(data=data)
+            assert im.info.data_bytes <= len(data)
+        except _lib.RzError as e:
+            assert e.code in (3, 11)
+
+    @settings(max_examples=300, deadline=None, derandomize=True)
+    @given(st.lists(st.tuples(st.integers(0, len(good) - 1), st.integers(0, 255)), max_size=8),
+           st.integers(0, len(good)))
+    def mutated(edits, cut):
+        data = bytearray(good)
+        for pos, val in edits:
+            data[pos] = val
+        data = bytes(data[:cut])
+        try:
+            im = dds.DdsImage(data=data)
+            assert 148 + im.info.data_bytes <= len(data)
+            assert im.info.levels >= 1 and im.info.width > 0 and im.info.height > 0
+        except _lib.RzError as e:
+            assert e.code in (3, 11)
+
+    random_bytes()
+    mutated()
