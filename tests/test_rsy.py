@@ -157,3 +157,45 @@ def test_rsy_scene_gpu_matches_oracle(tmp_path, gpu, oracle):
     assert np.array_equal(got["ids"], want["ids"])
     assert np.array_equal(got["depth"], want["depth"])
     assert np.abs(got["color"].astype(int) - want["color"].astype(int)).max() <= 1
+
+
+def test_rsy_reader_survives_mutated_files(tmp_path, renderer_lib):
+    """Random byte edits and truncations of a valid file: the reader returns a
+    result code or an asset whose counts are consistent, never crashes."""
+    pytest.importorskip("hypothesis")
+    from hypothesis import given, settings
+    from hypothesis import strategies as st
+
+    a, _ = _asset()
+    path = str(tmp_path / "good.rsy")
+    rsy.write_rsy(path, a)
+    good = open(path, "rb").read()
+    bad = str(tmp_path / "bad.rsy")
+
+    @settings(max_examples=200, deadline=None, derandomize=True)
+    @given(st.lists(st.tuples(st.integers(0, len(good) - 1), st.integers(0, 255)), max_size=6),
+           st.integers(0, len(good)))
+    def mutated(edits, cut):
+        data = bytearray(good)
+        for pos, val in edits:
+            data[pos] = val
+        with open(bad, "wb") as f:
+            f.write(bytes(data[:cut]))
+        try:
+            f = rsy.RsyFile(bad)
+        except RzError as e:
+            assert e.code in (3, 11)
+            return
+        try:
+            meshes = f.meshes()
+            assert len(meshes) == f.info.mesh_count
+            assert len(f.materials()) == f.info.material_count
+            f.images()
+            try:
+                f.scene_objects()
+            except RzError as e:  # a damaged scene graph is reported, not followed
+                assert e.code == 3
+        finally:
+            f.close()
+
+    mutated()
