@@ -94,6 +94,15 @@ def ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
+def texel_bytes(width: int, height: int, levels: int, fmt: int) -> int:
+    """Bytes of a texture's level chain: 4 per texel (RGBA8) or 16 per 4 x 4 block (BC7)."""
+    n = 0
+    for l in range(levels):
+        w, h = max(1, width >> l), max(1, height >> l)
+        n += max(1, (w + 3) // 4) * max(1, (h + 3) // 4) * 16 if fmt == TEXELS_BC7 else w * h * 4
+    return n
+
+
 class Marshalled:
     """Keeps the numpy/ctypes buffers of one scene alive while C code uses them."""
 
@@ -104,6 +113,9 @@ class Marshalled:
         self.mesh_table = np.ascontiguousarray(np.asarray(s.meshes, np.uint32).reshape(-1, 4))
         self.meshes = (RzMesh * len(s.meshes))()
         for i, (vo, vc, io, ic) in enumerate(s.meshes):
+            # the library reads through these pointers: every range must lie inside its array
+            if not (0 <= vo and vo + vc <= len(self.vertices) and 0 <= io and io + ic <= len(self.indices)):
+                raise ValueError(f"mesh {i} lies outside the vertex or index array")
             self.meshes[i].positions = ptr(self.vertices) + int(vo) * 64
             self.meshes[i].position_count = int(vc)
             self.meshes[i].index_count = int(ic)
@@ -121,6 +133,9 @@ class Marshalled:
             self.textures[i].image_type = t.image_type
             self.textures[i].texels = ptr(self.tex_data[i])
             self.textures[i].format = getattr(t, "format", TEXELS_RGBA8)
+            if 0 < t.width and 0 < t.height and 0 < t.levels <= 16 and \
+                    self.tex_data[i].nbytes < texel_bytes(t.width, t.height, t.levels, self.textures[i].format):
+                raise ValueError(f"texture {i} holds fewer bytes than its level chain")
         self.scene_rec = np.ascontiguousarray(s.scene)
         self.draw_config = np.ascontiguousarray(s.draw_config)
 

@@ -308,11 +308,14 @@ int append_asset(rz_ctx* c, const rz_mesh* meshes, uint32_t mesh_count, const rz
     if (nv >= 0xFFFFFFFFull || ni >= 0xFFFFFFFFull) return fail(c, RZ_OVERFLOW, "asset too large");
     for (uint32_t i = 0; i < tex_count; ++i) {
         const rz_texture& t = textures[i];
-        if (t.width == 0 || t.height == 0 || t.levels == 0 || t.levels > 16 || !t.texels ||
+        // extents up to 2^30 keep the sampler's int texel arithmetic exact
+        if (t.width == 0 || t.height == 0 || t.width > (1u << 30) || t.height > (1u << 30) || t.levels == 0 ||
+            t.levels > 16 || !t.texels ||
             (t.format != RZ_TEXELS_RGBA8 && t.format != RZ_TEXELS_BC7))
             return fail(c, RZ_INVALID_ARGUMENT, "texture " + std::to_string(i) + " is malformed");
+        // levels <= 16 is checked above, so counting stops there (a shift by 32 is undefined)
         uint32_t max_levels = 1;
-        while ((t.width >> max_levels) || (t.height >> max_levels)) ++max_levels;
+        while (max_levels < 16 && ((t.width >> max_levels) || (t.height >> max_levels))) ++max_levels;
         if (t.levels > max_levels) return fail(c, RZ_INVALID_ARGUMENT, "texture has too many levels");
     }
     SceneHost sh;

@@ -86,3 +86,30 @@ def test_texture_entry_points_reject_bad_arguments_without_touching_the_gpu(rend
     assert renderer_lib.rz_dds_parse(None, 16, C.byref(out)) == 3
     assert renderer_lib.rz_dds_get_info(None, None) == 3
     renderer_lib.rz_dds_free(None)
+
+
+def test_marshalling_rejects_ranges_outside_their_arrays():
+    """The library reads meshes and texels through raw pointers, so the Python side
+    checks every range against its array before handing the pointers over."""
+    import dataclasses
+
+    import pytest
+
+    s = sc.tiny(0)
+    _abi.Marshalled(s)  # the scene as made is accepted
+    bad = dataclasses.replace(s, meshes=[(0, len(s.vertices) + 1, 0, len(s.indices))])
+    with pytest.raises(ValueError, match="mesh 0"):
+        _abi.Marshalled(bad)
+    bad = dataclasses.replace(s, meshes=[(0, len(s.vertices), 3, len(s.indices))])
+    with pytest.raises(ValueError, match="mesh 0"):
+        _abi.Marshalled(bad)
+    t = s.textures[0]
+    short = dataclasses.replace(t, texels=t.texels[:-1])
+    with pytest.raises(ValueError, match="texture 0"):
+        _abi.Marshalled(dataclasses.replace(s, textures=[short] + s.textures[1:]))
+    huge = dataclasses.replace(t, width=1 << 31, height=1, levels=1)
+    with pytest.raises(ValueError, match="texture 0"):
+        _abi.Marshalled(dataclasses.replace(s, textures=[huge] + s.textures[1:]))
+    # BC7 chains are counted in 16-byte blocks
+    assert _abi.texel_bytes(6, 5, 3, _abi.TEXELS_BC7) == (2 * 2 + 1 * 1 + 1 * 1) * 16
+    assert _abi.texel_bytes(6, 5, 3, _abi.TEXELS_RGBA8) == (30 + 6 + 1) * 4
