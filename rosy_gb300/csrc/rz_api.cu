@@ -181,6 +181,7 @@ struct rz_ctx {
     cudaEvent_t frame_done = nullptr;
     bool frame_pending = false;
     bool timing = false;
+    uint32_t frame_launches = 0;  // kernels the last enqueued frame launches (graph replays included)
     cudaEvent_t stage_ev[RZ_STAGE_COUNT + 1] = {};
     uint32_t frames = 0;
 };
@@ -921,6 +922,7 @@ void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
 // the camera passes, joining before the shading (which reads the shadow maps).
 int enqueue_frame(rz_ctx* c) {
     cudaStream_t s = c->stream;
+    take_launches();  // start this frame's count
     const ShadeParams sh = shade_params(c);
     if (!c->batched && !c->blended_tris && !c->timing) {
         // per-view launches clear the pass headers view by view; the error words once per frame
@@ -958,6 +960,7 @@ int enqueue_frame(rz_ctx* c) {
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
     RZ_CUDA(c, cudaMemcpyAsync(c->h_report, c->d_report, sizeof(FrameReport), cudaMemcpyDeviceToHost, s),
             "read frame report");
+    c->frame_launches = take_launches();
     return RZ_OK;
 }
 
@@ -1437,9 +1440,7 @@ int rz_get_stats(rz_ctx* c, rz_stats* out) {
     out->shadow_stamps = c->h_report->shadow.stamps;
     out->camera_stamps = c->h_report->camera.stamps;
     out->error_flags = c->h_report->errors();
-    // clears (2) + shadow prep/setup/raster + camera prep/setup/raster + vertex + shade (+ blended: prep, setup, vertex, blend)
-    out->kernel_launches = 2u + (c->shadow_tris ? 3u : 0u) + 1u + (c->opaque_tris ? 1u + c->samples : 0u) +
-                           (c->varying_count ? 1u : 0u) + 1u + (c->blended_tris ? 4u : 0u);
+    out->kernel_launches = c->frame_launches;  // counted by the launchers as the frame was enqueued
     return RZ_OK;
 }
 

@@ -221,7 +221,11 @@ struct ClearList {
     int count;
 };
 
-// Launchers (rz_raster.cu / rz_shade.cu). All enqueue on `stream`.
+// Launchers (rz_raster.cu / rz_shade.cu). All enqueue on `stream`, and add the
+// kernels they enqueue to a per-thread count: take_launches() returns the count
+// since its last call and starts a new one (a frame's exact launch count).
+void note_launch();
+uint32_t take_launches();
 void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream);
 void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
                  float* out_mvp, cudaStream_t stream);

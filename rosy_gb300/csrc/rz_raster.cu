@@ -56,10 +56,23 @@ __global__ void k_prep(const DrawRec* __restrict__ draws, uint32_t n, const rz_o
     for (int i = 0; i < 16; ++i) out[16 * d + i] = C[i];
 }
 
+namespace {
+thread_local uint32_t t_launches = 0;
+}  // namespace
+
+void note_launch() { ++t_launches; }
+
+uint32_t take_launches() {
+    const uint32_t n = t_launches;
+    t_launches = 0;
+    return n;
+}
+
 void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views, float* out_mvp,
                  cudaStream_t stream) {
     if (n == 0) return;
     k_prep<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, views, out_mvp);
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -96,6 +109,7 @@ void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream) {
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     k_clear<<<(unsigned)blocks, 256, 0, stream>>>(list);
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -597,6 +611,7 @@ void launch_setup(const PassParams& p, cudaStream_t stream) {
     const int ctas = setup_ctas(p.tri_total);
     if (ctas == 0) return;
     k_setup<<<ctas, kSetupThreads, 0, stream>>>(p);
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -991,6 +1006,7 @@ void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream) {
     const int blocks = sm_count * occ[t];
     if (p.write_id) k_raster<true><<<blocks, 256, 0, stream>>>(p);
     else k_raster<false><<<blocks, 256, 0, stream>>>(p);
+    note_launch();
 }
 
 }  // namespace rz

@@ -105,6 +105,7 @@ void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objec
                         DrawConsts* out, cudaStream_t stream) {
     if (n == 0) return;
     k_prep_camera<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, views, out);
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -697,11 +698,13 @@ __global__ void __launch_bounds__(256) k_vertex(ShadeParams P, uint32_t first) {
 void launch_vertex(const ShadeParams& p, cudaStream_t stream) {
     if (p.varying_count == 0 || p.draw_count == 0) return;
     k_vertex<<<(p.varying_count + 255) / 256, 256, 0, stream>>>(p, 0u);
+    note_launch();
 }
 
 void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stream) {
     if (p.varying_count <= first || p.draw_count == 0) return;
     k_vertex<<<(p.varying_count - first + 255) / 256, 256, 0, stream>>>(p, first);
+    note_launch();
 }
 
 // Shade triangle `tri` (pass-global id) at pixel (px, py) from the varying
@@ -987,6 +990,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
     if (p.shade_blocks == 0) return;
+    note_launch();
     if (p.samples > 1) {
         k_shade_msaa<<<p.shade_blocks, dim3(16, 16), 0, stream>>>(p);
         return;
@@ -1133,6 +1137,7 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
 void launch_blend(const BlendParams& p, cudaStream_t stream) {
     if (p.sh.shade_blocks == 0) return;
     k_blend<<<p.sh.shade_blocks, dim3(16, 16), 0, stream>>>(p);
+    note_launch();
 }
 
 }  // namespace rz

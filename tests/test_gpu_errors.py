@@ -87,3 +87,27 @@ def test_stage_timing(gpu):
         g.sync()
     finally:
         g.deinit()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("samples", [1, 4])
+def test_launch_count_is_exact(gpu, samples):
+    """kernel_launches counts what the launchers enqueued: for one opaque view, a clear per
+    pass, shadow prep / setup / raster, camera prep / setup, one raster per sample, the
+    vertex stage and the shading; the same through the frame graph, a replay of it, and
+    the stage-timed direct launches."""
+    s = sc.tiny(2)
+    g = Graphics()
+    g.init(s.width, s.height, s.shadow_size, samples=samples)
+    try:
+        g.set_asset(s)
+        g.set_graphic_objects(s.objects, s.surfaces)
+        g.update(s.scene)
+        expected = 2 + 3 + 2 + samples + 1 + 1
+        for timed in (False, False, True):
+            g.set_stage_timing(timed)
+            g.render()
+            g.sync()
+            assert g.stats().kernel_launches == expected
+    finally:
+        g.deinit()
