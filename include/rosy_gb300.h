@@ -552,6 +552,41 @@ int rz_set_gbuffer(struct rz_ctx* ctx, uint32_t enable);
  * rendered with the G-buffer on). */
 int rz_get_view_gbuffer(struct rz_ctx* ctx, uint32_t view, rz_gbuffer* out);
 
+/* ---- Debug-line overlay --------------------------------------------------
+ * The reference's DRAW DEBUG step (src/Engine/Graphics.cpp:5694-5738, shaders
+ * src/shaders/debug.slang, objects src/Engine/Types.h:81-98): after the blended
+ * list, each object draws LINE_LIST segments 5 pixels wide in one constant
+ * colour (alpha 1), depth-tested GREATER_OR_EQUAL against the opaque depth
+ * with depth writes off (the state the blended list left), into every view.
+ * A line or cross object draws vertices 0-1 of the reference's vertex table
+ * (Graphics.cpp:3222-3249: the segment (0,0,0)-(0,0,1)); a circle draws
+ * vertices 8-107 (50 segments of the unit circle in the xy plane).
+ * flags selects the vertex stage by equality, as debug.slang does: 1 screen
+ * space (transform * (x, y * width/height, z, w), then z = w = 1), 2 view
+ * space (proj * transform * v, then z = w = 1), 4 "transform is points" (the
+ * segment joins the transform's first two columns, times view_projection;
+ * lines and crosses only), anything else world space (view_projection *
+ * transform * v). Lines are rasterised as rectangles (Vulkan's strict lines),
+ * at every coverage sample with 4x multisampling. */
+#define RZ_DEBUG_LINE 0u
+#define RZ_DEBUG_CIRCLE 1u
+#define RZ_DEBUG_CROSS 2u /* drawn as the line, as the reference's draw switch does */
+#define RZ_DEBUG_SCREEN_SPACE 1u
+#define RZ_DEBUG_VIEW_SPACE 2u
+#define RZ_DEBUG_TRANSFORM_IS_POINTS 4u
+#define RZ_MAX_DEBUG_OBJECTS 65536u
+
+typedef struct rz_debug_object {
+    uint32_t type;       /* RZ_DEBUG_LINE / RZ_DEBUG_CIRCLE / RZ_DEBUG_CROSS */
+    uint32_t flags;      /* see above */
+    float transform[16]; /* column-major, as glm stores it */
+    float color[4];      /* rgb drawn, alpha ignored (the shader writes 1) */
+} rz_debug_object;
+
+/* Replaces the overlay's objects (count 0 turns the overlay off); used by
+ * every following frame, in this order (later segments cover earlier ones). */
+int rz_set_debug_objects(struct rz_ctx* ctx, const rz_debug_object* objects, uint32_t count);
+
 /* ---- Learned upsampler ---------------------------------------------------
  * Reconstructs a 2W x 2H RGBA8 sRGB frame from a W x H G-buffer. The network is
  * four 3x3 convolutions with zero padding, 16 -> 32 -> 32 -> 32 -> 12 channels,

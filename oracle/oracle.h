@@ -44,6 +44,8 @@ typedef struct oracle_scene {
     uint32_t height;
     uint32_t shadow_size;
     uint32_t samples;               /* camera-pass samples per pixel: 0 or 1, or 4 (standard 4x positions) */
+    uint32_t debug_object_count;    /* debug-line overlay, drawn after the blended list (may be 0) */
+    const rz_debug_object* debug_objects;
 } oracle_scene;
 
 typedef struct oracle_out {

@@ -52,7 +52,7 @@ class OracleScene(C.Structure):
         ("textures", C.c_void_p), ("texture_count", C.c_uint32), ("sampler_count", C.c_uint32),
         ("samplers", C.c_void_p), ("scene", C.c_void_p), ("draw_config", C.c_void_p),
         ("width", C.c_uint32), ("height", C.c_uint32), ("shadow_size", C.c_uint32),
-        ("samples", C.c_uint32),
+        ("samples", C.c_uint32), ("debug_object_count", C.c_uint32), ("debug_objects", C.c_void_p),
     ]
 
 
@@ -100,6 +100,9 @@ def _scene_struct(m: Marshalled) -> OracleScene:
     o.draw_config = ptr(m.draw_config)
     o.width, o.height, o.shadow_size = s.width, s.height, s.shadow_size
     o.samples = getattr(s, "samples", 1)
+    if m.debug_objects is not None and len(m.debug_objects):
+        o.debug_objects = ptr(m.debug_objects)
+        o.debug_object_count = len(m.debug_objects)
     return o
 
 

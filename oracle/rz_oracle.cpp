@@ -1219,6 +1219,180 @@ void shading_pass(const Ctx& c, const float* shadow, const float* depth, const u
     }
 }
 
+// ----------------------------------------------------------------------------
+// Debug-line overlay: DRAW DEBUG of src/Engine/Graphics.cpp:5694-5738 with the
+// vertex stage of src/shaders/debug.slang:5-35 and the vertex table of
+// Graphics.cpp:3222-3249. Contract shared with k_debug_prep / k_blend:
+//  * vertex: flags == 4 -> view_projection * point (the transform's columns 0
+//    and 1); flags == 1 -> transform * (x, y*aspect, z, w), z = w = 1;
+//    flags == 2 -> (proj * transform) * v, z = w = 1; else
+//    (view_projection * transform) * v; M * v is the chain M0r*x -> fma(M1r, y)
+//    -> fma(M2r, z) -> fma(M3r, w);
+//  * clipping against the triangle planes in order; when exactly one end is
+//    outside, the point fma(t, b-a, a) with t = da/(da-db) replaces it;
+//  * viewport and 8-bit sub-pixel snap as for triangles;
+//  * coverage of a sample: 0 <= along < |d|^2 and -(w/2)|d| < perp <= (w/2)|d|
+//    (exact integers; the rectangle of Vulkan's strict lines, width 5);
+//  * depth fma(along/|d|^2, z1 - z0, z0) clamped to [0,1], tested
+//    GREATER_OR_EQUAL against the opaque depth, never written;
+//  * the sample takes the line's colour (alpha 1: SRC_ALPHA blending keeps
+//    only the source), rounded to RGBA16F.
+// ----------------------------------------------------------------------------
+
+constexpr int64_t kDebugHalfWidth2 = 640 * 640;  // (2.5 px in 1/256 px)^2
+
+struct DebugPair {
+    float a[4], b[4];
+    uint32_t object;
+};
+
+std::vector<DebugPair> debug_pairs(const rz_debug_object* objs, uint32_t n) {
+    // unit circle of the vertex table: 101 vertex pairs from angle step, step 4*pi/100
+    const float target = (float)3.141592653589793 * 4.0f;
+    const float step = target / 100.0f;
+    std::vector<DebugPair> out;
+    for (uint32_t o = 0; o < n; ++o) {
+        const rz_debug_object& d = objs[o];
+        if (d.flags == RZ_DEBUG_TRANSFORM_IS_POINTS) {
+            DebugPair p{};
+            for (int k = 0; k < 4; ++k) {
+                p.a[k] = d.transform[k];
+                p.b[k] = d.transform[4 + k];
+            }
+            p.object = o;
+            out.push_back(p);
+        } else if (d.type == RZ_DEBUG_CIRCLE) {
+            for (int i = 0; i < 50; ++i) {
+                const float cur = step * (float)(i + 1), next = cur + step;
+                out.push_back(DebugPair{{std::sin(cur), std::cos(cur), 0.0f, 1.0f},
+                                        {std::sin(next), std::cos(next), 0.0f, 1.0f}, o});
+            }
+        } else {
+            out.push_back(DebugPair{{0.0f, 0.0f, 0.0f, 1.0f}, {0.0f, 0.0f, 1.0f, 1.0f}, o});
+        }
+    }
+    return out;
+}
+
+CV transform4(const float* M, const float* p) {
+    CV o;
+    for (int r = 0; r < 4; ++r) {
+        float acc = M[0 * 4 + r] * p[0];
+        acc = std::fmaf(M[1 * 4 + r], p[1], acc);
+        acc = std::fmaf(M[2 * 4 + r], p[2], acc);
+        acc = std::fmaf(M[3 * 4 + r], p[3], acc);
+        o.v[r] = acc;
+    }
+    return o;
+}
+
+CV debug_vertex(const rz_scene_data& sd, const rz_debug_object& d, const float* v) {
+    float M[16];
+    CV c;
+    if (d.flags == RZ_DEBUG_TRANSFORM_IS_POINTS) return transform4(sd.view_projection, v);
+    if (d.flags == RZ_DEBUG_SCREEN_SPACE) {
+        const float aspect = sd.draw_extent[0] / sd.draw_extent[1];
+        const float q[4] = {v[0], v[1] * aspect, v[2], v[3]};
+        c = transform4(d.transform, q);
+        c.v[2] = c.v[3] = 1.0f;
+        return c;
+    }
+    if (d.flags == RZ_DEBUG_VIEW_SPACE) {
+        mat4_mul(sd.proj, d.transform, M);
+        c = transform4(M, v);
+        c.v[2] = c.v[3] = 1.0f;
+        return c;
+    }
+    mat4_mul(sd.view_projection, d.transform, M);
+    return transform4(M, v);
+}
+
+struct DebugSeg {
+    bool live = false;
+    SV a{}, b{};
+};
+
+DebugSeg debug_segment(const rz_scene_data& sd, const rz_debug_object& d, const DebugPair& pr, int W, int H) {
+    CV a = debug_vertex(sd, d, pr.a), b = debug_vertex(sd, d, pr.b);
+    DebugSeg s;
+    for (int p = 0; p < 6; ++p) {
+        const float da = plane_dist(a, p), db = plane_dist(b, p);
+        const bool ia = da >= 0.0f, ib = db >= 0.0f;
+        if (!ia && !ib) return s;
+        if (ia != ib) {
+            const float t = da / (da - db);
+            CV c;
+            for (int k = 0; k < 4; ++k) c.v[k] = std::fmaf(t, b.v[k] - a.v[k], a.v[k]);
+            if (ia) b = c;
+            else a = c;
+        }
+    }
+    if (!(a.v[3] > 0.0f) || !(b.v[3] > 0.0f)) return s;
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    s.a = to_screen(a, hw, hh);
+    s.b = to_screen(b, hw, hh);
+    s.live = true;
+    return s;
+}
+
+bool debug_covers(const DebugSeg& s, int32_t PX, int32_t PY, float& z) {
+    const int64_t dx = (int64_t)s.b.X - s.a.X, dy = (int64_t)s.b.Y - s.a.Y;
+    const int64_t len2 = dx * dx + dy * dy;
+    if (len2 == 0) return false;
+    const int64_t ex = (int64_t)PX - s.a.X, ey = (int64_t)PY - s.a.Y;
+    const int64_t along = ex * dx + ey * dy;
+    if (along < 0 || along >= len2) return false;
+    const int64_t perp = dx * ey - dy * ex;
+    const __int128 lhs = (__int128)perp * perp, rhs = (__int128)kDebugHalfWidth2 * len2;
+    if (perp >= 0 ? lhs > rhs : lhs >= rhs) return false;
+    const float t = (float)along / (float)len2;
+    float zz = std::fmaf(t, s.b.z - s.a.z, s.a.z);
+    if (!(zz > 0.0f)) zz = 0.0f;
+    if (zz > 1.0f) zz = 1.0f;
+    z = zz;
+    return true;
+}
+
+// Draws the overlay over the per-sample draw image (color16 with T = float,
+// FP64 values in out64 with T = double); depth holds each sample's opaque depth.
+template <class T>
+void debug_overlay(const Ctx& c, const float* depth, float* color16, double* out64, int threads) {
+    const oracle_scene* sc = c.s;
+    if (!sc->debug_objects || sc->debug_object_count == 0) return;
+    const int W = (int)sc->width, H = (int)sc->height, n = samples_of(sc);
+    const size_t plane = (size_t)W * H;
+    const std::vector<DebugPair> pairs = debug_pairs(sc->debug_objects, sc->debug_object_count);
+    std::vector<DebugSeg> segs(pairs.size());
+    for (size_t i = 0; i < pairs.size(); ++i)
+        segs[i] = debug_segment(*sc->scene, sc->debug_objects[pairs[i].object], pairs[i], W, H);
+    parallel_rows(H, threads, [&](int r0, int r1) {
+        for (size_t i = 0; i < segs.size(); ++i) {
+            const DebugSeg& s = segs[i];
+            if (!s.live) continue;
+            const float* col = sc->debug_objects[pairs[i].object].color;
+            const int x0 = std::max(0, (std::min(s.a.X, s.b.X) - 640) >> 8);
+            const int x1 = std::min(W - 1, (std::max(s.a.X, s.b.X) + 640) >> 8);
+            const int y0 = std::max(r0, (std::min(s.a.Y, s.b.Y) - 640) >> 8);
+            const int y1 = std::min(r1 - 1, (std::max(s.a.Y, s.b.Y) + 640) >> 8);
+            for (int py = y0; py <= y1; ++py)
+                for (int px = x0; px <= x1; ++px)
+                    for (int k = 0; k < n; ++k) {
+                        const int32_t PX = px * 256 + (n > 1 ? kSampleX[k] : 128);
+                        const int32_t PY = py * 256 + (n > 1 ? kSampleY[k] : 128);
+                        float z;
+                        const size_t q = k * plane + (size_t)py * W + px;
+                        if (!debug_covers(s, PX, PY, z) || !(z >= depth[q])) continue;
+                        for (int ch = 0; ch < 3; ++ch) {
+                            if constexpr (sizeof(T) == 4) color16[4 * q + ch] = to_half_and_back(col[ch]);
+                            else out64[4 * q + ch] = (double)col[ch];
+                        }
+                        if constexpr (sizeof(T) == 4) color16[4 * q + 3] = 1.0f;
+                        else out64[4 * q + 3] = 1.0;
+                    }
+        }
+    });
+}
+
 int threads_or_default(int threads) {
     if (threads > 0) return threads;
     const unsigned h = std::thread::hardware_concurrency();
@@ -1316,6 +1490,7 @@ static int render_rgba8(const oracle_scene* s, oracle_out* out, int threads) {
     }
     std::vector<float> color16(np * 4 * ns);
     shading_pass<float>(c, shadow.data(), depth.data(), ids.data(), color16.data(), nullptr, threads, mp, smp);
+    debug_overlay<float>(c, depth.data(), color16.data(), nullptr, threads);
     // AVERAGE resolve of the samples into the RGBA16F draw image ((s0 + s1) + (s2 + s3)) / 4
     // (src/Engine/Graphics.cpp:5571-5572), then the blit to sRGB 8-bit
     auto resolved = [&](size_t p, int k) -> float {
@@ -1332,6 +1507,7 @@ static int render_rgba8(const oracle_scene* s, oracle_out* out, int threads) {
     if (out->color_f64) {
         std::vector<double> c64(np * 4 * ns);
         shading_pass<double>(c, shadow.data(), depth.data(), ids.data(), nullptr, c64.data(), threads, nullptr, nullptr);
+        debug_overlay<double>(c, depth.data(), nullptr, c64.data(), threads);
         for (size_t p = 0; p < np; ++p)
             for (int k = 0; k < 4; ++k) {
                 const double* q = c64.data() + 4 * p + k;

@@ -137,6 +137,8 @@ class Marshalled:
                     self.tex_data[i].nbytes < texel_bytes(t.width, t.height, t.levels, self.textures[i].format):
                 raise ValueError(f"texture {i} holds fewer bytes than its level chain")
         self.scene_rec = np.ascontiguousarray(s.scene)
+        dbg = getattr(s, "debug_objects", None)
+        self.debug_objects = None if dbg is None else np.ascontiguousarray(dbg, sc.DEBUG_OBJECT_DTYPE)
         self.draw_config = np.ascontiguousarray(s.draw_config)
 
     @property

@@ -27,6 +27,7 @@ EXPORTS = [
     "rz_get_stats", "rz_get_stream", "rz_last_error", "rz_abi_version", "rz_set_stage_timing",
     "rz_get_stage_times", "rz_shadow_depth_static", "rz_add_scene", "rz_set_views", "rz_update_view",
     "rz_get_view_frame", "rz_set_tuning", "rz_get_tuning", "rz_autotune", "rz_set_gbuffer", "rz_get_view_gbuffer",
+    "rz_set_debug_objects",
     "rz_upsampler_create", "rz_upsampler_destroy", "rz_upsampler_set_params", "rz_upsampler_get_params",
     "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads", "rz_upsampler_adam_step",
     "rz_upsampler_status", "rz_upsampler_selftest_gemm", "rz_rsy_read", "rz_rsy_free", "rz_rsy_get_info",
@@ -92,6 +93,7 @@ def load(build_if_missing: bool = False):
         getattr(lib, name).restype = C.c_int
     G = C.POINTER(_abi.RzGbuffer)
     lib.rz_set_gbuffer.argtypes = [P, u32]
+    lib.rz_set_debug_objects.argtypes = [P, P, u32]
     lib.rz_get_view_gbuffer.argtypes = [P, u32, G]
     lib.rz_upsampler_create.argtypes = [C.POINTER(P), C.c_int, u32, u32]
     lib.rz_upsampler_destroy.argtypes = [P]
@@ -105,7 +107,7 @@ def load(build_if_missing: bool = False):
     lib.rz_upsampler_adam_step.argtypes = [P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P]
     lib.rz_upsampler_status.argtypes = [P, C.POINTER(u32), P]
     lib.rz_upsampler_selftest_gemm.argtypes = [P, P, P, u32, u32, P]
-    for name in ("rz_set_gbuffer", "rz_get_view_gbuffer", "rz_upsampler_create", "rz_upsampler_set_params",
+    for name in ("rz_set_gbuffer", "rz_set_debug_objects", "rz_get_view_gbuffer", "rz_upsampler_create", "rz_upsampler_set_params",
                  "rz_upsampler_get_params", "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads",
                  "rz_upsampler_adam_step", "rz_upsampler_status", "rz_upsampler_selftest_gemm"):
         getattr(lib, name).restype = C.c_int

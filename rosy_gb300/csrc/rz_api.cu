@@ -182,6 +182,15 @@ struct rz_ctx {
     bool frame_pending = false;
     bool timing = false;
     uint32_t frame_launches = 0;  // kernels the last enqueued frame launches (graph replays included)
+    // debug-line overlay: objects and their segments (host), their device copies, and
+    // the segments of every view after the vertex stage (k_debug_prep)
+    std::vector<rz_debug_object> debug_objects;
+    std::vector<DebugPair> debug_pairs;
+    rz_debug_object* d_debug_objects = nullptr;
+    DebugPair* d_debug_pairs = nullptr;
+    DebugSeg* d_debug_segs = nullptr;
+    size_t debug_seg_capacity = 0;
+    uint32_t debug_count = 0;     // segments per view in the current layout (0: overlay off)
     cudaEvent_t stage_ev[RZ_STAGE_COUNT + 1] = {};
     uint32_t frames = 0;
 };
@@ -596,7 +605,9 @@ int build_layout(rz_ctx* c) {
         RZ_CUDA(c, dalloc(&c->d_shadow, shadow), "shadow maps");
         c->shadow_capacity = shadow;
     }
-    if (!blended.empty() && pix > c->color16_capacity) {
+    // the overlay draws into the per-sample RGBA16F draw images, as the blended list does
+    const bool overlay = !c->debug_pairs.empty();
+    if ((!blended.empty() || overlay) && pix > c->color16_capacity) {
         dfree(c->d_color16);
         c->color16_capacity = 0;
         RZ_CUDA(c, dalloc(&c->d_color16, pix * c->samples), "RGBA16F draw images");
@@ -609,6 +620,25 @@ int build_layout(rz_ctx* c) {
         RZ_CUDA(c, dalloc(&c->d_gb_albedo, pix), "G-buffer albedo");
         RZ_CUDA(c, dalloc(&c->d_gb_normal, pix), "G-buffer normals");
         c->gb_capacity = pix;
+    }
+    dfree(c->d_debug_objects);
+    dfree(c->d_debug_pairs);
+    c->debug_count = 0;
+    if (overlay) {
+        const size_t segs = c->debug_pairs.size() * c->views.size();
+        if (segs > c->debug_seg_capacity) {
+            dfree(c->d_debug_segs);
+            c->debug_seg_capacity = 0;
+            RZ_CUDA(c, dalloc(&c->d_debug_segs, segs), "overlay segments");
+            c->debug_seg_capacity = segs;
+        }
+        RZ_CUDA(c, dalloc(&c->d_debug_objects, c->debug_objects.size()), "overlay objects");
+        RZ_CUDA(c, dalloc(&c->d_debug_pairs, c->debug_pairs.size()), "overlay vertices");
+        RZ_CUDA(c, cudaMemcpy(c->d_debug_objects, c->debug_objects.data(), c->debug_objects.size() * sizeof(rz_debug_object),
+                              cudaMemcpyHostToDevice), "upload overlay objects");
+        RZ_CUDA(c, cudaMemcpy(c->d_debug_pairs, c->debug_pairs.data(), c->debug_pairs.size() * sizeof(DebugPair),
+                              cudaMemcpyHostToDevice), "upload overlay vertices");
+        c->debug_count = (uint32_t)c->debug_pairs.size();
     }
     c->view_recs.resize(c->views.size());
     for (uint32_t vi = 0; vi < c->views.size(); ++vi) {
@@ -753,7 +783,7 @@ ShadeParams shade_params(rz_ctx* c) {
     sh.samplers = c->d_samplers;
     sh.sampler_count = (uint32_t)c->samplers.size();
     sh.srgb_table = c->d_srgb;
-    sh.blended = c->blended_tris ? 1 : 0;
+    sh.blended = (c->blended_tris || c->debug_count) ? 1 : 0;  // k_blend finishes the frame
     return sh;
 }
 
@@ -924,7 +954,7 @@ int enqueue_frame(rz_ctx* c) {
     cudaStream_t s = c->stream;
     take_launches();  // start this frame's count
     const ShadeParams sh = shade_params(c);
-    if (!c->batched && !c->blended_tris && !c->timing) {
+    if (!c->batched && !c->blended_tris && !c->timing && !c->debug_count) {
         // per-view launches clear the pass headers view by view; the error words once per frame
         RZ_CUDA(c, cudaMemsetAsync(c->d_report, 0, sizeof(FrameReport), s), "clear frame report");
         launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s);
@@ -944,8 +974,11 @@ int enqueue_frame(rz_ctx* c) {
         RZ_CUDA(c, cudaEventRecord(c->join, c->side), "join");
         RZ_CUDA(c, cudaStreamWaitEvent(s, c->join, 0), "join");
     }
-    if (c->batched || c->blended_tris || c->timing) launch_shade(sh, s);
-    if (c->blended_tris) {
+    if (c->batched || c->blended_tris || c->timing || c->debug_count) launch_shade(sh, s);
+    if (c->blended_tris || c->debug_count) {
+        if (c->debug_count)
+            launch_debug_prep(c->d_debug_pairs, c->debug_count, c->d_debug_objects, c->d_views, (uint32_t)c->views.size(),
+                              c->d_debug_segs, s);
         BlendParams bp{};
         bp.sh = sh;
         bp.sh.draws = c->d_blended_draws;
@@ -954,6 +987,8 @@ int enqueue_frame(rz_ctx* c) {
         bp.records = c->blended_pass.records;
         bp.header = &c->d_report->blended;
         bp.record_capacity = c->blended_pass.record_capacity;
+        bp.debug = c->d_debug_segs;
+        bp.debug_count = c->debug_count;
         launch_blend(bp, s);
     }
     if (c->timing) stamp(c, 7);
@@ -1026,6 +1061,47 @@ rz_frame_out frame_of(rz_ctx* c, uint32_t v) {
     o.shadow_map_size = (uint32_t)r.shadow_w;
     o.triangle_id_base = c->view_id_base[v];
     return o;
+}
+
+// The overlay's segments before the vertex stage, in draw order. Vertex table of
+// src/Engine/Graphics.cpp:3222-3249: a line (0,0,0)-(0,0,1) at vertices 0-1 and,
+// from vertex 8, pairs of unit-circle points at angles step*(i+1) and that plus
+// step, step = (float)pi * 4 / 100 in float arithmetic; a circle draws 100
+// vertices from 8 (50 segments), a line or cross 2 from 0 (Graphics.cpp:5727-5737).
+std::vector<DebugPair> debug_pairs_of(const rz_debug_object* objects, uint32_t count) {
+    const float step = (float)3.141592653589793 * 4.0f / 100.0f;
+    std::vector<DebugPair> out;
+    for (uint32_t o = 0; o < count; ++o) {
+        const rz_debug_object& d = objects[o];
+        DebugPair p{};
+        p.object = o;
+        if (d.flags == RZ_DEBUG_TRANSFORM_IS_POINTS) {  // the transform's columns 0 and 1
+            for (int k = 0; k < 4; ++k) {
+                p.a[k] = d.transform[k];
+                p.b[k] = d.transform[4 + k];
+            }
+            out.push_back(p);
+        } else if (d.type == RZ_DEBUG_CIRCLE) {
+            for (int i = 0; i < 50; ++i) {
+                const float cur = step * (float)(i + 1), next = cur + step;
+                p.a[0] = std::sin(cur);
+                p.a[1] = std::cos(cur);
+                p.a[2] = 0.0f;
+                p.a[3] = 1.0f;
+                p.b[0] = std::sin(next);
+                p.b[1] = std::cos(next);
+                p.b[2] = 0.0f;
+                p.b[3] = 1.0f;
+                out.push_back(p);
+            }
+        } else {
+            p.a[3] = 1.0f;
+            p.b[2] = 1.0f;
+            p.b[3] = 1.0f;
+            out.push_back(p);
+        }
+    }
+    return out;
 }
 
 }  // namespace
@@ -1119,6 +1195,9 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_depth);
     dfree(c->d_shadow);
     dfree(c->d_color16);
+    dfree(c->d_debug_objects);
+    dfree(c->d_debug_pairs);
+    dfree(c->d_debug_segs);
     dfree(c->d_gb_albedo);
     dfree(c->d_gb_normal);
     dfree(c->d_shadow_draws);
@@ -1387,6 +1466,35 @@ int rz_get_view_frame(rz_ctx* c, uint32_t view, rz_frame_out* out) {
 }
 
 int rz_get_frame(rz_ctx* c, rz_frame_out* out) { return rz_get_view_frame(c, 0, out); }
+
+int rz_set_debug_objects(rz_ctx* c, const rz_debug_object* objects, uint32_t count) {
+    if (!c) return RZ_INVALID_ARGUMENT;
+    if (count && !objects) return fail(c, RZ_INVALID_ARGUMENT, "null debug objects with a non-zero count");
+    if (count > RZ_MAX_DEBUG_OBJECTS) return fail(c, RZ_INVALID_ARGUMENT, "too many debug objects");
+    for (uint32_t i = 0; i < count; ++i) {
+        if (objects[i].type > RZ_DEBUG_CROSS) return fail(c, RZ_INVALID_ARGUMENT, "unknown debug object type");
+        // a circle's vertex ids (8-107) index past the transform's four points
+        if (objects[i].flags == RZ_DEBUG_TRANSFORM_IS_POINTS && objects[i].type == RZ_DEBUG_CIRCLE)
+            return fail(c, RZ_INVALID_ARGUMENT, "a circle cannot take its points from the transform");
+    }
+    std::vector<DebugPair> pairs = debug_pairs_of(objects, count);
+    cudaSetDevice(c->device);
+    const bool same_shape = !c->layout_dirty && c->debug_count != 0 && count == c->debug_objects.size() &&
+                            pairs.size() == c->debug_pairs.size();
+    const bool was_on = !c->debug_pairs.empty();
+    c->debug_objects.assign(objects, objects + count);
+    c->debug_pairs = std::move(pairs);
+    if (same_shape) {
+        // same buffers: the new contents follow the frames already enqueued on the stream
+        RZ_CUDA(c, cudaMemcpyAsync(c->d_debug_objects, c->debug_objects.data(), count * sizeof(rz_debug_object),
+                                   cudaMemcpyHostToDevice, c->stream), "upload overlay objects");
+        RZ_CUDA(c, cudaMemcpyAsync(c->d_debug_pairs, c->debug_pairs.data(), c->debug_pairs.size() * sizeof(DebugPair),
+                                   cudaMemcpyHostToDevice, c->stream), "upload overlay vertices");
+        return RZ_OK;
+    }
+    if (was_on || count) c->layout_dirty = true;  // new buffers and frame graph at the next rz_render
+    return RZ_OK;
+}
 
 int rz_set_gbuffer(rz_ctx* c, uint32_t enable) {
     if (!c) return RZ_INVALID_ARGUMENT;

@@ -207,11 +207,38 @@ struct ShadeParams {
 };
 
 // The blended list (src/Engine/Graphics.cpp:5654-5691) over the opaque result.
+// Debug-line overlay (src/Engine/Graphics.cpp:5694-5738): one segment before
+// the vertex stage: its two vertices (from the vertex table, or the points of a
+// "transform is points" object) and its object; 48 bytes.
+struct DebugPair {
+    float a[4], b[4];
+    uint32_t object;
+    uint32_t pad[3];
+};
+
+// One segment of one view after the vertex stage, clipping and the viewport:
+// window ends in 1/256 pixel, their depths, the inclusive pixel box
+// (x | y << 16) that can hold covered samples, the object's colour; 64 bytes.
+struct DebugSeg {
+    int32_t X0, Y0, X1, Y1;
+    float z0, z1;
+    uint32_t p0, p1;
+    float rgb[3];
+    uint32_t live;                // 0: clipped away or outside the view
+    uint32_t pad[4];
+};
+
+// (half the line width of 5 pixels, in 1/256 pixel)^2
+constexpr int64_t kDebugHalfWidth2 = 640 * 640;
+constexpr int32_t kDebugHalfWidth = 640;
+
 struct BlendParams {
     ShadeParams sh;               // blended draws, their constants and varyings
     const TriRecord* records;     // setup records of the blended triangles, in submission order
     const PassHeader* header;
     uint32_t record_capacity;
+    uint32_t debug_count;         // overlay segments per view (0: no overlay)
+    const DebugSeg* debug;        // view v's segments at debug + v * debug_count, in draw order
 };
 
 // Up to four buffers to zero in one launch (16-byte stores, byte tail).
@@ -238,6 +265,9 @@ void launch_vertex(const ShadeParams& p, cudaStream_t stream);
 // (whose varying_base values start at `first`).
 void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stream);
 void launch_blend(const BlendParams& p, cudaStream_t stream);
+// k_debug_prep: the overlay's `count` segments for each of the `view_count` views.
+void launch_debug_prep(const DebugPair* pairs, uint32_t count, const rz_debug_object* objects, const ViewRec* views,
+                       uint32_t view_count, DebugSeg* out, cudaStream_t stream);
 void launch_shade(const ShadeParams& p, cudaStream_t stream);
 
 // BC7 (rz_bc7.cu): bytes of a mip chain's blocks, and the decode of a chain

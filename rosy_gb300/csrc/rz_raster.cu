@@ -1009,4 +1009,108 @@ void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream) {
     note_launch();
 }
 
+// ---------------------------------------------------------------------------
+// debug-line overlay: vertex stage, clipping and viewport of each segment
+// ---------------------------------------------------------------------------
+
+// M * (x, y, z, w) as the chain M0r*x -> fma(M1r, y) -> fma(M2r, z) -> fma(M3r, w).
+__device__ __forceinline__ CV transform4(const float* __restrict__ M, const float* v) {
+    CV o;
+    o.x = fmaf(M[12], v[3], fmaf(M[8], v[2], fmaf(M[4], v[1], M[0] * v[0])));
+    o.y = fmaf(M[13], v[3], fmaf(M[9], v[2], fmaf(M[5], v[1], M[1] * v[0])));
+    o.z = fmaf(M[14], v[3], fmaf(M[10], v[2], fmaf(M[6], v[1], M[2] * v[0])));
+    o.w = fmaf(M[15], v[3], fmaf(M[11], v[2], fmaf(M[7], v[1], M[3] * v[0])));
+    return o;
+}
+
+// debugVertMain (src/shaders/debug.slang:5-35): flags select the space by equality.
+__device__ CV debug_vertex(const rz_scene_data& sd, const rz_debug_object& d, const float* v) {
+    float M[16];
+    CV c;
+    if (d.flags == RZ_DEBUG_TRANSFORM_IS_POINTS) return transform4(sd.view_projection, v);
+    if (d.flags == RZ_DEBUG_SCREEN_SPACE) {
+        const float aspect = sd.draw_extent[0] / sd.draw_extent[1];
+        const float q[4] = {v[0], v[1] * aspect, v[2], v[3]};
+        c = transform4(d.transform, q);
+        c.z = c.w = 1.0f;
+        return c;
+    }
+    if (d.flags == RZ_DEBUG_VIEW_SPACE) {
+        mat4_mul(sd.proj, d.transform, M);
+        c = transform4(M, v);
+        c.z = c.w = 1.0f;
+        return c;
+    }
+    mat4_mul(sd.view_projection, d.transform, M);
+    return transform4(M, v);
+}
+
+// One thread per (view, segment). The segment is clipped against the triangle
+// planes in order (an end outside one plane is replaced by the crossing
+// fma(t, b-a, a), t = da/(da-db)), mapped to the viewport and snapped to
+// 1/256 pixel; its pixel box is widened by half the line width.
+__global__ void __launch_bounds__(128) k_debug_prep(const DebugPair* __restrict__ pairs, uint32_t count,
+                                                    const rz_debug_object* __restrict__ objects,
+                                                    const ViewRec* __restrict__ views, uint32_t view_count,
+                                                    DebugSeg* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)count * view_count) return;
+    const uint32_t v = (uint32_t)(i / count), k = (uint32_t)(i % count);
+    const DebugPair pr = pairs[k];
+    const rz_debug_object& d = objects[pr.object];
+    const ViewRec& VR = views[v];
+    DebugSeg s{};
+    s.rgb[0] = d.color[0];
+    s.rgb[1] = d.color[1];
+    s.rgb[2] = d.color[2];
+    CV a = debug_vertex(*VR.scene, d, pr.a), b = debug_vertex(*VR.scene, d, pr.b);
+    bool live = true;
+    for (int p = 0; p < 6 && live; ++p) {
+        const float da = plane_dist(a, p), db = plane_dist(b, p);
+        const bool ia = da >= 0.0f, ib = db >= 0.0f;
+        if (!ia && !ib) {
+            live = false;
+        } else if (ia != ib) {
+            const float t = da / (da - db);
+            CV c;
+            c.x = fmaf(t, b.x - a.x, a.x);
+            c.y = fmaf(t, b.y - a.y, a.y);
+            c.z = fmaf(t, b.z - a.z, a.z);
+            c.w = fmaf(t, b.w - a.w, a.w);
+            if (ia) b = c;
+            else a = c;
+        }
+    }
+    live = live && a.w > 0.0f && b.w > 0.0f;
+    if (live) {
+        const float hw = (float)VR.width * 0.5f, hh = (float)VR.height * 0.5f;
+        const SV sa = to_screen(a, hw, hh), sb = to_screen(b, hw, hh);
+        s.X0 = sa.X;
+        s.Y0 = sa.Y;
+        s.X1 = sb.X;
+        s.Y1 = sb.Y;
+        s.z0 = sa.z;
+        s.z1 = sb.z;
+        const int x0 = max(0, (min(sa.X, sb.X) - kDebugHalfWidth) >> 8);
+        const int x1 = min(VR.width - 1, (max(sa.X, sb.X) + kDebugHalfWidth) >> 8);
+        const int y0 = max(0, (min(sa.Y, sb.Y) - kDebugHalfWidth) >> 8);
+        const int y1 = min(VR.height - 1, (max(sa.Y, sb.Y) + kDebugHalfWidth) >> 8);
+        live = x0 <= x1 && y0 <= y1;
+        if (live) {
+            s.p0 = (uint32_t)x0 | ((uint32_t)y0 << 16);
+            s.p1 = (uint32_t)x1 | ((uint32_t)y1 << 16);
+        }
+    }
+    s.live = live ? 1u : 0u;
+    out[i] = s;
+}
+
+void launch_debug_prep(const DebugPair* pairs, uint32_t count, const rz_debug_object* objects, const ViewRec* views,
+                       uint32_t view_count, DebugSeg* out, cudaStream_t stream) {
+    const uint64_t n = (uint64_t)count * view_count;
+    if (n == 0) return;
+    k_debug_prep<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(pairs, count, objects, views, view_count, out);
+    note_launch();
+}
+
 }  // namespace rz

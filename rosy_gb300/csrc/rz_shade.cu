@@ -1011,6 +1011,63 @@ void launch_shade(const ShadeParams& p, cudaStream_t stream) {
 // (src/Engine/Graphics.cpp:5654-5691). Then the sRGB blit.
 constexpr int kBlendBatch = 1024;
 
+// Ordered compaction of the items [start, min(start + kBlendBatch, n)) that `hit`
+// selects (4 consecutive items per thread) into s_list, in item order; returns
+// their count. Every thread of the 256-thread CTA calls it.
+template <class Hit>
+__device__ __forceinline__ uint32_t compact_batch(uint32_t start, uint32_t n, int tid, uint32_t* s_list,
+                                                  uint32_t* s_count, Hit hit) {
+    const int lane = tid & 31, warp = tid >> 5;
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t r = start + 4 * tid + k;
+        if (r < n && hit(r)) mask |= 1u << k;
+    }
+    const uint32_t cnt = __popc(mask);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    __syncthreads();
+    if (lane == 31) s_count[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, total = 0;
+    for (int w = 0; w < 8; ++w) {
+        if (w < warp) base += s_count[w];
+        total += s_count[w];
+    }
+    uint32_t pos = base + incl - cnt;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (mask & (1u << k)) s_list[pos++] = start + 4 * tid + k;
+    __syncthreads();
+    return total;
+}
+
+// Whether the 5-pixel line `s` covers the sample at (PX, PY) (1/256 pixel), and
+// its depth there: the rectangle 0 <= along < |d|^2, -(w/2)|d| < perp <= (w/2)|d|
+// in exact integers; depth fma(along/|d|^2, z1 - z0, z0) clamped to [0, 1].
+__device__ __forceinline__ bool debug_covers(const DebugSeg& s, int32_t PX, int32_t PY, float& z) {
+    const long long dx = (long long)s.X1 - s.X0, dy = (long long)s.Y1 - s.Y0;
+    const long long len2 = dx * dx + dy * dy;
+    if (len2 == 0) return false;
+    const long long ex = (long long)PX - s.X0, ey = (long long)PY - s.Y0;
+    const long long along = ex * dx + ey * dy;
+    if (along < 0 || along >= len2) return false;
+    const long long perp = dx * ey - dy * ex;
+    const __int128 lhs = (__int128)perp * perp, rhs = (__int128)kDebugHalfWidth2 * len2;
+    if (perp >= 0 ? lhs > rhs : lhs >= rhs) return false;
+    const float t = (float)along / (float)len2;
+    float zz = fmaf(t, s.z1 - s.z0, s.z0);
+    if (!(zz > 0.0f)) zz = 0.0f;
+    if (zz > 1.0f) zz = 1.0f;
+    z = zz;
+    return true;
+}
+
 __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
     __shared__ float s_srgb[256], s_unorm[256];
     __shared__ uint32_t s_list[kBlendBatch];
@@ -1125,6 +1182,42 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
             }
         }
         __syncthreads();
+    }
+    // Debug-line overlay after the blended list (src/Engine/Graphics.cpp:5694-5738): the same
+    // blend state and depth test, depth writes off; a covered sample in front of the opaque
+    // depth takes the line's colour (SRC_ALPHA with alpha 1 keeps only the source).
+    if (B.debug_count) {
+        const DebugSeg* __restrict__ segs = B.debug + (size_t)view * B.debug_count;
+        for (uint32_t start = 0; start < B.debug_count; start += kBlendBatch) {
+            const uint32_t total = compact_batch(start, B.debug_count, tid, s_list, s_count, [&](uint32_t r) {
+                const DebugSeg& sg = segs[r];
+                const int bx0 = sg.p0 & 0xffff, by0 = sg.p0 >> 16, bx1 = sg.p1 & 0xffff, by1 = sg.p1 >> 16;
+                return sg.live && bx1 >= tx0 && bx0 <= tx0 + 15 && by1 >= ty0 && by0 <= ty0 + 15;
+            });
+            if (inside) {
+                for (uint32_t j = 0; j < total; ++j) {
+                    const DebugSeg& sg = segs[s_list[j]];
+                    const int bx0 = sg.p0 & 0xffff, by0 = sg.p0 >> 16, bx1 = sg.p1 & 0xffff, by1 = sg.p1 >> 16;
+                    if (px < bx0 || px > bx1 || py < by0 || py > by1) continue;
+                    uint32_t pass = 0;  // samples covered and in front of the opaque depth
+                    for (int k = 0; k < nsamples; ++k) {
+                        const int32_t PX = px * 256 + (nsamples > 1 ? msaa_x(k) : 128);
+                        const int32_t PY = py * 256 + (nsamples > 1 ? msaa_y(k) : 128);
+                        float z;
+                        if (debug_covers(sg, PX, PY, z) && z >= dst_depth[k]) pass |= 1u << k;
+                    }
+                    if (!pass) continue;
+#pragma unroll
+                    for (int k = 0; k < kMsaaSamples; ++k) {
+                        if (!(pass & (1u << k))) continue;
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) col[k][i] = half_round(sg.rgb[i]);
+                        col[k][3] = 1.0f;
+                    }
+                }
+            }
+            __syncthreads();
+        }
     }
     if (!inside) return;
     float o[4];

@@ -14,6 +14,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi, _lib
+from . import scene as sc
 from .scene import Scene
 
 
@@ -127,6 +128,15 @@ class Graphics:
     def set_gbuffer(self, enable: bool) -> None:
         """Makes the shading pass also write albedo and octahedral normals (the upsampler's inputs)."""
         self._check(self._lib.rz_set_gbuffer(self._ctx, 1 if enable else 0), "rz_set_gbuffer")
+
+    def set_debug_objects(self, objects: np.ndarray | None) -> None:
+        """The debug-line overlay of every following frame (DEBUG_OBJECT_DTYPE records, drawn in
+        order after the blended list); None or an empty array turns it off."""
+        if objects is None or len(objects) == 0:
+            self._check(self._lib.rz_set_debug_objects(self._ctx, None, 0), "rz_set_debug_objects")
+            return
+        objs = np.ascontiguousarray(objects, sc.DEBUG_OBJECT_DTYPE)
+        self._check(self._lib.rz_set_debug_objects(self._ctx, _abi.ptr(objs), len(objs)), "rz_set_debug_objects")
 
     def gbuffer(self, view: int = 0) -> _abi.RzGbuffer:
         """Device pointers of one view's G-buffer (after sync)."""
@@ -266,6 +276,8 @@ def render_scene(scene: Scene, device: int = 0) -> dict:
         g.set_asset(scene)
         g.set_graphic_objects(scene.objects, scene.surfaces)
         g.set_draw_config(scene.draw_config)
+        if getattr(scene, "debug_objects", None) is not None:
+            g.set_debug_objects(scene.debug_objects)
         g.update(scene.scene)
         g.render()
         if g.sync_code() == 14:  # RZ_OVERFLOW: the work queue grew; render the frame again

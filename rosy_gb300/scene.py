@@ -59,6 +59,22 @@ SURFACE_DTYPE = np.dtype([
     ("index_count", "<u4"), ("start_index", "<u4"), ("blended", "<u4"),
 ])
 
+# rz_debug_object: the debug-line overlay (src/Engine/Types.h:81-98)
+DEBUG_OBJECT_DTYPE = np.dtype([("type", "<u4"), ("flags", "<u4"), ("transform", "<f4", 16), ("color", "<f4", 4)])
+DEBUG_LINE, DEBUG_CIRCLE, DEBUG_CROSS = 0, 1, 2
+DEBUG_SCREEN_SPACE, DEBUG_VIEW_SPACE, DEBUG_TRANSFORM_IS_POINTS = 1, 2, 4
+
+
+def debug_object(kind: int, transform, color, flags: int = 0) -> np.ndarray:
+    """One overlay object; `transform` is a row-major math matrix (stored column-major)."""
+    o = np.zeros(1, DEBUG_OBJECT_DTYPE)
+    o["type"] = kind
+    o["flags"] = flags
+    o["transform"] = colmajor(transform)
+    o["color"] = color
+    return o
+
+
 SCENE_DTYPE = np.dtype([
     ("view", "<f4", 16), ("proj", "<f4", 16), ("view_projection", "<f4", 16),
     ("shadow_projection_near", "<f4", 16),
@@ -131,6 +147,7 @@ class Scene:
     draw_config: np.ndarray  # DRAW_CONFIG_DTYPE, shape (1,)
     cameras: list = field(default_factory=list)  # extra SCENE_DTYPE records (one per frame)
     samples: int = 1  # camera-pass samples per pixel (1, or 4: the reference's 4x MSAA)
+    debug_objects: np.ndarray | None = None  # DEBUG_OBJECT_DTYPE: the debug-line overlay, or None
 
     @property
     def triangle_count(self) -> int:
@@ -440,6 +457,49 @@ def random_triangles(seed: int = 0, triangles: int = 4096, width: int = 640, hei
         materials=material(color_image=0, sampler=0),
         textures=[tex], samplers=linear_sampler(),
         scene=sc, draw_config=default_draw_config(pcf_mode), cameras=[sc])
+
+
+def _rotation(rng) -> np.ndarray:
+    q = rng.normal(size=4)
+    w, x, y, z = q / np.linalg.norm(q)
+    r = np.eye(4)
+    r[:3, :3] = [[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                 [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                 [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]]
+    return r
+
+
+def random_debug_objects(seed: int, n: int, extent: float = 2.5) -> np.ndarray:
+    """n seeded overlay objects of every kind around a scene of half-size ~1 seen from
+    distance 3: world-space lines (some crossing the near plane), crosses and circles,
+    screen- and view-space lines and circles, "transform is points" lines, and flags
+    that match none of the spaces (3, 5: world space, as the shader's equality tests give)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        kind = i % 8
+        color = (*rng.random(3), 1.0)
+        if kind in (0, 1):  # world-space line / cross between two random points
+            a, b = rng.uniform(-extent, extent, 3), rng.uniform(-extent, extent, 3)
+            t = np.eye(4)
+            t[:3, 2] = b - a
+            t[:3, 3] = a
+            out.append(debug_object(DEBUG_LINE if kind == 0 else DEBUG_CROSS, t, color, int(rng.choice([0, 3, 5]))))
+        elif kind == 2:  # world-space circle
+            t = _translate(rng.uniform(-1.5, 1.5, 3)) @ _rotation(rng) @ _scale(rng.uniform(0.2, 1.5))
+            out.append(debug_object(DEBUG_CIRCLE, t, color))
+        elif kind in (3, 4):  # screen-space line / circle
+            t = _translate((*rng.uniform(-1, 1, 2), 0.0)) @ _rotation(rng) @ _scale(rng.uniform(0.05, 0.6))
+            out.append(debug_object(DEBUG_LINE if kind == 3 else DEBUG_CIRCLE, t, color, DEBUG_SCREEN_SPACE))
+        elif kind in (5, 6):  # view-space line / circle
+            t = _translate((*rng.uniform(-1, 1, 2), -rng.uniform(1, 5))) @ _rotation(rng) @ _scale(rng.uniform(0.1, 1))
+            out.append(debug_object(DEBUG_LINE if kind == 5 else DEBUG_CIRCLE, t, color, DEBUG_VIEW_SPACE))
+        else:  # points: columns 0 and 1 are the ends
+            pts = np.ones((4, 4))
+            pts[:3, 0] = rng.uniform(-extent, extent, 3)
+            pts[:3, 1] = rng.uniform(-extent, extent, 3)
+            out.append(debug_object(DEBUG_LINE, pts, color, DEBUG_TRANSFORM_IS_POINTS))
+    return np.concatenate(out)
 
 
 # --- config 2: many tessellated meshes, materials, camera spline -------------------

@@ -46,14 +46,16 @@ def test_header_compiles_as_c_and_matches_sizes(tmp_path):
         '#include "rosy_gb300.h"\n#include <stdio.h>\n'
         'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(rz_vertex), sizeof(rz_object),'
         ' sizeof(rz_scene_data), sizeof(rz_surface), sizeof(rz_material), sizeof(rz_sampler),'
-        ' sizeof(rz_draw_config), sizeof(rz_texture), sizeof(rz_mesh), sizeof(rz_dds_info)); return 0;}\n')
+        ' sizeof(rz_draw_config), sizeof(rz_texture), sizeof(rz_mesh), sizeof(rz_dds_info));'
+        ' printf("%zu\\n", sizeof(rz_debug_object)); return 0;}\n')
     exe = tmp_path / "sizes"
     import subprocess
 
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
                     str(exe)], check=True)
     got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
-    assert [int(x) for x in got] == [64, 164, 408, 28, sc.MATERIAL_DTYPE.itemsize, 8, 32, 32, 24, 40]
+    assert [int(x) for x in got] == [64, 164, 408, 28, sc.MATERIAL_DTYPE.itemsize, 8, 32, 32, 24, 40,
+                                     sc.DEBUG_OBJECT_DTYPE.itemsize]
 
 
 def test_calls_without_a_context_are_rejected(renderer_lib):

@@ -9,12 +9,14 @@ from rosy_gb300.graphics import Graphics
 from test_gpu_parity import check_parity
 
 
-def render_batch(scenes, views, samples=1):
+def render_batch(scenes, views, samples=1, debug_objects=None):
     g = Graphics()
     g.init(64, 64, 64, samples=samples)
     try:
         idx = [g.add_scene(s) for s in scenes]
         g.set_views([(idx[k], v.width, v.height, v.shadow_size, v.draw_config) for k, v in views])
+        if debug_objects is not None:
+            g.set_debug_objects(debug_objects)
         for i, (_, v) in enumerate(views):
             g.update_view(i, v.scene)
         g.render()
