@@ -162,3 +162,56 @@ def test_fp64_output_carries_the_overlay(oracle):
     out = oracle.render(s, threads=1, fp64=True)
     srgb = [c * 12.92 if c <= 0.0031308 else 1.055 * c ** (1 / 2.4) - 0.055 for c in (0.25, 0.5, 0.75)]
     assert np.allclose(out["color_f64"][8, 12, :3], srgb) and out["color_f64"][8, 12, 3] == 1.0
+
+
+@pytest.mark.parametrize("vertical", [False, True])
+def test_axis_aligned_lines_are_five_pixels_wide_at_any_offset(oracle, vertical):
+    """The half-open band (c - 2.5, c + 2.5] holds exactly five pixel centres wherever the
+    line lies, and the ends cover the centres in [x0, x1)."""
+    W, H = 48, 48
+    rng = np.random.default_rng(7)
+    objs, spans = [], []
+    for i in range(6):
+        c = 6.0 + 7.0 * i + rng.integers(0, 256) / 256.0  # exact in 1/256 pixel
+        x0 = 4.0 + rng.integers(0, 256) / 256.0
+        x1 = x0 + 20.0 + rng.integers(0, 2048) / 256.0
+        a, b = ((c, x0), (c, x1)) if vertical else ((x0, c), (x1, c))
+        objs.append(sc.debug_object(sc.DEBUG_LINE, window_line(a, b, W, H), (1.0, 0.0, 0.0, 1.0),
+                                    sc.DEBUG_SCREEN_SPACE))
+        spans.append((c, x0, x1))
+    for (c, x0, x1), o in zip(spans, objs):
+        out = oracle.render(with_lines(background_scene(W, H), [o]), threads=1)
+        m = painted(out, (255, 0, 0))
+        if vertical:
+            m = m.T
+        rows = np.nonzero(m.any(axis=1))[0]
+        cols = np.nonzero(m.any(axis=0))[0]
+        # perp > 0 on the side of larger y for a line running towards +x; towards +y it is the side of
+        # smaller x, so the included edge swaps between the two cases
+        if vertical:
+            assert rows.tolist() == [r for r in range(W) if -2.5 <= (r + 0.5) - c < 2.5]
+        else:
+            assert rows.tolist() == [r for r in range(H) if -2.5 < (r + 0.5) - c <= 2.5]
+        assert cols.tolist() == [k for k in range(W) if x0 <= k + 0.5 < x1]
+        assert m[rows][:, cols].all()
+
+
+def test_reversed_segment_covers_the_same_interior(oracle):
+    """Swapping a segment's ends changes only the tie rules at its ends and edges."""
+    W, H = 40, 40
+    rng = np.random.default_rng(3)
+    for _ in range(5):
+        a = rng.uniform(5, 35, 2)
+        b = rng.uniform(5, 35, 2)
+        f = sc.debug_object(sc.DEBUG_LINE, window_line(a, b, W, H), RED, sc.DEBUG_SCREEN_SPACE)
+        r = sc.debug_object(sc.DEBUG_LINE, window_line(b, a, W, H), RED, sc.DEBUG_SCREEN_SPACE)
+        mf = painted(oracle.render(with_lines(background_scene(W, H), [f]), threads=1), (255, 0, 0))
+        mr = painted(oracle.render(with_lines(background_scene(W, H), [r]), threads=1), (255, 0, 0))
+        ys, xs = np.nonzero(mf ^ mr)
+        if len(xs):  # only centres on the rectangle's boundary can differ
+            p = np.stack([xs + 0.5, ys + 0.5], 1)
+            d = b - a
+            along = (p - a) @ d / (d @ d)
+            perp = np.abs((p - a) @ np.array([-d[1], d[0]])) / np.linalg.norm(d)
+            on_edge = (np.abs(perp - 2.5) < 0.01) | (np.abs(along) < 0.01) | (np.abs(along - 1) < 0.01)
+            assert on_edge.all()
