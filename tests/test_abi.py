@@ -62,6 +62,7 @@ def test_calls_without_a_context_are_rejected(renderer_lib):
     P = C.c_void_p
     assert renderer_lib.rz_render(None) == 3
     assert renderer_lib.rz_sync(None, 0) == 3
+    assert renderer_lib.rz_set_debug_objects(None, None, 0) == 3
     out = C.c_void_p()
     assert renderer_lib.rz_create(C.byref(out), None) == 3
     renderer_lib.rz_destroy(None)
