@@ -215,3 +215,25 @@ def test_reversed_segment_covers_the_same_interior(oracle):
             perp = np.abs((p - a) @ np.array([-d[1], d[0]])) / np.linalg.norm(d)
             on_edge = (np.abs(perp - 2.5) < 0.01) | (np.abs(along) < 0.01) | (np.abs(along - 1) < 0.01)
             assert on_edge.all()
+
+
+def test_view_space_uses_proj_without_a_divide(oracle):
+    """flags 2: (proj * transform) * v, then z = w = 1; with an identity proj a line lands where the
+    screen-space line does, and a scaled proj scales it without dividing by the original w."""
+    W, H = 32, 16
+    t = window_line((8, 8), (24, 8), W, H)
+    s = background_scene(W, H)
+    s.scene = s.scene.copy()
+    s.scene["proj"] = sc.colmajor(np.eye(4))
+    a = painted(oracle.render(with_lines(s, [sc.debug_object(sc.DEBUG_LINE, t, RED, sc.DEBUG_VIEW_SPACE)]),
+                              threads=1), (255, 0, 0))
+    expected = np.zeros((H, W), bool)
+    expected[6:11, 8:24] = True
+    assert np.array_equal(a, expected)
+    # w = 2 in the proj's last row would halve x and y after a divide; the shader sets w = 1 instead
+    p = np.eye(4)
+    p[3, 3] = 2.0
+    s.scene["proj"] = sc.colmajor(p)
+    b = painted(oracle.render(with_lines(s, [sc.debug_object(sc.DEBUG_LINE, t, RED, sc.DEBUG_VIEW_SPACE)]),
+                              threads=1), (255, 0, 0))
+    assert np.array_equal(b, expected)
