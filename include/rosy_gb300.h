@@ -261,7 +261,7 @@ typedef struct rz_stats {
     uint64_t shadow_stamps;         /* 8x4-pixel stamps rasterised, shadow pass */
     uint64_t camera_stamps;         /* 8x4-pixel stamps rasterised, camera pass */
     uint32_t error_flags;           /* device-side error bits of the last frame */
-    uint32_t kernel_launches;       /* kernels enqueued by the last rz_render */
+    uint32_t kernel_launches;       /* kernels the last rz_render launched (counted as its frame was built) */
 } rz_stats;
 
 /* graphics::init (src/Engine/Graphics.h:17): creates the CUDA stream and the
