@@ -11,8 +11,9 @@
  *   render              src/Engine/Graphics.cpp:4934   -> rz_render
  *   init / deinit       src/Engine/Graphics.cpp:6119-6170, 6217-6228 -> rz_create / rz_destroy
  *   resize              src/Engine/Graphics.cpp:6200   -> rz_resize
+ *   (DRAW DEBUG)        src/Engine/Graphics.cpp:5694-5738 -> rz_set_debug_objects
  *
- * Windowing, swapchain, imgui and debug lines are not part of this path: the
+ * Windowing, swapchain and imgui are not part of this path: the
  * frame is rendered into headless device buffers (RGBA8 sRGB colour, D32 depth,
  * a 64-bit visibility buffer and the D32 shadow map) that the caller reads with
  * rz_get_frame (device pointers) or rz_read_frame (copy to host memory).
