@@ -14,6 +14,8 @@
 //                            5845-5879 (blit to the sRGB swapchain)
 //   samplers                 src/Engine/Graphics.cpp:2697-2725, 3421-3438, 3996-4014
 //   material packing         src/Engine/Graphics.cpp:4071-4150
+//   debug-line overlay       src/shaders/debug.slang:5-35, src/Engine/Graphics.cpp:3222-3249 (vertex
+//                            table), 5694-5738 (DRAW DEBUG)
 //   draw lists               src/Engine/Graphics.cpp:4691-4735
 // The fixed-function stages (clipping, viewport, rasterisation, depth bias,
 // depth test, texel filtering, depth compare, blending, sRGB conversion) follow
