@@ -377,6 +377,14 @@ typedef struct rz_tuning {
 int rz_set_tuning(struct rz_ctx* ctx, const rz_tuning* tuning);
 int rz_get_tuning(struct rz_ctx* ctx, rz_tuning* tuning);
 
+/* Diagnostic: the bound of each look-back wait of the blended list's ordered
+ * setup (iterations of about 32 ns) for the following frames; 0 restores the
+ * default (2^22). A wait that runs out flags the frame (rz_sync returns
+ * RZ_GRAPHICS_FRAME_FAILURE) and the blended list is left out of that frame.
+ * This library addition has no counterpart in the reference, whose ordering
+ * comes from the hardware; tests use it to make the waits run out. */
+int rz_set_wait_limit(struct rz_ctx* ctx, uint32_t lookback_spins);
+
 /* Autotuner: renders the current views `frames` times (after one warm-up
  * frame) with every candidate of chunk_stamps in {16, 32, 64} x small_extent in
  * {4, 8, 12}, measures device time with CUDA events, applies the fastest and
@@ -408,7 +416,7 @@ int rz_get_stage_times(struct rz_ctx* ctx, float* ms, uint32_t capacity, uint32_
  * point has no counterpart in the reference. It rasterises one draw into a D32
  * depth target exactly as rz_render's shadow pass does (clear to 0, MVP =
  * projection * world, clipping, culling, depth bias, GREATER_OR_EQUAL), using
- * only a fixed scratch array compiled into the library (about 2.9 MiB per
+ * only a fixed scratch array compiled into the library (about 3.3 MiB per
  * device, held until the process exits); it allocates nothing.
  *   positions: device array of vertex_count float4 (x, y, z, unused)
  *   indices:   device array of index_count u32 (a multiple of 3, at most
@@ -416,11 +424,14 @@ int rz_get_stage_times(struct rz_ctx* ctx, float* ms, uint32_t capacity, uint32_
  *   projection, world: host column-major 4x4 matrices
  *   depth_out: device array of width * height floats, overwritten
  * Runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it.
- * Returns RZ_OVERFLOW if the coverage needs more than the fixed work queue
- * (65,536 chunks of 32 8x4-pixel stamps). Calls share the scratch array: calls
- * that overlap on the GPU race and must be serialised by the caller. The first
- * call on a device looks up the array's device address; make it before any
- * stream capture starts on that device. */
+ * Returns RZ_OVERFLOW (the depth target is then incomplete) if the coverage
+ * needs more than the fixed work queue (65,536 chunks of 32 8x4-pixel stamps),
+ * or if clipping fans the triangles out into more than 24,576 setup records.
+ * Calls share the scratch array: calls that overlap on the GPU race and must be
+ * serialised by the caller. The first call on a device looks up the array's
+ * device address (and, with lazy module loading, may load the module that
+ * holds it); make it before any stream capture starts on that device, as a
+ * warm-up call at start-up where a frame loop must not allocate. */
 int rz_shadow_depth_static(const void* positions, uint32_t vertex_count, const uint32_t* indices,
                            uint32_t index_count, const float projection[16], const float world[16],
                            const rz_draw_config* cfg, uint32_t width, uint32_t height, float* depth_out,
@@ -648,9 +659,19 @@ int rz_upsampler_get_grads(struct rz_upsampler* u, float* grads, uint32_t count,
 int rz_upsampler_adam_step(struct rz_upsampler* u, float lr, float beta1, float beta2, float eps, float grad_scale,
                            void* stream);
 
-/* Device-side error bits of the upsampler's kernels so far (a tensor-core wait
- * that ran out of its iteration limit sets bit 0); synchronises `stream`. */
+/* Device-side error bits of the upsampler's kernels so far (a copy or
+ * tensor-core wait that ran out of its time limit sets bit 0; the bits stay set
+ * for the life of the object); synchronises `stream`. */
 int rz_upsampler_status(struct rz_upsampler* u, uint32_t* flags, void* stream);
+
+/* Diagnostic: the time limit, in SM clock cycles, of each wait inside the
+ * upsampler's kernels (TMA copies landed, MMAs done, accumulators drained) for
+ * the following calls; 0 restores the default (about one second). A wait that
+ * runs out sets bit 0 of the status and its kernel stops early, after its copies
+ * and MMAs in flight have completed, with its output incomplete. This library
+ * addition has no counterpart in the reference; tests use it to make the waits
+ * run out. */
+int rz_upsampler_set_wait_limit(struct rz_upsampler* u, uint64_t cycles);
 
 /* Tensor-core self-test: D (128 x n, f32) = A (128 x k, bf16, row-major) *
  * B (n x k, bf16, row-major)^T with one CTA, the MMA layout the convolutions

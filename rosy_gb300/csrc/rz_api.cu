@@ -98,6 +98,7 @@ struct rz_ctx {
     uint32_t queue_chunks = 0;    // fixed work-queue depth (0 = sized from the scene)
     uint32_t chunk_stamps = kChunkStamps;
     uint32_t small_extent = kSmallExtent;
+    uint32_t lookback_spins = kLookbackSpins;
     bool batched = true;          // false: per-view sequential launches
     std::string last_error;
 
@@ -719,6 +720,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
     p.error_flags = kind == 0 ? &c->d_report->shadow_errors : &c->d_report->camera_errors;
     p.chunk_stamps = c->chunk_stamps;
     p.small_extent = c->small_extent;
+    p.lookback_spins = c->lookback_spins;
     p.sample_x = 128;  // pixel centre
     p.sample_y = 128;
     p.sample_plane = 0;
@@ -986,6 +988,7 @@ int enqueue_frame(rz_ctx* c) {
         bp.sh.consts = c->d_blended_consts;
         bp.records = c->blended_pass.records;
         bp.header = &c->d_report->blended;
+        bp.error_flags = &c->d_report->camera_errors;
         bp.record_capacity = c->blended_pass.record_capacity;
         bp.debug = c->d_debug_segs;
         bp.debug_count = c->debug_count;
@@ -1595,6 +1598,15 @@ int rz_set_tuning(rz_ctx* c, const rz_tuning* t) {
         c->layout_dirty = true;
     }
     drop_graph(c);
+    return RZ_OK;
+}
+
+int rz_set_wait_limit(rz_ctx* c, uint32_t lookback_spins) {
+    if (!c) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    c->lookback_spins = lookback_spins ? lookback_spins : kLookbackSpins;
+    drop_graph(c);  // the limit is a kernel argument captured in the frame graph
     return RZ_OK;
 }
 

@@ -125,6 +125,10 @@ constexpr uint32_t kErrStampOverflow = 1u << 1;
 constexpr uint32_t kErrLookbackTimeout = 1u << 2;
 constexpr uint32_t kErrBadIndex = 1u << 3;
 
+// Iterations a look-back wait spins (about 32 ns each) before it gives up with
+// kErrLookbackTimeout; rz_set_wait_limit can lower it.
+constexpr uint32_t kLookbackSpins = 1u << 22;
+
 // Per-pass scratch header, cleared before each pass.
 struct PassHeader {
     uint32_t ticket;          // CTA tile ticket of the setup kernel
@@ -170,6 +174,7 @@ struct PassParams {
     uint32_t chunk_capacity;
     PassHeader* header;
     uint32_t* error_flags;
+    uint32_t lookback_spins;  // bound of each look-back wait (ordered passes)
     // coverage sample of this raster launch, in 1/256 pixel: the pixel centre
     // (128, 128) or one of the standard 4x positions; camera-pass target plane
     int32_t sample_x, sample_y;
@@ -236,6 +241,7 @@ struct BlendParams {
     ShadeParams sh;               // blended draws, their constants and varyings
     const TriRecord* records;     // setup records of the blended triangles, in submission order
     const PassHeader* header;
+    const uint32_t* error_flags;  // the blended pass's flags: its records are not used after a look-back timeout
     uint32_t record_capacity;
     uint32_t debug_count;         // overlay segments per view (0: no overlay)
     const DebugSeg* debug;        // view v's segments at debug + v * debug_count, in draw order

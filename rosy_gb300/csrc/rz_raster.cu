@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
                 const unsigned last = incl ? (unsigned)(__ffs(incl) - 1) : 31u;
                 const unsigned need = last == 31u ? 0xffffffffu : ((2u << last) - 1u);
                 if (zero & need) {
-                    if (++spins > (1u << 22)) {
+                    if (++spins > P.lookback_spins) {
                         if (lane == 0) atomicOr(P.error_flags, kErrLookbackTimeout);
                         break;
                     }

@@ -1108,7 +1108,9 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
         }
     }
     const Sampler smp{&P, s_srgb, s_unorm};
-    const uint32_t n = min(B.header->records, B.record_capacity);
+    // a pass whose look-back gave up has records at unreliable slots: blend none of them
+    const bool records_ok = !B.error_flags || !(*B.error_flags & kErrLookbackTimeout);
+    const uint32_t n = records_ok ? min(B.header->records, B.record_capacity) : 0u;
     const int lane = tid & 31, warp = tid >> 5;
     for (uint32_t start = 0; start < n; start += kBlendBatch) {
         // ordered compaction of the records whose box meets this tile (4 per thread)

@@ -9,17 +9,30 @@
 // flags) in one file-scope __device__ array of fixed size. The caller passes the
 // inputs and the output; nothing is allocated here.
 //
-// Limits: at most kStaticMaxTriangles triangles per call and kStaticChunks work
-// chunks (kStaticChunks * 32 stamps of 8x4 pixels). Larger inputs are rejected
-// with RZ_INVALID_ARGUMENT; a call whose coverage needs more chunks returns
-// RZ_OVERFLOW. The array (about 2.9 MiB) stays resident on every device that
+// Limits: at most kStaticMaxTriangles triangles per call (larger draws are
+// rejected with RZ_INVALID_ARGUMENT), kStaticRecords setup records and
+// kStaticChunks work chunks (kStaticChunks * 32 stamps of 8x4 pixels). A call
+// whose coverage needs more chunks, or whose clipped triangles fan out into more
+// records than that (the same slack as rz_render's first frame: a quarter of the
+// triangles plus 4,096), returns RZ_OVERFLOW and leaves the depth target
+// incomplete. The array (about 3.3 MiB) stays resident on every device that
 // loads the library until the process exits. All calls share it: calls that
 // overlap on the GPU (on different streams, or from different host threads)
 // race on it and must be serialised by the caller.
 //
 // The first call on a device resolves the array's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture begins on the device.
+// first call before any stream capture begins on the device. With lazy module
+// loading (the CUDA default) that first call may also be what loads the module
+// and places the array, so a caller with a strict frame loop makes one warm-up
+// call per device at start-up.
+//
+// Leftovers of earlier calls in the array do no harm: k_static_prep zeroes the
+// pass header, the look-back words and the error flags; every chunk-map entry
+// below the pass's chunk count is rewritten by the record holding that chunk's
+// first stamp, unless that record overflowed, in which case the raster meets
+// either a record index past the capacity or a record of this call whose stamp
+// range does not hold the chunk, and stops with the overflow flag set.
 #include <mutex>
 
 #include "rz_device.cuh"
@@ -27,7 +40,7 @@
 namespace rz {
 
 constexpr uint32_t kStaticMaxTriangles = 16384;
-constexpr uint32_t kStaticRecords = kStaticMaxTriangles + kStaticMaxTriangles / 4 + 1024;
+constexpr uint32_t kStaticRecords = kStaticMaxTriangles + kStaticMaxTriangles / 4 + 4096;
 constexpr uint32_t kStaticTiles = (kStaticMaxTriangles + kSetupThreads - 1) / kSetupThreads + 1;
 constexpr uint32_t kStaticChunks = 65536;
 
@@ -164,6 +177,7 @@ extern "C" int rz_shadow_depth_static(const void* positions, uint32_t vertex_cou
         p.chunk_capacity = kStaticChunks;
         p.header = reinterpret_cast<PassHeader*>(scratch + kOffHeader);
         p.error_flags = reinterpret_cast<uint32_t*>(scratch + kOffFlags);
+        p.lookback_spins = kLookbackSpins;
         p.sample_x = 128;
         p.sample_y = 128;
         p.bb_hi = 128;

@@ -29,9 +29,12 @@
 // distance between core matrices along K and the stride byte offset the
 // distance between 8-row groups along M (or N).
 //
-// Every wait on a tensor-core completion barrier has a time limit; a wait that
-// runs out sets kErrMmaTimeout, skips the epilogue, frees the tensor memory and
-// returns.
+// Every wait on a copy or tensor-core completion barrier has a time limit
+// (about a second; rz_upsampler_set_wait_limit can shorten it); a wait that runs
+// out sets kErrMmaTimeout and skips the rest of the kernel's work. Before the CTA
+// frees its tensor memory and returns, the thread that issued TMA copies waits
+// (with the full limit again) for the copies it has in flight, and the thread
+// that issued MMAs for its last commit.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda.h>
@@ -135,11 +138,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Waits for the barrier phase of `parity`; false if the time limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Waits for the barrier phase of `parity`; false if `limit` clock cycles ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitCycles) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     }
     return true;
 }
@@ -277,6 +280,7 @@ struct ConvArgs {
     __nv_bfloat16* dy;              // planar [2][H][W][8]: gradient of the loss sum (final, training)
     double* loss;                   // loss sum accumulator (final, training)
     uint32_t* err;
+    long long wait_cycles;          // bound of each pipeline wait
 };
 
 // Shared memory of the persistent convolution: the weights (B operand) once,
@@ -505,9 +509,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         // producer: the weights once (one bulk copy), then the TMA loads of each tile's halo
         mbar_expect_tx(wbar, L::B_BYTES);
         bulk_load(sB, a.wimg, L::B_BYTES, wbar);
+        int issued = 0;
         for (int j = 0; j < my_tiles && ok; ++j) {
             const int buf = j % NS;
-            if (j >= NS && !mbar_wait(&empty[buf], (uint32_t)((j - NS) / NS) & 1u)) {
+            if (j >= NS && !mbar_wait(&empty[buf], (uint32_t)((j - NS) / NS) & 1u, a.wait_cycles)) {
                 ok = false;
                 break;
             }
@@ -519,9 +524,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
 #pragma unroll
                 for (int g = 0; g < L::G; ++g)
                     tma_load_3d(A + r * L::S_R + g * L::S_G, &in_map, &full[buf], 2 * (x0 - 1), y0 - 1 + r, g);
+            issued = j + 1;
         }
-        // the copies still in flight land before the CTA exits
-        for (int j = my_tiles - NS > 0 ? my_tiles - NS : 0; j < my_tiles; ++j)
+        // the copies still in flight (the last NS tiles issued, and the weights) land
+        // before the CTA exits; a buffer's barrier cannot have moved past these phases
+        for (int j = issued - NS > 0 ? issued - NS : 0; j < issued; ++j)
             if (!mbar_wait(&full[j % NS], (uint32_t)(j / NS) & 1u)) ok = false;
         if (!mbar_wait(wbar, 0)) ok = false;
     } else if (warp == kConvEpilogueWarps + 1 && lane == 0) {
@@ -529,11 +536,12 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         constexpr uint32_t idesc = idesc_bf16(128, 3 * N);
         constexpr uint32_t lbo_b = 3 * N * 16;  // between the weight image's 8-channel groups
         const uint64_t db0 = umma_desc(smem_u32(sB), lbo_b, 128);
-        if (my_tiles > 0 && !mbar_wait(wbar, 0)) ok = false;
+        if (my_tiles > 0 && !mbar_wait(wbar, 0, a.wait_cycles)) ok = false;
+        int committed = 0;
         for (int j = 0; j < my_tiles && ok; ++j) {
             const int buf = j % NS, acc = j & 1;
-            if (!mbar_wait(&full[buf], (uint32_t)(j / NS) & 1u) ||
-                (j >= 2 && !mbar_wait(&tempty[acc], (uint32_t)((j - 2) >> 1) & 1u))) {
+            if (!mbar_wait(&full[buf], (uint32_t)(j / NS) & 1u, a.wait_cycles) ||
+                (j >= 2 && !mbar_wait(&tempty[acc], (uint32_t)((j - 2) >> 1) & 1u, a.wait_cycles))) {
                 ok = false;
                 break;
             }
@@ -556,9 +564,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
             }
             mma_commit(&empty[buf]);
             mma_commit(&tfull[acc]);
+            committed = j + 1;
         }
-        // the last MMAs complete before the CTA frees its tensor memory
-        if (ok && my_tiles > 0 && !mbar_wait(&empty[(my_tiles - 1) % NS], (uint32_t)((my_tiles - 1) / NS) & 1u))
+        // the MMAs issued complete before the CTA frees its tensor memory: the last
+        // commit tracks every earlier one
+        if (committed > 0 && !mbar_wait(&empty[(committed - 1) % NS], (uint32_t)((committed - 1) / NS) & 1u))
             ok = false;
     } else if (warp < kConvEpilogueWarps) {
         const int quad = warp & 3, row0 = (warp >> 2) * (kTileRows * 4 / kConvEpilogueWarps);
@@ -568,7 +578,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         for (int c = 0; c < N; ++c) bias[c] = s_bias[c];
         for (int j = 0; j < my_tiles; ++j) {
             const int buf = j & 1;
-            if (!mbar_wait(&tfull[buf], (uint32_t)(j >> 1) & 1u)) {
+            if (!mbar_wait(&tfull[buf], (uint32_t)(j >> 1) & 1u, a.wait_cycles)) {
                 ok = false;
                 break;
             }
@@ -613,6 +623,7 @@ struct WgradArgs {
     float* db;                // [N], accumulated
     int W, H;
     uint32_t* err;
+    long long wait_cycles;    // bound of each wait for the previous tile's MMAs
 };
 
 template <int CIN, int N>
@@ -657,7 +668,7 @@ __global__ void __launch_bounds__(kThreads) k_wgrad(WgradArgs a) {
     bool ok = true;
     int iter = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++iter) {
-        if (iter > 0) ok = ok && mbar_wait(bar, (uint32_t)(iter - 1) & 1u);
+        if (iter > 0) ok = ok && mbar_wait(bar, (uint32_t)(iter - 1) & 1u, a.wait_cycles);
         if (!__syncthreads_and(ok ? 1 : 0)) {
             ok = false;
             break;
@@ -720,8 +731,11 @@ __global__ void __launch_bounds__(kThreads) k_wgrad(WgradArgs a) {
             mma_commit(bar);
         }
     }
-    if (ok && iter > 0) ok = mbar_wait(bar, (uint32_t)(iter - 1) & 1u);
+    if (ok && iter > 0) ok = mbar_wait(bar, (uint32_t)(iter - 1) & 1u, a.wait_cycles);
     ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    // after a wait ran out, the MMAs of the last tile (committed by thread 0) still
+    // complete before the tensor memory is freed
+    if (!ok && tid == 0 && iter > 0) mbar_wait(bar, (uint32_t)(iter - 1) & 1u);
     tc_fence_after();
     if (ok && iter > 0) {
         for (int b = 0; b < L::NB; ++b) {
@@ -836,6 +850,7 @@ __global__ void __launch_bounds__(kThreads) k_selftest(const __nv_bfloat16* A, c
         for (int c = 0; c < N; ++c) D[m * N + c] = acc[c];
     } else if (tid == 0) {
         atomicOr(err, kErrMmaTimeout);
+        mbar_wait(bar, 0);  // the MMAs complete before the tensor memory is freed
     }
     tc_fence_before();
     __syncthreads();
@@ -865,6 +880,7 @@ struct rz_upsampler {
     uint32_t* d_err = nullptr;
     uint64_t values = 0;
     int adam_t = 0;
+    long long wait_cycles = kWaitCycles;  // bound of the pipeline waits (rz_upsampler_set_wait_limit)
 };
 
 namespace {
@@ -976,6 +992,7 @@ ConvArgs conv_args(const rz_upsampler* u, int W, int H) {
     a.W = W;
     a.H = H;
     a.err = u->d_err;
+    a.wait_cycles = u->wait_cycles;
     return a;
 }
 
@@ -1101,6 +1118,7 @@ int rz_upsampler_accumulate(rz_upsampler* u, const rz_gbuffer* in, const void* t
     w.W = W;
     w.H = H;
     w.err = u->d_err;
+    w.wait_cycles = u->wait_cycles;
     ConvArgs d = conv_args(u, W, H);
     // layer 3
     w.x = u->d_act[2];
@@ -1176,6 +1194,12 @@ int rz_upsampler_adam_step(rz_upsampler* u, float lr, float beta1, float beta2, 
     if (cudaMemsetAsync(u->d_loss, 0, sizeof(double), s) != cudaSuccess) return RZ_ERROR;
     u->values = 0;
     return cudaGetLastError() == cudaSuccess ? RZ_OK : RZ_ERROR;
+}
+
+int rz_upsampler_set_wait_limit(rz_upsampler* u, uint64_t cycles) {
+    if (!u) return RZ_INVALID_ARGUMENT;
+    u->wait_cycles = (cycles == 0 || cycles > (uint64_t)kWaitCycles) ? kWaitCycles : (long long)cycles;
+    return RZ_OK;
 }
 
 int rz_upsampler_status(rz_upsampler* u, uint32_t* flags, void* stream) {

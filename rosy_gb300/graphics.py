@@ -88,6 +88,10 @@ class Graphics:
         t = _abi.RzTuning(chunk_stamps, small_extent, queue_chunks, 1 if batched else 0)
         self._check(self._lib.rz_set_tuning(self._ctx, C.byref(t)), "rz_set_tuning")
 
+    def set_wait_limit(self, lookback_spins: int) -> None:
+        """Bound of each look-back wait of the blended list's ordered setup (0: default)."""
+        self._check(self._lib.rz_set_wait_limit(self._ctx, lookback_spins), "rz_set_wait_limit")
+
     def tuning(self) -> dict:
         t = _abi.RzTuning()
         self._check(self._lib.rz_get_tuning(self._ctx, C.byref(t)), "rz_get_tuning")

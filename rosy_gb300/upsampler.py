@@ -126,6 +126,10 @@ class Upsampler:
         self._check(self._lib.rz_upsampler_status(self._u, C.byref(f), stream), "rz_upsampler_status")
         return f.value
 
+    def set_wait_limit(self, cycles: int) -> None:
+        """Time limit (SM cycles) of each wait in the kernels of the following calls (0: default)."""
+        self._check(self._lib.rz_upsampler_set_wait_limit(self._u, cycles), "rz_upsampler_set_wait_limit")
+
 
 def selftest_gemm(a_ptr: int, b_ptr: int, d_ptr: int, n: int, k: int, stream: int | None = None) -> int:
     """Runs the tensor-core self-test GEMM (see rz_upsampler_selftest_gemm); returns its status code."""

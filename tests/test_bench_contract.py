@@ -19,6 +19,7 @@ def test_reference_arm_prints_one_contract_line():
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in j, key
     assert j["impl"] == "reference" and j["value"] > 0 and j["steps"] >= 1
+    assert j["warmup"] == 3  # the requested warm-up frames ran
     assert j["higher_is_better"] is True and j["config"]["workload"]
     assert j["cpu_baseline"]["kind"] == "port" and j["cpu_baseline"]["cores"] >= 1
     assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["e2e"]["d2h_bytes_per_step"] == 0

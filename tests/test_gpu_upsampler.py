@@ -98,7 +98,7 @@ def test_gbuffer_albedo_and_normal(gpu):
     g.deinit()
 
 
-@pytest.mark.parametrize("w,h", [(96, 64), (200, 70)])
+@pytest.mark.parametrize("w,h", [(96, 64), (200, 70), (960, 540)])
 def test_upsampler_forward_matches_oracle(gpu, w, h):
     import torch
 
@@ -144,7 +144,7 @@ def test_zero_network_is_exactly_the_bilinear_base(gpu):
     hi.deinit()
 
 
-@pytest.mark.parametrize("w,h", [(96, 64), (200, 70)])
+@pytest.mark.parametrize("w,h", [(96, 64), (200, 70), (960, 540)])
 def test_upsampler_gradients_match_oracle(gpu, w, h):
     import torch
 
