@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RZ_ABI_VERSION 1u
+#define RZ_ABI_VERSION 2u
 
 /* Opaque renderer context (one per host thread). */
 struct rz_ctx;
@@ -548,12 +548,23 @@ int rz_bc7_decode_texture_unit(const void* blocks, uint32_t width, uint32_t heig
  * pixel, else 0) and the interpolated world-space normal, octahedral-encoded as
  * two f16 (x in the low half). With 4x multisampling both are averaged over the
  * pixel's samples (the normal renormalised) and the albedo's alpha is the
- * covered fraction of the samples. */
+ * covered fraction of the samples.
+ * Single-sampled frames also get the sub-pixel sources of the upsampler's x2
+ * base, a u16 per pixel: for each point k = 2 * (y half) + (x half) at
+ * (x + 0.25 / 0.75, y + 0.25 / 0.75) that a full-resolution pixel samples, the
+ * front-most of the triangles visible at the 3x3 neighbourhood's pixel centres
+ * (float edge functions, the depth plane through the vertices' z / w), and
+ * bit 4k + s set when bilinear source s of that pixel (0 own, 1 horizontal,
+ * 2 vertical, 3 diagonal neighbour, clamped at the borders) shows the same
+ * triangle (or background); 0xFFFF where the neighbourhood shows one triangle.
+ * The upsampler renormalises the bilinear weights over the marked sources.
+ * NULL (4x multisampling, or a caller's own G-buffer) means plain bilinear. */
 typedef struct rz_gbuffer {
     const void* color_rgba8;      /* width*height RGBA8 sRGB (the frame's colour) */
     const void* depth_f32;        /* width*height f32 (reverse-Z, 0 = background) */
     const void* albedo_rgba8;     /* width*height RGBA8 */
     const void* normal_oct_f16x2; /* width*height u32 */
+    const void* sources_u16;      /* width*height u16 sub-pixel sources, or NULL */
     uint32_t width;
     uint32_t height;
 } rz_gbuffer;

@@ -63,6 +63,17 @@ int oracle_render(const oracle_scene* scene, oracle_out* out, int threads);
 /* Only the raster passes: the shadow map and the camera pass's depth/ids. */
 int oracle_raster(const oracle_scene* scene, oracle_out* out, int threads);
 
+/* Sub-pixel sources of the learned path's triangle-aware base (the renderer's
+ * k_subpixel_sources; no counterpart in the reference): for each pixel of the
+ * scene's width*height visibility `ids` (triangle id + 1, 0 = background), the
+ * front-most triangle (largest depth plane value through the vertices' z / w)
+ * of its 3x3 neighbourhood at each of the four sample points
+ * (x + 0.25 / 0.75, y + 0.25 / 0.75) of the 2x image, and which of each point's
+ * four bilinear sources (own, horizontal, vertical, diagonal neighbour, clamped
+ * at the borders) show that triangle: bit 4k + s of out[pixel] for point
+ * k = 2 * (y half) + (x half) and source s. */
+int oracle_subpixel_sources(const oracle_scene* scene, const uint32_t* ids, uint16_t* out, int threads);
+
 /* BC7 (bc7_oracle.cpp): one 16-byte block to 16 RGBA8 texels (row-major), and
  * one image of max(1,(w+3)/4) x max(1,(h+3)/4) blocks in rows to w x h RGBA8.
  * oracle_render decodes the scene's RZ_TEXELS_BC7 textures with it first. */

@@ -74,6 +74,8 @@ def lib():
             fn.restype = C.c_int
         _lib.oracle_bc7_decode.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
         _lib.oracle_bc7_decode.restype = C.c_int
+        _lib.oracle_subpixel_sources.argtypes = [C.POINTER(OracleScene), C.c_void_p, C.c_void_p, C.c_int]
+        _lib.oracle_subpixel_sources.restype = C.c_int
     return _lib
 
 
@@ -164,6 +166,19 @@ def raster(s, threads: int = 0) -> dict:
     rc = lib().oracle_raster(C.byref(o), C.byref(oo), int(threads))
     if rc != 0:
         raise RuntimeError(f"oracle_raster failed: {rc}")
+    return out
+
+
+def subpixel_sources(s, ids: np.ndarray, threads: int = 0) -> np.ndarray:
+    """(H, W) u16 sub-pixel source masks of the learned path's x2 base for the
+    scene's camera and the (H, W) visibility `ids` (triangle id + 1)."""
+    m = Marshalled(s)
+    o = _scene_struct(m)
+    ids = np.ascontiguousarray(ids, np.uint32).reshape(s.height, s.width)
+    out = np.zeros((s.height, s.width), np.uint16)
+    rc = lib().oracle_subpixel_sources(C.byref(o), ptr(ids), ptr(out), int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_subpixel_sources failed: {rc}")
     return out
 
 

@@ -17,6 +17,8 @@
 //   debug-line overlay       src/shaders/debug.slang:5-35, src/Engine/Graphics.cpp:3222-3249 (vertex
 //                            table), 5694-5738 (DRAW DEBUG)
 //   draw lists               src/Engine/Graphics.cpp:4691-4735
+// and, with no counterpart in the reference, the renderer's sub-pixel sources
+// of the learned half-resolution path (oracle_subpixel_sources).
 // The fixed-function stages (clipping, viewport, rasterisation, depth bias,
 // depth test, texel filtering, depth compare, blending, sRGB conversion) follow
 // the Vulkan specification's rules; the reference delegates them to the driver.
@@ -1427,6 +1429,110 @@ extern "C" int oracle_raster(const oracle_scene* s, oracle_out* out, int threads
     }
     shadow_pass(c, shadow, threads);
     camera_pass(c, depth, ids, threads);
+    return 0;
+}
+
+// ---- sub-pixel sources of the learned path's triangle-aware x2 base -----------
+// (the renderer's k_subpixel_sources, restated; the reference has no such pass)
+
+namespace {
+
+struct SubTri {
+    float X[3], Y[3], Z[3];  // screen position (pixels) and NDC depth z / w of each vertex
+    float inv_area;          // 1 / twice the signed screen area (0 when degenerate)
+    bool valid;              // every w > 0
+};
+
+SubTri sub_triangle(const Ctx& c, uint32_t id, float hw, float hh) {
+    const uint32_t tri = id - 1;
+    const Draw& d = find_draw(c.opaque, tri);
+    const uint32_t t = tri - d.tri_base;
+    SubTri g;
+    g.valid = true;
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = d.vertex_base + c.s->indices[d.first_index + 3 * t + k];
+        float cp[4];
+        clip_position<float>(c, d, vi, cp);
+        g.valid = g.valid && cp[3] > 0.0f;
+        const float rw = 1.0f / cp[3];
+        g.X[k] = (cp[0] * rw) * hw + hw;
+        g.Y[k] = (cp[1] * rw) * hh + hh;
+        g.Z[k] = cp[2] * rw;
+    }
+    const float area = (g.X[1] - g.X[0]) * (g.Y[2] - g.Y[0]) - (g.X[2] - g.X[0]) * (g.Y[1] - g.Y[0]);
+    g.inv_area = area != 0.0f ? 1.0f / area : 0.0f;
+    return g;
+}
+
+uint16_t subpixel_mask(const Ctx& c, const uint32_t* ids, int W, int H, int x, int y, float hw, float hh) {
+    uint32_t nb[9];
+    int n9 = 0;
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int yy = std::min(std::max(y + dy, 0), H - 1), xx = std::min(std::max(x + dx, 0), W - 1);
+            nb[n9++] = ids[(size_t)yy * W + xx];
+        }
+    const uint32_t own = nb[4];
+    bool same = true;
+    for (int i = 0; i < 9; ++i) same = same && nb[i] == own;
+    if (same) return 0xFFFF;
+    uint32_t cand[9];
+    int n = 0;
+    for (int i = 0; i < 9; ++i) {
+        bool seen = nb[i] == 0;
+        for (int j = 0; j < n; ++j) seen = seen || cand[j] == nb[i];
+        if (!seen) cand[n++] = nb[i];
+    }
+    uint32_t best[4] = {0, 0, 0, 0};
+    float best_z[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int ci = 0; ci < n; ++ci) {
+        const SubTri g = sub_triangle(c, cand[ci], hw, hh);
+        for (int k = 0; k < 4; ++k) {
+            const float sx = (float)x + ((k & 1) ? 0.75f : 0.25f), sy = (float)y + ((k >> 1) ? 0.75f : 0.25f);
+            bool inside;
+            float z;
+            if (!g.valid) {  // a vertex behind the eye: only the pixel's own triangle, behind every other
+                inside = cand[ci] == own;
+                z = -3.0e38f;
+            } else {
+                const float e0 = (g.X[2] - g.X[1]) * (sy - g.Y[1]) - (g.Y[2] - g.Y[1]) * (sx - g.X[1]);
+                const float e1 = (g.X[0] - g.X[2]) * (sy - g.Y[2]) - (g.Y[0] - g.Y[2]) * (sx - g.X[2]);
+                const float e2 = (g.X[1] - g.X[0]) * (sy - g.Y[0]) - (g.Y[1] - g.Y[0]) * (sx - g.X[0]);
+                inside = g.inv_area != 0.0f &&
+                         ((e0 >= 0.0f && e1 >= 0.0f && e2 >= 0.0f) || (e0 <= 0.0f && e1 <= 0.0f && e2 <= 0.0f));
+                z = ((e0 * g.Z[0] + e1 * g.Z[1]) + e2 * g.Z[2]) * g.inv_area;
+            }
+            if (inside && z > best_z[k]) {  // reverse-Z: larger is nearer, as in the depth test
+                best[k] = cand[ci];
+                best_z[k] = z;
+            }
+        }
+    }
+    uint16_t mask = 0;
+    for (int k = 0; k < 4; ++k) {
+        const int xs = std::min(std::max(x + ((k & 1) ? 1 : -1), 0), W - 1);
+        const int ys = std::min(std::max(y + ((k >> 1) ? 1 : -1), 0), H - 1);
+        const uint32_t src[4] = {ids[(size_t)y * W + x], ids[(size_t)y * W + xs], ids[(size_t)ys * W + x],
+                                 ids[(size_t)ys * W + xs]};
+        for (int s = 0; s < 4; ++s)
+            if (src[s] == best[k]) mask |= (uint16_t)(1u << (4 * k + s));
+    }
+    return mask;
+}
+
+}  // namespace
+
+extern "C" int oracle_subpixel_sources(const oracle_scene* s, const uint32_t* ids, uint16_t* out, int threads) {
+    if (!s || !ids || !out) return 3;
+    threads = threads_or_default(threads);
+    Ctx c;
+    build_ctx(s, c);
+    const int W = (int)s->width, H = (int)s->height;
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    parallel_rows(H, threads, [&](int r0, int r1) {
+        for (int y = r0; y < r1; ++y)
+            for (int x = 0; x < W; ++x) out[(size_t)y * W + x] = subpixel_mask(c, ids, W, H, x, y, hw, hh);
+    });
     return 0;
 }
 

@@ -3,9 +3,14 @@
 A numpy restatement of the network the CUDA kernels in
 rosy_gb300/csrc/rz_upsample.cu run: input features from the G-buffer, four 3x3
 convolutions with zero padding (16 -> 32 -> 32 -> 32 -> 12 channels, ReLU after
-the first three), pixel shuffle x2 added to the bilinear x2 upsampling of the
-input colour, the loss sum of squared errors against a full-resolution target,
-and the gradients of that sum with respect to every parameter.
+the first three), pixel shuffle x2 added to the x2 base of the input colour,
+the loss sum of squared errors against a full-resolution target, and the
+gradients of that sum with respect to every parameter.
+
+The x2 base is bilinear; with the G-buffer's sub-pixel sources (a u16 mask per
+pixel: bit 4k + s = source s of sample point k shows the point's triangle) it
+keeps only the bilinear sources that show the triangle at each full-resolution
+pixel and renormalises their weights (plain bilinear where none does).
 
 Values are rounded to BF16 (round to nearest even) at exactly the points where
 the kernels store BF16: the features, the weights, the activations after ReLU,
@@ -25,7 +30,8 @@ import numpy as np
 
 LAYERS = [(16, 32), (32, 32), (32, 32), (32, 16)]
 OUT_CHANNELS = 12
-REAL_IN_CHANNELS = 10
+REAL_IN_CHANNELS = 14  # colour 3, albedo 3, normal 2, coverage, depth, matched source weight of 4 points
+BILINEAR_WEIGHTS = (0.5625, 0.1875, 0.1875, 0.0625)  # own, horizontal, vertical, diagonal source
 
 
 def layer_offsets():
@@ -72,7 +78,20 @@ def features(gb: dict, exact: bool = False) -> np.ndarray:
     f[..., 6:8] = gb["normal"].astype(ft)
     f[..., 8] = a[..., 3] / ft(255.0)
     f[..., 9] = np.minimum(gb["depth"].astype(ft) * ft(16.0), ft(4.0))
+    src = gb.get("sources")
+    if src is not None:
+        for k in range(4):
+            f[..., 10 + k] = matched_weight(src, k, ft)
     return f if exact else bf16(f)
+
+
+def matched_weight(sources: np.ndarray, k: int, ft=np.float32) -> np.ndarray:
+    """Sum of the bilinear weights of sample point k's sources that show its triangle."""
+    m = (sources.astype(np.uint32) >> (4 * k)) & 15
+    ws = np.zeros(sources.shape, ft)
+    for s, w in enumerate(BILINEAR_WEIGHTS):
+        ws = np.where((m >> s) & 1, ws + ft(w), ws)
+    return ws
 
 
 def conv3x3(x: np.ndarray, w: np.ndarray) -> np.ndarray:
@@ -111,6 +130,37 @@ def conv3x3_weight_grad(x: np.ndarray, dy: np.ndarray) -> np.ndarray:
         ky, kx = divmod(tap, 3)
         dw[:, tap, :] = d.T @ xp[ky:ky + H, kx:kx + W].reshape(-1, cin)
     return dw
+
+
+def x2_base(color: np.ndarray, sources: np.ndarray | None = None, ft=np.float32) -> np.ndarray:
+    """(2H, 2W, 3) x2 base of RGBA8 colour / 255: bilinear, or with sub-pixel sources
+    the same weighted sum over the sources that show each point's triangle, times the
+    reciprocal of the sum of their weights (summed in the kernels' order; bilinear
+    where none does)."""
+    bil = bilinear_base(color, ft)
+    if sources is None:
+        return bil
+    c = color[..., :3].astype(ft) / ft(255.0)
+    H, W = c.shape[:2]
+    out = np.zeros((2 * H, 2 * W, 3), ft)
+    ys = np.arange(H)
+    xs = np.arange(W)
+    for i in range(2):
+        yn = np.clip(ys - 1, 0, H - 1) if i == 0 else np.clip(ys + 1, 0, H - 1)
+        for j in range(2):
+            xn = np.clip(xs - 1, 0, W - 1) if j == 0 else np.clip(xs + 1, 0, W - 1)
+            k = 2 * i + j
+            m = ((sources.astype(np.uint32) >> (4 * k)) & 15)[..., None]
+            srcs = (c, c[:, xn], c[yn, :], c[yn][:, xn])
+            b = np.zeros((H, W, 3), ft)
+            ws = np.zeros((H, W, 1), ft)
+            for s, (cs, w) in enumerate(zip(srcs, BILINEAR_WEIGHTS)):
+                on = ((m >> s) & 1).astype(bool)
+                b = np.where(on, b + ft(w) * cs, b)
+                ws = np.where(on, ws + ft(w), ws)
+            inv = ft(1.0) / np.where(m == 0, ft(1.0), ws)
+            out[i::2, j::2] = np.where(m == 0, bil[i::2, j::2], b * inv)
+    return out
 
 
 def bilinear_base(color: np.ndarray, ft=np.float32) -> np.ndarray:
@@ -182,7 +232,7 @@ def forward(params: np.ndarray, gb: dict, target: np.ndarray | None = None, exac
         acts.append(rnd(np.maximum(y, 0.0).astype(ft)))
     w3, b3 = layers[3]
     net = (conv3x3(acts[-1], rnd(w3)).astype(ft) + b3.astype(ft))[..., :OUT_CHANNELS]
-    v = bilinear_base(gb["color"], ft) + shuffle(net)
+    v = x2_base(gb["color"], gb.get("sources"), ft) + shuffle(net)
     out = {"acts": acts, "v": v, "rgba8": to_rgba8(v)}
     if target is not None:
         t = target[..., :3].astype(ft) / ft(255.0)

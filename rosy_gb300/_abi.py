@@ -59,7 +59,8 @@ class RzFrameOut(C.Structure):
 
 class RzGbuffer(C.Structure):
     _fields_ = [("color_rgba8", C.c_void_p), ("depth_f32", C.c_void_p), ("albedo_rgba8", C.c_void_p),
-                ("normal_oct_f16x2", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
+                ("normal_oct_f16x2", C.c_void_p), ("sources_u16", C.c_void_p), ("width", C.c_uint32),
+                ("height", C.c_uint32)]
 
 
 class RzRsyInfo(C.Structure):

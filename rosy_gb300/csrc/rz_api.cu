@@ -151,6 +151,7 @@ struct rz_ctx {
     uint32_t samples = 1;             // camera-pass samples per pixel (1 or 4)
     uint32_t* d_gb_albedo = nullptr;
     uint32_t* d_gb_normal = nullptr;
+    uint16_t* d_gb_sources = nullptr;
     size_t gb_capacity = 0;
     size_t pix_capacity = 0, shadow_capacity = 0, color16_capacity = 0;
     size_t pix_total = 0, shadow_total = 0;
@@ -617,9 +618,11 @@ int build_layout(rz_ctx* c) {
     if (c->gbuffer && pix > c->gb_capacity) {
         dfree(c->d_gb_albedo);
         dfree(c->d_gb_normal);
+        dfree(c->d_gb_sources);
         c->gb_capacity = 0;
         RZ_CUDA(c, dalloc(&c->d_gb_albedo, pix), "G-buffer albedo");
         RZ_CUDA(c, dalloc(&c->d_gb_normal, pix), "G-buffer normals");
+        RZ_CUDA(c, dalloc(&c->d_gb_sources, pix), "G-buffer sub-pixel sources");
         c->gb_capacity = pix;
     }
     dfree(c->d_debug_objects);
@@ -666,6 +669,7 @@ int build_layout(rz_ctx* c) {
         r.scene = c->d_scene_data + vi;
         r.gb_albedo = c->gbuffer ? c->d_gb_albedo + pix_off[vi] : nullptr;
         r.gb_normal = c->gbuffer ? c->d_gb_normal + pix_off[vi] : nullptr;
+        r.gb_sources = (c->gbuffer && c->samples == 1) ? c->d_gb_sources + pix_off[vi] : nullptr;
         c->view_recs[vi] = r;
     }
     dfree(c->d_views);
@@ -977,6 +981,7 @@ int enqueue_frame(rz_ctx* c) {
         RZ_CUDA(c, cudaStreamWaitEvent(s, c->join, 0), "join");
     }
     if (c->batched || c->blended_tris || c->timing || c->debug_count) launch_shade(sh, s);
+    if (c->gbuffer && c->samples == 1) launch_subpixel_sources(sh, s);  // the learned path's x2 base
     if (c->blended_tris || c->debug_count) {
         if (c->debug_count)
             launch_debug_prep(c->d_debug_pairs, c->debug_count, c->d_debug_objects, c->d_views, (uint32_t)c->views.size(),
@@ -1203,6 +1208,7 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_debug_segs);
     dfree(c->d_gb_albedo);
     dfree(c->d_gb_normal);
+    dfree(c->d_gb_sources);
     dfree(c->d_shadow_draws);
     dfree(c->d_opaque_draws);
     dfree(c->d_blended_draws);
@@ -1520,6 +1526,7 @@ int rz_get_view_gbuffer(rz_ctx* c, uint32_t view, rz_gbuffer* out) {
     g.depth_f32 = r.depth;
     g.albedo_rgba8 = r.gb_albedo;
     g.normal_oct_f16x2 = r.gb_normal;
+    g.sources_u16 = r.gb_sources;
     g.width = (uint32_t)r.width;
     g.height = (uint32_t)r.height;
     *out = g;

@@ -45,6 +45,7 @@ struct ViewRec {
     int samples;                  // camera-pass samples per pixel (1 or 4): vis holds `samples` planes of width*height
     uint32_t* gb_albedo;          // width*height RGBA8 sRGB albedo, or null (G-buffer off)
     uint32_t* gb_normal;          // width*height world normal, octahedral 2 x f16, or null
+    uint16_t* gb_sources;         // width*height sub-pixel source masks (single-sampled G-buffer), or null
 };
 
 // gpu_material, src/Engine/Graphics.cpp:345-360, packed as in 4071-4150.
@@ -275,6 +276,7 @@ void launch_blend(const BlendParams& p, cudaStream_t stream);
 void launch_debug_prep(const DebugPair* pairs, uint32_t count, const rz_debug_object* objects, const ViewRec* views,
                        uint32_t view_count, DebugSeg* out, cudaStream_t stream);
 void launch_shade(const ShadeParams& p, cudaStream_t stream);
+void launch_subpixel_sources(const ShadeParams& p, cudaStream_t stream);
 
 // BC7 (rz_bc7.cu): bytes of a mip chain's blocks, and the decode of a chain
 // (device blocks) into RGBA8 texels (device, level l starting at level_off[l]).

@@ -999,6 +999,134 @@ void launch_shade(const ShadeParams& p, cudaStream_t stream) {
 }
 
 // ---------------------------------------------------------------------------
+// sub-pixel sources of the learned half-resolution path (G-buffer)
+// ---------------------------------------------------------------------------
+
+// Screen position (pixels) and NDC depth of the three vertices of an opaque
+// triangle: the clip position the vertex stage computes (the draw's MVP times
+// the mesh position), divided by w.
+struct SubTri {
+    float X[3], Y[3], Z[3];
+    float inv_area;  // 1 / twice the signed screen area (0 when degenerate)
+    bool valid;      // every w > 0
+};
+
+__device__ __forceinline__ SubTri sub_triangle(const ShadeParams& P, uint32_t id, float hw, float hh) {
+    const uint32_t tri = id - 1u;
+    const uint32_t d = find_draw(P.draws, P.draw_count, tri);
+    const DrawRec dr = P.draws[d];
+    const uint32_t t = tri - dr.tri_base;
+    const float* M = P.consts[d].mvp;
+    SubTri g;
+    g.valid = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = __ldg(&P.indices[dr.first_index + 3u * t + k]) + dr.vertex_base;
+        const float* pos = P.vertices[vi].position;
+        const float4 c = transform_point(M, __ldg(pos), __ldg(pos + 1), __ldg(pos + 2));
+        g.valid = g.valid && c.w > 0.0f;
+        const float rw = 1.0f / c.w;
+        g.X[k] = (c.x * rw) * hw + hw;
+        g.Y[k] = (c.y * rw) * hh + hh;
+        g.Z[k] = c.z * rw;
+    }
+    const float area = (g.X[1] - g.X[0]) * (g.Y[2] - g.Y[0]) - (g.X[2] - g.X[0]) * (g.Y[1] - g.Y[0]);
+    g.inv_area = area != 0.0f ? 1.0f / area : 0.0f;
+    return g;
+}
+
+// For the x2 reconstruction of the learned path: which triangle is in front at
+// each of the four points (x + 0.25 / 0.75, y + 0.25 / 0.75) that the pixel's
+// four full-resolution pixels sample, among the triangles visible at the 3x3
+// neighbourhood's pixel centres (covered by the float edge functions, front-most
+// by the depth plane through the vertices' z / w, larger nearer as in the depth
+// test), and which of each point's bilinear sources (own, horizontal, vertical,
+// diagonal neighbour, clamped at the borders) show it: bit 4k + s,
+// k = 2 * (y half) + (x half). A pixel whose neighbourhood shows one triangle
+// (or none) keeps every source (0xFFFF). The arithmetic is plain float without
+// contraction, restated by the oracle bit for bit. The reference has no learned
+// path; nothing here follows a reference file.
+__global__ void __launch_bounds__(256) k_subpixel_sources(ShadeParams P) {
+    __shared__ uint32_t s_view;
+    __shared__ uint32_t s_ids[18][18];  // the tile's triangle ids with a one-pixel border (clamped)
+    if (threadIdx.x == 0 && threadIdx.y == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
+    __syncthreads();
+    const ViewRec& VR = P.views[s_view];
+    if (!VR.gb_sources) return;
+    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
+    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
+    const int x0 = (int)(lt % tiles_x) * 16, y0 = (int)(lt / tiles_x) * 16;
+    const int W = VR.width, H = VR.height;
+    for (int i = threadIdx.y * 16 + threadIdx.x; i < 18 * 18; i += 256) {
+        const int yy = min(max(y0 + i / 18 - 1, 0), H - 1), xx = min(max(x0 + i % 18 - 1, 0), W - 1);
+        s_ids[i / 18][i % 18] = (uint32_t)VR.vis[(size_t)yy * W + xx];
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= W || y >= H) return;
+    uint32_t nb[9];
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) nb[dy * 3 + dx] = s_ids[threadIdx.y + dy][threadIdx.x + dx];
+    const uint32_t own = nb[4];
+    bool same = true;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) same = same && nb[i] == own;
+    uint32_t mask = 0xFFFFu;
+    if (!same) {
+        const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+        uint32_t best[4] = {0u, 0u, 0u, 0u};
+        float best_z[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (int ci = 0; ci < 9; ++ci) {
+            const uint32_t id = nb[ci];
+            bool seen = id == 0u;
+            for (int j = 0; j < ci; ++j) seen = seen || nb[j] == id;
+            if (seen) continue;  // candidates: distinct triangles in neighbourhood order
+            const SubTri g = sub_triangle(P, id, hw, hh);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float sx = (float)x + ((k & 1) ? 0.75f : 0.25f), sy = (float)y + ((k >> 1) ? 0.75f : 0.25f);
+                bool inside;
+                float z;
+                if (!g.valid) {  // a vertex behind the eye: only the pixel's own triangle, behind every other
+                    inside = id == own;
+                    z = -3.0e38f;
+                } else {
+                    const float e0 = (g.X[2] - g.X[1]) * (sy - g.Y[1]) - (g.Y[2] - g.Y[1]) * (sx - g.X[1]);
+                    const float e1 = (g.X[0] - g.X[2]) * (sy - g.Y[2]) - (g.Y[0] - g.Y[2]) * (sx - g.X[2]);
+                    const float e2 = (g.X[1] - g.X[0]) * (sy - g.Y[0]) - (g.Y[1] - g.Y[0]) * (sx - g.X[0]);
+                    inside = g.inv_area != 0.0f &&
+                             ((e0 >= 0.0f && e1 >= 0.0f && e2 >= 0.0f) || (e0 <= 0.0f && e1 <= 0.0f && e2 <= 0.0f));
+                    z = ((e0 * g.Z[0] + e1 * g.Z[1]) + e2 * g.Z[2]) * g.inv_area;
+                }
+                if (inside && z > best_z[k]) {
+                    best[k] = id;
+                    best_z[k] = z;
+                }
+            }
+        }
+        mask = 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // sources of point k: own, horizontal, vertical and diagonal neighbour (the 3x3 entries)
+            const int hx = (k & 1) ? 2 : 0, vy = (k >> 1) ? 2 : 0;
+            const uint32_t src[4] = {own, nb[3 + hx], nb[vy * 3 + 1], nb[vy * 3 + hx]};
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+                if (src[s] == best[k]) mask |= 1u << (4 * k + s);
+        }
+    }
+    VR.gb_sources[(size_t)y * W + x] = (uint16_t)mask;
+}
+
+void launch_subpixel_sources(const ShadeParams& p, cudaStream_t stream) {
+    if (p.shade_blocks == 0 || p.samples > 1) return;
+    k_subpixel_sources<<<p.shade_blocks, dim3(16, 16), 0, stream>>>(p);
+    note_launch();
+}
+
+// ---------------------------------------------------------------------------
 // blended list
 // ---------------------------------------------------------------------------
 

@@ -236,6 +236,17 @@ __device__ __forceinline__ size_t act_index(int W, int H, int x, int y, int c) {
 // ---- features -----------------------------------------------------------------
 
 // One pixel's 16 input channels from the G-buffer (see rz_upsampler_* in the header).
+// Sum of the bilinear x2 weights of a sample point's marked sources: own pixel
+// 9/16, horizontal and vertical neighbour 3/16 each, diagonal 1/16.
+__device__ __forceinline__ float matched_weight(uint32_t m4) {
+    float ws = 0.0f;
+    if (m4 & 1u) ws = ws + 0.5625f;
+    if (m4 & 2u) ws = ws + 0.1875f;
+    if (m4 & 4u) ws = ws + 0.1875f;
+    if (m4 & 8u) ws = ws + 0.0625f;
+    return ws;
+}
+
 __global__ void k_features(rz_gbuffer g, __nv_bfloat16* __restrict__ feat) {
     const int n = (int)(g.width * g.height);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -259,6 +270,11 @@ __global__ void k_features(rz_gbuffer g, __nv_bfloat16* __restrict__ feat) {
     f[9] = fminf(d * 16.0f, 4.0f);
 #pragma unroll
     for (int k = 10; k < 16; ++k) f[k] = 0.0f;
+    if (g.sources_u16) {  // per sample point: the bilinear weight of the sources that show its triangle
+        const uint32_t m = __ldg(static_cast<const uint16_t*>(g.sources_u16) + i);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) f[10 + k] = matched_weight(m >> (4 * k));
+    }
     uint4* dst0 = reinterpret_cast<uint4*>(feat + (size_t)i * 8);
     uint4* dst1 = reinterpret_cast<uint4*>(feat + (size_t)(n + i) * 8);
     *dst0 = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
@@ -275,6 +291,7 @@ struct ConvArgs {
     __nv_bfloat16* out;             // planar [N / 8][H][W][8] (relu, mask)
     const __nv_bfloat16* mask_src;  // planar like out: out = acc where mask_src > 0, else 0 (mask)
     const uint32_t* color_lr;       // H x W RGBA8: bilinear base (final)
+    const uint16_t* sources;        // H x W sub-pixel sources of the base, or null: plain bilinear (final)
     uint32_t* out_rgba8;            // 2H x 2W, or null (final)
     const uint32_t* target;         // 2H x 2W RGBA8, or null (final, training)
     __nv_bfloat16* dy;              // planar [2][H][W][8]: gradient of the loss sum (final, training)
@@ -366,6 +383,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
                 for (int k = 0; k < 3; ++k) f[r][q][k] = unorm8((c >> (8 * k)) & 255u);
             }
         }
+        const uint32_t srcmask = a.sources ? (uint32_t)__ldg(a.sources + (size_t)y * W + x) : 0xFFFFu;
         float g[kOutChannels];
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
@@ -379,12 +397,25 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
                 const int qs = j == 0 ? 0 : 2;
                 const uint32_t tj = j == 0 ? t.x : t.y;
                 uint32_t ov = 255u << 24;
+                // the sources of this point that show its triangle (all four: bilinear, none: bilinear too)
+                const uint32_t m4 = (srcmask >> (4 * (2 * i + j))) & 15u;
+                const float inv_ws = m4 ? 1.0f / matched_weight(m4) : 0.0f;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    float base = 0.5625f * f[1][1][k];
-                    base = base + 0.1875f * f[1][qs][k];
-                    base = base + 0.1875f * f[rs][1][k];
-                    base = base + 0.0625f * f[rs][qs][k];
+                    float base;
+                    if (m4 == 0u) {
+                        base = 0.5625f * f[1][1][k];
+                        base = base + 0.1875f * f[1][qs][k];
+                        base = base + 0.1875f * f[rs][1][k];
+                        base = base + 0.0625f * f[rs][qs][k];
+                    } else {
+                        base = 0.0f;
+                        if (m4 & 1u) base = base + 0.5625f * f[1][1][k];
+                        if (m4 & 2u) base = base + 0.1875f * f[1][qs][k];
+                        if (m4 & 4u) base = base + 0.1875f * f[rs][1][k];
+                        if (m4 & 8u) base = base + 0.0625f * f[rs][qs][k];
+                        base = base * inv_ws;
+                    }
                     const float v = base + net[(2 * i + j) * 3 + k];
                     const float qv = fminf(fmaxf(v, 0.0f), 1.0f);
                     ov |= (uint32_t)floorf(qv * 255.0f + 0.5f) << (8 * k);
@@ -1020,6 +1051,7 @@ bool forward(rz_upsampler* u, const rz_gbuffer* g, const void* target, void* out
     f.wimg = u->d_img + fwd_img_off(3);
     f.bias = u->d_params + layer_boff(3);
     f.color_lr = static_cast<const uint32_t*>(g->color_rgba8);
+    f.sources = static_cast<const uint16_t*>(g->sources_u16);
     f.out_rgba8 = static_cast<uint32_t*>(out);
     f.target = static_cast<const uint32_t*>(target);
     f.dy = u->d_dy3;

@@ -150,16 +150,19 @@ class Graphics:
 
     def download_gbuffer(self, view: int = 0) -> dict:
         """Host copies of one view's G-buffer: colour and albedo (H, W, 4) u8, depth (H, W) f32,
-        normal (H, W, 2) f16."""
+        normal (H, W, 2) f16, and (single-sampled frames) the sub-pixel sources (H, W) u16."""
         self.sync()
         g = self.gbuffer(view)
         H, W = g.height, g.width
-        return {
+        out = {
             "color": device_array(g.color_rgba8, (H, W, 4), np.uint8),
             "depth": device_array(g.depth_f32, (H, W), np.float32),
             "albedo": device_array(g.albedo_rgba8, (H, W, 4), np.uint8),
             "normal": device_array(g.normal_oct_f16x2, (H, W, 2), np.float16),
         }
+        if g.sources_u16:
+            out["sources"] = device_array(g.sources_u16, (H, W), np.uint16)
+        return out
 
     def update_objects(self, offset: int, objects: np.ndarray) -> None:
         """The go_update upload (mob transforms) of src/Engine/Graphics.cpp:5120-5138."""
@@ -268,6 +271,9 @@ def device_array(ptr: int, shape, dtype) -> np.ndarray:
     if dt == np.uint64:  # torch has no uint64 copy path on every version: move raw int64
         view = torch.as_tensor(_DeviceView(ptr, shape, "<i8"), device="cuda")
         return view.cpu().numpy().view(np.uint64)
+    if dt == np.uint16:  # nor a uint16 one: move raw int16
+        view = torch.as_tensor(_DeviceView(ptr, shape, "<i2"), device="cuda")
+        return view.cpu().numpy().view(np.uint16)
     view = torch.as_tensor(_DeviceView(ptr, shape, dt.str), device="cuda")
     return view.cpu().numpy()
 

@@ -128,43 +128,58 @@ def _psnr_dev(a, b) -> tuple[float, int]:
 
 def evaluate(params: np.ndarray, cameras: int = TEST_CAMERAS, scene_seed: int = 0, width: int = 960,
              height: int = 540, samples: int = 1) -> dict:
-    """Per held-out frame: PSNR and max error of the learned reconstruction and of plain
-    bilinear upsampling, both against the plain full-resolution render."""
+    """Per held-out frame, against the plain full-resolution render: PSNR and max
+    error of the learned reconstruction, of the x2 base alone (the network's
+    parameters zero: the triangle-aware base where the G-buffer has sub-pixel
+    sources) and of plain bilinear upsampling (the base without sources)."""
     import torch
+
+    from .graphics import _DeviceView
 
     s = sc.random_triangles(seed=scene_seed, width=2 * width, height=2 * height)
     pr = PairRenderer(s, width, height, samples=samples)
     net = Upsampler(0, width, height)
     net.set_params(params)
-    bil = Upsampler(0, width, height)
-    bil.set_params(np.zeros(PARAM_COUNT, np.float32))
+    zero = Upsampler(0, width, height)
+    zero.set_params(np.zeros(PARAM_COUNT, np.float32))
     out_n = torch.zeros((2 * height, 2 * width), dtype=torch.int32, device="cuda")
+    out_z = torch.zeros_like(out_n)
     out_b = torch.zeros_like(out_n)
     dirs = sc.camera_dirs(cameras, TEST_CAMERA_SEED)
     stream = pr.low.stream
     frames = []
+
+    def img(t):
+        return t.view(torch.uint8).view(2 * height, 2 * width, 4)
+
     for d in dirs:
         pr.render_high(d)
         pr.render_low(d)
-        net.infer(pr.low.gbuffer(), out_n.data_ptr(), stream)
-        bil.infer(pr.low.gbuffer(), out_b.data_ptr(), stream)
+        gb = pr.low.gbuffer()
+        net.infer(gb, out_n.data_ptr(), stream)
+        zero.infer(gb, out_z.data_ptr(), stream)
+        gb.sources_u16 = None
+        zero.infer(gb, out_b.data_ptr(), stream)
         _stream_sync(stream)
         f = pr.high.frame()
-        from .graphics import _DeviceView
-
         ref = torch.as_tensor(_DeviceView(f.color_rgba8, (2 * height, 2 * width, 4), "|u1"), device="cuda")
-        pn, mn = _psnr_dev(out_n.view(torch.uint8).view(2 * height, 2 * width, 4), ref)
-        pb, mb = _psnr_dev(out_b.view(torch.uint8).view(2 * height, 2 * width, 4), ref)
-        frames.append({"psnr_db": pn, "max_abs_error": mn, "bilinear_psnr_db": pb, "bilinear_max_abs_error": mb})
+        pn, mn = _psnr_dev(img(out_n), ref)
+        pz, mz = _psnr_dev(img(out_z), ref)
+        pb, mb = _psnr_dev(img(out_b), ref)
+        frames.append({"psnr_db": pn, "max_abs_error": mn, "base_psnr_db": pz, "base_max_abs_error": mz,
+                       "bilinear_psnr_db": pb, "bilinear_max_abs_error": mb})
     net.close()
-    bil.close()
+    zero.close()
     pr.close()
     pn = [f["psnr_db"] for f in frames]
+    pz = [f["base_psnr_db"] for f in frames]
     pb = [f["bilinear_psnr_db"] for f in frames]
     return {
         "frames": len(frames), "psnr_db_mean": float(np.mean(pn)), "psnr_db_min": float(np.min(pn)),
         "psnr_db_median": float(np.median(pn)), "max_abs_error": int(max(f["max_abs_error"] for f in frames)),
         "frames_at_or_above_floor": int(sum(p >= PSNR_FLOOR_DB for p in pn)),
+        "base_psnr_db_mean": float(np.mean(pz)), "base_psnr_db_min": float(np.min(pz)),
+        "base_frames_at_or_above_floor": int(sum(p >= PSNR_FLOOR_DB for p in pz)),
         "bilinear_psnr_db_mean": float(np.mean(pb)), "bilinear_psnr_db_min": float(np.min(pb)),
         "bilinear_max_abs_error": int(max(f["bilinear_max_abs_error"] for f in frames)),
         "per_frame": frames,
@@ -285,6 +300,7 @@ def main():
         p, hist = train(args.steps, args.batch, args.lr, args.seed, samples=args.samples)
         ev = evaluate(p, args.cameras, samples=args.samples)
         meta = {"steps": args.steps, "batch": args.batch, "lr": args.lr, "seed": args.seed, "samples": args.samples,
+                "inputs": "colour, albedo, normal, coverage, depth" + (", sub-pixel sources" if args.samples == 1 else ""),
                 "train_cameras": TRAIN_CAMERAS, "train_camera_seed": TRAIN_CAMERA_SEED,
                 "test_cameras": args.cameras, "test_camera_seed": TEST_CAMERA_SEED,
                 "final_train_mse": float(np.mean(hist[-50:])), "train_seconds": time.perf_counter() - t0,

@@ -17,7 +17,7 @@ from . import _abi, _lib
 
 LAYERS = [(16, 32), (32, 32), (32, 32), (32, 16)]
 OUT_CHANNELS = 12
-REAL_IN_CHANNELS = 10
+REAL_IN_CHANNELS = 14  # colour 3, albedo 3, normal 2, coverage, depth, matched source weight of 4 points
 
 
 def _offsets():
@@ -32,7 +32,7 @@ OFFSETS, PARAM_COUNT = _offsets()
 
 
 def init_params(seed: int = 0, last_scale: float = 0.1) -> np.ndarray:
-    """He-normal weights on the real channels (padded input channels 10..15 of
+    """He-normal weights on the real channels (padded input channels 14..15 of
     layer 0 and output channels 12..15 of layer 3 stay zero), zero biases; the
     last layer is scaled by `last_scale` so the untrained network is close to
     plain bilinear upsampling."""
@@ -51,7 +51,7 @@ def init_params(seed: int = 0, last_scale: float = 0.1) -> np.ndarray:
 
 def conv_flops(width: int, height: int, real_channels: bool = True) -> int:
     """Multiply-add FLOPs (2 per MAC) of one inference at W x H: with real channels
-    (10 in, 12 out) or with the padded channels the tensor cores execute."""
+    (14 in, 12 out) or with the padded channels the tensor cores execute."""
     chans = [(REAL_IN_CHANNELS, 32), (32, 32), (32, 32), (32, OUT_CHANNELS)] if real_channels else LAYERS
     return sum(2 * 9 * ci * co for ci, co in chans) * width * height
 

@@ -25,7 +25,7 @@ def test_header_declares_the_bound_symbols():
 def test_library_exports_every_declared_symbol(renderer_lib):
     for name in declared_functions():
         assert hasattr(renderer_lib, name), name
-    assert renderer_lib.rz_abi_version() == 1
+    assert renderer_lib.rz_abi_version() == 2
 
 
 def test_record_layouts():

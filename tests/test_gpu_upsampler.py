@@ -98,6 +98,92 @@ def test_gbuffer_albedo_and_normal(gpu):
     g.deinit()
 
 
+def _orbit(s, cam, w, h):
+    out = sc.Scene(**{k: getattr(s, k) for k in s.__dataclass_fields__})
+    out.width, out.height = w, h
+    out.scene = sc.orbit_view(s, sc.camera_dirs(8, 2002)[cam], w, h)
+    out.cameras = [out.scene]
+    return out
+
+
+def _inside():  # the camera inside the cube: triangles cut by the near plane
+    s = sc.random_triangles(seed=3, triangles=2000, width=320, height=200, shadow_size=256, texture_size=32)
+    view = sc.camera_look_at_origin((0.2, 0.1, 0.3))
+    proj = sc.projection(320 / 200, np.radians(90.0))
+    s.scene = sc.scene_record(view, proj, s.scene["sun_position"][0], np.eye(4), (0.2, 0.1, 0.3), 320, 200)
+    s.scene["shadow_projection_near"] = s.cameras[0]["shadow_projection_near"]
+    s.cameras = [s.scene]
+    return s
+
+
+SUBPIXEL = {
+    "random_triangles_960x540": lambda: _orbit(sc.random_triangles(seed=0, width=1920, height=1080), 3, 960, 540),
+    "scene_scale_small": lambda: sc.scene_scale(seed=6, meshes=8, triangles_per_mesh=512, materials=3,
+                                                texture_size=32, width=320, height=180, shadow_size=256, frames=1),
+    "camera_inside_clipping": _inside,
+}
+
+
+@pytest.mark.parametrize("name", list(SUBPIXEL))
+def test_subpixel_sources_match_oracle(gpu, oracle, name):
+    """The G-buffer's sub-pixel sources (k_subpixel_sources) equal the oracle's
+    restatement bit for bit, from the same visibility."""
+    s = SUBPIXEL[name]()
+    g = _render(s)
+    try:
+        fr = g.download()
+        gb = g.download_gbuffer()
+        ref_ids = oracle.raster(s)["ids"]
+        assert np.array_equal(fr["ids"], ref_ids)
+        want = oracle.subpixel_sources(s, ref_ids)
+        assert (want != 0xFFFF).mean() > 0.01
+        assert np.array_equal(gb["sources"], want), f"{np.count_nonzero(gb['sources'] != want)} masks differ"
+    finally:
+        g.deinit()
+
+
+def test_subpixel_sources_in_batched_views_and_not_with_msaa(gpu, oracle):
+    """Per view of a batch (triangle ids are global; each view's plane resolves
+    them through the whole draw list) the sources equal the oracle's for that view
+    alone; multisampled frames have no sources plane (plain bilinear base)."""
+    scenes, views = sc.batch_views(seed=8, views=4, scenes=2, min_tris=800, max_tris=5000, min_size=60,
+                                   max_size=240, min_shadow=128, max_shadow=256, texture_size=32)
+    g = Graphics()
+    g.init(64, 64, 64)
+    try:
+        idx = [g.add_scene(x) for x in scenes]
+        g.set_views([(idx[k], v.width, v.height, v.shadow_size, v.draw_config) for k, v in views])
+        g.set_gbuffer(True)
+        for i, (_, v) in enumerate(views):
+            g.update_view(i, v.scene)
+        g.render()
+        if g.sync_code() == 14:
+            g.render()
+        g.sync()
+        for i, (_, v) in enumerate(views):
+            local = g.download_view(i)["ids"]  # triangle ids of the view alone
+            want = oracle.subpixel_sources(v, local)
+            assert (want != 0xFFFF).any()
+            assert np.array_equal(g.download_gbuffer(i)["sources"], want)
+    finally:
+        g.deinit()
+    s = sc.tiny(2)
+    s.samples = 4
+    g = Graphics()
+    g.init(s.width, s.height, s.shadow_size, samples=4)
+    try:
+        g.set_asset(s)
+        g.set_graphic_objects(s.objects, s.surfaces)
+        g.set_draw_config(s.draw_config)
+        g.set_gbuffer(True)
+        g.update(s.scene)
+        g.render()
+        g.sync()
+        assert "sources" not in g.download_gbuffer()
+    finally:
+        g.deinit()
+
+
 @pytest.mark.parametrize("w,h", [(96, 64), (200, 70), (960, 540)])
 def test_upsampler_forward_matches_oracle(gpu, w, h):
     import torch
@@ -122,10 +208,12 @@ def test_upsampler_forward_matches_oracle(gpu, w, h):
     hi.deinit()
 
 
-def test_zero_network_is_exactly_the_bilinear_base(gpu):
+def test_zero_network_is_exactly_the_x2_base(gpu):
     """With every parameter zero the network adds nothing, so the output is the
-    bilinear x2 base alone, and it equals the oracle's bit for bit: byte / 255,
-    the 9/16, 3/16, 3/16, 1/16 sum in order, clamping and rounding to 8 bits."""
+    x2 base alone, and it equals the oracle's bit for bit: byte / 255, the
+    9/16, 3/16, 3/16, 1/16 sum in order over the sub-pixel sources that show
+    each point's triangle, renormalised, clamping and rounding to 8 bits; and
+    plain bilinear when the G-buffer has no sources."""
     import torch
 
     w, h = 200, 70
@@ -136,6 +224,14 @@ def test_zero_network_is_exactly_the_bilinear_base(gpu):
     out = torch.zeros((2 * h, 2 * w), dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     u.infer(lo.gbuffer(), out.data_ptr())
+    assert u.status() == 0
+    got = out.cpu().numpy().view(np.uint8).reshape(2 * h, 2 * w, 4)
+    assert "sources" in gbh and (gbh["sources"] != 0xFFFF).any()
+    assert np.array_equal(got, U.to_rgba8(U.x2_base(gbh["color"], gbh["sources"])))
+    assert not np.array_equal(got, U.to_rgba8(U.bilinear_base(gbh["color"])))
+    g = lo.gbuffer()
+    g.sources_u16 = None
+    u.infer(g, out.data_ptr())
     assert u.status() == 0
     got = out.cpu().numpy().view(np.uint8).reshape(2 * h, 2 * w, 4)
     assert np.array_equal(got, U.to_rgba8(U.bilinear_base(gbh["color"])))

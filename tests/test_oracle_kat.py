@@ -291,3 +291,39 @@ def test_msaa_interior_pixels_match_single_sample(oracle):
     assert set(np.unique(r4["ids"])) <= set(np.unique(r1["ids"])) | set(range(1, s1.triangle_count + 1))
     # depth and ids agree per sample (0 depth exactly where no triangle)
     assert np.array_equal(r4["depth"] == 0, r4["ids"] == 0)
+
+
+def test_subpixel_sources_at_a_vertical_edge(oracle):
+    """Two triangles meet at x = 4.4 on an 8x8 target. Pixel 3 (centre 3.5) and
+    pixel 4 (centre 4.5) straddle the edge: at pixel 4 the points x = 4.25 lie on
+    the left triangle, whose bilinear sources there are the left neighbour and the
+    left diagonal (bits 1, 3: 0xA); its points x = 4.75 keep every source. At
+    pixel 3 the points x = 3.75 keep only own and vertical (bits 0, 2: 0x5).
+    Pixels whose neighbourhood shows one triangle keep every source."""
+    left = ((-20.0, -20.0, 0.5), (4.4, -20.0, 0.5), (4.4, 40.0, 0.5))
+    right = ((4.4, -20.0, 0.5), (30.0, -20.0, 0.5), (4.4, 40.0, 0.5))
+    s = flat_scene([left, right])
+    ids = oracle.raster(s)["ids"]
+    assert (ids[:, :4] == 1).all() and (ids[:, 4:] == 2).all()
+    m = oracle.subpixel_sources(s, ids)
+    want = np.full((8, 8), 0xFFFF, np.uint16)
+    want[:, 3] = 0x5F5F
+    want[:, 4] = 0xFAFA
+    assert np.array_equal(m, want), [hex(v) for v in m[0]]
+
+
+def test_subpixel_sources_nearer_triangle_wins(oracle):
+    """A small triangle in front (larger depth, reverse-Z) over a background
+    triangle, with w = 1 everywhere (so depth, not 1/w, must order them): the
+    point (2.25, 2.25) of pixel (2, 2) lies outside the front triangle (which
+    starts at 2.3) and takes the back one, shown by the horizontal, vertical and
+    diagonal sources (0b1110); the point (2.75, 2.75) lies inside it, and all four
+    of its sources show it."""
+    back = ((-20.0, -20.0, 0.2), (40.0, -20.0, 0.2), (-20.0, 40.0, 0.2))
+    front = ((2.3, 2.3, 0.8), (6.1, 2.3, 0.8), (2.3, 6.1, 0.8))
+    s = flat_scene([back, front])
+    ids = oracle.raster(s)["ids"]
+    m = oracle.subpixel_sources(s, ids)
+    assert ids[2, 2] == 2 and ids[1, 1] == 1
+    assert m[2, 2] & 0xF == 0b1110
+    assert (m[2, 2] >> 12) & 0xF == 0xF

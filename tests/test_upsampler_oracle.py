@@ -12,17 +12,21 @@ from rosy_gb300 import upsampler as up
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _gbuffer(rng, H, W):
+def _gbuffer(rng, H, W, sources=False):
     n = rng.normal(size=(H, W, 3))
     n /= np.linalg.norm(n, axis=-1, keepdims=True)
     s = np.abs(n).sum(-1, keepdims=True)
     oct_ = (n[..., :2] / s).astype(np.float16)
-    return {
+    gb = {
         "color": rng.integers(0, 256, (H, W, 4), dtype=np.uint8),
         "albedo": rng.integers(0, 256, (H, W, 4), dtype=np.uint8),
         "normal": oct_,
         "depth": rng.uniform(0.0, 0.3, (H, W)).astype(np.float32),
     }
+    if sources:  # every mask value, 0xFFFF and 0 included
+        gb["sources"] = rng.integers(0, 65536, (H, W), dtype=np.uint16)
+        gb["sources"][0, 0], gb["sources"][0, 1] = 0xFFFF, 0
+    return gb
 
 
 def test_bf16_rounding_known_values():
@@ -43,9 +47,35 @@ def test_parameter_layout_matches_header():
     q = U.init_params(3)
     assert np.array_equal(p, q)
     w0 = p[U.OFFSETS[0][0]:U.OFFSETS[0][1]].reshape(32, 9, 16)
-    assert np.all(w0[:, :, 10:] == 0)
+    assert np.all(w0[:, :, 14:] == 0) and np.all(w0[:, :, :14] != 0)
     w3 = p[U.OFFSETS[3][0]:U.OFFSETS[3][1]].reshape(16, 9, 32)
     assert np.all(w3[12:] == 0)
+
+
+def test_x2_base_with_sub_pixel_sources():
+    """Masks that keep every source (or none) give the bilinear base bit for bit;
+    one kept source gives its colour; two give their renormalised mean."""
+    rng = np.random.default_rng(4)
+    c = rng.integers(0, 256, (5, 7, 4), dtype=np.uint8)
+    bil = U.bilinear_base(c)
+    assert np.array_equal(U.x2_base(c, np.full((5, 7), 0xFFFF, np.uint16)), bil)
+    assert np.array_equal(U.x2_base(c, np.zeros((5, 7), np.uint16)), bil)
+    assert np.array_equal(U.x2_base(c, None), bil)
+    cf = c[..., :3].astype(np.float32) / np.float32(255.0)
+    y, x = 2, 3
+    m = np.full((5, 7), 0xFFFF, np.uint16)
+    # point k = 1 (upper row, right half): sources own, right, up, up-right
+    m[y, x] = (0xFFFF & ~(0xF << 4)) | (0b1000 << 4)  # only the up-right diagonal (weight 1/16, exact reciprocal)
+    b = U.x2_base(c, m)
+    assert np.array_equal(b[2 * y, 2 * x + 1], cf[y - 1, x + 1])
+    m[y, x] = (0xFFFF & ~(0xF << 4)) | (0b0101 << 4)  # own and the one above
+    b = U.x2_base(c, m, np.float64)
+    want = (0.5625 * cf[y, x].astype(np.float64) + 0.1875 * cf[y - 1, x]) / 0.75
+    assert np.allclose(b[2 * y, 2 * x + 1], want)
+    # the feature channels carry the kept weight of each point
+    gb = _gbuffer(rng, 5, 7, sources=True)
+    f = U.features(gb, exact=True)
+    assert f[0, 0, 10:14].tolist() == [1.0, 1.0, 1.0, 1.0] and f[0, 1, 10:14].tolist() == [0.0, 0.0, 0.0, 0.0]
 
 
 def test_shuffle_and_bilinear_conventions():
@@ -69,7 +99,7 @@ def test_shuffle_and_bilinear_conventions():
 def test_gradients_match_finite_differences():
     rng = np.random.default_rng(7)
     H, W = 5, 6
-    gb = _gbuffer(rng, H, W)
+    gb = _gbuffer(rng, H, W, sources=True)
     target = rng.integers(0, 256, (2 * H, 2 * W, 4), dtype=np.uint8)
     p = U.init_params(11, last_scale=1.0).astype(np.float64)
     for (wo, bo), (cin, cout) in zip(U.OFFSETS, U.LAYERS):
@@ -88,7 +118,7 @@ def test_gradients_match_finite_differences():
         assert abs(fd - g[i]) <= 1e-4 * max(1.0, abs(fd)), (i, fd, g[i])
     # padded channels have zero gradient
     w0 = g[U.OFFSETS[0][0]:U.OFFSETS[0][1]].reshape(32, 9, 16)
-    assert np.all(w0[:, :, 10:] == 0)
+    assert np.all(w0[:, :, 14:] == 0)
     w3 = g[U.OFFSETS[3][0]:U.OFFSETS[3][1]].reshape(16, 9, 32)
     assert np.all(w3[12:] == 0)
 
