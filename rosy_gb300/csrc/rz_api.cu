@@ -95,6 +95,7 @@ struct rz_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;  // shadow pass branch of the frame graph
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t camera_done = nullptr, sources_done = nullptr;  // the side branch of the G-buffer's sub-pixel sources
     uint32_t queue_chunks = 0;    // fixed work-queue depth (0 = sized from the scene)
     uint32_t chunk_stamps = kChunkStamps;
     uint32_t small_extent = kSmallExtent;
@@ -955,11 +956,15 @@ void enqueue_sequential(rz_ctx* c, cudaStream_t s, const ShadeParams& sh) {
 // Enqueues one frame (everything after the scene/object uploads). With stage
 // timing the stages run one after the other on the main stream between
 // events; otherwise the shadow passes run on a side stream concurrently with
-// the camera passes, joining before the shading (which reads the shadow maps).
+// the camera passes, joining before the shading (which reads the shadow maps),
+// and the G-buffer's sub-pixel sources (which read only the visibility) follow
+// the shadow passes on the side stream, concurrently with the shading.
 int enqueue_frame(rz_ctx* c) {
     cudaStream_t s = c->stream;
     take_launches();  // start this frame's count
     const ShadeParams sh = shade_params(c);
+    const bool sources = c->gbuffer && c->samples == 1;  // the learned path's x2 base
+    bool sources_side = false;
     if (!c->batched && !c->blended_tris && !c->timing && !c->debug_count) {
         // per-view launches clear the pass headers view by view; the error words once per frame
         RZ_CUDA(c, cudaMemsetAsync(c->d_report, 0, sizeof(FrameReport), s), "clear frame report");
@@ -978,10 +983,17 @@ int enqueue_frame(rz_ctx* c) {
         enqueue_shadow(c, c->side, false);
         enqueue_camera(c, s, false, sh);
         RZ_CUDA(c, cudaEventRecord(c->join, c->side), "join");
+        if (sources) {
+            RZ_CUDA(c, cudaEventRecord(c->camera_done, s), "camera done");
+            RZ_CUDA(c, cudaStreamWaitEvent(c->side, c->camera_done, 0), "camera done");
+            launch_subpixel_sources(sh, c->side);
+            RZ_CUDA(c, cudaEventRecord(c->sources_done, c->side), "sources done");
+            sources_side = true;
+        }
         RZ_CUDA(c, cudaStreamWaitEvent(s, c->join, 0), "join");
     }
     if (c->batched || c->blended_tris || c->timing || c->debug_count) launch_shade(sh, s);
-    if (c->gbuffer && c->samples == 1) launch_subpixel_sources(sh, s);  // the learned path's x2 base
+    if (sources && !sources_side) launch_subpixel_sources(sh, s);
     if (c->blended_tris || c->debug_count) {
         if (c->debug_count)
             launch_debug_prep(c->d_debug_pairs, c->debug_count, c->d_debug_objects, c->d_views, (uint32_t)c->views.size(),
@@ -1000,6 +1012,7 @@ int enqueue_frame(rz_ctx* c) {
         launch_blend(bp, s);
     }
     if (c->timing) stamp(c, 7);
+    if (sources_side) RZ_CUDA(c, cudaStreamWaitEvent(s, c->sources_done, 0), "sources done");
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
     RZ_CUDA(c, cudaMemcpyAsync(c->h_report, c->d_report, sizeof(FrameReport), cudaMemcpyDeviceToHost, s),
             "read frame report");
@@ -1138,7 +1151,9 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->camera_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sources_done, cudaEventDisableTiming) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
@@ -1227,6 +1242,8 @@ void rz_destroy(rz_ctx* c) {
     if (c->objects_copied) cudaEventDestroy(c->objects_copied);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
+    if (c->camera_done) cudaEventDestroy(c->camera_done);
+    if (c->sources_done) cudaEventDestroy(c->sources_done);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
