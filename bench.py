@@ -68,6 +68,7 @@ def learned_block(frames: int = 64, cameras: int = 256, samples: int = 1) -> dic
     ev = learned.evaluate(params, cameras, samples=samples)
     peak, src = bf16_peak()
     per = ev.pop("per_frame")
+    up_in = 14 if samples == 1 else 10  # real input channels: the sub-pixel sources exist single-sampled
     return {
         "workload": "random_triangles (4,096 triangles, 256^2 texture, 1024^2 shadow map): plain 1920x1080 vs "
                     "960x540 render + upsampler to 1920x1080; L2 flushed between frames",
@@ -76,16 +77,18 @@ def learned_block(frames: int = 64, cameras: int = 256, samples: int = 1) -> dic
         "speedup": round(t["speedup"], 3), "plain_ms": round(t["plain_ms"], 5), "learned_ms": round(t["learned_ms"], 5),
         "heldout": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in ev.items()},
         "psnr_floor_db": learned.PSNR_FLOOR_DB,
+        "frames_below_floor": ev["frames"] - ev["frames_at_or_above_floor"],
         "fallback_to_plain": ev["psnr_db_mean"] < learned.PSNR_FLOOR_DB,
         "per_frame_psnr_db": [round(f["psnr_db"], 2) for f in per],
         "per_frame_max_abs_error": [f["max_abs_error"] for f in per],
+        "per_frame_base_psnr_db": [round(f["base_psnr_db"], 2) for f in per],
         "upsampler_roofline": {"bound": "tensor", "achieved": round(t["upsampler_tflops"], 2), "peak": peak,
                                "unit": "TFLOP/s", "frac": round(t["upsampler_tflops"] / peak, 4),
                                "peak_source": src, "ms_per_frame": round(t["upsampler_ms"], 5),
                                "flops_per_frame": t["upsampler_flops"],
                                "flops_note": "2 x 9 x cin x cout x 960 x 540 over the real channels "
-                                             "(10-32-32-32-12)"},
-        "weights": {k: meta.get(k) for k in ("steps", "batch", "lr", "train_cameras", "train_seconds")},
+                                             f"({up_in}-32-32-32-12)"},
+        "weights": {k: meta.get(k) for k in ("steps", "batch", "lr", "train_cameras", "train_seconds", "inputs")},
     }
 
 

@@ -232,7 +232,7 @@ def time_paths(params: np.ndarray, frames: int = 64, warmup: int = 5, scene_seed
         raise RuntimeError("upsampler kernels reported an error")
     net.close()
     pr.close()
-    flops = conv_flops(width, height, real_channels=True)
+    flops = conv_flops(width, height, real_channels=True, real_in=14 if samples == 1 else 10)
     return {
         "plain_ms": plain, "plain_fps": 1e3 / plain, "learned_ms": learned, "learned_fps": 1e3 / learned,
         "speedup": plain / learned, "upsampler_ms": net_ms,

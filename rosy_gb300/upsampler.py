@@ -49,10 +49,11 @@ def init_params(seed: int = 0, last_scale: float = 0.1) -> np.ndarray:
     return p
 
 
-def conv_flops(width: int, height: int, real_channels: bool = True) -> int:
+def conv_flops(width: int, height: int, real_channels: bool = True, real_in: int = REAL_IN_CHANNELS) -> int:
     """Multiply-add FLOPs (2 per MAC) of one inference at W x H: with real channels
-    (14 in, 12 out) or with the padded channels the tensor cores execute."""
-    chans = [(REAL_IN_CHANNELS, 32), (32, 32), (32, 32), (32, OUT_CHANNELS)] if real_channels else LAYERS
+    (real_in in: 14 with sub-pixel sources, 10 without; 12 out) or with the padded
+    channels the tensor cores execute."""
+    chans = [(real_in, 32), (32, 32), (32, 32), (32, OUT_CHANNELS)] if real_channels else LAYERS
     return sum(2 * 9 * ci * co for ci, co in chans) * width * height
 
 
