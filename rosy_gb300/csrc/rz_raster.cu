@@ -23,6 +23,7 @@
 //    key is exactly what a sequential GREATER_OR_EQUAL test leaves: the largest
 //    depth, and among equal depths the last triangle submitted. The shadow map
 //    is a 32-bit atomicMax on the depth bits.
+#include <algorithm>
 #include <cstdio>
 
 #include "rz_device.cuh"
@@ -608,8 +609,17 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
 int setup_ctas(uint32_t tri_total) { return (int)((tri_total + kSetupThreads - 1) / kSetupThreads); }
 
 void launch_setup(const PassParams& p, cudaStream_t stream) {
-    const int ctas = setup_ctas(p.tri_total);
+    int ctas = setup_ctas(p.tri_total);
     if (ctas == 0) return;
+    if (!p.ordered && p.clear_count) {
+        // the depth target zeroed by this launch wants more CTAs than few triangles give
+        // (about 32 KB each); the extra CTAs draw tickets past the last triangle and set
+        // up nothing (the ordered list's look-back has one status word per triangle tile)
+        size_t most = 0;
+        for (uint32_t b = 0; b < p.clear_count; ++b) most = p.clear_bytes[b] > most ? p.clear_bytes[b] : most;
+        const size_t want = std::min<size_t>(most / 32768, 4096);
+        if ((size_t)ctas < want) ctas = (int)want;
+    }
     k_setup<<<ctas, kSetupThreads, 0, stream>>>(p);
     note_launch();
 }

@@ -1035,6 +1035,33 @@ __device__ __forceinline__ SubTri sub_triangle(const ShadeParams& P, uint32_t id
     return g;
 }
 
+// Shared-memory table of a tile's distinct triangles (open addressing, 128
+// slots): each triangle's geometry is computed once per tile, not once per
+// pixel that considers it. Key 0 marks an empty slot (ids are >= 1).
+constexpr int kSubSlots = 128;
+
+__device__ __forceinline__ uint32_t sub_slot(uint32_t id) { return (id * 2654435761u) >> 25; }
+
+__device__ __forceinline__ void sub_insert(uint32_t* keys, uint32_t id) {
+    uint32_t h = sub_slot(id);
+    for (int i = 0; i < kSubSlots; ++i) {
+        const uint32_t prev = atomicCAS(&keys[h], 0u, id);
+        if (prev == 0u || prev == id) return;
+        h = (h + 1) & (kSubSlots - 1);
+    }  // table full: pixels that need this triangle compute its geometry themselves
+}
+
+__device__ __forceinline__ int sub_find(const uint32_t* keys, uint32_t id) {
+    uint32_t h = sub_slot(id);
+    for (int i = 0; i < kSubSlots; ++i) {
+        const uint32_t k = keys[h];
+        if (k == id) return (int)h;
+        if (k == 0u) return -1;
+        h = (h + 1) & (kSubSlots - 1);
+    }
+    return -1;
+}
+
 // For the x2 reconstruction of the learned path: which triangle is in front at
 // each of the four points (x + 0.25 / 0.75, y + 0.25 / 0.75) that the pixel's
 // four full-resolution pixels sample, among the triangles visible at the 3x3
@@ -1049,21 +1076,26 @@ __device__ __forceinline__ SubTri sub_triangle(const ShadeParams& P, uint32_t id
 __global__ void __launch_bounds__(256) k_subpixel_sources(ShadeParams P) {
     __shared__ uint32_t s_view;
     __shared__ uint32_t s_ids[18][18];  // the tile's triangle ids with a one-pixel border (clamped)
-    if (threadIdx.x == 0 && threadIdx.y == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
+    __shared__ uint32_t s_keys[kSubSlots];
+    __shared__ SubTri s_geo[kSubSlots];
+    const int tid = threadIdx.y * 16 + threadIdx.x;
+    if (tid == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
+    if (tid < kSubSlots) s_keys[tid] = 0u;
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
-    if (!VR.gb_sources) return;
+    if (!VR.gb_sources) return;  // uniform over the block
     const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
     const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
     const int x0 = (int)(lt % tiles_x) * 16, y0 = (int)(lt / tiles_x) * 16;
     const int W = VR.width, H = VR.height;
-    for (int i = threadIdx.y * 16 + threadIdx.x; i < 18 * 18; i += 256) {
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    for (int i = tid; i < 18 * 18; i += 256) {
         const int yy = min(max(y0 + i / 18 - 1, 0), H - 1), xx = min(max(x0 + i % 18 - 1, 0), W - 1);
         s_ids[i / 18][i % 18] = (uint32_t)VR.vis[(size_t)yy * W + xx];
     }
     __syncthreads();
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-    if (x >= W || y >= H) return;
+    const bool live = x < W && y < H;
     uint32_t nb[9];
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy)
@@ -1073,9 +1105,16 @@ __global__ void __launch_bounds__(256) k_subpixel_sources(ShadeParams P) {
     bool same = true;
 #pragma unroll
     for (int i = 0; i < 9; ++i) same = same && nb[i] == own;
+    // the distinct triangles the tile's pixels consider, and their geometry once each
+    if (live && !same)
+        for (int i = 0; i < 9; ++i)
+            if (nb[i] != 0u) sub_insert(s_keys, nb[i]);
+    __syncthreads();
+    if (tid < kSubSlots && s_keys[tid] != 0u) s_geo[tid] = sub_triangle(P, s_keys[tid], hw, hh);
+    __syncthreads();
+    if (!live) return;
     uint32_t mask = 0xFFFFu;
     if (!same) {
-        const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
         uint32_t best[4] = {0u, 0u, 0u, 0u};
         float best_z[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
         for (int ci = 0; ci < 9; ++ci) {
@@ -1083,7 +1122,8 @@ __global__ void __launch_bounds__(256) k_subpixel_sources(ShadeParams P) {
             bool seen = id == 0u;
             for (int j = 0; j < ci; ++j) seen = seen || nb[j] == id;
             if (seen) continue;  // candidates: distinct triangles in neighbourhood order
-            const SubTri g = sub_triangle(P, id, hw, hh);
+            const int slot = sub_find(s_keys, id);
+            const SubTri g = slot >= 0 ? s_geo[slot] : sub_triangle(P, id, hw, hh);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const float sx = (float)x + ((k & 1) ? 0.75f : 0.25f), sy = (float)y + ((k >> 1) ? 0.75f : 0.25f);
