@@ -6,7 +6,12 @@ from seeded cameras on the radius-3 orbit of the random-triangles scene
 (4,096 training directions), and judged against the plain full-resolution
 render on 256 held-out directions. The plain render stays the reference and
 the fallback: `LearnedPath.render` returns the plain full-resolution frame
-whenever the network's held-out PSNR is below the quality floor.
+unless every held-out frame of the network reaches the quality floor.
+
+In single-sample mode the network adds a residual to a triangle-aware x2 base:
+the renderer marks, per half-resolution pixel, which bilinear sources show the
+triangle in front at each full-resolution pixel centre (the G-buffer's sub-pixel
+sources), and the base renormalises the bilinear weights over those.
 
     python -m rosy_gb300.learned train --steps 3000 --out weights.npz
     python -m rosy_gb300.learned eval --weights weights.npz
@@ -249,16 +254,19 @@ def load_weights(path: str = WEIGHTS) -> tuple[np.ndarray, dict]:
 
 class LearnedPath:
     """Renders 2W x 2H frames through the learned path, or through the plain path
-    when the network's held-out PSNR is below the floor (the fallback)."""
+    (the fallback) unless the plain render, judging each held-out frame, found
+    every one of them at or above the floor: `heldout_psnr_db` is the list of
+    per-frame PSNRs from `evaluate` (a single number is taken as the minimum)."""
 
-    def __init__(self, s: sc.Scene, width: int, height: int, params: np.ndarray, heldout_psnr_db: float,
+    def __init__(self, s: sc.Scene, width: int, height: int, params: np.ndarray, heldout_psnr_db,
                  samples: int = 1):
         import torch
 
         self.pr = PairRenderer(s, width, height, samples=samples)
         self.net = Upsampler(0, width, height)
         self.net.set_params(params)
-        self.use_network = heldout_psnr_db >= PSNR_FLOOR_DB
+        worst = float(np.min(np.asarray(heldout_psnr_db, np.float64)))
+        self.use_network = worst >= PSNR_FLOOR_DB
         self.out = torch.zeros((2 * height, 2 * width), dtype=torch.int32, device="cuda")
 
     def render(self, cam_dir) -> int:
