@@ -134,9 +134,10 @@ def conv3x3_weight_grad(x: np.ndarray, dy: np.ndarray) -> np.ndarray:
 
 def x2_base(color: np.ndarray, sources: np.ndarray | None = None, ft=np.float32) -> np.ndarray:
     """(2H, 2W, 3) x2 base of RGBA8 colour / 255: bilinear, or with sub-pixel sources
-    the same weighted sum over the sources that show each point's triangle, times the
-    reciprocal of the sum of their weights (summed in the kernels' order; bilinear
-    where none does)."""
+    the weighted sum of each point's four sources with the weights of its mask: the
+    bilinear weight times the reciprocal of the kept weights' sum for each kept
+    source, zero for the others (summed in the kernels' order; every source kept, or
+    none, is bilinear)."""
     bil = bilinear_base(color, ft)
     if sources is None:
         return bil
@@ -150,17 +151,26 @@ def x2_base(color: np.ndarray, sources: np.ndarray | None = None, ft=np.float32)
         for j in range(2):
             xn = np.clip(xs - 1, 0, W - 1) if j == 0 else np.clip(xs + 1, 0, W - 1)
             k = 2 * i + j
-            m = ((sources.astype(np.uint32) >> (4 * k)) & 15)[..., None]
+            m = ((sources.astype(np.uint32) >> (4 * k)) & 15)
+            wt = source_weights(ft)[m]  # (H, W, 4)
             srcs = (c, c[:, xn], c[yn, :], c[yn][:, xn])
-            b = np.zeros((H, W, 3), ft)
-            ws = np.zeros((H, W, 1), ft)
-            for s, (cs, w) in enumerate(zip(srcs, BILINEAR_WEIGHTS)):
-                on = ((m >> s) & 1).astype(bool)
-                b = np.where(on, b + ft(w) * cs, b)
-                ws = np.where(on, ws + ft(w), ws)
-            inv = ft(1.0) / np.where(m == 0, ft(1.0), ws)
-            out[i::2, j::2] = np.where(m == 0, bil[i::2, j::2], b * inv)
+            b = wt[..., 0:1] * srcs[0]
+            for s in range(1, 4):
+                b = b + wt[..., s:s + 1] * srcs[s]
+            out[i::2, j::2] = b
     return out
+
+
+def source_weights(ft=np.float32) -> np.ndarray:
+    """(16, 4) weights of the x2 base per source mask: for a kept source its bilinear
+    weight times the reciprocal of the kept weights' sum, zero for the others;
+    mask 0 is plain bilinear."""
+    t = np.zeros((16, 4), ft)
+    for m in range(16):
+        inv = ft(1.0) / matched_weight(np.array([m], np.uint16), 0, ft)[0] if m else ft(0.0)
+        for s, w in enumerate(BILINEAR_WEIGHTS):
+            t[m, s] = ft(w) if m == 0 else (ft(w) * inv if (m >> s) & 1 else ft(0.0))
+    return t
 
 
 def bilinear_base(color: np.ndarray, ft=np.float32) -> np.ndarray:

@@ -1078,8 +1078,13 @@ __global__ void __launch_bounds__(256) k_subpixel_sources(ShadeParams P) {
     __shared__ uint32_t s_ids[18][18];  // the tile's triangle ids with a one-pixel border (clamped)
     __shared__ uint32_t s_keys[kSubSlots];
     __shared__ SubTri s_geo[kSubSlots];
+    __shared__ uint32_t s_edge_count;
+    __shared__ uint8_t s_edges[256];  // the tile's pixels whose neighbourhood shows more than one triangle
     const int tid = threadIdx.y * 16 + threadIdx.x;
-    if (tid == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
+    if (tid == 0) {
+        s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
+        s_edge_count = 0u;
+    }
     if (tid < kSubSlots) s_keys[tid] = 0u;
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
@@ -1094,27 +1099,42 @@ __global__ void __launch_bounds__(256) k_subpixel_sources(ShadeParams P) {
         s_ids[i / 18][i % 18] = (uint32_t)VR.vis[(size_t)yy * W + xx];
     }
     __syncthreads();
-    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-    const bool live = x < W && y < H;
+    {
+        const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+        bool same = true;
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx) same = same && s_ids[threadIdx.y + dy][threadIdx.x + dx] == s_ids[threadIdx.y + 1][threadIdx.x + 1];
+        if (x < W && y < H) {
+            if (same) {
+                VR.gb_sources[(size_t)y * W + x] = 0xFFFFu;
+            } else {  // the distinct triangles the edge pixels consider (geometry once each), and the pixel
+#pragma unroll
+                for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx)
+                        if (s_ids[threadIdx.y + dy][threadIdx.x + dx] != 0u) sub_insert(s_keys, s_ids[threadIdx.y + dy][threadIdx.x + dx]);
+                s_edges[atomicAdd(&s_edge_count, 1u)] = (uint8_t)tid;
+            }
+        }
+    }
+    __syncthreads();
+    if (tid < kSubSlots && s_keys[tid] != 0u) s_geo[tid] = sub_triangle(P, s_keys[tid], hw, hh);
+    __syncthreads();
+    // the edge pixels, packed onto the first lanes of the block
+    const uint32_t n_edges = s_edge_count;
+    if ((uint32_t)tid >= n_edges) return;
+    const int ex = s_edges[tid] & 15, ey = s_edges[tid] >> 4;
+    const int x = x0 + ex, y = y0 + ey;
     uint32_t nb[9];
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
-        for (int dx = 0; dx < 3; ++dx) nb[dy * 3 + dx] = s_ids[threadIdx.y + dy][threadIdx.x + dx];
+        for (int dx = 0; dx < 3; ++dx) nb[dy * 3 + dx] = s_ids[ey + dy][ex + dx];
     const uint32_t own = nb[4];
-    bool same = true;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) same = same && nb[i] == own;
-    // the distinct triangles the tile's pixels consider, and their geometry once each
-    if (live && !same)
-        for (int i = 0; i < 9; ++i)
-            if (nb[i] != 0u) sub_insert(s_keys, nb[i]);
-    __syncthreads();
-    if (tid < kSubSlots && s_keys[tid] != 0u) s_geo[tid] = sub_triangle(P, s_keys[tid], hw, hh);
-    __syncthreads();
-    if (!live) return;
-    uint32_t mask = 0xFFFFu;
-    if (!same) {
+    uint32_t mask;
+    {
         uint32_t best[4] = {0u, 0u, 0u, 0u};
         float best_z[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
         for (int ci = 0; ci < 9; ++ci) {

@@ -236,6 +236,15 @@ __device__ __forceinline__ size_t act_index(int W, int H, int x, int y, int c) {
 // ---- features -----------------------------------------------------------------
 
 // One pixel's 16 input channels from the G-buffer (see rz_upsampler_* in the header).
+// byte / 255, correctly rounded: the product with the rounded reciprocal and one
+// residual-correction step (Markstein's method), which gives the correctly rounded
+// quotient for every byte value (checked exhaustively against IEEE division).
+__device__ __forceinline__ float unorm8(uint32_t b) {
+    const float x = (float)b, r = 1.0f / 255.0f;
+    const float q = x * r;
+    return __fmaf_rn(__fmaf_rn(-q, 255.0f, x), r, q);
+}
+
 // Sum of the bilinear x2 weights of a sample point's marked sources: own pixel
 // 9/16, horizontal and vertical neighbour 3/16 each, diagonal 1/16.
 __device__ __forceinline__ float matched_weight(uint32_t m4) {
@@ -258,15 +267,15 @@ __global__ void k_features(rz_gbuffer g, __nv_bfloat16* __restrict__ feat) {
     const __half2 h = *reinterpret_cast<const __half2*>(&nn);
     const float2 oct = __half22float2(h);
     float f[16];
-    f[0] = (float)(c & 255u) / 255.0f;
-    f[1] = (float)((c >> 8) & 255u) / 255.0f;
-    f[2] = (float)((c >> 16) & 255u) / 255.0f;
-    f[3] = (float)(a & 255u) / 255.0f;
-    f[4] = (float)((a >> 8) & 255u) / 255.0f;
-    f[5] = (float)((a >> 16) & 255u) / 255.0f;
+    f[0] = unorm8(c & 255u);
+    f[1] = unorm8((c >> 8) & 255u);
+    f[2] = unorm8((c >> 16) & 255u);
+    f[3] = unorm8(a & 255u);
+    f[4] = unorm8((a >> 8) & 255u);
+    f[5] = unorm8((a >> 16) & 255u);
     f[6] = oct.x;
     f[7] = oct.y;
-    f[8] = (float)(a >> 24) / 255.0f;
+    f[8] = unorm8(a >> 24);
     f[9] = fminf(d * 16.0f, 4.0f);
 #pragma unroll
     for (int k = 10; k < 16; ++k) f[k] = 0.0f;
@@ -327,18 +336,9 @@ static_assert(kTileRows * 4 % kConvEpilogueWarps == 0, "epilogue warps split the
 static_assert(2 * kHaloW <= 256, "a halo row is one TMA box (at most 256 elements)");
 static_assert(ConvSmem<32, 32>::S_G % 128 == 0 && ConvSmem<16, 32>::S_R % 128 == 0, "TMA destinations 128-byte aligned");
 
-// byte / 255, correctly rounded: the product with the rounded reciprocal and one
-// residual-correction step (Markstein's method), which gives the correctly rounded
-// quotient for every byte value (checked exhaustively against IEEE division).
-__device__ __forceinline__ float unorm8(uint32_t b) {
-    const float x = (float)b, r = 1.0f / 255.0f;
-    const float q = x * r;
-    return __fmaf_rn(__fmaf_rn(-q, 255.0f, x), r, q);
-}
-
 template <int N, int EPI>
 __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* acc, int x, int y, float& loss,
-                                              const float* bias) {
+                                              const float* bias, int xl, const float (*srcw)[4]) {
     const bool inside = x < a.W && y < a.H;
     if (EPI == kEpiRelu) {
         if (!inside) return;
@@ -364,25 +364,38 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
             }
             *reinterpret_cast<uint4*>(a.out + act_index(a.W, a.H, x, y, 8 * q)) = make_uint4(o[0], o[1], o[2], o[3]);
         }
-    } else {  // final: pixel shuffle + bilinear base (+ loss gradient)
-        if (!inside) return;
-        float net[kOutChannels];
-#pragma unroll
-        for (int c = 0; c < kOutChannels; ++c) net[c] = acc[c] + bias[c];
+    } else {  // final: pixel shuffle + x2 base (+ loss gradient)
         const int W = a.W, H = a.H;
-        // the 3x3 neighbourhood of low-resolution colours (edges clamped), as byte / 255
+        // The 3x3 neighbourhood of low-resolution colours (edges clamped), as byte / 255.
+        // The warp's lanes hold consecutive columns xl (the tile's dropped MMA rows
+        // included, clamped), so each lane loads and converts its own column of the
+        // three rows and takes its left and right neighbours' from the adjacent lanes;
+        // lanes 0 and 31 load the column past the warp's edge. Every lane takes part
+        // (the shuffles), then lanes outside the image return.
+        const int lane = threadIdx.x & 31;
+        const int xo = min(max(xl, 0), W - 1);
+        const int xe = min(max(lane == 0 ? xl - 1 : xl + 1, 0), W - 1);
+        const bool edge_lane = lane == 0 || lane == 31;
         float f[3][3][3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
             const int yy = min(max(y + r - 1, 0), H - 1);
+            const uint32_t c = __ldg(a.color_lr + (size_t)yy * W + xo);
+            const uint32_t ce = edge_lane ? __ldg(a.color_lr + (size_t)yy * W + xe) : 0u;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const int xx = min(max(x + q - 1, 0), W - 1);
-                const uint32_t c = __ldg(a.color_lr + (size_t)yy * W + xx);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) f[r][q][k] = unorm8((c >> (8 * k)) & 255u);
+            for (int k = 0; k < 3; ++k) {
+                const float own = unorm8((c >> (8 * k)) & 255u);
+                const float ext = edge_lane ? unorm8((ce >> (8 * k)) & 255u) : 0.0f;
+                const float lv = __shfl_up_sync(0xFFFFFFFFu, own, 1), rv = __shfl_down_sync(0xFFFFFFFFu, own, 1);
+                f[r][0][k] = lane == 0 ? ext : lv;
+                f[r][1][k] = own;
+                f[r][2][k] = lane == 31 ? ext : rv;
             }
         }
+        if (!inside) return;
+        float net[kOutChannels];
+#pragma unroll
+        for (int c = 0; c < kOutChannels; ++c) net[c] = acc[c] + bias[c];
         const uint32_t srcmask = a.sources ? (uint32_t)__ldg(a.sources + (size_t)y * W + x) : 0xFFFFu;
         float g[kOutChannels];
 #pragma unroll
@@ -397,25 +410,16 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* ac
                 const int qs = j == 0 ? 0 : 2;
                 const uint32_t tj = j == 0 ? t.x : t.y;
                 uint32_t ov = 255u << 24;
-                // the sources of this point that show its triangle (all four: bilinear, none: bilinear too)
+                // the weights of this point's sources (own, horizontal, vertical, diagonal) for
+                // its source mask: bilinear renormalised over the sources that show its triangle
                 const uint32_t m4 = (srcmask >> (4 * (2 * i + j))) & 15u;
-                const float inv_ws = m4 ? 1.0f / matched_weight(m4) : 0.0f;
+                const float w0 = srcw[m4][0], w1 = srcw[m4][1], w2 = srcw[m4][2], w3 = srcw[m4][3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    float base;
-                    if (m4 == 0u) {
-                        base = 0.5625f * f[1][1][k];
-                        base = base + 0.1875f * f[1][qs][k];
-                        base = base + 0.1875f * f[rs][1][k];
-                        base = base + 0.0625f * f[rs][qs][k];
-                    } else {
-                        base = 0.0f;
-                        if (m4 & 1u) base = base + 0.5625f * f[1][1][k];
-                        if (m4 & 2u) base = base + 0.1875f * f[1][qs][k];
-                        if (m4 & 4u) base = base + 0.1875f * f[rs][1][k];
-                        if (m4 & 8u) base = base + 0.0625f * f[rs][qs][k];
-                        base = base * inv_ws;
-                    }
+                    float base = w0 * f[1][1][k];
+                    base = base + w1 * f[1][qs][k];
+                    base = base + w2 * f[rs][1][k];
+                    base = base + w3 * f[rs][qs][k];
                     const float v = base + net[(2 * i + j) * 3 + k];
                     const float qv = fminf(fmaxf(v, 0.0f), 1.0f);
                     ov |= (uint32_t)floorf(qv * 255.0f + 0.5f) << (8 * k);
@@ -507,6 +511,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
     const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
     __shared__ float s_bias[N];
+    __shared__ float s_srcw[16][4];  // final layer: the x2 base's source weights for each source mask
     if (warp == 0) tmem_alloc(tmem_slot, L::TMEM_COLS);
     if (tid == 0) {
         for (int b = 0; b < NS; ++b) {
@@ -520,6 +525,13 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         mbar_init(wbar, 1);
     }
     if (tid < N) s_bias[tid] = EPI == kEpiMask ? 0.0f : a.bias[tid];
+    if (EPI == kEpiFinal && tid < 64) {
+        // mask m keeps the bilinear sources of its set bits, each weight times 1 / (their sum);
+        // no bit set is plain bilinear (as is every bit set: the sum is 1)
+        const uint32_t m = (uint32_t)tid >> 2, s = (uint32_t)tid & 3u;
+        const float w = s == 0 ? 0.5625f : (s == 3 ? 0.0625f : 0.1875f);
+        s_srcw[m][s] = m == 0u ? w : (((m >> s) & 1u) ? w * (1.0f / matched_weight(m)) : 0.0f);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -609,7 +621,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
         for (int c = 0; c < N; ++c) bias[c] = s_bias[c];
         for (int j = 0; j < my_tiles; ++j) {
             const int buf = j & 1;
-            if (!mbar_wait(&tfull[buf], (uint32_t)(j >> 1) & 1u, a.wait_cycles)) {
+            // one decision per warp: the epilogue's TMEM loads and shuffles are warp-wide
+            if (!__all_sync(0xFFFFFFFFu, mbar_wait(&tfull[buf], (uint32_t)(j >> 1) & 1u, a.wait_cycles))) {
                 ok = false;
                 break;
             }
@@ -626,7 +639,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv(ConvArgs a, const __gr
                 if constexpr (N == 32) tmem_ld32(ta, acc);
                 else tmem_ld16(ta, acc);
                 tmem_zero(ta, N);
-                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, bias);
+                conv_epilogue<N, EPI>(a, acc, x, y0 + t, loss, bias, x0 + col, s_srcw);
             }
             tc_fence_before();
             __syncwarp();
