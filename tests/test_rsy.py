@@ -199,3 +199,77 @@ def test_rsy_reader_survives_mutated_files(tmp_path, renderer_lib):
             f.close()
 
     mutated()
+
+
+GOLDEN_RSY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rsy")
+GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN_RSY) if f.endswith(".rsy"))
+
+
+class _JsonAsset:
+    """The asset the reference's own asset::read decoded, in the shape _expected_worlds wants."""
+
+    def __init__(self, d):
+        self.coordinate_system = np.array(d["coordinate_system"], np.float64).reshape(4, 4).T
+        self.root_scene = d["root_scene"]
+        self.scenes = d["scenes"]
+        self.nodes = [rsy.RsyNode(n["world_translate"], n["world_scale"], n["world_yaw"],
+                                  np.array(n["transform"], np.float64).reshape(4, 4).T, n["mesh_id"], n["children"],
+                                  n["name"]) for n in d["nodes"]]
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_reader_matches_files_the_reference_wrote(renderer_lib, case):
+    """Files written by the reference's asset::write (src/Asset/Asset.cpp:28-407,
+    compiled from its sources by oracle/ref_rsy, fixtures made by
+    tests/golden/make_rsy_golden.py): rz_rsy_read decodes every record to the
+    values the reference's own asset::read decoded, and flattens the root scene
+    by the level's rules."""
+    import json
+
+    d = json.load(open(os.path.join(GOLDEN_RSY, case + ".json")))
+    f = rsy.RsyFile(os.path.join(GOLDEN_RSY, case + ".rsy"))
+    info = f.info
+    assert (info.mesh_count, info.material_count, info.sampler_count, info.image_count, info.node_count,
+            info.scene_count, info.root_scene) == (len(d["meshes"]), len(d["materials"]), len(d["samplers"]),
+                                                   len(d["images"]), len(d["nodes"]), len(d["scenes"]),
+                                                   d["root_scene"])
+    assert np.array_equal(np.array(info.coordinate_system, np.float32), np.array(d["coordinate_system"], np.float32))
+    for (pos, idx), m in zip(f.meshes(), d["meshes"]):
+        assert np.array_equal(pos.reshape(-1), np.array(m["positions"], np.float32))
+        assert np.array_equal(idx, np.array(m["indices"], np.uint32))
+    mats = f.materials()
+    for got, m in zip(mats, d["materials"]):
+        assert np.array_equal(got["base_color_factor"], np.array(m["base_color_factor"], np.float32))
+        assert got["metallic_factor"] == np.float32(m["metallic_factor"])
+        assert got["roughness_factor"] == np.float32(m["roughness_factor"])
+        assert got["alpha_cutoff"] == np.float32(m["alpha_cutoff"])
+        assert got["alpha_mode"] == m["alpha_mode"] and got["double_sided"] == m["double_sided"]
+        names = ("color_image_index", "color_sampler_index", "normal_image_index", "normal_sampler_index",
+                 "metallic_image_index", "metallic_sampler_index", "mixmap_image_index", "mixmap_sampler_index")
+        assert [int(got[n]) for n in names] == m["indices"]
+    smp = f.samplers()
+    assert [[int(s[k]) for k in ("min_filter", "mag_filter", "wrap_s", "wrap_t")] for s in smp] == d["samplers"]
+    assert f.images() == [(im["type"], im["name"]) for im in d["images"]]
+    objs, surfs = f.scene_objects()
+    a = _JsonAsset(d)
+    statics, mobs = _expected_worlds(a)
+    assert info.static_object_count == len(statics) and info.object_count == len(statics) + len(mobs)
+    for k, w in enumerate(statics + mobs):
+        assert np.allclose(objs[k, :16].reshape(4, 4).T, w, atol=1e-5), k
+    # one surface per mesh surface of every object, with the mesh surface's material and range
+    want = []
+    queue = [(n, False) for n in d["scenes"][d["root_scene"]]]
+    order_static, order_mob = [], []
+    while queue:
+        i, mob = queue.pop(0)
+        n = d["nodes"][i]
+        if n["mesh_id"] != 0xFFFFFFFF:
+            (order_mob if mob else order_static).append(n["mesh_id"])
+        queue += [(c, mob or d["nodes"][c]["name"] == "mobs") for c in n["children"]]
+    for mesh_id in order_static + order_mob:
+        for s in d["meshes"][mesh_id]["surfaces"]:
+            want.append((s["material"], s["count"], s["start_index"],
+                         int(d["materials"][s["material"]]["alpha_mode"] != 0)))
+    assert [(int(s["material_index"]), int(s["index_count"]), int(s["start_index"]), int(s["blended"]))
+            for s in surfs] == want
+    f.close()
