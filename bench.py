@@ -11,8 +11,10 @@ uploaded inside the frame, everything else is resident); L2 is flushed by a
 256 MiB write between frames, outside the timed events. `e2e` is frames/s
 through the C ABI with host buffers: per frame, the scene constants and all
 object transforms go host->device from pinned memory and the RGBA8 frame comes
-back device->host into pinned memory, wall-clock timed, with two frames in
-flight (a host buffer is reused once the frame that last filled it has landed;
+back device->host into pinned memory (a device staging copy, then the copy to
+the host on the renderer's copy stream while the next frame renders),
+wall-clock timed, with two frames in flight (a host buffer is reused once the
+read-back that last filled it has landed, rz_read_sync;
 the reference's Vulkan renderer keeps up to three, src/Engine/Graphics.cpp:177).
 
 --impl reference times the CPU restatement of the reference's path (the oracle,
@@ -411,18 +413,15 @@ def run_rz(args):
     n_e2e = min(args.steps, 200)
     g.sync()
     barrier(ws)
-    done = [None] * ring
     t0 = time.perf_counter()
     for i in range(n_e2e):
         k = i % ring
-        if done[k] is not None:
-            done[k].synchronize()  # the frame that last used this host buffer has landed
+        if i >= ring:
+            g.read_sync(1)  # every read-back but the newest has landed: this host buffer is free
         g.update(scene_host[i % len(cams)].view(cams[0].dtype))
         g.update_objects(0, objects_host)
         g.render()
         g.read_frame(color_hosts[k])
-        done[k] = torch.cuda.Event()
-        done[k].record(stream)
     g.sync()
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
     e2e_value = ws * n_e2e / e2e_s

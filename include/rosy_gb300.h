@@ -322,9 +322,22 @@ int rz_sync(struct rz_ctx* ctx, uint32_t timeout_ms);
 int rz_get_frame(struct rz_ctx* ctx, rz_frame_out* out);
 
 /* Enqueues device-to-host copies of the colour (width*height*4 bytes) and/or
- * depth (width*height*4 bytes) images; NULL skips one. Complete after rz_sync. */
+ * depth (width*height*4 bytes) images of the frame rendered last; NULL skips
+ * one. The images are first copied on the device into one of two staging
+ * buffers (after the frame), then to the host on a copy stream of the context,
+ * so the next frame renders while they travel (the reference keeps several
+ * frames in flight, src/Engine/Graphics.cpp:177, and presents asynchronously).
+ * The host buffers are complete after rz_sync, or after rz_read_sync. The first
+ * call (or a larger frame) allocates the staging buffers. */
 int rz_read_frame(struct rz_ctx* ctx, void* color_host, size_t color_bytes,
                   void* depth_host, size_t depth_bytes);
+
+/* Waits until at most `pending` (0 or 1) of the read-backs queued by
+ * rz_read_frame are still travelling: 1 waits for all but the newest, so a
+ * caller with two host buffers may refill the older one. RZ_TIMEOUT after
+ * timeout_ms (0: no limit). Library addition (the reference presents to a
+ * swapchain instead). */
+int rz_read_sync(struct rz_ctx* ctx, uint32_t pending, uint32_t timeout_ms);
 
 /* Counters of the last completed frame (call after rz_sync). */
 int rz_get_stats(struct rz_ctx* ctx, rz_stats* out);

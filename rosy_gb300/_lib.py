@@ -27,7 +27,7 @@ EXPORTS = [
     "rz_get_stats", "rz_get_stream", "rz_last_error", "rz_abi_version", "rz_set_stage_timing",
     "rz_get_stage_times", "rz_shadow_depth_static", "rz_add_scene", "rz_set_views", "rz_update_view",
     "rz_get_view_frame", "rz_set_tuning", "rz_get_tuning", "rz_autotune", "rz_set_gbuffer", "rz_get_view_gbuffer",
-    "rz_set_debug_objects", "rz_set_wait_limit", "rz_upsampler_set_wait_limit",
+    "rz_set_debug_objects", "rz_set_wait_limit", "rz_upsampler_set_wait_limit", "rz_read_sync",
     "rz_upsampler_create", "rz_upsampler_destroy", "rz_upsampler_set_params", "rz_upsampler_get_params",
     "rz_upsampler_infer", "rz_upsampler_accumulate", "rz_upsampler_get_grads", "rz_upsampler_adam_step",
     "rz_upsampler_status", "rz_upsampler_selftest_gemm", "rz_rsy_read", "rz_rsy_free", "rz_rsy_get_info",
@@ -71,6 +71,8 @@ def load(build_if_missing: bool = False):
     lib.rz_sync.argtypes = [P, u32]
     lib.rz_get_frame.argtypes = [P, C.POINTER(_abi.RzFrameOut)]
     lib.rz_read_frame.argtypes = [P, P, C.c_size_t, P, C.c_size_t]
+    lib.rz_read_sync.argtypes = [P, u32, u32]
+    lib.rz_read_sync.restype = C.c_int
     lib.rz_get_stats.argtypes = [P, C.POINTER(_abi.RzStats)]
     lib.rz_get_stream.argtypes = [P]
     lib.rz_get_stream.restype = P

@@ -94,6 +94,13 @@ struct rz_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;  // shadow pass branch of the frame graph
+    // read-back (rz_read_frame): device staging copies on the frame stream, then
+    // device-to-host copies on their own stream so that the next frame renders meanwhile
+    cudaStream_t copy_stream = nullptr;
+    unsigned char* d_read_stage[2] = {nullptr, nullptr};
+    size_t read_stage_capacity = 0;
+    cudaEvent_t read_staged[2] = {nullptr, nullptr}, read_done[2] = {nullptr, nullptr};
+    uint64_t reads_issued = 0;
     cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t camera_done = nullptr, sources_done = nullptr;  // the side branch of the G-buffer's sub-pixel sources
     uint32_t queue_chunks = 0;    // fixed work-queue depth (0 = sized from the scene)
@@ -1125,6 +1132,23 @@ std::vector<DebugPair> debug_pairs_of(const rz_debug_object* objects, uint32_t c
     return out;
 }
 
+// Polls `done` (a stream or an event query) until it reports completion, an
+// error, or timeout_ms runs out (0: no limit).
+template <class Query>
+int wait_until(rz_ctx* c, Query done, uint32_t timeout_ms, const char* what) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t q = done();
+        if (q == cudaSuccess) return RZ_OK;
+        if (q != cudaErrorNotReady) return cuda_fail(c, q, what);
+        if (timeout_ms) {
+            const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if (ms >= (long long)timeout_ms) return fail(c, RZ_TIMEOUT, std::string(what) + " still running");
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1153,8 +1177,13 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->camera_done, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->sources_done, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->sources_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
+    for (int k = 0; k < 2; ++k)
+        if (cudaEventCreateWithFlags(&c->read_staged[k], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->read_done[k], cudaEventDisableTiming) != cudaSuccess)
+            return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->objects_copied, cudaEventDisableTiming) != cudaSuccess)
@@ -1244,6 +1273,13 @@ void rz_destroy(rz_ctx* c) {
     if (c->join) cudaEventDestroy(c->join);
     if (c->camera_done) cudaEventDestroy(c->camera_done);
     if (c->sources_done) cudaEventDestroy(c->sources_done);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    for (int k = 0; k < 2; ++k) {
+        if (c->read_staged[k]) cudaEventDestroy(c->read_staged[k]);
+        if (c->read_done[k]) cudaEventDestroy(c->read_done[k]);
+        if (c->d_read_stage[k]) cudaFree(c->d_read_stage[k]);
+    }
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1463,15 +1499,16 @@ int rz_sync(rz_ctx* c, uint32_t timeout_ms) {
     if (!c) return RZ_INVALID_ARGUMENT;
     cudaSetDevice(c->device);
     const auto t0 = std::chrono::steady_clock::now();
-    for (;;) {
-        const cudaError_t q = cudaStreamQuery(c->stream);
-        if (q == cudaSuccess) break;
-        if (q != cudaErrorNotReady) return cuda_fail(c, q, "frame");
+    int rc = wait_until(c, [&] { return cudaStreamQuery(c->stream); }, timeout_ms, "frame");
+    if (rc != RZ_OK) return rc;
+    if (c->reads_issued) {  // and the read-backs queued so far
+        uint32_t left = 0;
         if (timeout_ms) {
             const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
-            if (ms >= (long long)timeout_ms) return fail(c, RZ_TIMEOUT, "frame still running");
+            left = ms >= (long long)timeout_ms ? 1u : timeout_ms - (uint32_t)ms;
         }
-        std::this_thread::sleep_for(std::chrono::microseconds(50));
+        rc = wait_until(c, [&] { return cudaStreamQuery(c->copy_stream); }, left, "frame read-back");
+        if (rc != RZ_OK) return rc;
     }
     if (!c->frame_pending) return RZ_OK;
     c->frame_pending = false;
@@ -1558,11 +1595,45 @@ int rz_read_frame(rz_ctx* c, void* color_host, size_t color_bytes, void* depth_h
     if ((color_host && color_bytes < need) || (depth_host && depth_bytes < need))
         return fail(c, RZ_INVALID_ARGUMENT, "host buffer too small");
     cudaSetDevice(c->device);
-    if (color_host)
-        RZ_CUDA(c, cudaMemcpyAsync(color_host, r.color, need, cudaMemcpyDeviceToHost, c->stream), "read colour");
-    if (depth_host)
-        RZ_CUDA(c, cudaMemcpyAsync(depth_host, r.depth, need, cudaMemcpyDeviceToHost, c->stream), "read depth");
+    if (!color_host && !depth_host) return RZ_OK;
+    if (2 * need > c->read_stage_capacity) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamSynchronize(c->stream);
+        for (int k = 0; k < 2; ++k) {
+            cudaFree(c->d_read_stage[k]);
+            c->d_read_stage[k] = nullptr;
+        }
+        c->read_stage_capacity = 0;
+        for (int k = 0; k < 2; ++k)
+            RZ_CUDA(c, cudaMalloc(reinterpret_cast<void**>(&c->d_read_stage[k]), 2 * need), "read-back staging");
+        c->read_stage_capacity = 2 * need;
+        c->reads_issued = 0;
+    }
+    // the frame's images into a staging buffer (on the frame stream, after the frame),
+    // then to the host on the copy stream; the staging buffer's previous read-back
+    // (two calls ago) has landed first
+    const int slot = (int)(c->reads_issued & 1u);
+    unsigned char* st = c->d_read_stage[slot];
+    if (c->reads_issued >= 2) RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->read_done[slot], 0), "read-back slot");
+    if (color_host) RZ_CUDA(c, cudaMemcpyAsync(st, r.color, need, cudaMemcpyDeviceToDevice, c->stream), "stage colour");
+    if (depth_host) RZ_CUDA(c, cudaMemcpyAsync(st + need, r.depth, need, cudaMemcpyDeviceToDevice, c->stream), "stage depth");
+    RZ_CUDA(c, cudaEventRecord(c->read_staged[slot], c->stream), "staged");
+    RZ_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->read_staged[slot], 0), "staged");
+    if (color_host) RZ_CUDA(c, cudaMemcpyAsync(color_host, st, need, cudaMemcpyDeviceToHost, c->copy_stream), "read colour");
+    if (depth_host) RZ_CUDA(c, cudaMemcpyAsync(depth_host, st + need, need, cudaMemcpyDeviceToHost, c->copy_stream), "read depth");
+    RZ_CUDA(c, cudaEventRecord(c->read_done[slot], c->copy_stream), "read done");
+    ++c->reads_issued;
     return RZ_OK;
+}
+
+int rz_read_sync(rz_ctx* c, uint32_t pending, uint32_t timeout_ms) {
+    if (!c || pending > 1) return RZ_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (pending == 0 || c->reads_issued == 0)
+        return wait_until(c, [&] { return cudaStreamQuery(c->copy_stream); }, timeout_ms, "frame read-back");
+    if (c->reads_issued < 2) return RZ_OK;  // at most one read-back was ever queued
+    const int slot = (int)((c->reads_issued - 2) & 1u);  // all but the newest read-back
+    return wait_until(c, [&] { return cudaEventQuery(c->read_done[slot]); }, timeout_ms, "frame read-back");
 }
 
 int rz_get_stats(rz_ctx* c, rz_stats* out) {

@@ -206,8 +206,12 @@ class Graphics:
         self._check(self._lib.rz_get_frame(self._ctx, C.byref(out)), "rz_get_frame")
         return out
 
+    def read_sync(self, pending: int = 0, timeout_ms: int = 0) -> None:
+        """Waits until at most `pending` (0 or 1) read-backs are still travelling."""
+        self._check(self._lib.rz_read_sync(self._ctx, pending, timeout_ms), "rz_read_sync")
+
     def read_frame(self, color: np.ndarray | None = None, depth: np.ndarray | None = None) -> None:
-        """Enqueues device-to-host copies into caller arrays (complete after sync())."""
+        """Enqueues device-to-host copies into caller arrays (complete after sync() or read_sync())."""
         cp = _abi.ptr(color) if color is not None else None
         dp = _abi.ptr(depth) if depth is not None else None
         self._check(self._lib.rz_read_frame(self._ctx, cp, color.nbytes if color is not None else 0,

@@ -232,3 +232,46 @@ def test_shading_error_against_fp64_oracle(gpu, oracle):
     err = np.abs(out["color"][..., :3].astype(np.float64) - ref["color_f64"][..., :3] * 255.0)
     assert err.max() <= 1.5, err.max()
     assert err.mean() < 0.3, err.mean()
+
+
+@pytest.mark.gpu
+def test_read_back_with_frames_in_flight(gpu, oracle):
+    """Frames read back through rz_read_frame while the next ones render (two
+    host buffers, rz_read_sync before refilling one): every buffer holds its own
+    frame's colour and depth."""
+    import torch
+
+    from rosy_gb300.graphics import Graphics
+
+    s = sc.scene_scale(seed=7, meshes=8, triangles_per_mesh=512, materials=4, texture_size=64, width=320,
+                       height=180, shadow_size=512, frames=5)
+    g = Graphics()
+    g.init(s.width, s.height, s.shadow_size)
+    try:
+        g.set_asset(s)
+        g.set_graphic_objects(s.objects, s.surfaces)
+        g.set_draw_config(s.draw_config)
+        g.update(s.cameras[0])
+        g.render()
+        if g.sync_code() == 14:
+            g.render()
+        g.sync()
+        bufs = [(torch.empty((s.height, s.width, 4), dtype=torch.uint8, pin_memory=True).numpy(),
+                 torch.empty((s.height, s.width), dtype=torch.float32, pin_memory=True).numpy()) for _ in range(2)]
+        got = []
+        for i in range(5):
+            if i >= 2:
+                g.read_sync(1)
+                got.append((i - 2, bufs[i % 2][0].copy(), bufs[i % 2][1].copy()))
+            g.update(s.cameras[i])
+            g.render()
+            g.read_frame(*bufs[i % 2])
+        g.sync()
+        for i in (3, 4):
+            got.append((i, bufs[i % 2][0].copy(), bufs[i % 2][1].copy()))
+        for i, color, depth in got:
+            ref = oracle.render(s.with_camera(i))
+            assert np.array_equal(depth.view(np.uint32), ref["depth"].view(np.uint32)), i
+            assert np.abs(color.astype(np.int32) - ref["color"].astype(np.int32)).max() <= COLOR_TOL, i
+    finally:
+        g.deinit()
