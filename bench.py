@@ -676,6 +676,8 @@ def run_stress(args):
                    "views_per_batch": views, "plain_extent": [3840, 2160], "render_extent": [1920, 1080],
                    "l2": "flushed between batches (256 MiB write)"},
         "per_view": per, "psnr_db_mean": round(float(np.mean([p["psnr_db"] for p in per])), 3),
+        "psnr_floor_db": learned.PSNR_FLOOR_DB,
+        "fallback_to_plain": any(p["psnr_db"] < learned.PSNR_FLOOR_DB for p in per),  # judged per view
         "weights": {k: meta.get(k) for k in ("steps", "train_cameras")},
     }))
 
