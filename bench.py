@@ -451,8 +451,11 @@ def run_rz(args):
         "shadow_raster": raster_bytes(s, "shadow"),
         "camera_raster": raster_bytes(s, "camera"),
         "shade": shade_bytes(s, out0["ids"], extra.get("texel_bytes")) if out0 is not None else None,
-        "shadow_clear": 4 * s.shadow_size ** 2,
-        "camera_clear": 8 * s.width * s.height,
+        # a setup launch pulls the vertices, indices and objects and zeroes its pass's depth
+        # target: the same byte count as its raster launch (which reads the setup records and
+        # writes that target). The clear stages before them only reset pass headers.
+        "shadow_setup": raster_bytes(s, "shadow"),
+        "camera_setup": raster_bytes(s, "camera"),
     }
     roof = None
     if rank == 0:
