@@ -175,6 +175,7 @@ struct rz_ctx {
     DrawConsts* d_camera_consts = nullptr;
     DrawConsts* d_blended_consts = nullptr;
     float4* d_varyings = nullptr;
+    uint4* d_tri_refs = nullptr;  // per opaque triangle: its draw and varying records (written by the camera setup)
     uint32_t varying_count = 0, blended_varying_base = 0;
     bool layout_dirty = true;        // draw lists, pools and view table need a rebuild
 
@@ -688,6 +689,7 @@ int build_layout(rz_ctx* c) {
     dfree(c->d_camera_consts);
     dfree(c->d_blended_consts);
     dfree(c->d_varyings);
+    dfree(c->d_tri_refs);
     RZ_CUDA(c, dalloc(&c->d_views, c->view_recs.size()), "view table");
     RZ_CUDA(c, dalloc(&c->d_shadow_draws, std::max<size_t>(shadow_list.size(), 1)), "shadow draw list");
     RZ_CUDA(c, dalloc(&c->d_opaque_draws, std::max<size_t>(opaque.size(), 1)), "opaque draw list");
@@ -696,6 +698,7 @@ int build_layout(rz_ctx* c) {
     RZ_CUDA(c, dalloc(&c->d_camera_consts, std::max<size_t>(opaque.size(), 1)), "camera constants");
     RZ_CUDA(c, dalloc(&c->d_blended_consts, std::max<size_t>(blended.size(), 1)), "blended constants");
     RZ_CUDA(c, dalloc(&c->d_varyings, std::max<size_t>((size_t)varyings, 1) * 8), "varying records");
+    RZ_CUDA(c, dalloc(&c->d_tri_refs, std::max<size_t>((size_t)opaque_tris, 1)), "triangle references");
     RZ_CUDA(c, cudaMemcpy(c->d_views, c->view_recs.data(), c->view_recs.size() * sizeof(ViewRec), cudaMemcpyHostToDevice),
             "upload views");
     if (!shadow_list.empty())
@@ -774,6 +777,7 @@ PassParams pass_params(rz_ctx* c, int kind) {
     p.tile_status = pb->tile_status;
     p.chunk_map = pb->chunk_map;
     p.chunk_capacity = pb->chunk_capacity;
+    p.tri_refs = kind == 1 ? c->d_tri_refs : nullptr;
     return p;
 }
 
@@ -797,6 +801,7 @@ ShadeParams shade_params(rz_ctx* c) {
     sh.samplers = c->d_samplers;
     sh.sampler_count = (uint32_t)c->samplers.size();
     sh.srgb_table = c->d_srgb;
+    sh.tri_refs = c->d_tri_refs;
     sh.blended = (c->blended_tris || c->debug_count) ? 1 : 0;  // k_blend finishes the frame
     return sh;
 }
@@ -904,6 +909,7 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
         bs.draw_count = c->blended_draw_count;
         bs.consts = c->d_blended_consts;
         bs.varying_count = c->varying_count;
+        bs.tri_refs = nullptr;
         launch_vertex_range(bs, c->blended_varying_base, s);
     }
 }
@@ -1010,6 +1016,7 @@ int enqueue_frame(rz_ctx* c) {
         bp.sh.draws = c->d_blended_draws;
         bp.sh.draw_count = c->blended_draw_count;
         bp.sh.consts = c->d_blended_consts;
+        bp.sh.tri_refs = nullptr;  // the blended triangles are looked up through their draws
         bp.records = c->blended_pass.records;
         bp.header = &c->d_report->blended;
         bp.error_flags = &c->d_report->camera_errors;
@@ -1260,6 +1267,7 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_camera_consts);
     dfree(c->d_blended_consts);
     dfree(c->d_varyings);
+    dfree(c->d_tri_refs);
     dfree(c->d_report);
     if (c->h_scene_data) cudaFreeHost(c->h_scene_data);
     if (c->h_report) cudaFreeHost(c->h_report);

@@ -187,6 +187,9 @@ struct PassParams {
     void* clear_ptr[2];
     size_t clear_bytes[2];
     uint32_t clear_count;
+    // opaque camera pass only (else null): per triangle that produced a record,
+    // its draw and its three varying record indices, for the shading
+    uint4* tri_refs;
 };
 
 struct ShadeParams {
@@ -210,6 +213,10 @@ struct ShadeParams {
     const float* srgb_table;      // 256 entries
     int blended;                  // 1: k_shade stores the RGBA16F draw image (color16) for k_blend
     uint32_t samples;             // camera-pass samples per pixel of the views (1 or 4)
+    // the opaque camera setup's per-triangle (draw, varying record of each vertex),
+    // indexed by pass-global triangle id; null for the blended list, whose
+    // triangles are then looked up through the draw list and the index buffer
+    const uint4* tri_refs;
 };
 
 // The blended list (src/Engine/Graphics.cpp:5654-5691) over the opaque result.

@@ -305,6 +305,8 @@ __device__ __forceinline__ void setup_triangle(const PassParams& P, uint32_t tri
         atomicOr(P.error_flags, kErrBadIndex);
         return;
     }
+    emit.source(d, vi[0] - dr.vertex_base + dr.varying_base, vi[1] - dr.vertex_base + dr.varying_base,
+                vi[2] - dr.vertex_base + dr.varying_base);
     const ViewRec& VR = P.views[dr.view];
     ViewState V;
     V.view = dr.view | (dr.cascade << kViewBits);
@@ -386,6 +388,15 @@ struct CountEmit {
     uint32_t small = 0;
     TriRecord first;       // the first record, kept for the common case of exactly one
     bool first_small = false;
+    uint4* refs = nullptr; // opaque camera pass: where the triangle's draw and vertex records go
+    uint32_t tri = 0;
+    // every triangle with valid indices stores its draw and the varying records of
+    // its vertices: a triangle that owns a pixel of the visibility buffer is one of
+    // them, and the shading finds them here (one load instead of a search of the
+    // draw list and the index buffer)
+    __device__ void source(uint32_t d, uint32_t v0, uint32_t v1, uint32_t v2) {
+        if (refs) refs[tri] = make_uint4(d, v0, v1, v2);
+    }
     __device__ void operator()(const TriRecord& r, bool is_small) {
         if (recs + small == 0) {
             first = r;
@@ -408,6 +419,7 @@ struct WriteEmit {
     uint32_t rec;
     uint64_t stamp;
     uint32_t small;
+    __device__ void source(uint32_t, uint32_t, uint32_t, uint32_t) {}
     __device__ void operator()(TriRecord& r, bool is_small) {
         if (is_small) {
             if (small < P->small_capacity) store_record(P->small_records + small, r);
@@ -471,6 +483,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     const uint32_t tri = P.tri_offset + local;
 
     CountEmit cnt;
+    cnt.refs = P.tri_refs;
+    cnt.tri = tri;
     if (local < P.tri_total) setup_triangle(P, tri, cnt);
 
     // CTA-wide inclusive scan of (records, stamps) packed in one 64-bit word.

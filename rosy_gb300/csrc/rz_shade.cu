@@ -178,10 +178,20 @@ __device__ __forceinline__ void vertex_main(const rz_scene_data& sd, const rz_ob
 }
 
 // Perspective-correct barycentrics at pixel centre (px, py), 2D homogeneous form.
-__device__ __forceinline__ void barycentrics(const float4& c0, const float4& c1, const float4& c2, int px, int py, int W,
-                                             int H, float b[3]) {
-    const float xn = (float)(2 * px + 1 - W) / (float)W;
-    const float yn = (float)(2 * py + 1 - H) / (float)H;
+// Normalised device coordinate of pixel centre i of an extent of n pixels.
+__device__ __forceinline__ float ndc(int i, int n) { return (float)(2 * i + 1 - n) / (float)n; }
+
+// The normalised coordinates of the pixel centres of one 16x16 shading tile,
+// computed once per tile in shared memory (the same ndc() values, so every
+// pixel's barycentrics are unchanged): column x0 + i at xn[i], row y0 + j at yn[j].
+struct TileCoords {
+    const float* xn;
+    const float* yn;
+    int x0, y0;
+};
+
+__device__ __forceinline__ void barycentrics_n(const float4& c0, const float4& c1, const float4& c2, float xn, float yn,
+                                               float b[3]) {
     const V3 v0{c0.x, c0.y, c0.w}, v1{c1.x, c1.y, c1.w}, v2{c2.x, c2.y, c2.w};
     const V3 p{xn, yn, 1.0f};
     const float b0 = dot(cross(v1, v2), p), b1 = dot(cross(v2, v0), p), b2 = dot(cross(v0, v1), p);
@@ -189,6 +199,11 @@ __device__ __forceinline__ void barycentrics(const float4& c0, const float4& c1,
     b[0] = b0 * inv;
     b[1] = b1 * inv;
     b[2] = b2 * inv;
+}
+
+__device__ __forceinline__ void barycentrics(const float4& c0, const float4& c1, const float4& c2, int px, int py, int W,
+                                             int H, float b[3]) {
+    barycentrics_n(c0, c1, c2, ndc(px, W), ndc(py, H), b);
 }
 
 struct Frag {
@@ -711,16 +726,27 @@ void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stre
 // records of its three vertices.
 // With `aux` non-null it also returns the G-buffer values: albedo (the sampled
 // base colour, rgb) and the interpolated world-space normal (normalised, xyz).
+// With `tc` non-null the pixel lies in that tile and its coordinates come from there.
 __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_scene_data& sd, const Sampler& smp, uint32_t tri,
-                            int px, int py, float out[4], float* aux = nullptr) {
-    const uint32_t d = find_draw(P.draws, P.draw_count, tri);
-    const DrawRec dr = P.draws[d];
-    const GpuMaterial* md = dr.material >= 0 ? &P.materials[dr.material] : nullptr;
-    const uint32_t t = tri - dr.tri_base;
+                            int px, int py, float out[4], float* aux = nullptr, const TileCoords* tc = nullptr) {
+    uint32_t d;
     const float4* rec[3];
+    if (P.tri_refs) {  // the opaque list: the camera setup recorded the draw and the vertices
+        const uint4 r = __ldg(&P.tri_refs[tri]);
+        d = r.x;
+        rec[0] = P.varyings + (size_t)r.y * kVaryingF4;
+        rec[1] = P.varyings + (size_t)r.z * kVaryingF4;
+        rec[2] = P.varyings + (size_t)r.w * kVaryingF4;
+    } else {
+        d = find_draw(P.draws, P.draw_count, tri);
+        const DrawRec& dl = P.draws[d];
+        const uint32_t t = tri - dl.tri_base;
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-        rec[k] = P.varyings + (size_t)(__ldg(&P.indices[dr.first_index + 3u * t + k]) + dr.varying_base) * kVaryingF4;
+        for (int k = 0; k < 3; ++k)
+            rec[k] = P.varyings + (size_t)(__ldg(&P.indices[dl.first_index + 3u * t + k]) + dl.varying_base) * kVaryingF4;
+    }
+    const int32_t material = __ldg(&P.draws[d].material);
+    const GpuMaterial* md = material >= 0 ? &P.materials[material] : nullptr;
     float4 clip[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -728,11 +754,27 @@ __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_sc
         clip[k] = make_float4(q.y, q.z, 0.0f, q.w);
     }
     float b[3], bq0[3], bqx[3], bqy[3];
-    barycentrics(clip[0], clip[1], clip[2], px, py, VR.width, VR.height, b);
     const int qx = px & ~1, qy = py & ~1;
-    barycentrics(clip[0], clip[1], clip[2], qx, qy, VR.width, VR.height, bq0);
-    barycentrics(clip[0], clip[1], clip[2], qx + 1, qy, VR.width, VR.height, bqx);
-    barycentrics(clip[0], clip[1], clip[2], qx, qy + 1, VR.width, VR.height, bqy);
+    float xp, yp, xq, yq, xq1, yq1;  // ndc of px, py, qx, qy, qx + 1, qy + 1
+    if (tc) {
+        xp = tc->xn[px - tc->x0];
+        yp = tc->yn[py - tc->y0];
+        xq = tc->xn[qx - tc->x0];
+        yq = tc->yn[qy - tc->y0];
+        xq1 = tc->xn[qx + 1 - tc->x0];
+        yq1 = tc->yn[qy + 1 - tc->y0];
+    } else {
+        xp = ndc(px, VR.width);
+        yp = ndc(py, VR.height);
+        xq = ndc(qx, VR.width);
+        yq = ndc(qy, VR.height);
+        xq1 = ndc(qx + 1, VR.width);
+        yq1 = ndc(qy + 1, VR.height);
+    }
+    barycentrics_n(clip[0], clip[1], clip[2], xp, yp, b);
+    barycentrics_n(clip[0], clip[1], clip[2], xq, yq, bq0);
+    barycentrics_n(clip[0], clip[1], clip[2], xq1, yq, bqx);
+    barycentrics_n(clip[0], clip[1], clip[2], xq, yq1, bqy);
     const bool debug_extra = sd.fragment_output == 1 || sd.fragment_output == 7 || aux != nullptr;
     Frag f;
     float u0[2], ux[2], uy[2];
@@ -848,7 +890,7 @@ __device__ __forceinline__ float resolve4(float a, float b, float c, float d) {
 // samples are resolved and encoded here; with them they go to the RGBA16F
 // sample planes for k_blend. The depth output is sample 0's.
 __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& VR, const float* s_srgb,
-                                           const float* s_unorm, int px, int py, size_t p) {
+                                           const float* s_unorm, const TileCoords& tc, int px, int py, size_t p) {
     const size_t plane = (size_t)VR.width * VR.height;
     uint32_t ids[kMsaaSamples];
     unsigned long long key0 = 0;
@@ -879,7 +921,7 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
         }
         if (ids[k] != 0) {
             float o[4];
-            if (shade_pixel(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr)) {
+            if (shade_pixel(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) c[i] = o[i];
             }
@@ -920,8 +962,21 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
     VR.color[p] = encode_srgb8(r[0]) | (encode_srgb8(r[1]) << 8) | (encode_srgb8(r[2]) << 16) | (encode_unorm8(r[3]) << 24);
 }
 
+// The tile's view, its origin and its coordinate table (16 columns, 16 rows;
+// also the columns and rows past the view's edge, which quads reach).
+__device__ __forceinline__ TileCoords tile_setup(const ShadeParams& P, const ViewRec& VR, float* s_xn, float* s_yn) {
+    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
+    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
+    const int x0 = (int)(lt % tiles_x) * 16, y0 = (int)(lt / tiles_x) * 16;
+    if (threadIdx.y == 0) s_xn[threadIdx.x] = ndc(x0 + (int)threadIdx.x, VR.width);
+    if (threadIdx.y == 1) s_yn[threadIdx.x] = ndc(y0 + (int)threadIdx.x, VR.height);
+    __syncthreads();
+    return TileCoords{s_xn, s_yn, x0, y0};
+}
+
 __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ float s_xn[16], s_yn[16];
     __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -931,10 +986,9 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     }
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
-    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
-    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
-    const int px = (int)(lt % tiles_x) * 16 + threadIdx.x;
-    const int py = (int)(lt / tiles_x) * 16 + threadIdx.y;
+    const TileCoords tc = tile_setup(P, VR, s_xn, s_yn);
+    const int px = tc.x0 + (int)threadIdx.x;
+    const int py = tc.y0 + (int)threadIdx.y;
     if (px >= VR.width || py >= VR.height) return;
     const size_t p = (size_t)py * VR.width + px;
     const unsigned long long key = VR.vis[p];
@@ -945,7 +999,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     if (id != 0) {
         const Sampler smp{&P, s_srgb, s_unorm};
         float o[4];
-        if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o, gbuffer ? aux : nullptr)) {
+        if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) col[k] = o[k];
         }
@@ -971,6 +1025,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
 // k_shade for 4x multisampled views.
 __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ float s_xn[16], s_yn[16];
     __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -980,12 +1035,11 @@ __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     }
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
-    const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
-    const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
-    const int px = (int)(lt % tiles_x) * 16 + threadIdx.x;
-    const int py = (int)(lt / tiles_x) * 16 + threadIdx.y;
+    const TileCoords tc = tile_setup(P, VR, s_xn, s_yn);
+    const int px = tc.x0 + (int)threadIdx.x;
+    const int py = tc.y0 + (int)threadIdx.y;
     if (px >= VR.width || py >= VR.height) return;
-    shade_msaa(P, VR, s_srgb, s_unorm, px, py, (size_t)py * VR.width + px);
+    shade_msaa(P, VR, s_srgb, s_unorm, tc, px, py, (size_t)py * VR.width + px);
 }
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
