@@ -65,7 +65,7 @@ struct FrameReport {
     uint32_t pad1;
     uint32_t errors() const { return shadow_errors | camera_errors; }
 };
-static_assert(sizeof(FrameReport) == 160 && offsetof(FrameReport, camera) == 56, "frame report layout");
+static_assert(sizeof(FrameReport) == 136 && offsetof(FrameReport, camera) == 48, "frame report layout");
 
 // A scene: its slice of the concatenated asset and object arrays, and its surfaces.
 struct SceneHost {
@@ -857,8 +857,6 @@ void launch_camera_raster(rz_ctx* c, PassParams cp, cudaStream_t s) {
         cp.sample_x = kMsaaX[k];
         cp.sample_y = kMsaaY[k];
         cp.sample_plane = (uint32_t)k;
-        // each launch drains the small records through the header's cursor from the start
-        if (k > 0) cudaMemsetAsync(&cp.header->small_cursor, 0, sizeof(uint32_t), s);
         launch_raster(cp, c->sm_count, s);
     }
 }

@@ -138,12 +138,10 @@ struct PassHeader {
     uint32_t chunks;          // ceil(stamps / kChunkStamps), clamped to the capacity
     uint32_t records_needed;  // large records the frame produced (may exceed the capacity)
     uint32_t small_records;   // small records appended (may exceed the capacity)
-    uint32_t small_cursor;    // raster: next small record to take
     uint32_t done;            // setup CTAs finished (unordered passes)
-    uint32_t pad;
     uint64_t alloc;           // unordered passes: (records << 40) | stamps allocated so far
 };
-static_assert(sizeof(PassHeader) == 48, "PassHeader layout");
+static_assert(sizeof(PassHeader) == 40, "PassHeader layout");
 
 // A record is "small" when the triangle's own extent (not its clamped bounding
 // box) is at most kSmallExtent pixels in x and y: one lane rasterises it.

@@ -946,28 +946,25 @@ __device__ __forceinline__ void medium_step(const Target& T, const LargeRecord& 
     }
 }
 
-// Persistent raster: warps first take batches of 32 small records (one per
-// lane) from a shared cursor, then the chunks of kChunkStamps stamps of the
-// large records in a fixed grid-stride order (a shared cursor per chunk would
-// serialise on one L2 line).
+// Persistent raster: each warp first takes batches of 32 small records (one per
+// lane), then chunks of kChunkStamps stamps of the large records, both in a
+// fixed grid-stride order. (A shared cursor that every warp bumps with an
+// atomic serialises on one L2 line: a raster launch with its work skipped took
+// 12 us that way on the 4096^2 shadow pass of 262,144 triangles, 6 us without.)
 template <bool kWriteId>
 __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
     const int lane = threadIdx.x & 31;
     const int lx = lane & (kStampW - 1), ly = lane >> 3;
-    const uint32_t n_small = min(P.header->small_records, P.small_capacity);
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&P.header->small_cursor, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n_small) break;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_small = min(P.header->small_records, P.small_capacity);
+    for (uint64_t base = (uint64_t)warp_id * 32u; base < n_small; base += (uint64_t)warps * 32u)
         if (base + lane < n_small) raster_small<kWriteId>(P, P.small_records + base + lane);
-    }
     const uint32_t chunks = P.header->chunks;
     const uint64_t total = P.header->stamps;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     uint32_t cur_view = 0xffffffffu;  // the view whose target T holds
     Target T{nullptr, 0};
-    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < chunks; k += warps) {
+    for (uint32_t k = warp_id; k < chunks; k += warps) {
         uint64_t s = (uint64_t)k * P.chunk_stamps;
         const uint64_t s_end = (s + P.chunk_stamps < total) ? (s + P.chunk_stamps) : total;
         uint32_t r = P.chunk_map[k];
