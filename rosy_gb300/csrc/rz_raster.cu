@@ -730,9 +730,8 @@ struct LargeRecord {
     uint64_t begin, end;
 };
 
-__device__ __forceinline__ void load_large(const TriRecord* rec, int32_t, LargeRecord& L) {
-    const int4* src = reinterpret_cast<const int4*>(rec);
-    const int4 q0 = __ldg(src), q1 = __ldg(src + 1), q2 = __ldg(src + 2), q3 = __ldg(src + 3);
+// Decodes a large record from its four 16-byte words.
+__device__ __forceinline__ void decode_large(const int4 q0, const int4 q1, const int4 q2, const int4 q3, LargeRecord& L) {
     L.X[0] = q0.x;
     L.Y[0] = q0.y;
     L.X[1] = q0.z;
@@ -765,6 +764,35 @@ __device__ __forceinline__ void load_large(const TriRecord* rec, int32_t, LargeR
     L.medium = (flags & 8u) != 0;
     L.clipped = (flags & 16u) != 0;
     L.near_origin = (flags & 32u) != 0;
+}
+
+__device__ __forceinline__ void load_large(const TriRecord* rec, LargeRecord& L) {
+    const int4* src = reinterpret_cast<const int4*>(rec);
+    decode_large(__ldg(src), __ldg(src + 1), __ldg(src + 2), __ldg(src + 3), L);
+}
+
+// Record staging of the chunk walk: a warp copies the records a chunk starts
+// with (one per lane, kStageRecords at most) into shared memory with cp.async
+// while it rasterises the chunk before, so that a segment finds its record
+// there instead of waiting for a dependent global load.
+constexpr int kRasterThreads = 256;
+constexpr int kStageRecords = 32;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+// Lane `lane` copies record r0 + lane when it exists (below n_rec); one commit
+// group per call, also when it copies nothing.
+__device__ __forceinline__ void stage_records(int4 (*buf)[4], const TriRecord* records, uint32_t r0, uint32_t n_rec,
+                                              int lane) {
+    if ((uint64_t)r0 + (uint64_t)lane < (uint64_t)n_rec) {
+        const int4* src = reinterpret_cast<const int4*>(records + r0 + lane);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cp_async16(&buf[lane][i], src + i);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
 // Edge constants of the generic (64-bit) path.
@@ -952,7 +980,8 @@ __device__ __forceinline__ void medium_step(const Target& T, const LargeRecord& 
 // atomic serialises on one L2 line: a raster launch with its work skipped took
 // 12 us that way on the 4096^2 shadow pass of 262,144 triangles, 6 us without.)
 template <bool kWriteId>
-__global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
+__global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P) {
+    __shared__ int4 s_stage[kRasterThreads / 32][2][kStageRecords][4];
     const int lane = threadIdx.x & 31;
     const int lx = lane & (kStampW - 1), ly = lane >> 3;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -962,16 +991,32 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
         if (base + lane < n_small) raster_small<kWriteId>(P, P.small_records + base + lane);
     const uint32_t chunks = P.header->chunks;
     const uint64_t total = P.header->stamps;
+    const uint32_t n_rec = min(P.header->records, P.record_capacity);  // records the setup wrote
     uint32_t cur_view = 0xffffffffu;  // the view whose target T holds
     Target T{nullptr, 0};
+    // chunk k's first record (r_cur, staged in buffer cb), the next chunk's (r_next)
+    int cb = 0;
+    uint32_t r_cur = warp_id < chunks ? P.chunk_map[warp_id] : n_rec;
+    stage_records(s_stage[threadIdx.x >> 5][0], P.records, r_cur, n_rec, lane);
+    uint32_t r_next = (uint64_t)warp_id + warps < chunks ? P.chunk_map[warp_id + warps] : n_rec;
     for (uint32_t k = warp_id; k < chunks; k += warps) {
         uint64_t s = (uint64_t)k * P.chunk_stamps;
         const uint64_t s_end = (s + P.chunk_stamps < total) ? (s + P.chunk_stamps) : total;
-        uint32_t r = P.chunk_map[k];
+        // stage the next chunk's records while this one is rasterised, and fetch
+        // the chunk map entry of the one after
+        stage_records(s_stage[threadIdx.x >> 5][cb ^ 1], P.records, r_next, n_rec, lane);
+        const uint64_t k_after = (uint64_t)k + 2u * (uint64_t)warps;
+        const uint32_t r_after = k_after < chunks ? P.chunk_map[k_after] : n_rec;
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this lane's copies of chunk k
+        __syncwarp();                                          // and every other lane's
+        int4 (*const st)[4] = s_stage[threadIdx.x >> 5][cb];
+        uint32_t r = r_cur;
         while (s < s_end) {
             if (r >= P.record_capacity) break;
             LargeRecord L;
-            load_large(P.records + r, P.bb_hi, L);
+            const uint32_t j = r - r_cur;
+            if (j < (uint32_t)kStageRecords && r < n_rec) decode_large(st[j][0], st[j][1], st[j][2], st[j][3], L);
+            else load_large(P.records + r, L);
             if (s < L.begin || s >= L.end) {  // cannot happen with a consistent chunk map
                 atomicOr(P.error_flags, kErrStampOverflow);
                 break;
@@ -1011,7 +1056,12 @@ __global__ void __launch_bounds__(256, 3) k_raster(PassParams P) {
             s = seg_end;
             ++r;
         }
+        __syncwarp();  // every lane is done with this buffer before it is staged again
+        r_cur = r_next;
+        r_next = r_after;
+        cb ^= 1;
     }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream) {
@@ -1020,13 +1070,13 @@ void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream) {
     const int t = p.write_id ? 1 : 0;
     if (!occ[t]) {
         int n = 0;
-        if (p.write_id) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<true>, 256, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<false>, 256, 0);
+        if (p.write_id) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<true>, kRasterThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster<false>, kRasterThreads, 0);
         occ[t] = n > 0 ? n : 1;
     }
     const int blocks = sm_count * occ[t];
-    if (p.write_id) k_raster<true><<<blocks, 256, 0, stream>>>(p);
-    else k_raster<false><<<blocks, 256, 0, stream>>>(p);
+    if (p.write_id) k_raster<true><<<blocks, kRasterThreads, 0, stream>>>(p);
+    else k_raster<false><<<blocks, kRasterThreads, 0, stream>>>(p);
     note_launch();
 }
 
