@@ -471,14 +471,21 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     __shared__ uint64_t s_base_recs, s_base_stamps;
     __shared__ uint32_t s_small_warp[kSetupThreads / 32];
     __shared__ uint32_t s_small_base;
-    if (threadIdx.x == 0) s_tile = atomicAdd(&P.header->ticket, 1u);
+    // The ordered list's look-back needs tiles numbered in the order the CTAs
+    // start (a CTA only waits on tiles that have started); the unordered passes
+    // wait on nobody and use the block index, sparing one same-address atomic
+    // per CTA.
+    if (P.ordered && threadIdx.x == 0) s_tile = atomicAdd(&P.header->ticket, 1u);
     // the pass's depth target is zeroed by the same launch: its stores overlap the
     // setup arithmetic, and the raster (the next launch) sees it cleared
     for (uint32_t b = 0; b < P.clear_count; ++b)
         zero_share(P.clear_ptr[b], P.clear_bytes[b], (size_t)blockIdx.x * blockDim.x + threadIdx.x,
                    (size_t)gridDim.x * blockDim.x);
+    const uint32_t tri_ctas = (P.tri_total + kSetupThreads - 1) / kSetupThreads;
+    // CTAs launched only to share the zeroing hold no triangles: done
+    if (!P.ordered && blockIdx.x >= tri_ctas) return;
     __syncthreads();
-    const uint32_t tile = s_tile;
+    const uint32_t tile = P.ordered ? s_tile : blockIdx.x;
     const uint32_t local = tile * kSetupThreads + threadIdx.x;
     const uint32_t tri = P.tri_offset + local;
 
@@ -529,11 +536,12 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(PassParams P) {
     // keeps submission order with a decoupled look-back instead.
     if (!P.ordered) {
         if (threadIdx.x == 0) {
-            const uint64_t old = atomicAdd(reinterpret_cast<unsigned long long*>(&P.header->alloc), (unsigned long long)total);
+            const uint64_t old =
+                total ? atomicAdd(reinterpret_cast<unsigned long long*>(&P.header->alloc), (unsigned long long)total) : 0ull;
             s_base_recs = old >> kStampBits;
             s_base_stamps = old & kStampMask;
             __threadfence();
-            if (atomicAdd(&P.header->done, 1u) == gridDim.x - 1) {
+            if (atomicAdd(&P.header->done, 1u) == tri_ctas - 1) {
                 // last CTA: publish the totals for the raster and the host
                 const uint64_t fin = atomicAdd(reinterpret_cast<unsigned long long*>(&P.header->alloc), 0ull);
                 const uint64_t recs = fin >> kStampBits, st = fin & kStampMask;
@@ -627,8 +635,8 @@ void launch_setup(const PassParams& p, cudaStream_t stream) {
     if (ctas == 0) return;
     if (!p.ordered && p.clear_count) {
         // the depth target zeroed by this launch wants more CTAs than few triangles give
-        // (about 32 KB each); the extra CTAs draw tickets past the last triangle and set
-        // up nothing (the ordered list's look-back has one status word per triangle tile)
+        // (about 32 KB each); the extra CTAs, past the last triangle tile, only zero
+        // (the ordered list's look-back has one status word per triangle tile)
         size_t most = 0;
         for (uint32_t b = 0; b < p.clear_count; ++b) most = p.clear_bytes[b] > most ? p.clear_bytes[b] : most;
         const size_t want = std::min<size_t>(most / 32768, 4096);
