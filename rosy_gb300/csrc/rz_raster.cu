@@ -24,6 +24,7 @@
 //    depth, and among equal depths the last triangle submitted. The shadow map
 //    is a 32-bit atomicMax on the depth bits.
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 
 #include "rz_device.cuh"
@@ -281,7 +282,7 @@ __device__ __forceinline__ int make_record(const SV& v0, const SV& v1, const SV&
     r.z0 = v0.z;
     r.dzdx = dzdx;
     r.dzdy = dzdy;
-    r.bias = o;
+    r.bias = o + 0.0f;  // -0 -> +0 (biased_depth relies on it; the sums are unchanged)
     r.p0 = (uint32_t)px0 | ((uint32_t)py0 << 16);
     r.p1 = (uint32_t)px1 | ((uint32_t)py1 << 16);
     r.id = id;
@@ -670,17 +671,40 @@ __device__ __forceinline__ Target view_target(const PassParams& P, uint32_t view
                   V.shadow_w};
 }
 
+// The stored depth of a fragment: the interpolated z plus the record's depth bias
+// (+0 in the camera pass), saturated to [0, 1] in the same instruction. The
+// saturation maps NaN and every value <= 0 to +0 and every value >= 1 to 1; the
+// sum is never -0 because the bias is never -0 (make_record), so this equals
+// adding the bias and then clamping with NaN -> 0.
+__device__ __forceinline__ float biased_depth(float z, float bias) {
+    float r;
+    asm("add.rn.sat.f32 %0, %1, %2;" : "=f"(r) : "f"(z), "f"(bias));
+    return r;
+}
+
+// The pixel's word of the target: u64 visibility key or u32 depth bits.
 template <bool kWriteId>
-__device__ __forceinline__ void write_fragment(const Target& T, int px, int py, float z, uint32_t id) {
-    if (!(z > 0.0f)) z = 0.0f;
-    if (z > 1.0f) z = 1.0f;
-    const size_t p = (size_t)py * (size_t)T.pitch + (size_t)px;
+using TargetWord = typename std::conditional<kWriteId, unsigned long long, unsigned int>::type;
+
+template <bool kWriteId>
+__device__ __forceinline__ TargetWord<kWriteId>* target_word(const Target& T, int px, int py) {
+    return reinterpret_cast<TargetWord<kWriteId>*>(T.ptr) + ((size_t)py * (size_t)T.pitch + (size_t)px);
+}
+
+// The depth test and write: atomicMax of the fragment's key (z = biased_depth).
+template <bool kWriteId>
+__device__ __forceinline__ void write_word(TargetWord<kWriteId>* w, float z, uint32_t id) {
     if (kWriteId) {
         const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
-        atomicMax(reinterpret_cast<unsigned long long*>(T.ptr) + p, key);
+        atomicMax(reinterpret_cast<unsigned long long*>(w), key);
     } else {
-        atomicMax(reinterpret_cast<unsigned int*>(T.ptr) + p, __float_as_uint(z));
+        atomicMax(reinterpret_cast<unsigned int*>(w), __float_as_uint(z));
     }
+}
+
+template <bool kWriteId>
+__device__ __forceinline__ void write_fragment(const Target& T, int px, int py, float z, uint32_t id) {
+    write_word<kWriteId>(target_word<kWriteId>(T, px, py), z, id);
 }
 
 // One lane rasterises one small triangle: its extent is at most the pass's
@@ -715,8 +739,7 @@ __device__ __forceinline__ void raster_small(const PassParams& P, const TriRecor
             const int32_t e1 = c[1] + dx[1] * ry - dy[1] * rx;
             const int32_t e2 = c[2] + dx[2] * ry - dy[2] * rx;
             if ((e0 | e1 | e2) >= 0) {
-                float z = fmaf(dzdx, (float)rx, fmaf(dzdy, (float)ry, z0));
-                if (!kWriteId) z = z + bias;
+                const float z = biased_depth(fmaf(dzdx, (float)rx, fmaf(dzdy, (float)ry, z0)), bias);
                 write_fragment<kWriteId>(T, px, py, z, id);
             }
         }
@@ -910,30 +933,31 @@ __device__ __forceinline__ void raster_stamp(const Target& T, const LargeRecord&
         fx = (float)(px * 256 + ox - L.X0);
         fy = (float)(py * 256 + oy - L.Y0);
     }
-    float z = fmaf(L.dzdx, fx, fmaf(L.dzdy, fy, L.z0));
-    if (!kWriteId) z = z + L.bias;
+    const float z = biased_depth(fmaf(L.dzdx, fx, fmaf(L.dzdy, fy, L.z0)), L.bias);
     write_fragment<kWriteId>(T, px, py, z, L.id);
 }
 
 // Incremental walk over the stamps of a medium record in raster order. Each
-// lane holds its edge values and its float offsets from vertex 0; moving one
-// stamp right adds a constant, moving to the next stamp row restarts from the
-// row's first stamp. The float offsets stay exact integers below 2^24, so the
-// depth is bit-identical to fma(dzdx, (float)(PX-X0), fma(dzdy, (float)(PY-Y0), z0)).
+// lane holds its edge values, its float offsets from vertex 0 and the address of
+// its pixel's word; moving one stamp right adds a constant, moving to the next
+// stamp row restarts from the row's first stamp. The float offsets stay exact
+// integers below 2^24, so the depth is bit-identical to
+// fma(dzdx, (float)(PX-X0), fma(dzdy, (float)(PY-Y0), z0)).
+template <bool kWriteId>
 struct MediumWalk {
     int32_t e[3], er[3], stepx[3], stepy[3];
     float fx, fxr, fy, zrow;
     int px, pxr, py;
-    uint32_t sx, sy;
+    TargetWord<kWriteId>* w;   // the lane's pixel in the current stamp
+    TargetWord<kWriteId>* wr;  // and in the row's first stamp
 };
 
 // Edge values relative to vertex 0 in wrapping 32-bit arithmetic: for a medium
 // triangle the true value at every pixel of the walk fits in int32, so the
 // wrapped result equals it.
-__device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, uint32_t sy, int lx, int ly, int32_t ox,
-                                             int32_t oy, MediumWalk& w) {
-    w.sx = sx;
-    w.sy = sy;
+template <bool kWriteId>
+__device__ __forceinline__ void medium_start(const Target& T, const LargeRecord& L, uint32_t sx, uint32_t sy, int lx, int ly,
+                                             int32_t ox, int32_t oy, MediumWalk<kWriteId>& w) {
     w.pxr = L.px0 + lx;
     w.px = w.pxr + (int)sx * kStampW;
     w.py = L.py0 + (int)sy * kStampH + ly;
@@ -952,33 +976,44 @@ __device__ __forceinline__ void medium_start(const LargeRecord& L, uint32_t sx, 
     w.fxr = (float)rxr;
     w.fy = (float)ry;
     w.zrow = fmaf(L.dzdy, w.fy, L.z0);
+    w.wr = target_word<kWriteId>(T, w.pxr, w.py);
+    w.w = w.wr + (int)sx * kStampW;
 }
 
+// n stamps of the walk from stamp column sx: runs along a stamp row, then the
+// move to the next row.
 template <bool kWriteId, bool kBoxCheck>
-__device__ __forceinline__ void medium_step(const Target& T, const LargeRecord& L, MediumWalk& w) {
-    if (((w.e[0] | w.e[1] | w.e[2]) >= 0) && (!kBoxCheck || (w.px <= L.px1 && w.py <= L.py1))) {
-        float z = fmaf(L.dzdx, w.fx, w.zrow);
-        if (!kWriteId) z = z + L.bias;
-        write_fragment<kWriteId>(T, w.px, w.py, z, L.id);
-    }
-    if (++w.sx == L.nsx) {
-        w.sx = 0;
-        ++w.sy;
+__device__ __forceinline__ void medium_walk(const Target& T, const LargeRecord& L, uint32_t sx, uint32_t n,
+                                            MediumWalk<kWriteId>& w) {
+    const size_t row_step = (size_t)kStampH * (size_t)T.pitch;
+    while (true) {
+        const uint32_t run = min(n, L.nsx - sx);
+        for (uint32_t j = 0; j < run; ++j) {
+            if (((w.e[0] | w.e[1] | w.e[2]) >= 0) && (!kBoxCheck || (w.px <= L.px1 && w.py <= L.py1)))
+                write_word<kWriteId>(w.w, biased_depth(fmaf(L.dzdx, w.fx, w.zrow), L.bias), L.id);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) w.e[i] = (int32_t)((uint32_t)w.e[i] + (uint32_t)w.stepx[i]);
+            w.w += kStampW;
+            w.fx += (float)(kStampW * 256);
+            if (kBoxCheck) w.px += kStampW;
+        }
+        n -= run;
+        if (n == 0) return;
+        sx = 0;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             w.er[i] = (int32_t)((uint32_t)w.er[i] + (uint32_t)w.stepy[i]);
             w.e[i] = w.er[i];
         }
-        w.px = w.pxr;
-        w.py += kStampH;
+        w.wr += row_step;
+        w.w = w.wr;
         w.fx = w.fxr;
         w.fy += (float)(kStampH * 256);
         w.zrow = fmaf(L.dzdy, w.fy, L.z0);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 3; ++i) w.e[i] = (int32_t)((uint32_t)w.e[i] + (uint32_t)w.stepx[i]);
-        w.px += kStampW;
-        w.fx += (float)(kStampW * 256);
+        if (kBoxCheck) {
+            w.px = w.pxr;
+            w.py += kStampH;
+        }
     }
 }
 
@@ -1038,12 +1073,10 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(PassParams P) {
                 cur_view = L.view;
             }
             if (L.medium) {
-                MediumWalk w;
-                medium_start(L, sx, sy, lx, ly, P.sample_x, P.sample_y, w);
-                if (L.clipped)
-                    for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId, true>(T, L, w);
-                else
-                    for (uint32_t j = 0; j < n; ++j) medium_step<kWriteId, false>(T, L, w);
+                MediumWalk<kWriteId> w;
+                medium_start<kWriteId>(T, L, sx, sy, lx, ly, P.sample_x, P.sample_y, w);
+                if (L.clipped) medium_walk<kWriteId, true>(T, L, sx, n, w);
+                else medium_walk<kWriteId, false>(T, L, sx, n, w);
             } else {
                 GenericEdges G;
                 generic_edges(L, G);

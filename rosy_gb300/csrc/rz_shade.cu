@@ -324,10 +324,19 @@ __device__ __forceinline__ void sample_coords(const TexDesc& t, SamplerBits st, 
     }
 }
 
+// byte / 255 rounded to nearest: the product with the rounded reciprocal and one
+// residual step, exact for every byte (it equals the IEEE quotient, as a table
+// of (float)b / 255.0f would, without the shared-memory lookup and its bank
+// conflicts).
+__device__ __forceinline__ float unorm8(uint32_t b) {
+    const float x = (float)b, r = 1.0f / 255.0f;
+    const float q = x * r;
+    return fmaf(fmaf(-q, 255.0f, x), r, q);
+}
+
 struct Sampler {
     const ShadeParams* P;
     const float* srgb;   // shared-memory table: sRGB byte -> linear
-    const float* unorm;  // shared-memory table: byte -> byte / 255
 
     __device__ __forceinline__ void texel(const TexDesc& t, uint32_t off, int w, int i, int j, float out[4]) const {
         const uint32_t v = __ldg(reinterpret_cast<const uint32_t*>(t.base) + off + (uint32_t)j * (uint32_t)w + (uint32_t)i);
@@ -337,11 +346,11 @@ struct Sampler {
             out[1] = srgb[g];
             out[2] = srgb[b];
         } else {
-            out[0] = unorm[r];
-            out[1] = unorm[g];
-            out[2] = unorm[b];
+            out[0] = unorm8(r);
+            out[1] = unorm8(g);
+            out[2] = unorm8(b);
         }
-        out[3] = unorm[a];
+        out[3] = unorm8(a);
     }
 
     __device__ __forceinline__ void fetch_level(const TexDesc& t, const LevelCoords& c, bool linear, float out[4]) const {
@@ -890,7 +899,7 @@ __device__ __forceinline__ float resolve4(float a, float b, float c, float d) {
 // samples are resolved and encoded here; with them they go to the RGBA16F
 // sample planes for k_blend. The depth output is sample 0's.
 __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& VR, const float* s_srgb,
-                                           const float* s_unorm, const TileCoords& tc, int px, int py, size_t p) {
+                                           const TileCoords& tc, int px, int py, size_t p) {
     const size_t plane = (size_t)VR.width * VR.height;
     uint32_t ids[kMsaaSamples];
     unsigned long long key0 = 0;
@@ -901,7 +910,7 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
         ids[k] = (uint32_t)key;
     }
     float cs[kMsaaSamples][4];
-    const Sampler smp{&P, s_srgb, s_unorm};
+    const Sampler smp{&P, s_srgb};
     const bool gbuffer = VR.gb_albedo != nullptr;
     float gs[kMsaaSamples][6];  // G-buffer values per sample (albedo rgb, normal xyz)
 #pragma unroll
@@ -975,13 +984,12 @@ __device__ __forceinline__ TileCoords tile_setup(const ShadeParams& P, const Vie
 }
 
 __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
-    __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ float s_srgb[256];
     __shared__ float s_xn[16], s_yn[16];
     __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
         s_srgb[t] = P.srgb_table[t];
-        s_unorm[t] = (float)t / 255.0f;
         if (t == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
     }
     __syncthreads();
@@ -997,7 +1005,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     const bool gbuffer = VR.gb_albedo != nullptr;
     float aux[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     if (id != 0) {
-        const Sampler smp{&P, s_srgb, s_unorm};
+        const Sampler smp{&P, s_srgb};
         float o[4];
         if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
 #pragma unroll
@@ -1024,13 +1032,12 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
 
 // k_shade for 4x multisampled views.
 __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
-    __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ float s_srgb[256];
     __shared__ float s_xn[16], s_yn[16];
     __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
         s_srgb[t] = P.srgb_table[t];
-        s_unorm[t] = (float)t / 255.0f;
         if (t == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
     }
     __syncthreads();
@@ -1039,7 +1046,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     const int px = tc.x0 + (int)threadIdx.x;
     const int py = tc.y0 + (int)threadIdx.y;
     if (px >= VR.width || py >= VR.height) return;
-    shade_msaa(P, VR, s_srgb, s_unorm, tc, px, py, (size_t)py * VR.width + px);
+    shade_msaa(P, VR, s_srgb, tc, px, py, (size_t)py * VR.width + px);
 }
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
@@ -1311,14 +1318,13 @@ __device__ __forceinline__ bool debug_covers(const DebugSeg& s, int32_t PX, int3
 }
 
 __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
-    __shared__ float s_srgb[256], s_unorm[256];
+    __shared__ float s_srgb[256];
     __shared__ uint32_t s_list[kBlendBatch];
     __shared__ uint32_t s_count[256 / 32 + 1];
     __shared__ uint32_t s_view;
     const ShadeParams& P = B.sh;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     s_srgb[tid] = P.srgb_table[tid];
-    s_unorm[tid] = (float)tid / 255.0f;
     if (tid == 0) s_view = tile_view(P.views, P.view_count, blockIdx.x + P.block_offset);
     __syncthreads();
     const uint32_t view = s_view;
@@ -1349,7 +1355,7 @@ __global__ void __launch_bounds__(256) k_blend(BlendParams B) {
             dst_depth[k] = nsamples > 1 ? __uint_as_float((uint32_t)(VR.vis[p + k * plane] >> 32)) : VR.depth[p];
         }
     }
-    const Sampler smp{&P, s_srgb, s_unorm};
+    const Sampler smp{&P, s_srgb};
     // a pass whose look-back gave up has records at unreliable slots: blend none of them
     const bool records_ok = !B.error_flags || !(*B.error_flags & kErrLookbackTimeout);
     const uint32_t n = records_ok ? min(B.header->records, B.record_capacity) : 0u;
