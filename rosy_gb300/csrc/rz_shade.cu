@@ -528,6 +528,13 @@ __device__ __forceinline__ const float* select_cascade(const ViewRec& VR, const 
 }
 
 // fragmentMain, src/shaders/basic.slang:137-344. Returns false on discard.
+// kLit: the caller has checked that the view renders the default output
+// (fragment_output 0) with the light, its shadow and the BRDF on, so those
+// branches are taken without testing them and the debug outputs are not
+// compiled into this copy. A view takes the same branches at every pixel, and
+// the shading kernel runs the specialised copy for such views: the code its
+// warps execute is then smaller (fewer instruction-fetch stalls).
+template <bool kLit = false>
 __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const GpuMaterial* md, const Frag& bv,
                               const Sampler& smp, float out[4], float* albedo = nullptr) {
     const V3 ambientLight{sd.ambient_color[0], sd.ambient_color[1], sd.ambient_color[2]};
@@ -580,7 +587,7 @@ __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const 
     const float nDotV = clamp01(dot(N, V));
     V3 c3;
     bool set = true;
-    switch (sd.fragment_output) {
+    switch (kLit ? 0u : sd.fragment_output) {
         case 0: c3 = V3{imageTextureColor[0], imageTextureColor[1], imageTextureColor[2]}; break;
         case 1: c3 = fnormalize(bv.worldNormal) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
         case 2: c3 = fnormalize(bv.tangent) * 0.5f + V3{0.5f, 0.5f, 0.5f}; break;
@@ -605,15 +612,15 @@ __device__ bool fragment_main(const ViewRec& VR, const rz_scene_data& sd, const 
         outFragColor[2] = c3.z;
         outFragColor[3] = alpha;
     }
-    if (sd.light_enabled > 0) {
+    if (kLit || sd.light_enabled > 0) {
         float shadowFactor = 1.0f;
-        if (sd.shadows_enabled == 1)
+        if (kLit || sd.shadows_enabled == 1)
         {
             float cc[4];
             const float* map = select_cascade(VR, bv.csm, cc);
             shadowFactor = pcf(map, VR.shadow_w, cc, VR.pcf_mode);
         }
-        if (sd.brdf_lighting_enabled == 0) {
+        if (!kLit && sd.brdf_lighting_enabled == 0) {
             const float ml = fmaxf(cosTheta, 0.0f);
             const V3 sunLight{sd.sunlight_color[0] * ml, sd.sunlight_color[1] * ml, sd.sunlight_color[2] * ml};
             outFragColor[0] = outFragColor[0] * fmaxf(ambientLight.x, sunLight.x * shadowFactor);
@@ -736,6 +743,7 @@ void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stre
 // With `aux` non-null it also returns the G-buffer values: albedo (the sampled
 // base colour, rgb) and the interpolated world-space normal (normalised, xyz).
 // With `tc` non-null the pixel lies in that tile and its coordinates come from there.
+template <bool kLit = false>
 __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_scene_data& sd, const Sampler& smp, uint32_t tri,
                             int px, int py, float out[4], float* aux = nullptr, const TileCoords* tc = nullptr) {
     uint32_t d;
@@ -784,7 +792,7 @@ __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_sc
     barycentrics_n(clip[0], clip[1], clip[2], xq, yq, bq0);
     barycentrics_n(clip[0], clip[1], clip[2], xq1, yq, bqx);
     barycentrics_n(clip[0], clip[1], clip[2], xq, yq1, bqy);
-    const bool debug_extra = sd.fragment_output == 1 || sd.fragment_output == 7 || aux != nullptr;
+    const bool debug_extra = (!kLit && (sd.fragment_output == 1 || sd.fragment_output == 7)) || aux != nullptr;
     Frag f;
     float u0[2], ux[2], uy[2];
 #pragma unroll
@@ -854,7 +862,13 @@ __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_sc
         aux[4] = n.y;
         aux[5] = n.z;
     }
-    return fragment_main(VR, sd, md, f, smp, out, aux);
+    return fragment_main<kLit>(VR, sd, md, f, smp, out, aux);
+}
+
+// Whether a view renders the default output with the light, its shadow and the
+// BRDF on (the branches fragment_main<true> takes without testing).
+__device__ __forceinline__ bool lit_view(const rz_scene_data& sd) {
+    return sd.fragment_output == 0 && sd.light_enabled > 0 && sd.shadows_enabled == 1 && sd.brdf_lighting_enabled != 0;
 }
 
 // Octahedral encoding of a unit vector into two f16 (x in the low half).
@@ -898,6 +912,7 @@ __device__ __forceinline__ float resolve4(float a, float b, float c, float d) {
 // covers; uncovered samples keep the clear colour. Without blended surfaces the
 // samples are resolved and encoded here; with them they go to the RGBA16F
 // sample planes for k_blend. The depth output is sample 0's.
+template <bool kLit>
 __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& VR, const float* s_srgb,
                                            const TileCoords& tc, int px, int py, size_t p) {
     const size_t plane = (size_t)VR.width * VR.height;
@@ -930,7 +945,7 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
         }
         if (ids[k] != 0) {
             float o[4];
-            if (shade_pixel(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
+            if (shade_pixel<kLit>(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) c[i] = o[i];
             }
@@ -1007,7 +1022,10 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     if (id != 0) {
         const Sampler smp{&P, s_srgb};
         float o[4];
-        if (shade_pixel(P, VR, *VR.scene, smp, id - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
+        const rz_scene_data& sd = *VR.scene;
+        float* const ax = gbuffer ? aux : nullptr;
+        if (lit_view(sd) ? shade_pixel<true>(P, VR, sd, smp, id - 1u, px, py, o, ax, &tc)
+                         : shade_pixel<false>(P, VR, sd, smp, id - 1u, px, py, o, ax, &tc)) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) col[k] = o[k];
         }
@@ -1046,7 +1064,8 @@ __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     const int px = tc.x0 + (int)threadIdx.x;
     const int py = tc.y0 + (int)threadIdx.y;
     if (px >= VR.width || py >= VR.height) return;
-    shade_msaa(P, VR, s_srgb, tc, px, py, (size_t)py * VR.width + px);
+    if (lit_view(*VR.scene)) shade_msaa<true>(P, VR, s_srgb, tc, px, py, (size_t)py * VR.width + px);
+    else shade_msaa<false>(P, VR, s_srgb, tc, px, py, (size_t)py * VR.width + px);
 }
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
