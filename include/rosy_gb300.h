@@ -318,17 +318,20 @@ int rz_render(struct rz_ctx* ctx);
  * RZ_GRAPHICS_FRAME_FAILURE if the device flagged an error in a frame. */
 int rz_sync(struct rz_ctx* ctx, uint32_t timeout_ms);
 
-/* Device pointers of the frame buffers (valid until the next rz_resize/rz_destroy). */
+/* Device pointers of the buffers of the frame rendered last (valid until the
+ * next rz_resize/rz_destroy). The colour and depth targets are double-buffered:
+ * frames alternate between two target sets, so color_rgba8 and depth_f32
+ * change from one frame to the next; take them after each frame. */
 int rz_get_frame(struct rz_ctx* ctx, rz_frame_out* out);
 
 /* Enqueues device-to-host copies of the colour (width*height*4 bytes) and/or
  * depth (width*height*4 bytes) images of the frame rendered last; NULL skips
- * one. The images are first copied on the device into one of two staging
- * buffers (after the frame), then to the host on a copy stream of the context,
- * so the next frame renders while they travel (the reference keeps several
- * frames in flight, src/Engine/Graphics.cpp:177, and presents asynchronously).
- * The host buffers are complete after rz_sync, or after rz_read_sync. The first
- * call (or a larger frame) allocates the staging buffers. */
+ * one. They are copied straight from the frame's target set on a copy stream of
+ * the context, after the frame, while the next frame renders into the other
+ * set (the reference keeps several frames in flight, src/Engine/Graphics.cpp:177,
+ * and presents asynchronously); the frame after that, which renders into the
+ * same set again, waits for the copies. The host buffers are complete after
+ * rz_sync, or after rz_read_sync. */
 int rz_read_frame(struct rz_ctx* ctx, void* color_host, size_t color_bytes,
                   void* depth_host, size_t depth_bytes);
 

@@ -97,9 +97,11 @@ struct rz_ctx {
     // read-back (rz_read_frame): device staging copies on the frame stream, then
     // device-to-host copies on their own stream so that the next frame renders meanwhile
     cudaStream_t copy_stream = nullptr;
-    unsigned char* d_read_stage[2] = {nullptr, nullptr};
-    size_t read_stage_capacity = 0;
-    cudaEvent_t read_staged[2] = {nullptr, nullptr}, read_done[2] = {nullptr, nullptr};
+    // read-back (rz_read_frame): the D2H copies of a frame's colour and depth,
+    // which are read straight from its target set, one completion event per set
+    cudaEvent_t read_done[2] = {nullptr, nullptr};
+    bool read_issued[2] = {false, false};
+    uint32_t read_newest = 0;     // target set of the newest read-back
     uint64_t reads_issued = 0;
     cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t camera_done = nullptr, sources_done = nullptr;  // the side branch of the G-buffer's sub-pixel sources
@@ -140,8 +142,15 @@ struct rz_ctx {
     rz_scene_data* h_scene_data = nullptr;  // pinned staging, one per view
     uint32_t scene_data_capacity = 0;
     cudaEvent_t scene_copied = nullptr;
-    ViewRec* d_views = nullptr;
-    std::vector<ViewRec> view_recs;
+    // The colour and depth targets are double-buffered: frames alternate between
+    // two target sets, so the read-back of one frame copies its images to the
+    // host while the next frame renders into the other set. Each set has its
+    // view table (whose ViewRec.color / .depth point into it) and its frame graph.
+    ViewRec* d_views = nullptr;          // the view table of the frame being enqueued
+    ViewRec* d_views_set[2] = {nullptr, nullptr};
+    uint32_t parity = 0;                 // target set of the next frame
+    uint32_t last_parity = 0;            // target set of the last frame enqueued
+    std::vector<ViewRec> view_recs;      // target set 0
     std::vector<uint32_t> view_id_base;  // first opaque triangle id of each view
     // per-view ranges for sequential launches
     struct ViewRange {
@@ -186,7 +195,7 @@ struct rz_ctx {
     bool grow_records = false, grow_chunks = false;
 
     // frame sequencing
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph_set[2] = {nullptr, nullptr};  // one per target set
     bool graph_dirty = true;
     bool use_graph = true;
     cudaEvent_t frame_done = nullptr;
@@ -225,8 +234,10 @@ int cuda_fail(rz_ctx* ctx, cudaError_t e, const char* what) {
     } while (0)
 
 void drop_graph(rz_ctx* c) {
-    if (c->graph) cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        if (c->graph_set[k]) cudaGraphExecDestroy(c->graph_set[k]);
+        c->graph_set[k] = nullptr;
+    }
     c->graph_dirty = true;
 }
 
@@ -522,6 +533,7 @@ uint32_t cascades_of(const ViewHost& v) {
 int build_layout(rz_ctx* c) {
     if (c->views.empty()) return fail(c, RZ_INVALID_STATE, "no views");
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->copy_stream);  // read-backs copy straight from the targets
     drop_graph(c);
     // pools
     size_t pix = 0, shadow = 0;
@@ -604,10 +616,10 @@ int build_layout(rz_ctx* c) {
         dfree(c->d_depth);
         c->pix_capacity = 0;
         RZ_CUDA(c, dalloc(&c->d_vis, pix * c->samples), "visibility buffers");
-        RZ_CUDA(c, dalloc(&c->d_color, pix), "colour buffers");
-        RZ_CUDA(c, dalloc(&c->d_depth, pix), "depth buffers");
-        RZ_CUDA(c, cudaMemset(c->d_color, 0, pix * 4), "clear colour");
-        RZ_CUDA(c, cudaMemset(c->d_depth, 0, pix * 4), "clear depth");
+        RZ_CUDA(c, dalloc(&c->d_color, 2 * pix), "colour buffers");
+        RZ_CUDA(c, dalloc(&c->d_depth, 2 * pix), "depth buffers");
+        RZ_CUDA(c, cudaMemset(c->d_color, 0, 2 * pix * 4), "clear colour");
+        RZ_CUDA(c, cudaMemset(c->d_depth, 0, 2 * pix * 4), "clear depth");
         c->pix_capacity = pix;
     }
     if (shadow > c->shadow_capacity) {
@@ -681,7 +693,8 @@ int build_layout(rz_ctx* c) {
         r.gb_sources = (c->gbuffer && c->samples == 1) ? c->d_gb_sources + pix_off[vi] : nullptr;
         c->view_recs[vi] = r;
     }
-    dfree(c->d_views);
+    for (int k = 0; k < 2; ++k) dfree(c->d_views_set[k]);
+    c->d_views = nullptr;
     dfree(c->d_shadow_draws);
     dfree(c->d_opaque_draws);
     dfree(c->d_blended_draws);
@@ -690,7 +703,7 @@ int build_layout(rz_ctx* c) {
     dfree(c->d_blended_consts);
     dfree(c->d_varyings);
     dfree(c->d_tri_refs);
-    RZ_CUDA(c, dalloc(&c->d_views, c->view_recs.size()), "view table");
+    for (int k = 0; k < 2; ++k) RZ_CUDA(c, dalloc(&c->d_views_set[k], c->view_recs.size()), "view table");
     RZ_CUDA(c, dalloc(&c->d_shadow_draws, std::max<size_t>(shadow_list.size(), 1)), "shadow draw list");
     RZ_CUDA(c, dalloc(&c->d_opaque_draws, std::max<size_t>(opaque.size(), 1)), "opaque draw list");
     RZ_CUDA(c, dalloc(&c->d_blended_draws, std::max<size_t>(blended.size(), 1)), "blended draw list");
@@ -699,8 +712,18 @@ int build_layout(rz_ctx* c) {
     RZ_CUDA(c, dalloc(&c->d_blended_consts, std::max<size_t>(blended.size(), 1)), "blended constants");
     RZ_CUDA(c, dalloc(&c->d_varyings, std::max<size_t>((size_t)varyings, 1) * 8), "varying records");
     RZ_CUDA(c, dalloc(&c->d_tri_refs, std::max<size_t>((size_t)opaque_tris, 1)), "triangle references");
-    RZ_CUDA(c, cudaMemcpy(c->d_views, c->view_recs.data(), c->view_recs.size() * sizeof(ViewRec), cudaMemcpyHostToDevice),
-            "upload views");
+    for (int k = 0; k < 2; ++k) {
+        std::vector<ViewRec> set = c->view_recs;
+        for (ViewRec& r : set) {
+            r.color += (size_t)k * pix;
+            r.depth += (size_t)k * pix;
+        }
+        RZ_CUDA(c, cudaMemcpy(c->d_views_set[k], set.data(), set.size() * sizeof(ViewRec), cudaMemcpyHostToDevice),
+                "upload views");
+    }
+    c->d_views = c->d_views_set[0];
+    c->parity = 0;
+    c->last_parity = 0;
     if (!shadow_list.empty())
         RZ_CUDA(c, cudaMemcpy(c->d_shadow_draws, shadow_list.data(), shadow_list.size() * sizeof(DrawRec), cudaMemcpyHostToDevice), "upload draws");
     if (!opaque.empty())
@@ -1085,8 +1108,8 @@ int grow_queues(rz_ctx* c) {
 rz_frame_out frame_of(rz_ctx* c, uint32_t v) {
     rz_frame_out o{};
     const ViewRec& r = c->view_recs[v];
-    o.color_rgba8 = r.color;
-    o.depth_f32 = r.depth;
+    o.color_rgba8 = r.color + (size_t)c->last_parity * c->pix_total;
+    o.depth_f32 = r.depth + (size_t)c->last_parity * c->pix_total;
     o.visibility_u64 = r.vis;
     o.shadow_map_f32 = r.shadow;
     o.width = (uint32_t)r.width;
@@ -1186,8 +1209,7 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
     for (int k = 0; k < 2; ++k)
-        if (cudaEventCreateWithFlags(&c->read_staged[k], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->read_done[k], cudaEventDisableTiming) != cudaSuccess)
+        if (cudaEventCreateWithFlags(&c->read_done[k], cudaEventDisableTiming) != cudaSuccess)
             return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
@@ -1232,6 +1254,7 @@ void rz_destroy(rz_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     drop_graph(c);
     free_asset(c);
     free_pass(c->shadow_pass);
@@ -1246,7 +1269,7 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_objects);
     dfree(c->d_srgb);
     dfree(c->d_scene_data);
-    dfree(c->d_views);
+    for (int k = 0; k < 2; ++k) dfree(c->d_views_set[k]);
     dfree(c->d_vis);
     dfree(c->d_color);
     dfree(c->d_depth);
@@ -1281,9 +1304,7 @@ void rz_destroy(rz_ctx* c) {
     if (c->sources_done) cudaEventDestroy(c->sources_done);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     for (int k = 0; k < 2; ++k) {
-        if (c->read_staged[k]) cudaEventDestroy(c->read_staged[k]);
         if (c->read_done[k]) cudaEventDestroy(c->read_done[k]);
-        if (c->d_read_stage[k]) cudaFree(c->d_read_stage[k]);
     }
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->side) cudaStreamDestroy(c->side);
@@ -1446,6 +1467,16 @@ int rz_update_view(rz_ctx* c, uint32_t view, const rz_scene_data* scene) {
 
 int rz_update(rz_ctx* c, const rz_scene_data* scene) { return rz_update_view(c, 0, scene); }
 
+// After a frame is enqueued: its completion event, and the next frame's target set.
+int frame_enqueued(rz_ctx* c) {
+    RZ_CUDA(c, cudaEventRecord(c->frame_done, c->stream), "record frame");
+    c->frame_pending = true;
+    ++c->frames;
+    c->last_parity = c->parity;
+    c->parity ^= 1u;
+    return RZ_OK;
+}
+
 int rz_render(rz_ctx* c) {
     const int ready = check_ready(c);
     if (ready != RZ_OK) return ready;
@@ -1462,9 +1493,15 @@ int rz_render(rz_ctx* c) {
         const int rc = grow_queues(c);
         if (rc != RZ_OK) return rc;
     }
+    // The frame renders into target set `parity`: the read-back of the frame that
+    // last rendered there has to have landed first.
+    if (c->read_issued[c->parity])
+        RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->read_done[c->parity], 0), "read-back of the target set");
+    c->d_views = c->d_views_set[c->parity];
+    cudaGraphExec_t& graph = c->graph_set[c->parity];
     // Stage timing records events between the stages and enqueues directly.
     if (c->use_graph && !c->timing) {
-        if (c->graph_dirty || !c->graph) {
+        if (!graph) {
             cudaGraph_t g = nullptr;
             RZ_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             const int rc = enqueue_frame(c);
@@ -1474,31 +1511,25 @@ int rz_render(rz_ctx* c) {
                 return rc;
             }
             cudaError_t ie = e;
-            if (e == cudaSuccess) ie = cudaGraphInstantiate(&c->graph, g, 0);
+            if (e == cudaSuccess) ie = cudaGraphInstantiate(&graph, g, 0);
             if (g) cudaGraphDestroy(g);
             if (ie != cudaSuccess) {
                 // capture of this frame shape is not supported here: enqueue directly from now on
                 cudaGetLastError();
-                c->graph = nullptr;
+                graph = nullptr;
                 c->use_graph = false;
                 const int rc2 = enqueue_frame(c);
                 if (rc2 != RZ_OK) return rc2;
-                RZ_CUDA(c, cudaEventRecord(c->frame_done, c->stream), "record frame");
-                c->frame_pending = true;
-                ++c->frames;
-                return RZ_OK;
+                return frame_enqueued(c);
             }
             c->graph_dirty = false;
         }
-        RZ_CUDA(c, cudaGraphLaunch(c->graph, c->stream), "launch frame graph");
+        RZ_CUDA(c, cudaGraphLaunch(graph, c->stream), "launch frame graph");
     } else {
         const int rc = enqueue_frame(c);
         if (rc != RZ_OK) return rc;
     }
-    RZ_CUDA(c, cudaEventRecord(c->frame_done, c->stream), "record frame");
-    c->frame_pending = true;
-    ++c->frames;
-    return RZ_OK;
+    return frame_enqueued(c);
 }
 
 int rz_sync(rz_ctx* c, uint32_t timeout_ms) {
@@ -1582,8 +1613,8 @@ int rz_get_view_gbuffer(rz_ctx* c, uint32_t view, rz_gbuffer* out) {
     if (c->layout_dirty || view >= c->view_recs.size()) return fail(c, RZ_INVALID_STATE, "no rendered frame for this view");
     const ViewRec& r = c->view_recs[view];
     rz_gbuffer g{};
-    g.color_rgba8 = r.color;
-    g.depth_f32 = r.depth;
+    g.color_rgba8 = r.color + (size_t)c->last_parity * c->pix_total;
+    g.depth_f32 = r.depth + (size_t)c->last_parity * c->pix_total;
     g.albedo_rgba8 = r.gb_albedo;
     g.normal_oct_f16x2 = r.gb_normal;
     g.sources_u16 = r.gb_sources;
@@ -1602,32 +1633,19 @@ int rz_read_frame(rz_ctx* c, void* color_host, size_t color_bytes, void* depth_h
         return fail(c, RZ_INVALID_ARGUMENT, "host buffer too small");
     cudaSetDevice(c->device);
     if (!color_host && !depth_host) return RZ_OK;
-    if (2 * need > c->read_stage_capacity) {
-        cudaStreamSynchronize(c->copy_stream);
-        cudaStreamSynchronize(c->stream);
-        for (int k = 0; k < 2; ++k) {
-            cudaFree(c->d_read_stage[k]);
-            c->d_read_stage[k] = nullptr;
-        }
-        c->read_stage_capacity = 0;
-        for (int k = 0; k < 2; ++k)
-            RZ_CUDA(c, cudaMalloc(reinterpret_cast<void**>(&c->d_read_stage[k]), 2 * need), "read-back staging");
-        c->read_stage_capacity = 2 * need;
-        c->reads_issued = 0;
-    }
-    // the frame's images into a staging buffer (on the frame stream, after the frame),
-    // then to the host on the copy stream; the staging buffer's previous read-back
-    // (two calls ago) has landed first
-    const int slot = (int)(c->reads_issued & 1u);
-    unsigned char* st = c->d_read_stage[slot];
-    if (c->reads_issued >= 2) RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->read_done[slot], 0), "read-back slot");
-    if (color_host) RZ_CUDA(c, cudaMemcpyAsync(st, r.color, need, cudaMemcpyDeviceToDevice, c->stream), "stage colour");
-    if (depth_host) RZ_CUDA(c, cudaMemcpyAsync(st + need, r.depth, need, cudaMemcpyDeviceToDevice, c->stream), "stage depth");
-    RZ_CUDA(c, cudaEventRecord(c->read_staged[slot], c->stream), "staged");
-    RZ_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->read_staged[slot], 0), "staged");
-    if (color_host) RZ_CUDA(c, cudaMemcpyAsync(color_host, st, need, cudaMemcpyDeviceToHost, c->copy_stream), "read colour");
-    if (depth_host) RZ_CUDA(c, cudaMemcpyAsync(depth_host, st + need, need, cudaMemcpyDeviceToHost, c->copy_stream), "read depth");
-    RZ_CUDA(c, cudaEventRecord(c->read_done[slot], c->copy_stream), "read done");
+    // the last frame's images, straight from its target set, on the copy stream
+    // after the frame; the frame after next, which renders into the same set,
+    // waits for this read-back (rz_render)
+    const uint32_t set = c->last_parity;
+    const size_t off = (size_t)set * c->pix_total;
+    RZ_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->frame_done, 0), "frame before its read-back");
+    if (color_host)
+        RZ_CUDA(c, cudaMemcpyAsync(color_host, r.color + off, need, cudaMemcpyDeviceToHost, c->copy_stream), "read colour");
+    if (depth_host)
+        RZ_CUDA(c, cudaMemcpyAsync(depth_host, r.depth + off, need, cudaMemcpyDeviceToHost, c->copy_stream), "read depth");
+    RZ_CUDA(c, cudaEventRecord(c->read_done[set], c->copy_stream), "read done");
+    c->read_issued[set] = true;
+    c->read_newest = set;
     ++c->reads_issued;
     return RZ_OK;
 }
@@ -1638,8 +1656,11 @@ int rz_read_sync(rz_ctx* c, uint32_t pending, uint32_t timeout_ms) {
     if (pending == 0 || c->reads_issued == 0)
         return wait_until(c, [&] { return cudaStreamQuery(c->copy_stream); }, timeout_ms, "frame read-back");
     if (c->reads_issued < 2) return RZ_OK;  // at most one read-back was ever queued
-    const int slot = (int)((c->reads_issued - 2) & 1u);  // all but the newest read-back
-    return wait_until(c, [&] { return cudaEventQuery(c->read_done[slot]); }, timeout_ms, "frame read-back");
+    // all but the newest: the copy stream runs the read-backs in order, so they
+    // have all landed once the last read-back of the other target set has
+    const uint32_t older = c->read_newest ^ 1u;
+    if (!c->read_issued[older]) return RZ_OK;
+    return wait_until(c, [&] { return cudaEventQuery(c->read_done[older]); }, timeout_ms, "frame read-back");
 }
 
 int rz_get_stats(rz_ctx* c, rz_stats* out) {
