@@ -851,10 +851,11 @@ void enqueue_shadow(rz_ctx* c, cudaStream_t s, bool stamps) {
         cl.bytes[1] = c->shadow_total * 4;
         cl.count = 2;
     }
-    launch_clear(cl, c->sm_count, s);
+    // the per-draw matrices and the clear in one launch
+    if (c->shadow_tris) launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s, &cl, c->sm_count);
+    else launch_clear(cl, c->sm_count, s);
     if (stamps) stamp(c, 1);
     if (c->shadow_tris) {
-        launch_prep(c->d_shadow_draws, c->shadow_draw_count, c->d_objects, c->d_views, c->d_shadow_mvp, s);
         PassParams sp = pass_params(c, 0);
         sp.clear_ptr[0] = c->d_shadow;
         sp.clear_bytes[0] = c->shadow_total * 4;
@@ -906,8 +907,8 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
         cl.bytes[cl.count] = (size_t)setup_ctas(c->blended_tris) * 8;
         ++cl.count;
     }
-    launch_clear(cl, c->sm_count, s);
-    launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s);
+    // the per-draw constants and the clear in one launch
+    launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s, &cl, c->sm_count);
     if (stamps) stamp(c, 4);
     if (c->opaque_tris) {
         PassParams cp = pass_params(c, 1);

@@ -47,4 +47,26 @@ __device__ __forceinline__ uint32_t find_draw(const DrawRec* __restrict__ draws,
     return lo;
 }
 
+// Thread `tid` of `stride` threads' share of zeroing n bytes at ptr: 16-byte
+// stores on the 16-byte-aligned body, byte stores on the unaligned head and
+// tail, so any start address and size is safe.
+__device__ __forceinline__ void zero_share(void* ptr, size_t n, size_t tid, size_t stride) {
+    unsigned char* base = static_cast<unsigned char*>(ptr);
+    size_t head = (16 - ((size_t)base & 15)) & 15;
+    if (head > n) head = n;
+    if (tid < head) base[tid] = 0;
+    const size_t n16 = (n - head) / 16;
+    uint4* body = reinterpret_cast<uint4*>(base + head);
+    for (size_t i = tid; i < n16; i += stride) body[i] = make_uint4(0u, 0u, 0u, 0u);
+    const size_t done = head + n16 * 16;
+    if (tid < n - done) base[done + tid] = 0;
+}
+
+// This thread's share of zeroing every range of L (all threads of the grid).
+__device__ __forceinline__ void clear_share(const ClearList& L) {
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (int b = 0; b < L.count; ++b) zero_share(L.ptr[b], L.bytes[b], tid, stride);
+}
+
 }  // namespace rz

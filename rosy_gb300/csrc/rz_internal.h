@@ -266,10 +266,13 @@ struct ClearList {
 void note_launch();
 uint32_t take_launches();
 void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream);
+// blocks of `threads` threads that zero a clear list (0 if it is empty)
+unsigned clear_blocks(const ClearList& list, int sm_count, unsigned threads);
+// The per-draw matrices; with `clear` the same launch also zeroes that list.
 void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
-                 float* out_mvp, cudaStream_t stream);
+                 float* out_mvp, cudaStream_t stream, const ClearList* clear = nullptr, int sm_count = 0);
 void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
-                        DrawConsts* out, cudaStream_t stream);
+                        DrawConsts* out, cudaStream_t stream, const ClearList* clear = nullptr, int sm_count = 0);
 void launch_setup(const PassParams& p, cudaStream_t stream);
 void launch_raster(const PassParams& p, int sm_count, cudaStream_t stream);
 void launch_vertex(const ShadeParams& p, cudaStream_t stream);

@@ -35,9 +35,12 @@ namespace rz {
 // per-draw matrices
 // ---------------------------------------------------------------------------
 
+// Also zeroes the clear list L (the pass's header and look-back words), so that
+// the two need one launch.
 __global__ void k_prep(const DrawRec* __restrict__ draws, uint32_t n, const rz_object* __restrict__ objects,
-                       const ViewRec* __restrict__ views, float* __restrict__ out) {
+                       const ViewRec* __restrict__ views, float* __restrict__ out, ClearList L) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    clear_share(L);
     if (d >= n) return;
     const float* P = views[draws[d].view].scene->shadow_projection_near;
     float A[16], B[16], C[16];
@@ -71,9 +74,12 @@ uint32_t take_launches() {
 }
 
 void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views, float* out_mvp,
-                 cudaStream_t stream) {
-    if (n == 0) return;
-    k_prep<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, views, out_mvp);
+                 cudaStream_t stream, const ClearList* clear, int sm_count) {
+    const ClearList none{};
+    const ClearList& L = clear ? *clear : none;
+    const unsigned blocks = std::max((n + 127) / 128, clear_blocks(L, sm_count, 128));
+    if (blocks == 0) return;
+    k_prep<<<blocks, 128, 0, stream>>>(draws, n, objects, views, out_mvp, L);
     note_launch();
 }
 
@@ -81,36 +87,22 @@ void launch_prep(const DrawRec* draws, uint32_t n, const rz_object* objects, con
 // clears (the load-op CLEAR of the depth attachments, scratch headers)
 // ---------------------------------------------------------------------------
 
-// Thread `tid` of `stride` threads' share of zeroing n bytes at ptr: 16-byte
-// stores on the 16-byte-aligned body, byte stores on the unaligned head and
-// tail, so any start address and size is safe.
-__device__ __forceinline__ void zero_share(void* ptr, size_t n, size_t tid, size_t stride) {
-    unsigned char* base = static_cast<unsigned char*>(ptr);
-    size_t head = (16 - ((size_t)base & 15)) & 15;
-    if (head > n) head = n;
-    if (tid < head) base[tid] = 0;
-    const size_t n16 = (n - head) / 16;
-    uint4* body = reinterpret_cast<uint4*>(base + head);
-    for (size_t i = tid; i < n16; i += stride) body[i] = make_uint4(0u, 0u, 0u, 0u);
-    const size_t done = head + n16 * 16;
-    if (tid < n - done) base[done + tid] = 0;
-}
+__global__ void __launch_bounds__(256) k_clear(ClearList L) { clear_share(L); }
 
-__global__ void __launch_bounds__(256) k_clear(ClearList L) {
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (int b = 0; b < L.count; ++b) zero_share(L.ptr[b], L.bytes[b], tid, stride);
+unsigned clear_blocks(const ClearList& list, int sm_count, unsigned threads) {
+    size_t most = 0;
+    for (int b = 0; b < list.count; ++b) most = list.bytes[b] > most ? list.bytes[b] : most;
+    if (most == 0) return 0;
+    size_t blocks = (most / 16 + threads - 1) / threads;
+    const size_t cap = (size_t)sm_count * 8 * (256 / threads);
+    if (blocks > cap) blocks = cap;
+    return blocks ? (unsigned)blocks : 1u;
 }
 
 void launch_clear(const ClearList& list, int sm_count, cudaStream_t stream) {
-    size_t most = 0;
-    for (int b = 0; b < list.count; ++b) most = list.bytes[b] > most ? list.bytes[b] : most;
-    if (most == 0) return;
-    size_t blocks = (most / 16 + 255) / 256;
-    const size_t cap = (size_t)sm_count * 8;
-    if (blocks > cap) blocks = cap;
-    if (blocks == 0) blocks = 1;
-    k_clear<<<(unsigned)blocks, 256, 0, stream>>>(list);
+    const unsigned blocks = clear_blocks(list, sm_count, 256);
+    if (blocks == 0) return;
+    k_clear<<<blocks, 256, 0, stream>>>(list);
     note_launch();
 }
 

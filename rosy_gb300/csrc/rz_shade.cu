@@ -25,6 +25,8 @@
 // approximate division; its output stays within the 1/255 bound.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "rz_device.cuh"
 
 namespace rz {
@@ -58,9 +60,12 @@ __device__ __forceinline__ V3 mulm3v(const float* N, V3 v) {
 // per-draw constants
 // ---------------------------------------------------------------------------
 
+// Also zeroes the clear list L (the camera pass's headers and look-back words),
+// so that the two need one launch.
 __global__ void k_prep_camera(const DrawRec* __restrict__ draws, uint32_t n, const rz_object* __restrict__ objects,
-                              const ViewRec* __restrict__ views, DrawConsts* __restrict__ out) {
+                              const ViewRec* __restrict__ views, DrawConsts* __restrict__ out, ClearList L) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    clear_share(L);
     if (d >= n) return;
     const rz_scene_data* sd = views[draws[d].view].scene;
     const rz_object& gd = objects[draws[d].object];
@@ -102,9 +107,12 @@ __global__ void k_prep_camera(const DrawRec* __restrict__ draws, uint32_t n, con
 }
 
 void launch_prep_camera(const DrawRec* draws, uint32_t n, const rz_object* objects, const ViewRec* views,
-                        DrawConsts* out, cudaStream_t stream) {
-    if (n == 0) return;
-    k_prep_camera<<<(n + 127) / 128, 128, 0, stream>>>(draws, n, objects, views, out);
+                        DrawConsts* out, cudaStream_t stream, const ClearList* clear, int sm_count) {
+    const ClearList none{};
+    const ClearList& L = clear ? *clear : none;
+    const unsigned blocks = std::max((n + 127) / 128, clear_blocks(L, sm_count, 128));
+    if (blocks == 0) return;
+    k_prep_camera<<<blocks, 128, 0, stream>>>(draws, n, objects, views, out, L);
     note_launch();
 }
 

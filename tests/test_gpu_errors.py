@@ -92,10 +92,10 @@ def test_stage_timing(gpu):
 @pytest.mark.gpu
 @pytest.mark.parametrize("samples", [1, 4])
 def test_launch_count_is_exact(gpu, samples):
-    """kernel_launches counts what the launchers enqueued: for one opaque view, a clear per
-    pass, shadow prep / setup / raster, camera prep / setup, one raster per sample, the
-    vertex stage and the shading; the same through the frame graph, a replay of it, and
-    the stage-timed direct launches."""
+    """kernel_launches counts what the launchers enqueued: for one opaque view, the shadow
+    prep (with the pass's clear) / setup / raster, the camera prep (with its clear) /
+    setup, one raster per sample, the vertex stage and the shading; the same through the
+    frame graph, a replay of it, and the stage-timed direct launches."""
     s = sc.tiny(2)
     g = Graphics()
     g.init(s.width, s.height, s.shadow_size, samples=samples)
@@ -103,7 +103,7 @@ def test_launch_count_is_exact(gpu, samples):
         g.set_asset(s)
         g.set_graphic_objects(s.objects, s.surfaces)
         g.update(s.scene)
-        expected = 2 + 3 + 2 + samples + 1 + 1
+        expected = 3 + 2 + samples + 1 + 1
         for timed in (False, False, True):
             g.set_stage_timing(timed)
             g.render()
