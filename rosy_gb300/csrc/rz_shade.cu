@@ -189,13 +189,10 @@ __device__ __forceinline__ void vertex_main(const rz_scene_data& sd, const rz_ob
 // Normalised device coordinate of pixel centre i of an extent of n pixels.
 __device__ __forceinline__ float ndc(int i, int n) { return (float)(2 * i + 1 - n) / (float)n; }
 
-// The normalised coordinates of the pixel centres of one 16x16 shading tile,
-// computed once per tile in shared memory (the same ndc() values, so every
-// pixel's barycentrics are unchanged): column x0 + i at xn[i], row y0 + j at yn[j].
-struct TileCoords {
-    const float* xn;
-    const float* yn;
-    int x0, y0;
+// The normalised coordinates a pixel's barycentrics use: its centre (xp, yp) and
+// its quad's (xq, yq), (xq1 = column + 1, yq1 = row + 1).
+struct PixelNdc {
+    float xp, yp, xq, yq, xq1, yq1;
 };
 
 __device__ __forceinline__ void barycentrics_n(const float4& c0, const float4& c1, const float4& c2, float xn, float yn,
@@ -750,10 +747,10 @@ void launch_vertex_range(const ShadeParams& p, uint32_t first, cudaStream_t stre
 // records of its three vertices.
 // With `aux` non-null it also returns the G-buffer values: albedo (the sampled
 // base colour, rgb) and the interpolated world-space normal (normalised, xyz).
-// With `tc` non-null the pixel lies in that tile and its coordinates come from there.
+// With `pn` non-null the pixel-centre coordinates come from there (see pixel_ndc).
 template <bool kLit = false>
 __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_scene_data& sd, const Sampler& smp, uint32_t tri,
-                            int px, int py, float out[4], float* aux = nullptr, const TileCoords* tc = nullptr) {
+                            int px, int py, float out[4], float* aux = nullptr, const PixelNdc* pn = nullptr) {
     uint32_t d;
     const float4* rec[3];
     if (P.tri_refs) {  // the opaque list: the camera setup recorded the draw and the vertices
@@ -781,13 +778,13 @@ __device__ bool shade_pixel(const ShadeParams& P, const ViewRec& VR, const rz_sc
     float b[3], bq0[3], bqx[3], bqy[3];
     const int qx = px & ~1, qy = py & ~1;
     float xp, yp, xq, yq, xq1, yq1;  // ndc of px, py, qx, qy, qx + 1, qy + 1
-    if (tc) {
-        xp = tc->xn[px - tc->x0];
-        yp = tc->yn[py - tc->y0];
-        xq = tc->xn[qx - tc->x0];
-        yq = tc->yn[qy - tc->y0];
-        xq1 = tc->xn[qx + 1 - tc->x0];
-        yq1 = tc->yn[qy + 1 - tc->y0];
+    if (pn) {
+        xp = pn->xp;
+        yp = pn->yp;
+        xq = pn->xq;
+        yq = pn->yq;
+        xq1 = pn->xq1;
+        yq1 = pn->yq1;
     } else {
         xp = ndc(px, VR.width);
         yp = ndc(py, VR.height);
@@ -922,7 +919,7 @@ __device__ __forceinline__ float resolve4(float a, float b, float c, float d) {
 // sample planes for k_blend. The depth output is sample 0's.
 template <bool kLit>
 __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& VR, const float* s_srgb,
-                                           const TileCoords& tc, int px, int py, size_t p) {
+                                           const PixelNdc& pn, int px, int py, size_t p) {
     const size_t plane = (size_t)VR.width * VR.height;
     uint32_t ids[kMsaaSamples];
     unsigned long long key0 = 0;
@@ -953,7 +950,7 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
         }
         if (ids[k] != 0) {
             float o[4];
-            if (shade_pixel<kLit>(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr, &tc)) {
+            if (shade_pixel<kLit>(P, VR, *VR.scene, smp, ids[k] - 1u, px, py, o, gbuffer ? aux : nullptr, &pn)) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) c[i] = o[i];
             }
@@ -994,21 +991,29 @@ __device__ __forceinline__ void shade_msaa(const ShadeParams& P, const ViewRec& 
     VR.color[p] = encode_srgb8(r[0]) | (encode_srgb8(r[1]) << 8) | (encode_srgb8(r[2]) << 16) | (encode_unorm8(r[3]) << 24);
 }
 
-// The tile's view, its origin and its coordinate table (16 columns, 16 rows;
-// also the columns and rows past the view's edge, which quads reach).
-__device__ __forceinline__ TileCoords tile_setup(const ShadeParams& P, const ViewRec& VR, float* s_xn, float* s_yn) {
+// The pixel (px, py) of this thread in the block's 16x16 tile, and its
+// pixel-centre coordinates. Each lane of a warp (16 columns, 2 rows) computes its
+// column's and its row's coordinate (the values ndc() gives) and takes its quad's
+// from the lanes of its quad's first column and of the two rows, so the tile needs
+// no shared table and no second block barrier. All lanes take part (shuffles).
+__device__ __forceinline__ PixelNdc pixel_ndc(const ShadeParams& P, const ViewRec& VR, int& px, int& py) {
     const uint32_t lt = blockIdx.x + P.block_offset - VR.shade_block_base;
     const uint32_t tiles_x = ((uint32_t)VR.width + 15) / 16;
-    const int x0 = (int)(lt % tiles_x) * 16, y0 = (int)(lt / tiles_x) * 16;
-    if (threadIdx.y == 0) s_xn[threadIdx.x] = ndc(x0 + (int)threadIdx.x, VR.width);
-    if (threadIdx.y == 1) s_yn[threadIdx.x] = ndc(y0 + (int)threadIdx.x, VR.height);
-    __syncthreads();
-    return TileCoords{s_xn, s_yn, x0, y0};
+    px = (int)(lt % tiles_x) * 16 + (int)threadIdx.x;
+    py = (int)(lt / tiles_x) * 16 + (int)threadIdx.y;
+    const int lane = (int)(threadIdx.x + 16 * (threadIdx.y & 1));
+    PixelNdc pn;
+    pn.xp = ndc(px, VR.width);
+    pn.yp = ndc(py, VR.height);
+    pn.xq = __shfl_sync(0xffffffffu, pn.xp, lane & 14);
+    pn.xq1 = __shfl_sync(0xffffffffu, pn.xp, (lane & 14) + 1);
+    pn.yq = __shfl_sync(0xffffffffu, pn.yp, lane & 15);
+    pn.yq1 = __shfl_sync(0xffffffffu, pn.yp, (lane & 15) + 16);
+    return pn;
 }
 
 __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     __shared__ float s_srgb[256];
-    __shared__ float s_xn[16], s_yn[16];
     __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -1017,9 +1022,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
     }
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
-    const TileCoords tc = tile_setup(P, VR, s_xn, s_yn);
-    const int px = tc.x0 + (int)threadIdx.x;
-    const int py = tc.y0 + (int)threadIdx.y;
+    int px, py;
+    const PixelNdc pn = pixel_ndc(P, VR, px, py);
     if (px >= VR.width || py >= VR.height) return;
     const size_t p = (size_t)py * VR.width + px;
     const unsigned long long key = VR.vis[p];
@@ -1032,8 +1036,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
         float o[4];
         const rz_scene_data& sd = *VR.scene;
         float* const ax = gbuffer ? aux : nullptr;
-        if (lit_view(sd) ? shade_pixel<true>(P, VR, sd, smp, id - 1u, px, py, o, ax, &tc)
-                         : shade_pixel<false>(P, VR, sd, smp, id - 1u, px, py, o, ax, &tc)) {
+        if (lit_view(sd) ? shade_pixel<true>(P, VR, sd, smp, id - 1u, px, py, o, ax, &pn)
+                         : shade_pixel<false>(P, VR, sd, smp, id - 1u, px, py, o, ax, &pn)) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) col[k] = o[k];
         }
@@ -1059,7 +1063,6 @@ __global__ void __launch_bounds__(256, 4) k_shade(ShadeParams P) {
 // k_shade for 4x multisampled views.
 __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     __shared__ float s_srgb[256];
-    __shared__ float s_xn[16], s_yn[16];
     __shared__ uint32_t s_view;
     {
         const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -1068,12 +1071,12 @@ __global__ void __launch_bounds__(256, 4) k_shade_msaa(ShadeParams P) {
     }
     __syncthreads();
     const ViewRec& VR = P.views[s_view];
-    const TileCoords tc = tile_setup(P, VR, s_xn, s_yn);
-    const int px = tc.x0 + (int)threadIdx.x;
-    const int py = tc.y0 + (int)threadIdx.y;
+    int px, py;
+    const PixelNdc pn = pixel_ndc(P, VR, px, py);
     if (px >= VR.width || py >= VR.height) return;
-    if (lit_view(*VR.scene)) shade_msaa<true>(P, VR, s_srgb, tc, px, py, (size_t)py * VR.width + px);
-    else shade_msaa<false>(P, VR, s_srgb, tc, px, py, (size_t)py * VR.width + px);
+    const size_t p = (size_t)py * VR.width + px;
+    if (lit_view(*VR.scene)) shade_msaa<true>(P, VR, s_srgb, pn, px, py, p);
+    else shade_msaa<false>(P, VR, s_srgb, pn, px, py, p);
 }
 
 void launch_shade(const ShadeParams& p, cudaStream_t stream) {
