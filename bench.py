@@ -11,8 +11,8 @@ uploaded inside the frame, everything else is resident); L2 is flushed by a
 256 MiB write between frames, outside the timed events. `e2e` is frames/s
 through the C ABI with host buffers: per frame, the scene constants and all
 object transforms go host->device from pinned memory and the RGBA8 frame comes
-back device->host into pinned memory (a device staging copy, then the copy to
-the host on the renderer's copy stream while the next frame renders),
+back device->host into pinned memory (copied straight from the frame's target
+set on the renderer's copy stream while the next frame renders into the other),
 wall-clock timed, with two frames in flight (a host buffer is reused once the
 read-back that last filled it has landed, rz_read_sync;
 the reference's Vulkan renderer keeps up to three, src/Engine/Graphics.cpp:177).
