@@ -94,6 +94,8 @@ struct rz_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;  // shadow pass branch of the frame graph
+    cudaStream_t vtx = nullptr;   // vertex stage, beside the camera pass's setup and raster
+    cudaEvent_t vtx_fork = nullptr, vtx_join = nullptr;
     // read-back (rz_read_frame): device staging copies on the frame stream, then
     // device-to-host copies on their own stream so that the next frame renders meanwhile
     cudaStream_t copy_stream = nullptr;
@@ -909,6 +911,15 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
     }
     // the per-draw constants and the clear in one launch
     launch_prep_camera(c->d_opaque_draws, c->opaque_draw_count, c->d_objects, c->d_views, c->d_camera_consts, s, &cl, c->sm_count);
+    // the vertex stage needs only the per-draw constants: outside stage timing it
+    // runs on a branch of its own beside the camera pass's setup and raster
+    const bool vtx_branch = !stamps;
+    if (vtx_branch) {
+        cudaEventRecord(c->vtx_fork, s);
+        cudaStreamWaitEvent(c->vtx, c->vtx_fork, 0);
+        launch_vertex(sh, c->vtx);
+        cudaEventRecord(c->vtx_join, c->vtx);
+    }
     if (stamps) stamp(c, 4);
     if (c->opaque_tris) {
         PassParams cp = pass_params(c, 1);
@@ -922,7 +933,8 @@ void enqueue_camera(rz_ctx* c, cudaStream_t s, bool stamps, const ShadeParams& s
     } else if (stamps) {
         stamp(c, 5);
     }
-    launch_vertex(sh, s);
+    if (vtx_branch) cudaStreamWaitEvent(s, c->vtx_join, 0);
+    else launch_vertex(sh, s);
     if (c->blended_tris) {
         launch_prep_camera(c->d_blended_draws, c->blended_draw_count, c->d_objects, c->d_views, c->d_blended_consts, s);
         launch_setup(pass_params(c, 2), s);
@@ -1203,6 +1215,9 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->vtx, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->vtx_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->vtx_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->camera_done, cudaEventDisableTiming) != cudaSuccess ||
@@ -1255,6 +1270,7 @@ void rz_destroy(rz_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
+    if (c->vtx) cudaStreamSynchronize(c->vtx);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     drop_graph(c);
     free_asset(c);
@@ -1300,6 +1316,8 @@ void rz_destroy(rz_ctx* c) {
     if (c->scene_copied) cudaEventDestroy(c->scene_copied);
     if (c->objects_copied) cudaEventDestroy(c->objects_copied);
     if (c->fork) cudaEventDestroy(c->fork);
+    if (c->vtx_fork) cudaEventDestroy(c->vtx_fork);
+    if (c->vtx_join) cudaEventDestroy(c->vtx_join);
     if (c->join) cudaEventDestroy(c->join);
     if (c->camera_done) cudaEventDestroy(c->camera_done);
     if (c->sources_done) cudaEventDestroy(c->sources_done);
@@ -1309,6 +1327,7 @@ void rz_destroy(rz_ctx* c) {
     }
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->vtx) cudaStreamDestroy(c->vtx);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
