@@ -63,6 +63,9 @@ def test_calls_without_a_context_are_rejected(renderer_lib):
     assert renderer_lib.rz_render(None) == 3
     assert renderer_lib.rz_sync(None, 0) == 3
     assert renderer_lib.rz_set_debug_objects(None, None, 0) == 3
+    assert renderer_lib.rz_read_frame(None, None, 0, None, 0) == 3
+    assert renderer_lib.rz_read_sync(None, 0, 0) == 3
+    assert renderer_lib.rz_get_frame(None, None) == 3
     out = C.c_void_p()
     assert renderer_lib.rz_create(C.byref(out), None) == 3
     renderer_lib.rz_destroy(None)
