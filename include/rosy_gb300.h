@@ -295,16 +295,19 @@ int rz_set_objects(struct rz_ctx* ctx,
                    const rz_surface* surfaces, uint32_t surface_count);
 
 /* Mob transform update (src/Engine/Graphics.cpp:5120-5138): overwrite
- * objects [offset, offset+count) before the next frame; enqueued on the stream. */
+ * objects [offset, offset+count) before the next frame. Staged in pinned memory
+ * and copied to the device by rz_render, like the scene constants. */
 int rz_update_objects(struct rz_ctx* ctx, uint32_t offset, const rz_object* objects, uint32_t count);
 
 /* Fixed-function state of the next frames (see rz_draw_config). */
 int rz_set_draw_config(struct rz_ctx* ctx, const rz_draw_config* cfg);
 
 /* graphics_device::update (src/Engine/Graphics.cpp:6016): the scene constants
- * of the next frame. The 408 bytes are staged in pinned memory and copied on
- * the stream, so a frame always uses its own constants (the reference writes
- * the next frame's buffer, 5064-5065; that one-frame lag is not reproduced). */
+ * of the next frame. The 408 bytes are staged in pinned memory and copied to the
+ * device by rz_render, before the frame reads them (into the buffer of the
+ * frame's target set, on an upload stream, overlapping the frame before), so a
+ * frame always uses its own constants (the reference writes the next frame's
+ * buffer, 5064-5065; that one-frame lag is not reproduced). */
 int rz_update(struct rz_ctx* ctx, const rz_scene_data* scene);
 
 /* graphics_device::render (src/Engine/Graphics.cpp:4934): enqueues the shadow

@@ -131,19 +131,28 @@ struct rz_ctx {
     GpuMaterial* d_materials = nullptr;
     TexDesc* d_textures = nullptr;
     SamplerBits* d_samplers = nullptr;
-    rz_object* d_objects = nullptr;
-    rz_object* h_objects = nullptr;  // pinned staging for rz_update_objects
+    // The per-frame inputs (object records, scene constants) are double-buffered
+    // with the target sets: the host stages them in pinned memory, and before a
+    // frame renders into set k they are copied into set k's buffers on the upload
+    // stream, once the frame that last used set k is done; the frame waits for
+    // that copy, which so overlaps the frame before it.
+    rz_object* d_objects = nullptr;       // the object records of the frame being enqueued
+    rz_object* d_objects_base = nullptr;  // both sets: set k at k * objects.size()
+    rz_object* h_objects = nullptr;       // pinned staging: every object, current
     size_t h_objects_capacity = 0;
-    cudaEvent_t objects_copied = nullptr;
+    cudaStream_t upload = nullptr;
+    cudaEvent_t upload_done[2] = {nullptr, nullptr};  // the last copy into set k
+    cudaEvent_t set_done[2] = {nullptr, nullptr};     // the last frame that used set k
+    uint64_t objects_version = 1, scene_version = 1;  // bumped by every update
+    uint64_t set_objects_version[2] = {0, 0}, set_scene_version[2] = {0, 0};
     float* d_srgb = nullptr;
     bool asset_dirty = true;         // device asset arrays need an upload
 
     // views
     std::vector<ViewHost> views;
-    rz_scene_data* d_scene_data = nullptr;  // one per view
+    rz_scene_data* d_scene_data = nullptr;  // one per view, per set: set k at k * scene_data_capacity
     rz_scene_data* h_scene_data = nullptr;  // pinned staging, one per view
     uint32_t scene_data_capacity = 0;
-    cudaEvent_t scene_copied = nullptr;
     // The colour and depth targets are double-buffered: frames alternate between
     // two target sets, so the read-back of one frame copies its images to the
     // host while the next frame renders into the other set. Each set has its
@@ -486,12 +495,23 @@ int upload_asset(rz_ctx* c) {
     return RZ_OK;
 }
 
+// Waits until the copies queued from the host staging have read it.
+cudaError_t wait_uploads(rz_ctx* c) {
+    for (int k = 0; k < 2; ++k) {
+        const cudaError_t e = cudaEventSynchronize(c->upload_done[k]);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int upload_objects(rz_ctx* c) {
     cudaStreamSynchronize(c->stream);
-    dfree(c->d_objects);
+    cudaStreamSynchronize(c->upload);
+    dfree(c->d_objects_base);
+    c->d_objects = nullptr;
     const size_t n = c->objects.size();
-    RZ_CUDA(c, dalloc(&c->d_objects, std::max<size_t>(n, 1)), "object buffer");
-    if (n) RZ_CUDA(c, cudaMemcpy(c->d_objects, c->objects.data(), n * sizeof(rz_object), cudaMemcpyHostToDevice), "upload objects");
+    RZ_CUDA(c, dalloc(&c->d_objects_base, 2 * std::max<size_t>(n, 1)), "object buffer");
+    c->d_objects = c->d_objects_base;
     if (n > c->h_objects_capacity) {
         if (c->h_objects) cudaFreeHost(c->h_objects);
         c->h_objects = nullptr;
@@ -499,6 +519,8 @@ int upload_objects(rz_ctx* c) {
         RZ_CUDA(c, cudaMallocHost(&c->h_objects, n * sizeof(rz_object)), "object staging");
         c->h_objects_capacity = n;
     }
+    if (n) std::memcpy(c->h_objects, c->objects.data(), n * sizeof(rz_object));
+    ++c->objects_version;  // both sets take the objects before their next frame
     c->layout_dirty = true;  // the graph holds the object buffer's address
     return RZ_OK;
 }
@@ -506,16 +528,14 @@ int upload_objects(rz_ctx* c) {
 int ensure_scene_data(rz_ctx* c, uint32_t n) {
     if (n <= c->scene_data_capacity) return RZ_OK;
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->upload);
     rz_scene_data* d = nullptr;
     rz_scene_data* h = nullptr;
-    RZ_CUDA(c, dalloc(&d, n), "scene constants");
+    RZ_CUDA(c, dalloc(&d, 2 * (size_t)n), "scene constants");
     RZ_CUDA(c, cudaMallocHost(&h, n * sizeof(rz_scene_data)), "scene staging");
     std::memset(h, 0, n * sizeof(rz_scene_data));
-    if (c->scene_data_capacity) {
-        RZ_CUDA(c, cudaMemcpy(d, c->d_scene_data, c->scene_data_capacity * sizeof(rz_scene_data), cudaMemcpyDeviceToDevice),
-                "copy scene constants");
-        std::memcpy(h, c->h_scene_data, c->scene_data_capacity * sizeof(rz_scene_data));
-    }
+    if (c->scene_data_capacity) std::memcpy(h, c->h_scene_data, c->scene_data_capacity * sizeof(rz_scene_data));
+    ++c->scene_version;  // both sets take the staged constants before their next frame
     dfree(c->d_scene_data);
     if (c->h_scene_data) cudaFreeHost(c->h_scene_data);
     c->d_scene_data = d;
@@ -719,6 +739,7 @@ int build_layout(rz_ctx* c) {
         for (ViewRec& r : set) {
             r.color += (size_t)k * pix;
             r.depth += (size_t)k * pix;
+            r.scene += (size_t)k * c->scene_data_capacity;
         }
         RZ_CUDA(c, cudaMemcpy(c->d_views_set[k], set.data(), set.size() * sizeof(ViewRec), cudaMemcpyHostToDevice),
                 "upload views");
@@ -1228,8 +1249,11 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         if (cudaEventCreateWithFlags(&c->read_done[k], cudaEventDisableTiming) != cudaSuccess)
             return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->scene_copied, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->objects_copied, cudaEventDisableTiming) != cudaSuccess)
+        cudaStreamCreateWithFlags(&c->upload, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->upload_done[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->upload_done[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->set_done[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->set_done[1], cudaEventDisableTiming) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
     if (dalloc(&c->d_report, 1) != cudaSuccess || cudaMemset(c->d_report, 0, sizeof(FrameReport)) != cudaSuccess ||
         dalloc(&c->d_srgb, 256) != cudaSuccess)
@@ -1272,6 +1296,7 @@ void rz_destroy(rz_ctx* c) {
     if (c->side) cudaStreamSynchronize(c->side);
     if (c->vtx) cudaStreamSynchronize(c->vtx);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    if (c->upload) cudaStreamSynchronize(c->upload);
     drop_graph(c);
     free_asset(c);
     free_pass(c->shadow_pass);
@@ -1283,7 +1308,8 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_materials);
     dfree(c->d_textures);
     dfree(c->d_samplers);
-    dfree(c->d_objects);
+    dfree(c->d_objects_base);
+    c->d_objects = nullptr;
     dfree(c->d_srgb);
     dfree(c->d_scene_data);
     for (int k = 0; k < 2; ++k) dfree(c->d_views_set[k]);
@@ -1313,8 +1339,11 @@ void rz_destroy(rz_ctx* c) {
     if (c->frame_done) cudaEventDestroy(c->frame_done);
     for (auto& e : c->stage_ev)
         if (e) cudaEventDestroy(e);
-    if (c->scene_copied) cudaEventDestroy(c->scene_copied);
-    if (c->objects_copied) cudaEventDestroy(c->objects_copied);
+    for (int k = 0; k < 2; ++k) {
+        if (c->upload_done[k]) cudaEventDestroy(c->upload_done[k]);
+        if (c->set_done[k]) cudaEventDestroy(c->set_done[k]);
+    }
+    if (c->upload) cudaStreamDestroy(c->upload);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->vtx_fork) cudaEventDestroy(c->vtx_fork);
     if (c->vtx_join) cudaEventDestroy(c->vtx_join);
@@ -1454,13 +1483,13 @@ int rz_update_objects(rz_ctx* c, uint32_t offset, const rz_object* objects, uint
     const SceneHost& sh = c->scenes[0];
     if (!objects || (uint64_t)offset + count > sh.object_count) return fail(c, RZ_INVALID_ARGUMENT, "object range");
     cudaSetDevice(c->device);
-    RZ_CUDA(c, cudaEventSynchronize(c->objects_copied), "wait staging");
+    // the staging is copied to the device before each frame (rz_render); the
+    // copies queued so far have read it before it changes
+    RZ_CUDA(c, wait_uploads(c), "wait staging");
     const uint32_t at = sh.object_base + offset;
     std::memcpy(c->h_objects + at, objects, (size_t)count * sizeof(rz_object));
     std::memcpy(c->objects.data() + at, objects, (size_t)count * sizeof(rz_object));
-    RZ_CUDA(c, cudaMemcpyAsync(c->d_objects + at, c->h_objects + at, (size_t)count * sizeof(rz_object),
-                               cudaMemcpyHostToDevice, c->stream), "upload objects");
-    RZ_CUDA(c, cudaEventRecord(c->objects_copied, c->stream), "record");
+    ++c->objects_version;
     return RZ_OK;
 }
 
@@ -1476,19 +1505,41 @@ int rz_update_view(rz_ctx* c, uint32_t view, const rz_scene_data* scene) {
     if (!c || !scene) return RZ_INVALID_ARGUMENT;
     if (view >= c->views.size()) return fail(c, RZ_INVALID_ARGUMENT, "no such view");
     cudaSetDevice(c->device);
-    RZ_CUDA(c, cudaEventSynchronize(c->scene_copied), "wait staging");
+    RZ_CUDA(c, wait_uploads(c), "wait staging");
     std::memcpy(c->h_scene_data + view, scene, sizeof(rz_scene_data));
-    RZ_CUDA(c, cudaMemcpyAsync(c->d_scene_data + view, c->h_scene_data + view, sizeof(rz_scene_data),
-                               cudaMemcpyHostToDevice, c->stream), "upload scene");
-    RZ_CUDA(c, cudaEventRecord(c->scene_copied, c->stream), "record");
+    ++c->scene_version;
     c->views[view].has_scene_data = true;
     return RZ_OK;
 }
 
 int rz_update(rz_ctx* c, const rz_scene_data* scene) { return rz_update_view(c, 0, scene); }
 
+// Copies the staged object records and scene constants into target set k when
+// they changed since set k's last frame, on the upload stream once that frame is
+// done, and makes the frame stream wait for the copy.
+int upload_set(rz_ctx* c, uint32_t k) {
+    const bool objs = c->set_objects_version[k] != c->objects_version;
+    const bool scene = c->set_scene_version[k] != c->scene_version;
+    if (!objs && !scene) return RZ_OK;
+    RZ_CUDA(c, cudaStreamWaitEvent(c->upload, c->set_done[k], 0), "set free");
+    const size_t n = c->objects.size();
+    if (objs && n)
+        RZ_CUDA(c, cudaMemcpyAsync(c->d_objects_base + (size_t)k * n, c->h_objects, n * sizeof(rz_object),
+                                   cudaMemcpyHostToDevice, c->upload), "upload objects");
+    if (scene)
+        RZ_CUDA(c, cudaMemcpyAsync(c->d_scene_data + (size_t)k * c->scene_data_capacity, c->h_scene_data,
+                                   c->views.size() * sizeof(rz_scene_data), cudaMemcpyHostToDevice, c->upload),
+                "upload scene");
+    RZ_CUDA(c, cudaEventRecord(c->upload_done[k], c->upload), "uploaded");
+    RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->upload_done[k], 0), "wait upload");
+    c->set_objects_version[k] = c->objects_version;
+    c->set_scene_version[k] = c->scene_version;
+    return RZ_OK;
+}
+
 // After a frame is enqueued: its completion event, and the next frame's target set.
 int frame_enqueued(rz_ctx* c) {
+    RZ_CUDA(c, cudaEventRecord(c->set_done[c->parity], c->stream), "record set");
     RZ_CUDA(c, cudaEventRecord(c->frame_done, c->stream), "record frame");
     c->frame_pending = true;
     ++c->frames;
@@ -1518,6 +1569,11 @@ int rz_render(rz_ctx* c) {
     if (c->read_issued[c->parity])
         RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->read_done[c->parity], 0), "read-back of the target set");
     c->d_views = c->d_views_set[c->parity];
+    c->d_objects = c->d_objects_base + (size_t)c->parity * c->objects.size();
+    {
+        const int rc = upload_set(c, c->parity);
+        if (rc != RZ_OK) return rc;
+    }
     cudaGraphExec_t& graph = c->graph_set[c->parity];
     // Stage timing records events between the stages and enqueues directly.
     if (c->use_graph && !c->timing) {
