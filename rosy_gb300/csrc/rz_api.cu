@@ -201,8 +201,15 @@ struct rz_ctx {
 
     // raster scratch
     PassBuffers shadow_pass, camera_pass, blended_pass;
-    FrameReport* d_report = nullptr;  // device frame report (pass headers, error words)
-    FrameReport* h_report = nullptr;  // pinned
+    // The frame report (pass headers, error words), one per target set: a frame
+    // fills its set's report, which is copied to the host on the copy stream
+    // after the frame (off the frame stream); the readers wait for that copy.
+    FrameReport* d_report = nullptr;       // the report of the frame being enqueued
+    FrameReport* d_report_base = nullptr;  // both sets
+    FrameReport* h_report = nullptr;       // pinned: the report of the last frame enqueued
+    FrameReport* h_report_base = nullptr;  // both sets
+    cudaEvent_t report_done[2] = {nullptr, nullptr};
+    bool report_issued[2] = {false, false};
     bool grow_records = false, grow_chunks = false;
 
     // frame sequencing
@@ -1083,8 +1090,6 @@ int enqueue_frame(rz_ctx* c) {
     if (c->timing) stamp(c, 7);
     if (sources_side) RZ_CUDA(c, cudaStreamWaitEvent(s, c->sources_done, 0), "sources done");
     RZ_CUDA(c, cudaGetLastError(), "kernel launch");
-    RZ_CUDA(c, cudaMemcpyAsync(c->h_report, c->d_report, sizeof(FrameReport), cudaMemcpyDeviceToHost, s),
-            "read frame report");
     c->frame_launches = take_launches();
     return RZ_OK;
 }
@@ -1104,6 +1109,7 @@ int check_ready(rz_ctx* c) {
 // reported by the device), with 25% headroom.
 int grow_queues(rz_ctx* c) {
     cudaStreamSynchronize(c->stream);
+    cudaEventSynchronize(c->report_done[c->last_parity]);
     drop_graph(c);
     c->queue_chunks = 0;
     auto grow = [&](PassBuffers& p, const PassHeader& h) -> int {
@@ -1255,11 +1261,16 @@ int rz_create(rz_ctx** out, const rz_config* cfg) {
         cudaEventCreateWithFlags(&c->set_done[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->set_done[1], cudaEventDisableTiming) != cudaSuccess)
         return bail(RZ_GRAPHICS_INIT_FAILURE);
-    if (dalloc(&c->d_report, 1) != cudaSuccess || cudaMemset(c->d_report, 0, sizeof(FrameReport)) != cudaSuccess ||
+    if (dalloc(&c->d_report_base, 2) != cudaSuccess || cudaMemset(c->d_report_base, 0, 2 * sizeof(FrameReport)) != cudaSuccess ||
         dalloc(&c->d_srgb, 256) != cudaSuccess)
         return bail(RZ_ALLOCATION_FAILURE);
-    if (cudaMallocHost(&c->h_report, sizeof(FrameReport)) != cudaSuccess) return bail(RZ_ALLOCATION_FAILURE);
-    std::memset(c->h_report, 0, sizeof(FrameReport));
+    if (cudaMallocHost(&c->h_report_base, 2 * sizeof(FrameReport)) != cudaSuccess) return bail(RZ_ALLOCATION_FAILURE);
+    std::memset(c->h_report_base, 0, 2 * sizeof(FrameReport));
+    c->d_report = c->d_report_base;
+    c->h_report = c->h_report_base;
+    for (int k = 0; k < 2; ++k)
+        if (cudaEventCreateWithFlags(&c->report_done[k], cudaEventDisableTiming) != cudaSuccess)
+            return bail(RZ_GRAPHICS_INIT_FAILURE);
     // sRGB decode table (colour, metallic-roughness and mixmap images are sRGB
     // formats, src/Engine/Graphics.cpp:3632-3647): IEC 61966-2-1 in double, rounded to float.
     float table[256];
@@ -1332,9 +1343,13 @@ void rz_destroy(rz_ctx* c) {
     dfree(c->d_blended_consts);
     dfree(c->d_varyings);
     dfree(c->d_tri_refs);
-    dfree(c->d_report);
+    dfree(c->d_report_base);
+    c->d_report = nullptr;
     if (c->h_scene_data) cudaFreeHost(c->h_scene_data);
-    if (c->h_report) cudaFreeHost(c->h_report);
+    if (c->h_report_base) cudaFreeHost(c->h_report_base);
+    c->h_report = nullptr;
+    for (int k = 0; k < 2; ++k)
+        if (c->report_done[k]) cudaEventDestroy(c->report_done[k]);
     if (c->h_objects) cudaFreeHost(c->h_objects);
     if (c->frame_done) cudaEventDestroy(c->frame_done);
     for (auto& e : c->stage_ev)
@@ -1539,7 +1554,16 @@ int upload_set(rz_ctx* c, uint32_t k) {
 
 // After a frame is enqueued: its completion event, and the next frame's target set.
 int frame_enqueued(rz_ctx* c) {
-    RZ_CUDA(c, cudaEventRecord(c->set_done[c->parity], c->stream), "record set");
+    const uint32_t k = c->parity;
+    RZ_CUDA(c, cudaEventRecord(c->set_done[k], c->stream), "record set");
+    // the frame report to the host, off the frame stream (on the copy stream: the
+    // upload stream's next copy must not wait for this frame's end)
+    RZ_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->set_done[k], 0), "frame before its report");
+    RZ_CUDA(c, cudaMemcpyAsync(c->h_report_base + k, c->d_report_base + k, sizeof(FrameReport), cudaMemcpyDeviceToHost,
+                               c->copy_stream), "read frame report");
+    RZ_CUDA(c, cudaEventRecord(c->report_done[k], c->copy_stream), "report read");
+    c->report_issued[k] = true;
+    c->h_report = c->h_report_base + k;
     RZ_CUDA(c, cudaEventRecord(c->frame_done, c->stream), "record frame");
     c->frame_pending = true;
     ++c->frames;
@@ -1570,6 +1594,10 @@ int rz_render(rz_ctx* c) {
         RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->read_done[c->parity], 0), "read-back of the target set");
     c->d_views = c->d_views_set[c->parity];
     c->d_objects = c->d_objects_base + (size_t)c->parity * c->objects.size();
+    c->d_report = c->d_report_base + c->parity;
+    // the frame zeroes its set's report: the copy of its previous contents has landed
+    if (c->report_issued[c->parity])
+        RZ_CUDA(c, cudaStreamWaitEvent(c->stream, c->report_done[c->parity], 0), "report of the target set");
     {
         const int rc = upload_set(c, c->parity);
         if (rc != RZ_OK) return rc;
@@ -1624,6 +1652,15 @@ int rz_sync(rz_ctx* c, uint32_t timeout_ms) {
         if (rc != RZ_OK) return rc;
     }
     if (!c->frame_pending) return RZ_OK;
+    {  // and the last frame's report
+        uint32_t left = 0;
+        if (timeout_ms) {
+            const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            left = ms >= (long long)timeout_ms ? 1u : timeout_ms - (uint32_t)ms;
+        }
+        rc = wait_until(c, [&] { return cudaEventQuery(c->report_done[c->last_parity]); }, left, "frame report");
+        if (rc != RZ_OK) return rc;
+    }
     c->frame_pending = false;
     const uint32_t e = c->h_report->errors();
     if (e & (kErrRecordOverflow)) c->grow_records = true;
@@ -1742,6 +1779,8 @@ int rz_read_sync(rz_ctx* c, uint32_t pending, uint32_t timeout_ms) {
 int rz_get_stats(rz_ctx* c, rz_stats* out) {
     if (!c || !out) return RZ_INVALID_ARGUMENT;
     std::memset(out, 0, sizeof(*out));
+    cudaSetDevice(c->device);
+    cudaEventSynchronize(c->report_done[c->last_parity]);  // the last frame's report has landed
     out->draw_call_count = c->shadow_draw_count + c->opaque_draw_count + c->blended_draw_count;
     out->triangle_count = c->shadow_tris + c->opaque_tris + c->blended_tris;
     out->shadow_setup_records = c->h_report->shadow.records + c->h_report->shadow.small_records;
