@@ -456,7 +456,11 @@ int rz_shadow_depth_static(const void* positions, uint32_t vertex_count, const u
                            const rz_draw_config* cfg, uint32_t width, uint32_t height, float* depth_out,
                            void* stream);
 
-/* The context's cudaStream_t, for callers that time or chain work on it. */
+/* The context's cudaStream_t, for callers that time or chain work on it: work
+ * enqueued on it after rz_render runs after that frame's kernels. (The context
+ * also uses streams of its own for the frame's concurrent branches, the uploads
+ * of the per-frame inputs and the read-backs; they are joined to this stream or
+ * waited for by rz_sync.) */
 void* rz_get_stream(struct rz_ctx* ctx);
 
 /* Human-readable message of the last failing call on this context. */
